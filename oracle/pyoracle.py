@@ -1,0 +1,141 @@
+"""ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module,
+and only to check or time against; the GPU library never calls it.
+
+State dictionaries use the C ABI's host layout (particle-major, row-major matrices):
+  x (n, dim), v (n, dim), F (n, dim, dim), C (n, dim, dim), Jp (n,), mass (n,), volume (n,).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBS: dict[str, ctypes.CDLL] = {}
+
+SNOW, JELLY, LIQUID = 0, 1, 2
+REFERENCE, CORRECTED = 0, 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int64)
+
+
+def _load(name: str, sub: str) -> ctypes.CDLL:
+    if name not in _LIBS:
+        path = os.path.join(HERE, sub, name)
+        if not os.path.isfile(path):
+            from oracle.build_oracle import build
+            build()
+        lib = ctypes.CDLL(path)
+        if name.startswith("liboracle"):
+            lib.oracle_advance.restype = ctypes.c_int
+            lib.oracle_advance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                           _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp,
+                                           _dp, _ip]
+            lib.oracle_svd.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp]
+            lib.oracle_polar.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]
+            lib.oracle_linspaced.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                             ctypes.POINTER(ctypes.c_float)]
+        else:
+            lib.ref_advance.restype = ctypes.c_int
+            lib.ref_advance.argtypes = [ctypes.c_int, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp,
+                                        _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, _dp, _dp]
+            lib.ref_cube.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                     ctypes.POINTER(ctypes.c_float)]
+        _LIBS[name] = lib
+    return _LIBS[name]
+
+
+def oracle_lib(fast: bool = False) -> ctypes.CDLL:
+    return _load("liboracle_fast.so" if fast else "liboracle.so", "_build")
+
+
+def ref_available() -> bool:
+    return os.path.isfile(os.path.join(HERE, "_ref", "libnclr_ref.so"))
+
+
+def ref_lib() -> ctypes.CDLL:
+    return _load("libnclr_ref.so", "_ref")
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _prep(state: dict, dim: int):
+    n = state["x"].shape[0]
+    out = {}
+    for k, shape in (("x", (n, dim)), ("v", (n, dim)), ("F", (n, dim, dim)), ("C", (n, dim, dim)),
+                     ("Jp", (n,)), ("mass", (n,)), ("volume", (n,))):
+        out[k] = np.ascontiguousarray(np.asarray(state[k], dtype=np.float64).reshape(shape)).copy()
+    return n, out
+
+
+def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-4,
+            E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, steps: int = 1,
+            fp64: bool = False, physics: int = REFERENCE, fast: bool = False,
+            want_grid: bool = True):
+    """Runs `steps` reference steps on a copy of `state`; returns (state, grid, status, counters).
+
+    grid = (velocity (nodes, dim), mass (nodes,)) of the last step, post grid update.
+    status 0 = ok, 2 = a grid index left the grid (the reference throws std::out_of_range).
+    """
+    n, s = _prep(state, dim)
+    nodes = (res + 1) ** dim
+    gv = np.zeros((nodes, dim)) if want_grid else None
+    gm = np.zeros((nodes,)) if want_grid else None
+    counters = np.zeros(2, dtype=np.int64)
+    st = oracle_lib(fast).oracle_advance(
+        dim, int(fp64), physics, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]), _p(s["Jp"]),
+        _p(s["mass"]), _p(s["volume"]), model, res, dt, E, nu, gravity, steps,
+        _p(gv) if want_grid else None, _p(gm) if want_grid else None,
+        counters.ctypes.data_as(_ip))
+    return s, ((gv, gm) if want_grid else None), st, counters
+
+
+def ref_advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-4,
+                E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, steps: int = 1):
+    """The reference's own MPMSimulation<dim>::advance() (compiled against the Eigen shim)."""
+    n, s = _prep(state, dim)
+    nodes = (res + 1) ** dim
+    gv = np.zeros((nodes, dim))
+    gm = np.zeros((nodes,))
+    st = ref_lib().ref_advance(dim, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]),
+                               _p(s["Jp"]), _p(s["mass"]), _p(s["volume"]), model, res, dt, E,
+                               nu, gravity, steps, _p(gv), _p(gm))
+    return s, (gv, gm), st
+
+
+def svd(A: np.ndarray, *, physics: int = REFERENCE, fp64: bool = False):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    d = A.shape[0]
+    U = np.zeros((d, d)); S = np.zeros(d); V = np.zeros((d, d))
+    oracle_lib().oracle_svd(d, int(fp64), physics, _p(A), _p(U), _p(S), _p(V))
+    return U, S, V
+
+
+def polar(A: np.ndarray, *, physics: int = REFERENCE, fp64: bool = False):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    d = A.shape[0]
+    R = np.zeros((d, d))
+    oracle_lib().oracle_polar(d, int(fp64), physics, _p(A), _p(R))
+    return R
+
+
+def linspaced(n: int, lo: float, hi: float) -> np.ndarray:
+    out = np.zeros(n, dtype=np.float32)
+    oracle_lib().oracle_linspaced(n, lo, hi, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    return out
+
+
+def ref_cube(dim: int, n: int, lo: float, hi: float) -> np.ndarray:
+    out = np.zeros((n ** dim, dim), dtype=np.float32)
+    ref_lib().ref_cube(dim, n, lo, hi, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    return out

@@ -1,0 +1,54 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+FIELDS = ("x", "v", "F", "C", "Jp")
+# Error of a field = max|a - b| / max(max|b|, floor); floors are in the field's natural units
+# (positions in the unit box, velocities of one gravity step, F and Jp near 1, C of order 1)
+# so that a field that is zero up to rounding does not produce a meaningless ratio.
+FLOORS = {"x": 1.0, "v": 1e-2, "F": 1.0, "C": 1.0, "Jp": 1.0, "grid_v": 1e-2, "grid_m": 1e-3}
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run on the GB300 box)")
+
+
+def field_err(a, b, name):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if a.size == 0:
+        return 0.0
+    return float(np.abs(a - b).max() / max(float(np.abs(b).max()), FLOORS.get(name, 1.0)))
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    state = {k: z[k] for k in ("x", "v", "F", "C", "Jp", "mass", "volume")}
+    params = dict(dim=int(z["dim"]), model=int(z["model"]), res=int(z["res"]), E=float(z["E"]),
+                  nu=float(z["nu"]), gravity=float(z["gravity"]), dt=float(z["dt"]))
+    return z, state, params, [int(s) for s in z["steps"]]
+
+
+def golden_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def state_at(z, k):
+    s = {f: z[f"{f}@{k}"] for f in FIELDS}
+    s["mass"] = z["mass"]
+    s["volume"] = z["volume"]
+    return s
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    from oracle import pyoracle
+    pyoracle.oracle_lib()
+    return pyoracle
