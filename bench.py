@@ -1,0 +1,324 @@
+"""Benchmark of the MLS-MPM time step on GB300: particle-steps/s.
+
+Workload (default): 3D jelly, 128^3 grid, 4 jittered cubes of 64^3 lattice particles
+(1,048,576 particles) with centres uniform in [0.25, 0.75]^3, jitter +-0.25 cell, per-cube
+velocity N(0, 0.5^2) per axis, dt = 1e-4, E = 1e4, nu = 0.2, gravity = -100, the
+reference's physics (MaterialModel::kJelly).  Seeded synthetic input.
+
+A step is one advance() over all particles.  Lines printed (rank 0, one JSON line):
+  value     particle-steps/s with the state resident in HBM: K steps of advance() on the
+            simulation's stream, CUDA events around them, max over ranks;
+  e2e       the same metric through the C ABI with host buffers: every step uploads the
+            particle state from pinned host memory (nclr_set_particles), advances one step and
+            reads the state back (nclr_get_particles);
+  roofline  the dominant kernel's algorithmic bytes per launch / its average launch time,
+            measured with CUDA events on the simulation's stream inside the timed region;
+  cpu_baseline  the CPU oracle (a restatement of the reference's step, built -Ofast like the
+            reference) on one host core, on a bounded sample of the same workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 (under torchrun): every rank runs its own replica of the scene on its own GPU (the
+step has no cross-scene exchange), value = all ranks' particle-steps / the slowest rank's
+time ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("particle-steps/s 1×GB300 (plain, batched, fwd+adjoint) vs CPU ref; "
+          "%HBM roofline")
+UNIT = "particle-steps/s"
+WORKLOAD = {"workload": "3D jelly (MaterialModel::kJelly), 4 cubes of 64^3 lattice particles",
+            "particles": 1_048_576, "grid": "128^3 (129^3 nodes)", "dim": 3, "dt": 1e-4,
+            "E": 1e4, "nu": 0.2, "gravity": -100.0, "physics": "reference", "seed": 0,
+            "l2": "inputs larger than L2 (particle state ~190 MB in HBM)"}
+
+# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each kernel from
+# one ncu capture of this workload (profiles/ holds the summaries); None until captured.
+NCU_TRAFFIC = {"p2g": None, "g2p": None}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(dim: int, n: int, active: int) -> dict:
+    """Bytes each kernel must move per launch given its interface (every input read once,
+    every output written once), FP32:
+      p2g: reads the per-particle P2G record (x, m, m v, fused affine A: 16 (3D) / 12 (2D)
+           floats) and writes one (m v, m) node per active node;
+      g2p: reads x, F, Jp, mass, volume and one node per active node; writes x, v, F, C, Jp and
+           the next step's P2G record."""
+    d2 = dim * dim
+    rec = 16 if dim == 3 else 12
+    node = 16
+    p2g = n * rec * 4 + active * node
+    g2p = n * (dim + d2 + 3) * 4 + active * node + n * (2 * dim + 2 * d2 + 1) * 4 + n * rec * 4
+    return {"p2g": p2g, "g2p": g2p}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v == "Active"})
+        top = max(r[0] for r in rows)
+        loaded = [r[0] for r in rows if r[0] >= 0.5 * top] or [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_scene():
+    from nuclearmpm_gb300 import scenes
+    return scenes.jelly_cubes_3d(seed=0, res=128)
+
+
+def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float):
+    """The CPU oracle (-Ofast build, one thread) on the workload: `warmup` untimed steps, then
+    `steps` timed steps, on the full scene if that fits `budget_s`, else on the first
+    particles of the scene (same per-particle work) so that it does."""
+    from oracle import pyoracle as po
+    from nuclearmpm_gb300 import scenes
+    n = len(scene["x"])
+    t0 = time.perf_counter()
+    state, _, st, _ = po.advance(scene, dim=3, model=scenes.JELLY, res=128, steps=1, fast=True,
+                                 want_grid=False)
+    one = time.perf_counter() - t0
+    total = max(1, steps + max(warmup - 1, 0))
+    frac = min(1.0, budget_s / max(one * total, 1e-9))
+    m = n if frac >= 1.0 else max(4096, int(n * frac) // 4096 * 4096)
+    sample = {k: (np.asarray(v)[:m] if k in ("x", "v", "F", "C", "Jp", "mass", "volume") else v)
+              for k, v in state.items()}
+    if warmup > 1:
+        sample, _, st, _ = po.advance(sample, dim=3, model=scenes.JELLY, res=128,
+                                      steps=warmup - 1, fast=True, want_grid=False)
+    t0 = time.perf_counter()
+    _, _, st, _ = po.advance(sample, dim=3, model=scenes.JELLY, res=128, steps=steps, fast=True,
+                             want_grid=False)
+    dt = time.perf_counter() - t0
+    if st != 0:
+        raise RuntimeError("CPU oracle reported an out-of-range stencil")
+    desc = (f"{m:,} of {n:,} particles (first cube) x {steps} steps, 128^3 grid"
+            if m < n else f"all {n:,} particles x {steps} steps, 128^3 grid")
+    return m * steps / dt, desc
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    scene = make_scene()
+    value, desc = cpu_reference_run(scene, args.steps, args.warmup, budget_s=150.0)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": dict(WORKLOAD), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": desc + "; the reference's step restated in C++ "
+                             "(oracle/, -Ofast like the reference build), single thread as "
+                             "the reference runs (its OpenMP pragmas are inert)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from nuclearmpm_gb300 import MPMSimulation, scenes
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    scene = make_scene()
+    n = len(scene["x"])
+    sim = MPMSimulation(dict(scene), scenes.JELLY, res=128, device=local, profile=True)
+    stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
+
+    # ---- device-resident throughput ---------------------------------------------------
+    sim.advance(args.warmup)
+    sim.profile_reset()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches_total = 0
+    with ClockSampler(local) as clocks:
+        barrier()
+        start.record(stream)
+        sim.advance(args.steps)
+        stop.record(stream)
+        stop.synchronize()
+        barrier()
+    launches_total += sim.stats()[0]
+    ms = start.elapsed_time(stop)
+    ms_max = max_over_ranks(ms)
+    prof = sim.profile()
+    active = sim.active_nodes()
+    clk = clocks.summary()
+    value = world * n * args.steps / (ms_max / 1e3)
+
+    # ---- roofline of the dominant kernel ------------------------------------------------
+    hbm_peak, peak_kind = peaks()
+    alg = algorithmic_bytes(3, n, active)
+    per_launch = {k: prof[k][0] / max(prof[k][1], 1) for k in ("p2g", "g2p")}
+    dom = max(per_launch, key=per_launch.get)
+    achieved = alg[dom] / (per_launch[dom] / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind,
+                "traffic": NCU_TRAFFIC.get(dom), "algorithmic_bytes": alg[dom],
+                "avg_launch_ms": per_launch[dom],
+                "kernels": {k: {"total_ms": prof[k][0], "launches": prof[k][1],
+                                "avg_ms": prof[k][0] / max(prof[k][1], 1),
+                                "share": prof[k][0] / max(ms, 1e-9)} for k in prof},
+                "active_nodes": active}
+
+    # ---- end to end through the C ABI with host buffers ----------------------------------
+    pin = lambda shape: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+    hx, hv, hF, hC, hJ = pin((n, 3)), pin((n, 3)), pin((n, 3, 3)), pin((n, 3, 3)), pin((n,))
+    hx[:] = scene["x"]; hv[:] = scene["v"]; hF[:] = scene["F"]; hC[:] = scene["C"]; hJ[:] = scene["Jp"]
+    ox, ov, oF, oC, oJ = pin((n, 3)), pin((n, 3)), pin((n, 3, 3)), pin((n, 3, 3)), pin((n,))
+    from nuclearmpm_gb300 import capi
+    from nuclearmpm_gb300.simulation import _ptr
+    L = capi.lib()
+    h = sim._h
+
+    def e2e_step():
+        capi.check(L.nclr_set_particles(h, _ptr(hx), _ptr(hv), _ptr(hF), _ptr(hC), _ptr(hJ)), h)
+        capi.check(L.nclr_advance(h, 1), h)
+        launches = sim.stats()[0]
+        capi.check(L.nclr_get_particles(h, _ptr(ox), _ptr(ov), _ptr(oF), _ptr(oC), _ptr(oJ)), h)
+        return launches
+
+    for _ in range(max(args.warmup, 1)):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        launches_total += e2e_step() + 2  # + the import/prepare and export kernels
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    barrier()
+    row = 4 * (2 * 3 + 2 * 9 + 1)
+    e2e = {"value": world * n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * row,
+           "d2h_bytes_per_step": n * row,
+           "path": "nclr_set_particles (pinned host) + nclr_advance(1) + nclr_get_particles"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, desc = cpu_reference_run(scene, steps=args.cpu_steps, warmup=1, budget_s=20.0)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": desc + "; the reference's step restated in C++ (oracle/, -Ofast like "
+                                "the reference build), one thread"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded scene with the workload's shapes and distributions)",
+                "config": dict(WORKLOAD, parallelism=f"replicas x{world}"),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches_total, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,147 @@
+/*
+ * nclr_gpu.h -- C ABI of the GB300 MLS-MPM step (libnclr_gpu.so).
+ *
+ * The reference exposes its step only as the header-only C++ class template
+ * nclr::MPMSimulation<dim> (src/nclr.h:63-384); it has no FFI of its own.  These entry
+ * points are what a binding of that class needs, one per member it offers:
+ *
+ *   nclr_create          MPMSimulation(particles, model, res, dt, E, nu, gravity)
+ *                          src/nclr.h:74-78 (and Particle<dim>, src/nclr.h:20-48)
+ *   nclr_advance         advance()                    src/nclr.h:80-84
+ *   nclr_get_particles   particles()                  src/nclr.h:86
+ *   nclr_get_grid        grid()                       src/nclr.h:87
+ *   nclr_get_lame        mu_0, lambda_0               src/nclr.h:71-72,77-78
+ *   nclr_destroy         ~MPMSimulation()
+ *   nclr_last_error      (errors: the reference throws std::out_of_range from vector::at,
+ *                          src/nclr.h:163-164,199; here a status code plus a message)
+ *
+ * plus nclr_set_particles (replace the particle state in place, for embedders that edit
+ * particles between steps) and device-pointer variants for callers whose data already
+ * lives on the GPU.  include/nclr.h wraps all of this back into the reference's C++ API.
+ *
+ * Host array layout (particle-major, matrices row-major):
+ *   x[p*dim + d], v[p*dim + d], F[(p*dim + r)*dim + c], C likewise, Jp[p], mass[p],
+ *   volume[p].  Grid: velocity[node*dim + d], mass[node], node = (i*(res+1) + j)*(res+1) + k
+ *   in 3D and i*(res+1) + j in 2D (the reference's index, src/nclr.h:141-142,152).
+ *
+ * Conventions: every call returns an nclr_status; no exception crosses the ABI.  A handle
+ * owns one CUDA stream and its device memory; calls on one handle must not overlap.
+ */
+#ifndef NCLR_GPU_H
+#define NCLR_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nclr_status {
+  NCLR_OK = 0,
+  NCLR_ERR_INVALID = 1,      /* bad argument (null handle, dim not 2/3, res < 1, ...) */
+  NCLR_ERR_OUT_OF_RANGE = 2, /* a particle's stencil left the grid: the reference's
+                                std::out_of_range (src/nclr.h:163-164,199) */
+  NCLR_ERR_CUDA = 3,         /* a CUDA runtime error (message in nclr_last_error) */
+  NCLR_ERR_NO_DEVICE = 4     /* no usable CUDA device */
+} nclr_status;
+
+/* MaterialModel, src/nclr.h:57-61 */
+enum { NCLR_SNOW = 0, NCLR_JELLY = 1, NCLR_LIQUID = 2 };
+
+/* Physics mode.  NCLR_PHYSICS_REFERENCE reproduces the reference bit-for-bit in
+ * semantics, including diag<3>(1) == diag(1,1,0) (src/nclr_math.h:13-19) and the 2D SVD
+ * sign fix being a no-op (src/nclr_math.h:63-71 write out of bounds in 2D).
+ * NCLR_PHYSICS_CORRECTED uses the true identity and applies the 2D sign fix to column 1. */
+enum { NCLR_PHYSICS_REFERENCE = 0, NCLR_PHYSICS_CORRECTED = 1 };
+
+typedef struct nclr_options {
+  int physics;             /* NCLR_PHYSICS_* (default REFERENCE) */
+  int sort_interval;       /* re-sort particles by grid cell every this many steps
+                              (0 = never; default 8) */
+  int p2g_particles_per_thread; /* 4, 8 or 16 (default 8) */
+  int device;              /* CUDA device ordinal (default 0) */
+  int use_graphs;          /* capture advance() step sequences in CUDA graphs (default 1) */
+  int profile;             /* time every kernel phase of advance() with CUDA events on the
+                              handle's stream (direct launches, no graphs; default 0) */
+} nclr_options;
+
+/* Kernel phases reported by nclr_profile_get. */
+enum { NCLR_PHASE_SORT = 0, NCLR_PHASE_CLEAR = 1, NCLR_PHASE_P2G = 2, NCLR_PHASE_G2P = 3,
+       NCLR_NUM_PHASES = 4 };
+
+typedef struct nclr_sim nclr_sim;
+
+/* Fills *opt with the defaults. */
+void nclr_default_options(nclr_options *opt);
+
+/* Creates a simulation of n particles (MPMSimulation ctor, src/nclr.h:74-78).  x, v, F, C,
+ * Jp, mass, volume are HOST arrays in the layout above; v, C may be NULL (zero), F NULL
+ * (diag<dim>(1) of the chosen physics), Jp/mass/volume NULL (1).  material may be NULL
+ * (every particle uses `model`) or hold one NCLR_* value per particle (an extension: the
+ * reference has one material per simulation).  opt may be NULL (defaults). */
+nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
+                        const float *F, const float *C, const float *Jp, const float *mass,
+                        const float *volume, const uint8_t *material, int model, int res,
+                        float dt, float E, float nu, float gravity, const nclr_options *opt);
+
+/* advance() repeated nsteps times (src/nclr.h:80-84).  Returns NCLR_ERR_OUT_OF_RANGE if any
+ * stencil left the grid during these steps (the state is then unspecified, as the
+ * reference's is after its exception).  Synchronises the handle's stream once at the end. */
+nclr_status nclr_advance(nclr_sim *sim, int64_t nsteps);
+
+/* particles() (src/nclr.h:86): copies the state, in the caller's original particle order,
+ * into HOST arrays (any may be NULL to skip that field). */
+nclr_status nclr_get_particles(nclr_sim *sim, float *x, float *v, float *F, float *C, float *Jp);
+
+/* Replaces the particle state (HOST arrays, same layout and NULL rules as nclr_get_particles;
+ * a NULL field keeps its current value).  Particle count and order are the caller's. */
+nclr_status nclr_set_particles(nclr_sim *sim, const float *x, const float *v, const float *F,
+                               const float *C, const float *Jp);
+
+/* grid() (src/nclr.h:87): the post-update grid of the last step, (res+1)^dim nodes, in the
+ * reference's node order.  Before the first advance the reference's grid is empty: returns
+ * NCLR_ERR_INVALID then. */
+nclr_status nclr_get_grid(nclr_sim *sim, float *velocity, float *mass);
+
+/* Device-pointer variants: same layouts, pointers into device memory of the handle's
+ * device.  They are ordered on the handle's stream and return without synchronising. */
+nclr_status nclr_get_particles_device(nclr_sim *sim, float *x, float *v, float *F, float *C,
+                                      float *Jp);
+nclr_status nclr_set_particles_device(nclr_sim *sim, const float *x, const float *v,
+                                      const float *F, const float *C, const float *Jp);
+
+/* Public constants of the simulation (src/nclr.h:66-72). */
+nclr_status nclr_get_lame(const nclr_sim *sim, float *mu_0, float *lambda_0);
+
+/* Sizes: particle count, dimension, grid resolution, grid node count. */
+int64_t nclr_num_particles(const nclr_sim *sim);
+int nclr_dim(const nclr_sim *sim);
+int nclr_res(const nclr_sim *sim);
+int64_t nclr_num_nodes(const nclr_sim *sim);
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own work on it. */
+void *nclr_stream(nclr_sim *sim);
+
+/* Counters of the last nclr_advance call: number of kernel launches it enqueued, and the
+ * number of grid nodes that received mass in its last step (0 if not tracked). */
+nclr_status nclr_stats(const nclr_sim *sim, int64_t *kernel_launches, int64_t *active_nodes);
+
+/* Number of grid nodes holding mass after the last step's P2G (a reduction over the grid). */
+nclr_status nclr_count_active_nodes(nclr_sim *sim, int64_t *active_nodes);
+
+/* With opt.profile set: accumulated device time (ms, CUDA events on the handle's stream) and
+ * launch count of one kernel phase over all advance() calls since the last reset. */
+nclr_status nclr_profile_get(const nclr_sim *sim, int phase, double *total_ms, int64_t *launches);
+nclr_status nclr_profile_reset(nclr_sim *sim);
+
+/* Message of the last failed call on this handle ("" if none); valid until the next call.
+ * With sim == NULL: the last failure of nclr_create on this thread. */
+const char *nclr_last_error(const nclr_sim *sim);
+
+void nclr_destroy(nclr_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NCLR_GPU_H */

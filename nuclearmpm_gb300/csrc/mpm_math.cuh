@@ -1,0 +1,290 @@
+// Register-resident small-matrix math for the MPM step: 2x2/3x3 determinant, products, the
+// reference's polar decomposition (src/nclr_math.h:76-98) and signed SVD (src/nclr_math.h:
+// 50-74).  Everything is plain FP32 on values held in registers; the functions are
+// __host__ __device__ so the same code can be exercised on a CPU.
+//
+// SVD conventions (what the reference's nclr_svd returns after its sign fix):
+//   3D: U, V rotations, sigma_1 >= sigma_2 >= |sigma_3|, sigma_3 carrying sign(det A).
+//   2D: U, V rotations and sigma_2 carrying sign(det A)  (corrected physics), or
+//       U, V possibly reflections and sigma >= 0          (reference physics: its 2D sign
+//       fix writes out of bounds and is a no-op).
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define MPM_HD __host__ __device__ __forceinline__
+#else
+#define MPM_HD inline
+#endif
+
+namespace mpm {
+
+MPM_HD float rsqrt_(float x) {
+#ifdef __CUDA_ARCH__
+  return rsqrtf(x);
+#else
+  return 1.0f / sqrtf(x);
+#endif
+}
+
+template <int D>
+struct Mat {
+  float a[D][D];
+};
+
+template <int D>
+MPM_HD Mat<D> mat_mul(const Mat<D> &x, const Mat<D> &y) {
+  Mat<D> r;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = x.a[i][0] * y.a[0][j];
+#pragma unroll
+      for (int k = 1; k < D; ++k) s = s + x.a[i][k] * y.a[k][j];
+      r.a[i][j] = s;
+    }
+  return r;
+}
+
+// x * y^T
+template <int D>
+MPM_HD Mat<D> mat_mul_t(const Mat<D> &x, const Mat<D> &y) {
+  Mat<D> r;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = x.a[i][0] * y.a[j][0];
+#pragma unroll
+      for (int k = 1; k < D; ++k) s = s + x.a[i][k] * y.a[j][k];
+      r.a[i][j] = s;
+    }
+  return r;
+}
+
+// Determinant by cofactor expansion along the first row.
+MPM_HD float det(const Mat<2> &m) { return m.a[0][0] * m.a[1][1] - m.a[0][1] * m.a[1][0]; }
+MPM_HD float det(const Mat<3> &m) {
+  return m.a[0][0] * (m.a[1][1] * m.a[2][2] - m.a[1][2] * m.a[2][1]) -
+         m.a[0][1] * (m.a[1][0] * m.a[2][2] - m.a[1][2] * m.a[2][0]) +
+         m.a[0][2] * (m.a[1][0] * m.a[2][1] - m.a[1][1] * m.a[2][0]);
+}
+
+// Reference 2D polar rotation (src/nclr_math.h:80-89): closed form.
+MPM_HD Mat<2> polar_rotation(const Mat<2> &m) {
+  const float x = m.a[0][0] + m.a[1][1];
+  const float y = m.a[1][0] - m.a[0][1];
+  const float scale = 1.0f / sqrtf(x * x + y * y);
+  const float c = x * scale, s = y * scale;
+  Mat<2> R;
+  R.a[0][0] = c;
+  R.a[0][1] = -s;
+  R.a[1][0] = s;
+  R.a[1][1] = c;
+  return R;
+}
+
+// 2x2 SVD in closed form.  With E=(a00+a11)/2, F=(a00-a11)/2, G=(a10+a01)/2,
+// H=(a10-a01)/2:  A = rot(phi) diag(Q+R, Q-R) rot(theta), Q = |(E,H)|, R = |(F,G)|,
+// phi = (atan2(H,E) + atan2(G,F))/2, theta = (atan2(H,E) - atan2(G,F))/2.
+// So U = rot(phi), V = rot(theta)^T; sigma_2 = Q - R carries sign(det A).
+template <bool kNonNegative>
+MPM_HD void svd2(const Mat<2> &A, Mat<2> &U, float sig[2], Mat<2> &V) {
+  const float E = 0.5f * (A.a[0][0] + A.a[1][1]);
+  const float F = 0.5f * (A.a[0][0] - A.a[1][1]);
+  const float G = 0.5f * (A.a[1][0] + A.a[0][1]);
+  const float H = 0.5f * (A.a[1][0] - A.a[0][1]);
+  const float Q = sqrtf(E * E + H * H);
+  const float R = sqrtf(F * F + G * G);
+  const float a1 = atan2f(G, F), a2 = atan2f(H, E);
+  const float phi = 0.5f * (a2 + a1), theta = 0.5f * (a2 - a1);
+  float sp, cp, st, ct;
+  sincosf(phi, &sp, &cp);
+  sincosf(theta, &st, &ct);
+  sig[0] = Q + R;
+  sig[1] = Q - R;
+  U.a[0][0] = cp;
+  U.a[0][1] = -sp;
+  U.a[1][0] = sp;
+  U.a[1][1] = cp;
+  // V = rot(theta)^T
+  V.a[0][0] = ct;
+  V.a[0][1] = st;
+  V.a[1][0] = -st;
+  V.a[1][1] = ct;
+  if (kNonNegative && sig[1] < 0.0f) {
+    sig[1] = -sig[1];
+    U.a[0][1] = -U.a[0][1];
+    U.a[1][1] = -U.a[1][1];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// 3x3 SVD following the structure of McAdams, Selle, Tamstorf, Teran, Sifakis, "Computing
+// the Singular Value Decomposition of 3x3 matrices with minimal branching and elementary
+// floating point operations" (UW-Madison TR1690, 2011), with exact Jacobi rotations:
+//   1. cyclic Jacobi eigen-analysis of S = A^T A, V = product of the rotations;
+//   2. B = A V, columns sorted by decreasing norm (one column negated per swap so that V
+//      stays a rotation);
+//   3. Givens QR of B: B = U R, with U a rotation; sigma = diag(R), so sigma_3 carries
+//      sign(det A).
+// ---------------------------------------------------------------------------------------
+namespace detail {
+
+// Conjugate symmetric S (stored full) by the Jacobi rotation in the (p,q) plane that zeroes
+// S_pq (the symmetric Schur rotation of Golub & Van Loan, Alg. 8.4.2, in the numerically
+// stable small-angle form); accumulate it into V (V <- V Q).
+template <int P, int Q>
+MPM_HD void jacobi_rotate(float S[3][3], float V[3][3]) {
+  const float app = S[P][P], aqq = S[Q][Q], apq = S[P][Q];
+  if (apq == 0.0f) return;
+  const float tau = (aqq - app) / (2.0f * apq);
+  const float t = copysignf(1.0f, tau) / (fabsf(tau) + sqrtf(1.0f + tau * tau));
+  const float c = rsqrt_(1.0f + t * t), s = t * c;
+  // S <- Q^T S Q with Q = I except Q_pp = c, Q_pq = s, Q_qp = -s, Q_qq = c
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {  // columns: S Q
+    const float skp = S[k][P], skq = S[k][Q];
+    S[k][P] = c * skp - s * skq;
+    S[k][Q] = s * skp + c * skq;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {  // rows: Q^T (S Q)
+    const float spk = S[P][k], sqk = S[Q][k];
+    S[P][k] = c * spk - s * sqk;
+    S[Q][k] = s * spk + c * sqk;
+  }
+  S[P][Q] = 0.0f;
+  S[Q][P] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float vkp = V[k][P], vkq = V[k][Q];
+    V[k][P] = c * vkp - s * vkq;
+    V[k][Q] = s * vkp + c * vkq;
+  }
+}
+
+// Swap columns i and j of B and V when |b_i| < |b_j|, negating the new column j so V stays
+// a rotation.
+template <int I, int J>
+MPM_HD void cond_swap(float B[3][3], float V[3][3], float rho[3]) {
+  if (rho[I] < rho[J]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float b = B[k][I];
+      B[k][I] = B[k][J];
+      B[k][J] = -b;
+      const float v = V[k][I];
+      V[k][I] = V[k][J];
+      V[k][J] = -v;
+    }
+    const float r = rho[I];
+    rho[I] = rho[J];
+    rho[J] = r;
+  }
+}
+
+// Givens rotation on rows (P,Q) of B zeroing B[Q][COL]; accumulates U <- U G.
+template <int P, int Q, int COL>
+MPM_HD void qr_givens(float B[3][3], float U[3][3]) {
+  const float a1 = B[P][COL], a2 = B[Q][COL];
+  const float n2 = a1 * a1 + a2 * a2;
+  float c = 1.0f, s = 0.0f;
+  if (n2 > 1e-38f) {
+    const float inv = rsqrt_(n2);
+    c = a1 * inv;
+    s = a2 * inv;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {  // rows: G^T B with G = [[c,-s],[s,c]] in (P,Q)
+    const float bp = B[P][k], bq = B[Q][k];
+    B[P][k] = c * bp + s * bq;
+    B[Q][k] = -s * bp + c * bq;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {  // U <- U G
+    const float up = U[k][P], uq = U[k][Q];
+    U[k][P] = c * up + s * uq;
+    U[k][Q] = -s * up + c * uq;
+  }
+}
+
+}  // namespace detail
+
+constexpr int kJacobiSweeps = 4;
+
+MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
+  using namespace detail;
+  float S[3][3], V[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
+      V[i][j] = (i == j) ? 1.0f : 0.0f;
+    }
+#pragma unroll
+  for (int sweep = 0; sweep < kJacobiSweeps; ++sweep) {
+    jacobi_rotate<0, 1>(S, V);
+    jacobi_rotate<1, 2>(S, V);
+    jacobi_rotate<0, 2>(S, V);
+  }
+  float B[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) B[i][j] = A.a[i][0] * V[0][j] + A.a[i][1] * V[1][j] + A.a[i][2] * V[2][j];
+  float rho[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) rho[j] = B[0][j] * B[0][j] + B[1][j] * B[1][j] + B[2][j] * B[2][j];
+  cond_swap<0, 1>(B, V, rho);
+  cond_swap<0, 2>(B, V, rho);
+  cond_swap<1, 2>(B, V, rho);
+  float U[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+  qr_givens<0, 1, 0>(B, U);
+  qr_givens<0, 2, 0>(B, U);
+  qr_givens<1, 2, 1>(B, U);
+  sig[0] = B[0][0];
+  sig[1] = B[1][1];
+  sig[2] = B[2][2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      Uo.a[i][j] = U[i][j];
+      Vo.a[i][j] = V[i][j];
+    }
+}
+
+// U diag(s) V^T
+template <int D>
+MPM_HD Mat<D> usv(const Mat<D> &U, const float s[D], const Mat<D> &V) {
+  Mat<D> US;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) US.a[i][j] = U.a[i][j] * s[j];
+  return mat_mul_t<D>(US, V);
+}
+
+// U V^T
+template <int D>
+MPM_HD Mat<D> uvt(const Mat<D> &U, const Mat<D> &V) {
+  return mat_mul_t<D>(U, V);
+}
+
+// Rotation part of the reference's nclr_polar: 2D closed form, 3D U V^T of the signed SVD.
+MPM_HD Mat<2> polar_R(const Mat<2> &F) { return polar_rotation(F); }
+MPM_HD Mat<3> polar_R(const Mat<3> &F) {
+  Mat<3> U, V;
+  float s[3];
+  svd3(F, U, s, V);
+  return uvt<3>(U, V);
+}
+
+MPM_HD float clampf_(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+}  // namespace mpm

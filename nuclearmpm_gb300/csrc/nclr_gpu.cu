@@ -1,0 +1,628 @@
+// Host side of the C ABI in include/nclr_gpu.h: one simulation handle = one CUDA stream, the
+// device-resident particle store (two SoA buffers that the cell sort ping-pongs between),
+// the P2G payload, the dense grid and the sort scratch.  advance() enqueues
+//   [every sort_interval steps: cell keys -> scan -> move]  zero grid -> P2G -> G2P
+// per step, replaying a captured CUDA graph for whole sort intervals.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "mpm_device.cuh"
+#include "mpm_launch.h"
+#include "nclr_gpu.h"
+
+using mpm::Params;
+using mpm::PState;
+
+struct nclr_sim {
+  int dim = 0, res = 0, device = 0;
+  int64_t n = 0;
+  nclr_options opt{};
+  Params P{};
+  bool ref = true;
+  bool has_mat = false;
+  cudaStream_t stream = nullptr;
+
+  void *slab[2] = {nullptr, nullptr};  // particle SoA buffers
+  PState ps[2]{};
+  float4 *pay[2] = {nullptr, nullptr};
+  int cur = 0;
+
+  float4 *grid = nullptr;
+  int *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *tile_sums = nullptr;
+  int *err_d = nullptr;
+  int *err_h = nullptr;  // pinned
+
+  float *staging = nullptr;       // particle-major transfer buffer (n * row floats)
+  float *grid_staging = nullptr;  // grid export buffer (nodes * (dim + 1) floats)
+
+  bool stepped = false;  // grid() is empty until the first advance (src/nclr.h:101)
+  int64_t steps_since_sort = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int64_t graph_steps = 0;
+  int64_t graph_launches = 0;
+  int64_t launches = 0;
+  int64_t active_nodes = 0;
+  unsigned long long *active_d = nullptr;
+
+  // opt.profile: event pairs of the current advance() call, folded into per-phase totals
+  std::vector<cudaEvent_t> ev_pool;
+  struct Timed {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<Timed> pending;
+  double prof_ms[NCLR_NUM_PHASES] = {};
+  int64_t prof_launches[NCLR_NUM_PHASES] = {};
+  std::string error;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int row_floats(int dim) { return 2 * dim + 2 * dim * dim + 1; }  // x, v, F, C, Jp
+
+nclr_status fail(nclr_sim *s, nclr_status st, const std::string &msg) {
+  if (s)
+    s->error = msg;
+  else
+    g_create_error = msg;
+  return st;
+}
+
+#define CUDA_TRY(sim, call)                                                                \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail((sim), NCLR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Carves the SoA fields of one particle buffer out of a single allocation.
+nclr_status alloc_particles(nclr_sim *s, int which) {
+  const int D = s->dim;
+  const size_t n = (size_t)std::max<int64_t>(s->n, 1);
+  const size_t fbytes = align_up(n * sizeof(float), 256);
+  const int nfloat_fields = 2 * D + 2 * D * D + 3;
+  size_t total = fbytes * nfloat_fields + align_up(n * sizeof(int), 256) + align_up(n, 256);
+  char *base = nullptr;
+  CUDA_TRY(s, cudaMalloc((void **)&base, total));
+  s->slab[which] = base;
+  PState &p = s->ps[which];
+  size_t off = 0;
+  auto take = [&](size_t comps) {
+    float *r = (float *)(base + off);
+    off += fbytes * comps;
+    return r;
+  };
+  p.x = take(D);
+  p.v = take(D);
+  p.F = take((size_t)D * D);
+  p.C = take((size_t)D * D);
+  p.Jp = take(1);
+  p.mass = take(1);
+  p.vol = take(1);
+  p.id = (int *)(base + off);
+  off += align_up(n * sizeof(int), 256);
+  p.mat = s->has_mat ? (uint8_t *)(base + off) : nullptr;
+  p.stride = (int)n;
+  return NCLR_OK;
+}
+
+template <typename F>
+void dispatch_dim(int dim, F &&f) {
+  if (dim == 2)
+    f(std::integral_constant<int, 2>{});
+  else
+    f(std::integral_constant<int, 3>{});
+}
+
+nclr_status check_launch(nclr_sim *s, const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return NCLR_OK;
+}
+
+cudaEvent_t take_event(nclr_sim *s) {
+  if (s->ev_pool.empty()) {
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  cudaEvent_t e = s->ev_pool.back();
+  s->ev_pool.pop_back();
+  return e;
+}
+
+// Brackets the work enqueued by `body` with a pair of events when profiling.
+template <typename Body>
+void phase(nclr_sim *s, int which, int launches, Body &&body) {
+  if (!s->opt.profile) {
+    body();
+    return;
+  }
+  nclr_sim::Timed t{which, take_event(s), take_event(s)};
+  cudaEventRecord(t.a, s->stream);
+  body();
+  cudaEventRecord(t.b, s->stream);
+  s->pending.push_back(t);
+  s->prof_launches[which] += launches;
+}
+
+// After the stream has drained: fold the pending event pairs into the phase totals.
+void collect_profile(nclr_sim *s) {
+  for (const auto &t : s->pending) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) s->prof_ms[t.phase] += ms;
+    s->ev_pool.push_back(t.a);
+    s->ev_pool.push_back(t.b);
+  }
+  s->pending.clear();
+}
+
+// Enqueues one step (optionally preceded by the cell sort) on the handle's stream.
+void enqueue_step(nclr_sim *s, bool sort) {
+  const int64_t nodes = s->P.nodes;
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int D = decltype(dc)::value;
+    if (sort && s->n > 1) {
+      phase(s, NCLR_PHASE_SORT, 5, [&] {
+        cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)nodes, s->stream);
+        mpm::launch_sort_keys<D>(s->ps[s->cur], s->P, s->key, s->rank, s->count, s->stream);
+        mpm::launch_exclusive_scan(s->count, nodes, s->start, s->tile_sums, s->stream);
+        mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->pay[s->cur],
+                                 s->pay[s->cur ^ 1], s->key, s->rank, s->start, s->stream);
+      });
+      s->cur ^= 1;
+      s->launches += 5;  // keys, 3 scan kernels, move
+    }
+    phase(s, NCLR_PHASE_CLEAR, 0, [&] {
+      cudaMemsetAsync(s->grid, 0, sizeof(float4) * (size_t)nodes, s->stream);
+    });
+    if (s->n > 0) {
+      phase(s, NCLR_PHASE_P2G, 1, [&] {
+        mpm::launch_p2g<D>(s->pay[s->cur], s->P, s->grid, s->err_d,
+                           s->opt.p2g_particles_per_thread, s->stream);
+      });
+      phase(s, NCLR_PHASE_G2P, 1, [&] {
+        mpm::launch_g2p<D>(s->ps[s->cur], s->P, s->grid, s->pay[s->cur], s->err_d, s->ref,
+                           s->stream);
+      });
+      s->launches += 2;
+    }
+  });
+}
+
+bool sort_due(const nclr_sim *s) {
+  return s->opt.sort_interval > 0 && s->steps_since_sort % s->opt.sort_interval == 0;
+}
+
+int64_t chunk_steps(const nclr_sim *s) { return s->opt.sort_interval > 0 ? s->opt.sort_interval : 16; }
+
+// Captures chunk_steps() steps starting at a sort boundary from buffer parity s->cur.
+nclr_status capture_graph(nclr_sim *s, int parity) {
+  const int saved_cur = s->cur;
+  const int64_t saved_launches = s->launches;
+  s->cur = parity;
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  const int64_t k = chunk_steps(s);
+  for (int64_t i = 0; i < k; ++i) enqueue_step(s, s->opt.sort_interval > 0 && i == 0);
+  cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  s->graph_launches = s->launches - saved_launches;
+  s->launches = saved_launches;
+  s->cur = saved_cur;
+  if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&s->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  s->graph_steps = k;
+  return NCLR_OK;
+}
+
+void fill_params(nclr_sim *s, int model, float dt, float E, float nu, float gravity) {
+  Params &P = s->P;
+  P.res = s->res;
+  P.N = s->res + 1;
+  P.n = (int)s->n;
+  P.model = model;
+  P.dt = dt;
+  // dx = 1.0 / res in double, narrowed (src/nclr.h:76); inv_dx = 1 / dx in float
+  P.dx = (float)(1.0 / s->res);
+  P.inv_dx = 1.0f / P.dx;
+  P.gravity = gravity;
+  P.allowed = (float)((double)P.dx * 0.9 / (double)dt);  // src/nclr.h:285
+  // mu_0, lambda_0 (src/nclr.h:77-78), evaluated in float like the reference's `real`
+  P.mu0 = E / (2.0f * (1.0f + nu));
+  P.lambda0 = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+  P.Dinv = 4.0f * P.inv_dx * P.inv_dx;
+  P.cscale = 4.0f * P.inv_dx;
+  P.dt_gravity = dt * gravity;
+  int64_t nodes = 1;
+  for (int d = 0; d < s->dim; ++d) nodes *= P.N;
+  P.nodes = nodes;
+}
+
+// Upload of caller-ordered rows that already sit in device memory, then the P2G payload.
+nclr_status import_rows(nclr_sim *s, const float *x, const float *v, const float *F,
+                        const float *C, const float *Jp) {
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int D = decltype(dc)::value;
+    mpm::launch_import_particles<D>(s->ps[s->cur], (int)s->n, x, v, F, C, Jp, s->stream);
+    mpm::launch_prepare<D>(s->ps[s->cur], s->P, s->pay[s->cur], s->ref, s->stream);
+  });
+  return check_launch(s, "import particles");
+}
+
+nclr_status ensure_staging(nclr_sim *s) {
+  if (!s->staging && s->n > 0)
+    CUDA_TRY(s, cudaMalloc((void **)&s->staging, sizeof(float) * (size_t)s->n * row_floats(s->dim)));
+  return NCLR_OK;
+}
+
+struct Rows {
+  float *x, *v, *F, *C, *Jp;
+};
+Rows staging_rows(nclr_sim *s) {
+  const size_t n = (size_t)s->n;
+  const int D = s->dim;
+  Rows r;
+  r.x = s->staging;
+  r.v = r.x + n * D;
+  r.F = r.v + n * D;
+  r.C = r.F + n * D * D;
+  r.Jp = r.C + n * D * D;
+  return r;
+}
+
+void release(nclr_sim *s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (auto &g : s->graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto p : s->slab) cudaFree(p);
+  for (auto p : s->pay) cudaFree(p);
+  cudaFree(s->grid);
+  cudaFree(s->key);
+  cudaFree(s->rank);
+  cudaFree(s->count);
+  cudaFree(s->start);
+  cudaFree(s->tile_sums);
+  cudaFree(s->err_d);
+  cudaFree(s->staging);
+  cudaFree(s->grid_staging);
+  cudaFree(s->active_d);
+  for (const auto &t : s->pending) {
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
+  for (auto e : s->ev_pool) cudaEventDestroy(e);
+  if (s->err_h) cudaFreeHost(s->err_h);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nclr_default_options(nclr_options *opt) {
+  if (!opt) return;
+  opt->physics = NCLR_PHYSICS_REFERENCE;
+  opt->sort_interval = 8;
+  opt->p2g_particles_per_thread = 8;
+  opt->device = 0;
+  opt->use_graphs = 1;
+  opt->profile = 0;
+}
+
+nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
+                        const float *F, const float *C, const float *Jp, const float *mass,
+                        const float *volume, const uint8_t *material, int model, int res,
+                        float dt, float E, float nu, float gravity, const nclr_options *opt) {
+  g_create_error.clear();
+  if (!out) return fail(nullptr, NCLR_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (dim != 2 && dim != 3) return fail(nullptr, NCLR_ERR_INVALID, "dim must be 2 or 3");
+  if (n < 0 || n > (int64_t)0x7fffffff / 2) return fail(nullptr, NCLR_ERR_INVALID, "bad particle count");
+  if (n > 0 && !x) return fail(nullptr, NCLR_ERR_INVALID, "x is NULL");
+  if (res < 1 || res > 1024) return fail(nullptr, NCLR_ERR_INVALID, "res must be in [1, 1024]");
+  if (model < 0 || model > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material model");
+  if (material)
+    for (int64_t p = 0; p < n; ++p)
+      if (material[p] > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material in material[]");
+
+  nclr_sim *s = new (std::nothrow) nclr_sim();
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "out of host memory");
+  nclr_default_options(&s->opt);
+  if (opt) s->opt = *opt;
+  if (s->opt.p2g_particles_per_thread != 4 && s->opt.p2g_particles_per_thread != 16)
+    s->opt.p2g_particles_per_thread = 8;
+  if (s->opt.sort_interval < 0) s->opt.sort_interval = 0;
+  s->dim = dim;
+  s->n = n;
+  s->res = res;
+  s->device = s->opt.device;
+  s->ref = s->opt.physics != NCLR_PHYSICS_CORRECTED;
+  s->has_mat = material != nullptr;
+
+  auto bail = [&](nclr_status st) {
+    g_create_error = s->error;
+    release(s);
+    return st;
+  };
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    s->error = "no CUDA device";
+    return bail(NCLR_ERR_NO_DEVICE);
+  }
+  if (s->device < 0 || s->device >= ndev) {
+    s->error = "device ordinal out of range";
+    return bail(NCLR_ERR_INVALID);
+  }
+  nclr_status st;
+#define CREATE_TRY(call)                                                   \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) {                                               \
+      s->error = std::string(#call) + ": " + cudaGetErrorString(e_);       \
+      return bail(NCLR_ERR_CUDA);                                          \
+    }                                                                      \
+  } while (0)
+  CREATE_TRY(cudaSetDevice(s->device));
+  CREATE_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  fill_params(s, model, dt, E, nu, gravity);
+  const int64_t nodes = s->P.nodes;
+  for (int b = 0; b < 2; ++b)
+    if ((st = alloc_particles(s, b)) != NCLR_OK) return bail(st);
+  const int R = (dim == 3) ? 4 : 3;
+  const size_t np = (size_t)std::max<int64_t>(n, 1);
+  for (int b = 0; b < 2; ++b) CREATE_TRY(cudaMalloc((void **)&s->pay[b], sizeof(float4) * R * np));
+  CREATE_TRY(cudaMalloc((void **)&s->grid, sizeof(float4) * (size_t)nodes));
+  CREATE_TRY(cudaMalloc((void **)&s->key, sizeof(int) * np));
+  CREATE_TRY(cudaMalloc((void **)&s->rank, sizeof(int) * np));
+  CREATE_TRY(cudaMalloc((void **)&s->count, sizeof(int) * (size_t)nodes));
+  CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (size_t)(nodes + 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles(nodes), 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->err_d, sizeof(int)));
+  CREATE_TRY(cudaMallocHost((void **)&s->err_h, sizeof(int)));
+  CREATE_TRY(cudaMemsetAsync(s->err_d, 0, sizeof(int), s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->grid, 0, sizeof(float4) * (size_t)nodes, s->stream));
+
+  if (n > 0) {
+    // Per-particle scalars go straight into the SoA (component stride == n there).
+    PState &p = s->ps[0];
+    std::vector<float> ones((size_t)n, 1.0f);
+    std::vector<int> iota((size_t)n);
+    for (int64_t i = 0; i < n; ++i) iota[(size_t)i] = (int)i;
+    CREATE_TRY(cudaMemcpyAsync(p.mass, mass ? mass : ones.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+    CREATE_TRY(cudaMemcpyAsync(p.vol, volume ? volume : ones.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+    CREATE_TRY(cudaMemcpyAsync(p.id, iota.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+    if (material) CREATE_TRY(cudaMemcpyAsync(p.mat, material, (size_t)n, cudaMemcpyHostToDevice, s->stream));
+
+    // Rows: x, v, F, C, Jp with the constructor's defaults for the NULL ones
+    // (Particle<dim>: v = 0, F = diag<dim>(1), C = 0, Jp = 1; src/nclr.h:46-47).
+    if ((st = ensure_staging(s)) != NCLR_OK) return bail(st);
+    const Rows r = staging_rows(s);
+    std::vector<float> host((size_t)n * row_floats(dim), 0.0f);
+    float *hx = host.data(), *hv = hx + n * dim, *hF = hv + n * dim, *hC = hF + n * dim * dim,
+          *hJ = hC + n * dim * dim;
+    std::memcpy(hx, x, sizeof(float) * n * dim);
+    if (v) std::memcpy(hv, v, sizeof(float) * n * dim);
+    if (F) {
+      std::memcpy(hF, F, sizeof(float) * n * dim * dim);
+    } else {
+      for (int64_t q = 0; q < n; ++q)
+        for (int d = 0; d < dim; ++d)
+          hF[(q * dim + d) * dim + d] = (d < 2 || !s->ref) ? 1.0f : 0.0f;
+    }
+    if (C) std::memcpy(hC, C, sizeof(float) * n * dim * dim);
+    if (Jp) {
+      std::memcpy(hJ, Jp, sizeof(float) * n);
+    } else {
+      for (int64_t q = 0; q < n; ++q) hJ[q] = 1.0f;
+    }
+    CREATE_TRY(cudaMemcpyAsync(r.x, host.data(), sizeof(float) * host.size(), cudaMemcpyHostToDevice, s->stream));
+    if ((st = import_rows(s, r.x, r.v, r.F, r.C, r.Jp)) != NCLR_OK) return bail(st);
+    CREATE_TRY(cudaStreamSynchronize(s->stream));  // `host` goes out of scope
+  }
+  CREATE_TRY(cudaStreamSynchronize(s->stream));
+#undef CREATE_TRY
+  *out = s;
+  return NCLR_OK;
+}
+
+nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  if (nsteps < 0) return fail(s, NCLR_ERR_INVALID, "nsteps < 0");
+  if (nsteps == 0) return NCLR_OK;
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  CUDA_TRY(s, cudaMemsetAsync(s->err_d, 0, sizeof(int), s->stream));
+  s->launches = 0;
+  int64_t left = nsteps;
+  const int64_t chunk = chunk_steps(s);
+  while (left > 0) {
+    const bool at_boundary = s->opt.sort_interval == 0 || sort_due(s);
+    if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left >= chunk) {
+      if (!s->graph[s->cur]) {
+        nclr_status st = capture_graph(s, s->cur);
+        if (st != NCLR_OK) return st;
+      }
+      CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur], s->stream));
+      s->launches += s->graph_launches;
+      if (s->opt.sort_interval > 0 && s->n > 1) s->cur ^= 1;
+      s->steps_since_sort += chunk;
+      left -= chunk;
+      continue;
+    }
+    enqueue_step(s, sort_due(s));
+    ++s->steps_since_sort;
+    --left;
+  }
+  nclr_status st = check_launch(s, "advance");
+  if (st != NCLR_OK) return st;
+  s->stepped = true;
+  CUDA_TRY(s, cudaMemcpyAsync(s->err_h, s->err_d, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  collect_profile(s);
+  if (*s->err_h & mpm::kErrOutOfRange)
+    return fail(s, NCLR_ERR_OUT_OF_RANGE,
+                "a particle's stencil left the grid (the reference's vector::at throws "
+                "std::out_of_range here)");
+  return NCLR_OK;
+}
+
+nclr_status nclr_get_particles_device(nclr_sim *s, float *x, float *v, float *F, float *C,
+                                      float *Jp) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int D = decltype(dc)::value;
+    mpm::launch_export_particles<D>(s->ps[s->cur], (int)s->n, x, v, F, C, Jp, s->stream);
+  });
+  return check_launch(s, "export particles");
+}
+
+nclr_status nclr_set_particles_device(nclr_sim *s, const float *x, const float *v,
+                                      const float *F, const float *C, const float *Jp) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  if (s->n == 0) return NCLR_OK;
+  return import_rows(s, x, v, F, C, Jp);
+}
+
+nclr_status nclr_get_particles(nclr_sim *s, float *x, float *v, float *F, float *C, float *Jp) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  if (s->n == 0) return NCLR_OK;
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  nclr_status st = ensure_staging(s);
+  if (st != NCLR_OK) return st;
+  const Rows r = staging_rows(s);
+  st = nclr_get_particles_device(s, x ? r.x : nullptr, v ? r.v : nullptr, F ? r.F : nullptr,
+                                 C ? r.C : nullptr, Jp ? r.Jp : nullptr);
+  if (st != NCLR_OK) return st;
+  const size_t n = (size_t)s->n, D = (size_t)s->dim;
+  if (x) CUDA_TRY(s, cudaMemcpyAsync(x, r.x, sizeof(float) * n * D, cudaMemcpyDeviceToHost, s->stream));
+  if (v) CUDA_TRY(s, cudaMemcpyAsync(v, r.v, sizeof(float) * n * D, cudaMemcpyDeviceToHost, s->stream));
+  if (F) CUDA_TRY(s, cudaMemcpyAsync(F, r.F, sizeof(float) * n * D * D, cudaMemcpyDeviceToHost, s->stream));
+  if (C) CUDA_TRY(s, cudaMemcpyAsync(C, r.C, sizeof(float) * n * D * D, cudaMemcpyDeviceToHost, s->stream));
+  if (Jp) CUDA_TRY(s, cudaMemcpyAsync(Jp, r.Jp, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return NCLR_OK;
+}
+
+nclr_status nclr_set_particles(nclr_sim *s, const float *x, const float *v, const float *F,
+                               const float *C, const float *Jp) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  if (s->n == 0) return NCLR_OK;
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  nclr_status st = ensure_staging(s);
+  if (st != NCLR_OK) return st;
+  const Rows r = staging_rows(s);
+  const size_t n = (size_t)s->n, D = (size_t)s->dim;
+  if (x) CUDA_TRY(s, cudaMemcpyAsync(r.x, x, sizeof(float) * n * D, cudaMemcpyHostToDevice, s->stream));
+  if (v) CUDA_TRY(s, cudaMemcpyAsync(r.v, v, sizeof(float) * n * D, cudaMemcpyHostToDevice, s->stream));
+  if (F) CUDA_TRY(s, cudaMemcpyAsync(r.F, F, sizeof(float) * n * D * D, cudaMemcpyHostToDevice, s->stream));
+  if (C) CUDA_TRY(s, cudaMemcpyAsync(r.C, C, sizeof(float) * n * D * D, cudaMemcpyHostToDevice, s->stream));
+  if (Jp) CUDA_TRY(s, cudaMemcpyAsync(r.Jp, Jp, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+  st = import_rows(s, x ? r.x : nullptr, v ? r.v : nullptr, F ? r.F : nullptr, C ? r.C : nullptr,
+                   Jp ? r.Jp : nullptr);
+  if (st != NCLR_OK) return st;
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers
+  return NCLR_OK;
+}
+
+nclr_status nclr_get_grid(nclr_sim *s, float *velocity, float *mass) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  if (!s->stepped) return fail(s, NCLR_ERR_INVALID, "grid() is empty before the first advance()");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  const size_t nodes = (size_t)s->P.nodes, D = (size_t)s->dim;
+  if (!s->grid_staging)
+    CUDA_TRY(s, cudaMalloc((void **)&s->grid_staging, sizeof(float) * nodes * (D + 1)));
+  float *dv = s->grid_staging, *dm = dv + nodes * D;
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    mpm::launch_export_grid<DD>(s->grid, s->P, dv, dm, s->stream);
+  });
+  nclr_status st = check_launch(s, "export grid");
+  if (st != NCLR_OK) return st;
+  if (velocity) CUDA_TRY(s, cudaMemcpyAsync(velocity, dv, sizeof(float) * nodes * D, cudaMemcpyDeviceToHost, s->stream));
+  if (mass) CUDA_TRY(s, cudaMemcpyAsync(mass, dm, sizeof(float) * nodes, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return NCLR_OK;
+}
+
+nclr_status nclr_get_lame(const nclr_sim *s, float *mu_0, float *lambda_0) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  if (mu_0) *mu_0 = s->P.mu0;
+  if (lambda_0) *lambda_0 = s->P.lambda0;
+  return NCLR_OK;
+}
+
+int64_t nclr_num_particles(const nclr_sim *s) { return s ? s->n : -1; }
+int nclr_dim(const nclr_sim *s) { return s ? s->dim : -1; }
+int nclr_res(const nclr_sim *s) { return s ? s->res : -1; }
+int64_t nclr_num_nodes(const nclr_sim *s) { return s ? s->P.nodes : -1; }
+void *nclr_stream(nclr_sim *s) { return s ? (void *)s->stream : nullptr; }
+
+nclr_status nclr_stats(const nclr_sim *s, int64_t *kernel_launches, int64_t *active_nodes) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  if (kernel_launches) *kernel_launches = s->launches;
+  if (active_nodes) *active_nodes = s->active_nodes;
+  return NCLR_OK;
+}
+
+nclr_status nclr_count_active_nodes(nclr_sim *s, int64_t *active_nodes) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  if (!s->active_d) CUDA_TRY(s, cudaMalloc((void **)&s->active_d, sizeof(unsigned long long)));
+  CUDA_TRY(s, cudaMemsetAsync(s->active_d, 0, sizeof(unsigned long long), s->stream));
+  mpm::launch_count_active(s->grid, s->P.nodes, s->active_d, s->stream);
+  nclr_status st = check_launch(s, "count active nodes");
+  if (st != NCLR_OK) return st;
+  unsigned long long h = 0;
+  CUDA_TRY(s, cudaMemcpyAsync(&h, s->active_d, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  s->active_nodes = (int64_t)h;
+  if (active_nodes) *active_nodes = s->active_nodes;
+  return NCLR_OK;
+}
+
+nclr_status nclr_profile_get(const nclr_sim *s, int which, double *total_ms, int64_t *launches) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  if (which < 0 || which >= NCLR_NUM_PHASES) return NCLR_ERR_INVALID;
+  if (total_ms) *total_ms = s->prof_ms[which];
+  if (launches) *launches = s->prof_launches[which];
+  return NCLR_OK;
+}
+
+nclr_status nclr_profile_reset(nclr_sim *s) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  for (int i = 0; i < NCLR_NUM_PHASES; ++i) {
+    s->prof_ms[i] = 0.0;
+    s->prof_launches[i] = 0;
+  }
+  return NCLR_OK;
+}
+
+const char *nclr_last_error(const nclr_sim *s) {
+  return s ? s->error.c_str() : g_create_error.c_str();
+}
+
+void nclr_destroy(nclr_sim *s) { release(s); }
+
+}  // extern "C"

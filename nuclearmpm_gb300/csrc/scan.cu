@@ -1,0 +1,123 @@
+// Exclusive prefix sum over the per-cell particle counts of the counting sort:
+// (1) per-tile totals, (2) one block scans the tile totals, (3) each tile scans its counts
+// and adds its tile offset.  Tiles are 2048 counts (256 threads x 8), read as int4 pairs
+// where aligned.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpm_launch.h"
+
+namespace mpm {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 8;
+constexpr int kTile = kThreads * kItems;
+
+__device__ __forceinline__ int warp_inclusive(int v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) >= o) v += u;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total in *total.
+__device__ __forceinline__ int block_exclusive(int v, int *total) {
+  __shared__ int warp_sums[kThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int inc = warp_inclusive(v);
+  if (lane == 31) warp_sums[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int s = (lane < kThreads / 32) ? warp_sums[lane] : 0;
+    s = warp_inclusive(s);
+    if (lane < kThreads / 32) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  const int before = (wid > 0) ? warp_sums[wid - 1] : 0;
+  *total = warp_sums[kThreads / 32 - 1];
+  __syncthreads();
+  return before + inc - v;
+}
+
+__global__ void __launch_bounds__(kThreads) tile_totals(const int *__restrict__ count, int64_t n,
+                                                        int *__restrict__ tile_sums) {
+  const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < kItems; ++i)
+    if (base + i < n) s += count[base + i];
+  int total;
+  block_exclusive(s, &total);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kThreads) scan_totals(int *__restrict__ tile_sums, int64_t ntiles,
+                                                        int *__restrict__ grand_total) {
+  int carry = 0;
+  for (int64_t b = 0; b < ntiles; b += kThreads) {
+    const int64_t i = b + threadIdx.x;
+    const int v = (i < ntiles) ? tile_sums[i] : 0;
+    int total;
+    const int ex = block_exclusive(v, &total);
+    if (i < ntiles) tile_sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) *grand_total = carry;
+}
+
+__global__ void __launch_bounds__(kThreads) tile_apply(const int *__restrict__ count, int64_t n,
+                                                       const int *__restrict__ tile_sums,
+                                                       int *__restrict__ start) {
+  const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
+  int v[kItems];
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) {
+    v[i] = (base + i < n) ? count[base + i] : 0;
+    s += v[i];
+  }
+  int total;
+  int run = block_exclusive(s, &total) + tile_sums[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kItems; ++i) {
+    if (base + i < n) start[base + i] = run;
+    run += v[i];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) count_active_kernel(const float4 *__restrict__ grid,
+                                                               int64_t nodes,
+                                                               unsigned long long *out) {
+  unsigned c = 0;
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < nodes;
+       i += (int64_t)gridDim.x * kThreads)
+    c += grid[i].w > 0.0f ? 1u : 0u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
+}
+
+}  // namespace
+
+void launch_count_active(const float4 *grid, int64_t nodes, unsigned long long *out, cudaStream_t st) {
+  if (nodes <= 0) return;
+  int64_t blocks = (nodes + kThreads - 1) / kThreads;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  count_active_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(grid, nodes, out);
+}
+
+int64_t scan_tiles(int64_t n) { return (n + kTile - 1) / kTile; }
+
+void launch_exclusive_scan(const int *count, int64_t n, int *start, int *tile_sums, cudaStream_t st) {
+  const int64_t nt = scan_tiles(n);
+  if (nt == 0) return;
+  tile_totals<<<(unsigned)nt, kThreads, 0, st>>>(count, n, tile_sums);
+  scan_totals<<<1, kThreads, 0, st>>>(tile_sums, nt, start + n);
+  tile_apply<<<(unsigned)nt, kThreads, 0, st>>>(count, n, tile_sums, start);
+}
+
+}  // namespace mpm

@@ -1,0 +1,251 @@
+"""Python mirror of the reference's solver API (src/nclr.h:20-102) over libnclr_gpu.so.
+
+    Particle(x, c, v=None, mass=1.0, volume=1.0)           src/nclr.h:20-48
+    Cell                                                   src/nclr.h:50-55
+    MaterialModel.kSnow / kJelly / kLiquid                 src/nclr.h:57-61
+    MPMSimulation(particles, model, res=64, dt=1e-4, E=1e4, nu=0.2, gravity=-100)
+        .advance()           src/nclr.h:80-84
+        .particles()         src/nclr.h:86   (ParticleArrays: SoA numpy views, caller order)
+        .grid()              src/nclr.h:87   (GridArrays: post-update grid of the last step;
+                                              empty before the first advance, as in the
+                                              reference)
+        .mu_0, .lambda_0, kBoundary, kSnowHardening, kJellyHardening, kLiquidHardening
+
+`particles` may be a list of Particle objects (as the reference takes a
+std::vector<Particle<dim>>) or, for large scenes, a dict of arrays in the C ABI host layout
+(x (n,dim), v, F (n,dim,dim), C, Jp, mass, volume).  Errors: a stencil that leaves the grid
+raises OutOfRange (an IndexError, like the reference's std::out_of_range); CUDA failures
+raise NclrError.  All compute runs in libnclr_gpu.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+
+
+class MaterialModel(enum.IntEnum):
+    kSnow = 0
+    kJelly = 1
+    kLiquid = 2
+
+
+def diag(dim: int, value: float, corrected: bool = False) -> np.ndarray:
+    """diag<dim>(v) (src/nclr_math.h:13-19): only (0,0) and (1,1) are set, so diag<3> is
+    diag(v, v, 0); `corrected=True` gives v*I."""
+    m = np.zeros((dim, dim), dtype=np.float32)
+    m[0, 0] = m[1, 1] = value
+    if corrected:
+        np.fill_diagonal(m, value)
+    return m
+
+
+@dataclass
+class Particle:
+    """Particle<dim> (src/nclr.h:20-48): F starts at diag<dim>(1), C at 0, Jp at 1."""
+    x: np.ndarray
+    c: int = 0
+    v: np.ndarray | None = None
+    mass: float = 1.0
+    volume: float = 1.0
+    F: np.ndarray | None = None
+    C: np.ndarray | None = None
+    Jp: float = 1.0
+
+    def __post_init__(self):
+        self.x = np.asarray(self.x, dtype=np.float32).copy()
+        dim = self.x.shape[0]
+        self.v = np.zeros(dim, np.float32) if self.v is None else np.asarray(self.v, np.float32).copy()
+        self.F = diag(dim, 1.0) if self.F is None else np.asarray(self.F, np.float32).copy()
+        self.C = np.zeros((dim, dim), np.float32) if self.C is None else np.asarray(self.C, np.float32).copy()
+
+
+@dataclass
+class ParticleArrays:
+    """The particle state in the caller's order: x (n,dim), v (n,dim), F (n,dim,dim),
+    C (n,dim,dim), Jp (n,), mass (n,), volume (n,), c (n,)."""
+    x: np.ndarray
+    v: np.ndarray
+    F: np.ndarray
+    C: np.ndarray
+    Jp: np.ndarray
+    mass: np.ndarray
+    volume: np.ndarray
+    c: np.ndarray
+
+    def __len__(self):
+        return self.x.shape[0]
+
+    def __getitem__(self, p: int) -> Particle:
+        return Particle(self.x[p], int(self.c[p]), self.v[p], float(self.mass[p]),
+                        float(self.volume[p]), self.F[p], self.C[p], float(self.Jp[p]))
+
+
+@dataclass
+class GridArrays:
+    """The grid in the reference's node order (x-major): velocity (nodes, dim), mass (nodes,)."""
+    velocity: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.float32))
+    mass: np.ndarray = field(default_factory=lambda: np.zeros((0,), np.float32))
+
+    def __len__(self):
+        return self.mass.shape[0]
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _soa_from(particles, dim_hint: int | None):
+    if isinstance(particles, dict):
+        x = np.ascontiguousarray(particles["x"], dtype=np.float32)
+        n, dim = x.shape
+        get = lambda k, shape: (None if particles.get(k) is None else  # noqa: E731
+                                np.ascontiguousarray(np.asarray(particles[k], np.float32).reshape(shape)))
+        return dim, dict(x=x, v=get("v", (n, dim)), F=get("F", (n, dim, dim)),
+                         C=get("C", (n, dim, dim)), Jp=get("Jp", (n,)), mass=get("mass", (n,)),
+                         volume=get("volume", (n,)),
+                         c=np.asarray(particles.get("c", np.zeros(n)), np.int32))
+    plist = list(particles)
+    if not plist:
+        dim = dim_hint or 2
+        z = lambda *s: np.zeros(s, np.float32)  # noqa: E731
+        return dim, dict(x=z(0, dim), v=z(0, dim), F=z(0, dim, dim), C=z(0, dim, dim), Jp=z(0),
+                         mass=z(0), volume=z(0), c=np.zeros(0, np.int32))
+    dim = plist[0].x.shape[0]
+    return dim, dict(
+        x=np.stack([p.x for p in plist]).astype(np.float32),
+        v=np.stack([p.v for p in plist]).astype(np.float32),
+        F=np.stack([p.F for p in plist]).astype(np.float32),
+        C=np.stack([p.C for p in plist]).astype(np.float32),
+        Jp=np.array([p.Jp for p in plist], np.float32),
+        mass=np.array([p.mass for p in plist], np.float32),
+        volume=np.array([p.volume for p in plist], np.float32),
+        c=np.array([p.c for p in plist], np.int32))
+
+
+class MPMSimulation:
+    """MPMSimulation<dim> (src/nclr.h:63-384) running on the GPU."""
+    kBoundary = 3
+    kSnowHardening = 10.0
+    kJellyHardening = 0.3
+    kLiquidHardening = 1.0
+
+    def __init__(self, particles, model: MaterialModel | int, res: int = 64, dt: float = 1e-4,
+                 E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, *, dim: int | None = None,
+                 material: np.ndarray | None = None, physics: int = capi.PHYSICS_REFERENCE,
+                 sort_interval: int = 8, particles_per_thread: int = 8, device: int = 0,
+                 use_graphs: bool = True, profile: bool = False):
+        L = capi.lib()
+        self.dim, soa = _soa_from(particles, dim)
+        self._c = soa.pop("c")
+        self._mass = soa["mass"] if soa["mass"] is not None else np.ones(len(self._c), np.float32)
+        self._volume = soa["volume"] if soa["volume"] is not None else np.ones(len(self._c), np.float32)
+        self.n = soa["x"].shape[0]
+        self.res = int(res)
+        self.model = MaterialModel(int(model))
+        mat = None if material is None else np.ascontiguousarray(material, dtype=np.uint8)
+        opt = capi.default_options(physics=physics, sort_interval=sort_interval,
+                                   p2g_particles_per_thread=particles_per_thread, device=device,
+                                   use_graphs=int(use_graphs), profile=int(profile))
+        h = ctypes.c_void_p()
+        st = L.nclr_create(ctypes.byref(h), self.dim, self.n, _ptr(soa["x"]), _ptr(soa["v"]),
+                           _ptr(soa["F"]), _ptr(soa["C"]), _ptr(soa["Jp"]), _ptr(soa["mass"]),
+                           _ptr(soa["volume"]), _ptr(mat), int(self.model), self.res, float(dt),
+                           float(E), float(nu), float(gravity), ctypes.byref(opt))
+        capi.check(st, None)
+        self._h = h
+        mu, lam = ctypes.c_float(), ctypes.c_float()
+        capi.check(L.nclr_get_lame(h, ctypes.byref(mu), ctypes.byref(lam)), h)
+        self.mu_0, self.lambda_0 = float(mu.value), float(lam.value)
+        self._stepped = False
+
+    # -- the reference's API ------------------------------------------------------------
+    def advance(self, steps: int = 1) -> None:
+        """advance() (src/nclr.h:80-84), `steps` times."""
+        capi.check(capi.lib().nclr_advance(self._h, int(steps)), self._h)
+        self._stepped = True
+
+    def particles(self) -> ParticleArrays:
+        n, d = self.n, self.dim
+        x = np.empty((n, d), np.float32); v = np.empty((n, d), np.float32)
+        F = np.empty((n, d, d), np.float32); C = np.empty((n, d, d), np.float32)
+        Jp = np.empty((n,), np.float32)
+        capi.check(capi.lib().nclr_get_particles(self._h, _ptr(x), _ptr(v), _ptr(F), _ptr(C),
+                                                 _ptr(Jp)), self._h)
+        return ParticleArrays(x, v, F, C, Jp, self._mass.copy(), self._volume.copy(), self._c.copy())
+
+    def grid(self) -> GridArrays:
+        if not self._stepped:
+            return GridArrays(np.zeros((0, self.dim), np.float32), np.zeros((0,), np.float32))
+        nodes = (self.res + 1) ** self.dim
+        vel = np.empty((nodes, self.dim), np.float32)
+        mass = np.empty((nodes,), np.float32)
+        capi.check(capi.lib().nclr_get_grid(self._h, _ptr(vel), _ptr(mass)), self._h)
+        return GridArrays(vel, mass)
+
+    # -- extensions ----------------------------------------------------------------------
+    def set_particles(self, x=None, v=None, F=None, C=None, Jp=None) -> None:
+        """Replaces fields of the particle state (caller order; None keeps a field)."""
+        n, d = self.n, self.dim
+        arr = lambda a, s: None if a is None else np.ascontiguousarray(np.asarray(a, np.float32).reshape(s))  # noqa: E731
+        x, v, F, C, Jp = arr(x, (n, d)), arr(v, (n, d)), arr(F, (n, d, d)), arr(C, (n, d, d)), arr(Jp, (n,))
+        capi.check(capi.lib().nclr_set_particles(self._h, _ptr(x), _ptr(v), _ptr(F), _ptr(C),
+                                                 _ptr(Jp)), self._h)
+
+    def get_particles_device(self, x=0, v=0, F=0, C=0, Jp=0) -> None:
+        """Device-pointer export (integers = device addresses, 0 skips); stream-ordered."""
+        capi.check(capi.lib().nclr_get_particles_device(self._h, x or None, v or None, F or None,
+                                                        C or None, Jp or None), self._h)
+
+    def set_particles_device(self, x=0, v=0, F=0, C=0, Jp=0) -> None:
+        capi.check(capi.lib().nclr_set_particles_device(self._h, x or None, v or None, F or None,
+                                                        C or None, Jp or None), self._h)
+
+    @property
+    def stream(self) -> int:
+        return int(capi.lib().nclr_stream(self._h) or 0)
+
+    def stats(self) -> tuple[int, int]:
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        capi.check(capi.lib().nclr_stats(self._h, ctypes.byref(a), ctypes.byref(b)), self._h)
+        return int(a.value), int(b.value)
+
+    def active_nodes(self) -> int:
+        """Grid nodes that received mass in the last step's P2G."""
+        a = ctypes.c_int64()
+        capi.check(capi.lib().nclr_count_active_nodes(self._h, ctypes.byref(a)), self._h)
+        return int(a.value)
+
+    def profile(self) -> dict:
+        """Per kernel phase: (total device ms, launches) since the last reset (profile=True)."""
+        out = {}
+        for i, name in enumerate(capi.PHASE_NAMES):
+            ms, n = ctypes.c_double(), ctypes.c_int64()
+            capi.check(capi.lib().nclr_profile_get(self._h, i, ctypes.byref(ms), ctypes.byref(n)),
+                       self._h)
+            out[name] = (float(ms.value), int(n.value))
+        return out
+
+    def profile_reset(self) -> None:
+        capi.check(capi.lib().nclr_profile_reset(self._h), self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            capi.lib().nclr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
