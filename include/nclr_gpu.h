@@ -30,6 +30,7 @@
 #ifndef NCLR_GPU_H
 #define NCLR_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -139,6 +140,41 @@ nclr_status nclr_profile_reset(nclr_sim *sim);
 const char *nclr_last_error(const nclr_sim *sim);
 
 void nclr_destroy(nclr_sim *sim);
+
+/* ---------------------------------------------------------------------------------------
+ * Particle-to-grid transfer without any allocation.  No counterpart in the reference: it is
+ * an addition for callers that cannot call cudaMalloc while they run -- applications whose
+ * own allocator already holds the device's memory, real-time loops where allocating (and the
+ * synchronisation it can imply) is not allowed, plugins inside a runtime that owns every
+ * allocation.  Everything else in this header allocates in nclr_create.
+ *
+ * Computes the reference's p2g() + grid_op() (src/nclr.h:104-165, 263-310) -- the grid that
+ * grid() returns after one advance() from this state -- for n particles in the caller's
+ * DEVICE memory (the host layout above: x[p*dim+d], F[(p*dim+r)*dim+c], ...; all seven
+ * arrays required) into the caller's DEVICE arrays grid_velocity[(res+1)^dim * dim] and
+ * grid_mass[(res+1)^dim], in the reference's node order.  Runs on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) of the calling thread's current device and synchronises it
+ * before returning.
+ *
+ * The only memory it uses beyond the caller's arrays is a static device array of
+ * NCLR_NOALLOC_MAX_NODES float4 nodes (16 MiB) in the library, held by every GPU that loads
+ * the library until the process exits.  So (res+1)^dim must not exceed
+ * NCLR_NOALLOC_MAX_NODES (3D: res <= 100; 2D: res <= 1023): larger grids return
+ * NCLR_ERR_INVALID.  The array is shared by all calls and keeps the last call's contents;
+ * each call clears it before use.  Calls whose GPU work overlaps (other threads or streams at
+ * the same time) race on it: serialise them.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Errors: NCLR_ERR_INVALID (bad argument, grid too large), NCLR_ERR_OUT_OF_RANGE (a
+ * stencil left the grid, the reference's std::out_of_range), NCLR_ERR_CUDA; when `message`
+ * is non-NULL, up to message_len - 1 bytes of explanation are written there.
+ * --------------------------------------------------------------------------------------- */
+#define NCLR_NOALLOC_MAX_NODES (1 << 20)
+nclr_status nclr_grid_transfer_noalloc(int dim, int64_t n, const float *x, const float *v,
+                                       const float *F, const float *C, const float *Jp,
+                                       const float *mass, const float *volume, int model,
+                                       int res, float dt, float E, float nu, float gravity,
+                                       float *grid_velocity, float *grid_mass, void *stream,
+                                       char *message, size_t message_len);
 
 #ifdef __cplusplus
 }

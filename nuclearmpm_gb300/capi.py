@@ -17,6 +17,7 @@ STATUS_NAMES = {0: "NCLR_OK", 1: "NCLR_ERR_INVALID", 2: "NCLR_ERR_OUT_OF_RANGE",
 PHYSICS_REFERENCE, PHYSICS_CORRECTED = 0, 1
 PHASE_SORT, PHASE_CLEAR, PHASE_P2G, PHASE_G2P = range(4)
 PHASE_NAMES = ("sort", "clear", "p2g", "g2p")
+NOALLOC_MAX_NODES = 1 << 20
 
 
 class Options(ctypes.Structure):
@@ -56,6 +57,10 @@ SIGNATURES = {
     "nclr_profile_reset": (ctypes.c_int, [_h]),
     "nclr_last_error": (ctypes.c_char_p, [_h]),
     "nclr_destroy": (None, [_h]),
+    "nclr_grid_transfer_noalloc": (ctypes.c_int, [ctypes.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                  _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                  ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                                  _vp, _vp, _vp, ctypes.c_char_p, ctypes.c_size_t]),
 }
 
 _LIB: ctypes.CDLL | None = None
