@@ -48,7 +48,7 @@ WORKLOAD = {"workload": "3D jelly (MaterialModel::kJelly), 4 cubes of 64^3 latti
 
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each kernel from
 # one ncu capture of this workload (profiles/ holds the summaries); None until captured.
-NCU_TRAFFIC = {"p2g": None, "g2p": None}
+NCU_TRAFFIC = {"g2p2g": None}
 
 
 def peaks():
@@ -61,18 +61,14 @@ def peaks():
 
 
 def algorithmic_bytes(dim: int, n: int, active: int) -> dict:
-    """Bytes each kernel must move per launch given its interface (every input read once,
-    every output written once), FP32:
-      p2g: reads the per-particle P2G record (x, m, m v, fused affine A: 16 (3D) / 12 (2D)
-           floats) and writes one (m v, m) node per active node;
-      g2p: reads x, F, Jp, mass, volume and one node per active node; writes x, v, F, C, Jp and
-           the next step's P2G record."""
+    """Bytes the fused step kernel must move per launch (every input read once, every output
+    written once, FP32).  g2p2g reads x, F, Jp, mass, volume (60 B in 3D) and writes x, F, Jp
+    (52 B); it reads one updated node (16 B) and adds one accumulated node (16 B) per active
+    node; v and C (48 B) are written only by the last step of an advance() call and are not
+    counted.  The grid sweep reads G and writes V and the cleared G: 48 B per node."""
     d2 = dim * dim
-    rec = 16 if dim == 3 else 12
-    node = 16
-    p2g = n * rec * 4 + active * node
-    g2p = n * (dim + d2 + 3) * 4 + active * node + n * (2 * dim + 2 * d2 + 1) * 4 + n * rec * 4
-    return {"p2g": p2g, "g2p": g2p}
+    g2p2g = n * ((dim + d2 + 3) + (dim + d2 + 1)) * 4 + active * 32
+    return {"g2p2g": g2p2g}
 
 
 class ClockSampler:
@@ -239,8 +235,8 @@ def run_ours(args):
     # ---- roofline of the dominant kernel ------------------------------------------------
     hbm_peak, peak_kind = peaks()
     alg = algorithmic_bytes(3, n, active)
-    per_launch = {k: prof[k][0] / max(prof[k][1], 1) for k in ("p2g", "g2p")}
-    dom = max(per_launch, key=per_launch.get)
+    per_launch = {k: prof[k][0] / max(prof[k][1], 1) for k in prof if prof[k][1] > 0}
+    dom = "g2p2g"
     achieved = alg[dom] / (per_launch[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind,

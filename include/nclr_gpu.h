@@ -57,17 +57,19 @@ enum { NCLR_PHYSICS_REFERENCE = 0, NCLR_PHYSICS_CORRECTED = 1 };
 
 typedef struct nclr_options {
   int physics;             /* NCLR_PHYSICS_* (default REFERENCE) */
-  int sort_interval;       /* re-sort particles by grid cell every this many steps
-                              (0 = never; default 8) */
-  int p2g_particles_per_thread; /* 4, 8 or 16 (default 8) */
+  int sort_interval;       /* re-sort particles by grid block every this many steps (0 = only
+                              after an upload; default 8) */
+  int p2g_particles_per_thread; /* reserved (ignored) */
   int device;              /* CUDA device ordinal (default 0) */
   int use_graphs;          /* capture advance() step sequences in CUDA graphs (default 1) */
   int profile;             /* time every kernel phase of advance() with CUDA events on the
                               handle's stream (direct launches, no graphs; default 0) */
 } nclr_options;
 
-/* Kernel phases reported by nclr_profile_get. */
-enum { NCLR_PHASE_SORT = 0, NCLR_PHASE_CLEAR = 1, NCLR_PHASE_P2G = 2, NCLR_PHASE_G2P = 3,
+/* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid
+ * update sweep (grid_op + clearing the accumulator), the stand-alone P2G that follows an
+ * upload, and the fused G2P + next-step P2G kernel that makes up the rest of a step. */
+enum { NCLR_PHASE_SORT = 0, NCLR_PHASE_GRID = 1, NCLR_PHASE_P2G = 2, NCLR_PHASE_G2P2G = 3,
        NCLR_NUM_PHASES = 4 };
 
 typedef struct nclr_sim nclr_sim;

@@ -15,8 +15,8 @@ NCLR_OK, NCLR_ERR_INVALID, NCLR_ERR_OUT_OF_RANGE, NCLR_ERR_CUDA, NCLR_ERR_NO_DEV
 STATUS_NAMES = {0: "NCLR_OK", 1: "NCLR_ERR_INVALID", 2: "NCLR_ERR_OUT_OF_RANGE",
                 3: "NCLR_ERR_CUDA", 4: "NCLR_ERR_NO_DEVICE"}
 PHYSICS_REFERENCE, PHYSICS_CORRECTED = 0, 1
-PHASE_SORT, PHASE_CLEAR, PHASE_P2G, PHASE_G2P = range(4)
-PHASE_NAMES = ("sort", "clear", "p2g", "g2p")
+PHASE_SORT, PHASE_GRID, PHASE_P2G, PHASE_G2P2G = range(4)
+PHASE_NAMES = ("sort", "grid", "p2g", "g2p2g")
 NOALLOC_MAX_NODES = 1 << 20
 
 

@@ -3,19 +3,19 @@
 //
 // HBM layout
 //   particles  SoA, component-major: field component c of particle slot p at
-//              field[c * stride + p] (x, v: dim comps; F, C: dim*dim comps, row-major;
+//              field[c * stride + p] (x: dim comps; F, C: dim*dim comps, row-major; v: dim;
 //              Jp, mass, volume: 1).  `id[p]` is the caller's index of slot p: slots are
-//              re-sorted by grid cell every few steps, the caller's order is restored on
-//              download.  `mat[p]` (optional) is a per-particle material.
-//   payload    the P2G input of each slot, computed by the previous G2P (or by
-//              prepare_payload after an upload): 3D {x0,x1,x2,m} {mv0,mv1,mv2,A00}
-//              {A01,A02,A10,A11} {A12,A20,A21,A22}; 2D {x0,x1,m,mv0} {mv1,A00,A01,A10}
-//              {A11,0,0,0}, where A is the fused APIC + stress matrix (src/nclr.h:313-337)
-//              and mv = m v.  One 64 B (3D) / 48 B (2D) record per slot, read whole.
-//   grid       dense (res+1)^dim float4 nodes {sum w m v (x,y,z), sum w m}, the reference's
-//              x-major node order; zeroed before each P2G.  The grid update (normalise,
-//              gravity, clamp, sticky boundary; src/nclr.h:263-310) is applied on the fly
-//              where nodes are read (G2P, grid export), never stored.
+//              re-sorted by grid block every few steps and the caller's order is restored on
+//              download.  `mat[p]` (optional) is a per-particle material.  v and C are written
+//              only by the last step of an advance() call (nothing else reads them: each
+//              G2P rebuilds them from the grid).
+//   G          dense (res+1)^dim float4 nodes {sum w (m v + A dpos), sum w m} (the reference's
+//              x-major node order): the P2G accumulator of the coming step.
+//   V          dense (res+1)^dim float4 nodes {v (post grid update), m}: the grid() of the
+//              last step, read by G2P.  The grid sweep turns G into V and zeroes G.
+//   blocks     the grid is tiled into blocks of BS^dim cells (BS = 4 in 3D, 8 in 2D); slots
+//              are sorted by the block of their base node, and the G2P+P2G kernel stages a
+//              (BS+4)^dim node tile of V and of the next G around each block in shared memory.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,6 +28,24 @@ namespace mpm {
 enum : int { kSnow = 0, kJelly = 1, kLiquid = 2 };
 enum : int { kErrOutOfRange = 1 };
 
+// Block tiling of the grid (see the layout note above).  Particles are sorted by block and,
+// inside a block, stored cell by cell in rounds (the first particle of every cell in x-major
+// cell order, then the second, ...), so the consecutive slots a warp takes sit in different,
+// neighbouring cells.
+// Both shared-memory tiles hold float4 nodes with a y stride of 12 (= 4 mod 8): the 8 lanes
+// of one 128-byte wavefront, which cover 2 (y) x 4 (z) neighbouring cells, then fall in
+// 8 different 16-byte bank groups.
+template <int D>
+struct Tiling {
+  static constexpr int BS = (D == 3) ? 4 : 8;  // cells per block side
+  static constexpr int CPB = (D == 3) ? BS * BS * BS : BS * BS;  // cells per block
+  static constexpr int T = BS + 4;             // tile side in nodes: block - 1 .. block + BS + 2
+  static constexpr int NODES = (D == 3) ? T * T * T : T * T;
+  // shared-memory strides of a tile (3D: x, y; z stride 1.  2D: x; y stride 1)
+  static constexpr int SX = (D == 3) ? (T - 1) * 12 + T : T, SY = 12;
+  static constexpr int SIZE = (D == 3) ? (T - 1) * SX + (T - 1) * SY + T : T * T;
+};
+
 struct Params {
   int res, N;           // N = res + 1 nodes per axis
   int n;                // particles
@@ -39,18 +57,15 @@ struct Params {
   float cscale;         // 4 inv_dx  (src/nclr.h:206,223)
   float dt_gravity;     // dt * gravity (src/nclr.h:292)
   int64_t nodes;        // N^dim
+  int nb;               // grid blocks per axis: ceil(N / Tiling<dim>::BS)
+  int nblocks;          // nb^dim
 };
 
 struct PState {
-  float *x, *v, *F, *C, *Jp, *mass, *vol;
+  float *x, *v, *F, *C, *Jp, *mass, *vol;  // v and C: see the layout note
   int *id;
   uint8_t *mat;  // may be null
   int stride;    // component stride (capacity)
-};
-
-template <int D>
-struct PayloadRecs {
-  static constexpr int value = (D == 3) ? 4 : 3;
 };
 
 // ---------------------------------------------------------------------------------------
@@ -146,43 +161,6 @@ __device__ __forceinline__ Mat<D> fused_affine(const Mat<D> &F, const Mat<D> &R,
 #pragma unroll
     for (int j = 0; j < D; ++j) A.a[i][j] = s * (P.Dinv * (PF.a[i][j] + lam)) + m * C.a[i][j];
   return A;
-}
-
-template <int D>
-__device__ __forceinline__ void store_payload(float4 *__restrict__ pay, int p, const float x[D],
-                                              float m, const float v[D], const Mat<D> &A) {
-  if (D == 3) {
-    float4 *r = pay + (size_t)p * 4;
-    r[0] = make_float4(x[0], x[1], x[D - 1], m);
-    r[1] = make_float4(v[0] * m, v[1] * m, v[D - 1] * m, A.a[0][0]);
-    r[2] = make_float4(A.a[0][1], A.a[0][D - 1], A.a[1][0], A.a[1][1]);
-    r[3] = make_float4(A.a[1][D - 1], A.a[D - 1][0], A.a[D - 1][1], A.a[D - 1][D - 1]);
-  } else {
-    float4 *r = pay + (size_t)p * 3;
-    r[0] = make_float4(x[0], x[1], m, v[0] * m);
-    r[1] = make_float4(v[1] * m, A.a[0][0], A.a[0][1], A.a[1][0]);
-    r[2] = make_float4(A.a[1][1], 0.0f, 0.0f, 0.0f);
-  }
-}
-
-template <int D>
-__device__ __forceinline__ void load_payload(const float4 *__restrict__ pay, int p, float x[D],
-                                             float &m, float mv[D], Mat<D> &A) {
-  if (D == 3) {
-    const float4 *r = pay + (size_t)p * 4;
-    const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), e = __ldg(r + 3);
-    x[0] = a.x; x[1] = a.y; x[D - 1] = a.z; m = a.w;
-    mv[0] = b.x; mv[1] = b.y; mv[D - 1] = b.z;
-    A.a[0][0] = b.w; A.a[0][1] = c.x; A.a[0][D - 1] = c.y;
-    A.a[1][0] = c.z; A.a[1][1] = c.w; A.a[1][D - 1] = e.x;
-    A.a[D - 1][0] = e.y; A.a[D - 1][1] = e.z; A.a[D - 1][D - 1] = e.w;
-  } else {
-    const float4 *r = pay + (size_t)p * 3;
-    const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
-    x[0] = a.x; x[1] = a.y; m = a.z; mv[0] = a.w;
-    mv[1] = b.x; A.a[0][0] = b.y; A.a[0][1] = b.z; A.a[1][0] = b.w;
-    A.a[1][1] = c.x;
-  }
 }
 
 template <int D>

@@ -1,5 +1,5 @@
 // Host-side launchers of the step kernels (instantiated for dim 2 and 3 in step2d.cu and
-// step3d.cu) and of the dimension-free scan (scan.cu).
+// step3d.cu) and of the dimension-free scan utilities (scan.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,14 +10,19 @@ namespace mpm {
 struct Params;
 struct PState;
 
-template <int D> void launch_prepare(const PState &s, const Params &P, float4 *pay, bool ref, cudaStream_t st);
-template <int D> void launch_p2g(const float4 *pay, const Params &P, float4 *grid, int *err, int K, cudaStream_t st);
-template <int D> void launch_g2p(const PState &s, const Params &P, const float4 *grid, float4 *pay, int *err, bool ref, cudaStream_t st);
+template <int D> void launch_p2g_state(const PState &s, const Params &P, float4 *G, int *err, cudaStream_t st);
+template <int D> void launch_grid_sweep(float4 *G, float4 *V, const Params &P, int *work, int sms, cudaStream_t st);
+template <int D> void launch_g2p2g(const PState &s, const Params &P, const float4 *V, float4 *G, const int *blocks,
+                                   const int *nactive, const int *bstart, int *work, int *err_now, int *err_next,
+                                   bool ref, bool final_step, int ctas, cudaStream_t st);
+template <int D> int g2p2g_ctas_per_sm();
+template <int D> void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st);
 template <int D> void launch_export_grid(const float4 *grid, const Params &P, float *vel, float *mass, cudaStream_t st);
 template <int D> void launch_export_particles(const PState &s, int n, float *x, float *v, float *F, float *C, float *Jp, cudaStream_t st);
 template <int D> void launch_import_particles(const PState &s, int n, const float *x, const float *v, const float *F, const float *C, const float *Jp, cudaStream_t st);
-template <int D> void launch_sort_keys(const PState &s, const Params &P, int *key, int *rank, int *count, cudaStream_t st);
-template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const float4 *pay_src, float4 *pay_dst, const int *key, const int *rank, const int *start, cudaStream_t st);
+template <int D> void launch_block_keys(const PState &s, const Params &P, int *key, int *rank, int *count, cudaStream_t st);
+template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank, const int *start, const int *count, cudaStream_t st);
+void launch_compact_blocks(const int *start, int nblocks, int cpb, int *list, int *nlist, cudaStream_t st);
 
 // Exclusive prefix sum of count[0..n) into start[0..n]; tile_sums must hold
 // scan_tiles(n) ints.  Three launches.

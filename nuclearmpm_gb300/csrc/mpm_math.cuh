@@ -226,7 +226,7 @@ MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
       S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
       V[i][j] = (i == j) ? 1.0f : 0.0f;
     }
-#pragma unroll
+#pragma unroll 1
   for (int sweep = 0; sweep < kJacobiSweeps; ++sweep) {
     jacobi_rotate<0, 1>(S, V);
     jacobi_rotate<1, 2>(S, V);

@@ -1,5 +1,12 @@
 // Kernels of one MLS-MPM step and of the host<->device transfers, templated on the
 // dimension; step2d.cu / step3d.cu instantiate them.
+//
+// Step k (the reference's advance(): p2g, grid_op, g2p; src/nclr.h:80-84) runs as
+//   grid_sweep:  V = grid_op(G) (normalise, gravity, clamp, sticky boundary), G = 0
+//   g2p2g:       per block of particles: G2P of step k from a shared-memory tile of V,
+//                F/C/Jp update, then the P2G of step k+1 from the updated particle into a
+//                shared-memory tile of G, flushed once per block with vector reductions.
+// The P2G of the first step after an upload comes from p2g_state.
 #pragma once
 
 #include "mpm_device.cuh"
@@ -7,212 +14,126 @@
 
 namespace mpm {
 
-// ---------------------------------------------------------------------------------------
-// prepare_payload: the P2G input of each slot from the particle state (src/nclr.h:129,162:
-// stress + APIC affine and m v), used after the state was uploaded or replaced.
-// ---------------------------------------------------------------------------------------
-template <int D, bool kRef>
-__global__ void __launch_bounds__(256) prepare_payload_kernel(PState s, Params P,
-                                                              float4 *__restrict__ pay) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.n) return;
-  const int st = s.stride;
-  float x[D], v[D];
+constexpr int kG2P2GThreads = 256;
+
+template <int D>
+__device__ __forceinline__ void stencil_offset(int o, int &oi, int &oj, int &ok) {
+  oi = (D == 3) ? o / 9 : o / 3;
+  oj = (D == 3) ? (o / 3) % 3 : o % 3;
+  ok = (D == 3) ? o % 3 : 0;
+}
+
+// Flat index of stencil node o relative to the node of flat index f0 (the reference's index
+// arithmetic, src/nclr.h:141-142,152: per-axis offsets folded into one flat index).
+template <int D>
+__device__ __forceinline__ int64_t stencil_flat(int64_t f0, int o, int N) {
+  int oi, oj, ok;
+  stencil_offset<D>(o, oi, oj, ok);
+  return (D == 3) ? f0 + ((int64_t)oi * N + oj) * N + ok : f0 + (int64_t)oi * N + oj;
+}
+
+// Shared-memory index of tile-local node (i, j, k).
+template <int D>
+__device__ __forceinline__ int tile_index(int i, int j, int k) {
+  using Tl = Tiling<D>;
+  if (D == 3) return i * Tl::SX + j * Tl::SY + k;
+  return i * Tl::SX + j;
+}
+
+template <int D>
+__device__ __forceinline__ int tile_offset(int o) {
+  int oi, oj, ok;
+  stencil_offset<D>(o, oi, oj, ok);
+  return tile_index<D>(oi, oj, ok);
+}
+
+// One node's contribution of the reference's compute_fused_momentum (src/nclr.h:160-165):
+// weight * (m v + A dpos) and weight * m, with dpos = (o - fx) dx.
+template <int D>
+__device__ __forceinline__ void p2g_contrib(int o, const float fx[D], const float w[3][D],
+                                            const float mv[D], float m, const Mat<D> &A, float dx,
+                                            float c[4]) {
+  int oi, oj, ok;
+  stencil_offset<D>(o, oi, oj, ok);
+  const int oo[3] = {oi, oj, ok};
+  float dpos[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) dpos[d] = ((float)oo[d] - fx[d]) * dx;
+  float weight = w[oi][0] * w[oj][1];
+  if (D == 3) weight = weight * w[ok][D - 1];
+  c[2] = 0.0f;
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float ad = A.a[r][0] * dpos[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) ad = ad + A.a[r][k] * dpos[k];
+    c[r] = weight * (mv[r] + ad);
+  }
+  c[3] = weight * m;
+}
+
+// One node's part of the G2P gather (src/nclr.h:197-225): v += w gv and
+// C += (w gv) dpos^T with dpos = o - fx; the caller scales C by 4 inv_dx once at the end
+// (the reference scales every term; the two differ only in rounding).
+template <int D>
+__device__ __forceinline__ void g2p_accumulate(int o, const float4 g, const float fx[D],
+                                               const float w[3][D], float v[D], Mat<D> &C) {
+  int oi, oj, ok;
+  stencil_offset<D>(o, oi, oj, ok);
+  const int oo[3] = {oi, oj, ok};
+  float weight = w[oi][0] * w[oj][1];
+  if (D == 3) weight = weight * w[ok][D - 1];
+  const float gv[3] = {g.x, g.y, g.z};
+  float wgv[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    x[d] = s.x[(size_t)d * st + p];
-    v[d] = s.v[(size_t)d * st + p];
+    wgv[d] = weight * gv[d];
+    v[d] += wgv[d];
   }
-  const Mat<D> F = load_mat<D>(s.F, st, p);
-  const Mat<D> C = load_mat<D>(s.C, st, p);
-  const float Jp = s.Jp[p], m = s.mass[p], vol = s.vol[p];
-  const int material = s.mat ? (int)s.mat[p] : P.model;
-  const Mat<D> R = polar_R(F);
-  const Mat<D> A = fused_affine<D>(F, R, C, Jp, m, vol, material, P);
-  store_payload<D>(pay, p, x, m, v, A);
-}
-
-// ---------------------------------------------------------------------------------------
-// P2G scatter (src/nclr.h:104-165).  Each thread takes K consecutive slots; slots are kept
-// sorted by grid cell, so consecutive particles usually share the same 3^dim stencil.
-// The thread accumulates its particles' contributions in registers while the cell stays
-// the same and flushes them with one 16-byte vector reduction per node when it changes.
-// ---------------------------------------------------------------------------------------
-template <int D, int K>
-__global__ void __launch_bounds__(128) p2g_kernel(const float4 *__restrict__ pay, Params P,
-                                                  float4 *__restrict__ grid, int *err) {
-  constexpr int S = (D == 3) ? 27 : 9;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i0 = t * K;
-  if (i0 >= P.n) return;
-  const int i1 = min(i0 + K, P.n);
-  float acc[S][4];
-  int cb[D];
-  int64_t cur = INT64_MIN;
-  const float dx = P.dx;
-  const int N = P.N;
-
-  auto flush = [&]() {
-    const int64_t f0 = flat_index<D>(cb, N);
-    // 3D: node (i,j,k) of the stencil is f0 + i N^2 + j N + k
-    const int64_t hi = (D == 3) ? f0 + 2 * (int64_t)N * N + 2 * N + 2 : f0 + 2 * (int64_t)N + 2;
-    const bool inside = f0 >= 0 && hi < P.nodes;
-#pragma unroll
-    for (int o = 0; o < S; ++o) {
-      const int oi = (D == 3) ? o / 9 : o / 3;
-      const int oj = (D == 3) ? (o / 3) % 3 : o % 3;
-      const int ok = (D == 3) ? o % 3 : 0;
-      const int64_t f = (D == 3) ? f0 + ((int64_t)oi * N + oj) * N + ok : f0 + (int64_t)oi * N + oj;
-      if (inside || (f >= 0 && f < P.nodes)) {
-        red_add_v4(grid + f, acc[o][0], acc[o][1], acc[o][2], acc[o][3]);
-      } else {
-        atomicOr(err, kErrOutOfRange);
-      }
-    }
-  };
-
-  for (int i = i0; i < i1; ++i) {
-    float x[D], mv[D], m;
-    Mat<D> A;
-    load_payload<D>(pay, i, x, m, mv, A);
-    int base[D];
-    float fx[D], w[3][D];
-    stencil<D>(x, P.inv_dx, base, fx, w);
-    const int64_t f = flat_index<D>(base, N);
-    if (f != cur) {
-      if (cur != INT64_MIN) flush();
-#pragma unroll
-      for (int o = 0; o < S; ++o) acc[o][0] = acc[o][1] = acc[o][2] = acc[o][3] = 0.0f;
-      cur = f;
-#pragma unroll
-      for (int d = 0; d < D; ++d) cb[d] = base[d];
-    }
-#pragma unroll
-    for (int o = 0; o < S; ++o) {
-      const int oi = (D == 3) ? o / 9 : o / 3;
-      const int oj = (D == 3) ? (o / 3) % 3 : o % 3;
-      const int ok = (D == 3) ? o % 3 : 0;
-      const int oo[3] = {oi, oj, ok};
-      float dpos[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) dpos[d] = ((float)oo[d] - fx[d]) * dx;
-      float weight = w[oi][0] * w[oj][1];
-      if (D == 3) weight = weight * w[ok][D - 1];
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        float ad = A.a[r][0] * dpos[0];
-#pragma unroll
-        for (int c = 1; c < D; ++c) ad = ad + A.a[r][c] * dpos[c];
-        acc[o][r] += weight * (mv[r] + ad);
-      }
-      acc[o][3] += weight * m;
-    }
-  }
-  if (cur != INT64_MIN) flush();
-}
-
-// ---------------------------------------------------------------------------------------
-// G2P (src/nclr.h:167-261) fused with the grid update (src/nclr.h:263-310) and with the
-// next step's stress (src/nclr.h:313-337): gathers the 3^dim post-update node velocities,
-// rebuilds v and the APIC C, advects x, updates F, applies the material's plasticity, and
-// writes the new state plus the payload the next P2G reads.
-// ---------------------------------------------------------------------------------------
-template <int D, bool kRef>
-__global__ void __launch_bounds__(128) g2p_kernel(PState s, Params P,
-                                                  const float4 *__restrict__ grid,
-                                                  float4 *__restrict__ pay, int *err) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.n) return;
-  const int st = s.stride;
-  const int N = P.N;
-  float x[D];
-#pragma unroll
-  for (int d = 0; d < D; ++d) x[d] = s.x[(size_t)d * st + p];
-  int base[D];
-  float fx[D], w[3][D];
-  stencil<D>(x, P.inv_dx, base, fx, w);
-  const int64_t f0 = flat_index<D>(base, N);
-  bool axes_inside = true;
-#pragma unroll
-  for (int d = 0; d < D; ++d) axes_inside &= base[d] >= 0 && base[d] + 2 < N;
-
-  float v[D];
-  Mat<D> C;
-#pragma unroll
-  for (int d = 0; d < D; ++d) v[d] = 0.0f;
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
-    for (int j = 0; j < D; ++j) C.a[i][j] = 0.0f;
+    for (int j = 0; j < D; ++j) C.a[i][j] += wgv[i] * ((float)oo[j] - fx[j]);
+}
 
-  constexpr int S = (D == 3) ? 27 : 9;
+template <int D>
+__device__ __forceinline__ void scale_mat(Mat<D> &C, float c) {
 #pragma unroll
-  for (int o = 0; o < S; ++o) {
-    const int oi = (D == 3) ? o / 9 : o / 3;
-    const int oj = (D == 3) ? (o / 3) % 3 : o % 3;
-    const int ok = (D == 3) ? o % 3 : 0;
-    const int oo[3] = {oi, oj, ok};
-    const int64_t f = (D == 3) ? f0 + ((int64_t)oi * N + oj) * N + ok : f0 + (int64_t)oi * N + oj;
-    float gv[D];
-    if (f >= 0 && f < P.nodes) {
-      int idx[D];
-      if (axes_inside) {
+  for (int i = 0; i < D; ++i)
 #pragma unroll
-        for (int d = 0; d < D; ++d) idx[d] = base[d] + oo[d];
-      } else {
-        unflatten<D>(f, N, idx);
-      }
-      float m;
-      grid_update<D>(__ldg(grid + f), idx, P, gv, m);
-    } else {
-      atomicOr(err, kErrOutOfRange);
-#pragma unroll
-      for (int d = 0; d < D; ++d) gv[d] = 0.0f;
-    }
-    float weight = w[oi][0] * w[oj][1];
-    if (D == 3) weight = weight * w[ok][D - 1];
-    float wgv[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      wgv[d] = weight * gv[d];
-      v[d] += wgv[d];
-    }
-#pragma unroll
-    for (int i = 0; i < D; ++i)
-#pragma unroll
-      for (int j = 0; j < D; ++j) C.a[i][j] += (P.cscale * wgv[i]) * ((float)oo[j] - fx[j]);
-  }
+    for (int j = 0; j < D; ++j) C.a[i][j] *= c;
+}
 
-#pragma unroll
-  for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];
+// The F update and plasticity of G2P (src/nclr.h:228-259) from the gathered C; returns the
+// rotation R of the updated F (the polar factor the next step's stress needs).
+template <int D, bool kRef>
+__device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp, int material,
+                                           float dt) {
   Mat<D> M;
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
-    for (int j = 0; j < D; ++j) M.a[i][j] = diag_one<D, kRef>(i, j) + P.dt * C.a[i][j];
-  const Mat<D> F = load_mat<D>(s.F, st, p);
+    for (int j = 0; j < D; ++j) M.a[i][j] = diag_one<D, kRef>(i, j) + dt * C.a[i][j];
   Mat<D> Fh = mat_mul<D>(M, F);
-  float Jp = s.Jp[p];
-  const int material = s.mat ? (int)s.mat[p] : P.model;
   Mat<D> R;
   if (material == kJelly) {
     R = polar_R(Fh);
   } else {
-    Mat<D> U, V;
+    Mat<D> U, Vm;
     float sig[D];
     if constexpr (D == 3) {
-      svd3(Fh, U, sig, V);
+      svd3(Fh, U, sig, Vm);
     } else {
-      svd2<kRef>(Fh, U, sig, V);
+      svd2<kRef>(Fh, U, sig, Vm);
     }
     if (material == kSnow) {
 #pragma unroll
       for (int d = 0; d < D; ++d) sig[d] = clampf_(sig[d], 1.0f - 2.5e-2f, 1.0f + 4.5e-3f);
       const float old_J = det(Fh);
-      Fh = usv<D>(U, sig, V);
+      Fh = usv<D>(U, sig, Vm);
       Jp = clampf_(Jp * old_J / det(Fh), 0.6f, 20.0f);
       if constexpr (D == 3) {
-        R = uvt<3>(U, V);  // the clamped sigma are positive: F = (U V^T)(V S V^T)
+        R = uvt<3>(U, Vm);  // the clamped sigma are positive: F = (U V^T)(V S V^T)
       } else {
         R = polar_rotation(Fh);
       }
@@ -228,22 +149,312 @@ __global__ void __launch_bounds__(128) g2p_kernel(PState s, Params P,
       R = polar_R(Fh);
     }
   }
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    s.x[(size_t)d * st + p] = x[d];
-    s.v[(size_t)d * st + p] = v[d];
-  }
-  store_mat<D>(s.F, st, p, Fh);
-  store_mat<D>(s.C, st, p, C);
-  s.Jp[p] = Jp;
-  const float m = s.mass[p], vol = s.vol[p];
-  const Mat<D> A = fused_affine<D>(Fh, R, C, Jp, m, vol, material, P);
-  store_payload<D>(pay, p, x, m, v, A);
+  F = Fh;
+  return R;
 }
 
 // ---------------------------------------------------------------------------------------
-// grid() export (src/nclr.h:87): the post-update grid in the reference's node order.
+// p2g_state: the P2G of the coming step from the stored particle state (after an upload):
+// stress + APIC affine (src/nclr.h:313-337) and the 3^dim contributions, reduced into G.
 // ---------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(256) p2g_state_kernel(PState s, Params P, float4 *__restrict__ G,
+                                                        int *err) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.n) return;
+  const int st = s.stride;
+  float x[D], mv[D];
+  const float m = s.mass[p], vol = s.vol[p];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    x[d] = s.x[(size_t)d * st + p];
+    mv[d] = s.v[(size_t)d * st + p] * m;
+  }
+  const Mat<D> F = load_mat<D>(s.F, st, p);
+  const Mat<D> C = load_mat<D>(s.C, st, p);
+  const int material = s.mat ? (int)s.mat[p] : P.model;
+  const Mat<D> A = fused_affine<D>(F, polar_R(F), C, s.Jp[p], m, vol, material, P);
+  int base[D];
+  float fx[D], w[3][D];
+  stencil<D>(x, P.inv_dx, base, fx, w);
+  const int64_t f0 = flat_index<D>(base, P.N);
+  constexpr int S = (D == 3) ? 27 : 9;
+#pragma unroll 1
+  for (int o = 0; o < S; ++o) {
+    const int64_t f = stencil_flat<D>(f0, o, P.N);
+    if (f < 0 || f >= P.nodes) {
+      atomicOr(err, kErrOutOfRange);
+      continue;
+    }
+    float c[4];
+    p2g_contrib<D>(o, fx, w, mv, m, A, P.dx, c);
+    red_add_v4(G + f, c[0], c[1], c[2], c[3]);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// grid_sweep: grid_op (src/nclr.h:263-310) on every node: V = update(G); then G = 0 for the
+// next P2G.  Also resets the g2p2g work counter.
+// ---------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
+                                                         float4 *__restrict__ V, Params P,
+                                                         int *__restrict__ work) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *work = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < P.nodes; f += stride) {
+    const float4 g = G[f];
+    int idx[D];
+    unflatten<D>(f, P.N, idx);
+    float v[D], m;
+    grid_update<D>(g, idx, P, v, m);
+    V[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
+    G[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// g2p2g: persistent CTAs take blocks of particles from the active-block list.  For each
+// block: stage the (BS+4)^dim node tile of V around it, run G2P for its particles (those
+// sorted into it; a particle that has since drifted out of the tile, or whose stencil leaves
+// the grid on some axis, reads V in global memory with the reference's flat-index arithmetic),
+// update F/C/Jp, compute the next stress and scatter the next P2G into a shared-memory tile
+// of G (again with a global fallback), then flush the tile with one vector reduction per
+// touched node.
+// ---------------------------------------------------------------------------------------
+template <int D, bool kRef, bool kFinal>
+__global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
+    PState s, Params P, const float4 *__restrict__ V, float4 *__restrict__ G,
+    const int *__restrict__ blocks, const int *__restrict__ nactive,
+    const int *__restrict__ bstart, int *__restrict__ work, int *__restrict__ err_now,
+    int *__restrict__ err_next) {
+  using Tl = Tiling<D>;
+  constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, CPB = Tl::CPB, GS = Tl::SIZE;
+  constexpr int S = (D == 3) ? 27 : 9;
+  constexpr int kWarps = kG2P2GThreads / 32;
+  extern __shared__ float4 smem[];
+  float4 *vt = smem;            // V tile
+  float4 *gt = smem + Tl::SIZE;  // kWarps private G tiles: [warp][SIZE]
+  __shared__ int s_item;
+  const int N = P.N;
+  const int st = s.stride;
+  const int nact = *nactive;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float4 *mytile = gt + warp * GS;
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(work, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= nact) return;
+    const int b = blocks[item];
+    int org[D];
+    {
+      int r = b;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        org[d] = (r % P.nb) * BS - 1;
+        r /= P.nb;
+      }
+    }
+    for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
+      int g[D], l[3] = {0, 0, 0};
+      bool in = true;
+      int r = t;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        l[d] = r % T;
+        g[d] = org[d] + l[d];
+        r /= T;
+        in &= g[d] >= 0 && g[d] < N;
+      }
+      vt[tile_index<D>(l[0], l[1], l[2])] =
+          in ? __ldg(V + flat_index<D>(g, N)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
+      gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    __syncthreads();
+
+    // The block's particles, stored cell by cell in rounds (see sort_move_kernel), one per
+    // thread in slot order.  Every lane of a warp runs the same number of iterations (the
+    // warp-wide steps below need them all).
+    const int p0 = bstart[b * CPB];
+    const int np = bstart[(b + 1) * CPB] - p0;
+    for (int j0 = 0; j0 < np; j0 += kG2P2GThreads) {
+      const int j = j0 + threadIdx.x;
+      const bool valid = j < np;
+      const int p = p0 + j;
+      // what the particle contributes to the next P2G
+      bool fast_s = false;
+      int tb_s = 0;
+      float fx_s[D], w_s[3][D], mv[D], m = 0.0f;
+      Mat<D> A;
+      if (valid) {
+        // ---- G2P of this step ----
+        float x[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) x[d] = s.x[(size_t)d * st + p];
+        int base[D];
+        float fx[D], w[3][D];
+        stencil<D>(x, P.inv_dx, base, fx, w);
+        bool fast = true;
+        int lb[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          lb[d] = base[d] - org[d];
+          fast &= lb[d] >= 0 && lb[d] + 2 < T && base[d] >= 0 && base[d] + 2 < N;
+        }
+        const int tb = tile_index<D>(lb[0], lb[1], lb[2]);
+        float v[D];
+        Mat<D> C;
+#pragma unroll
+        for (int d = 0; d < D; ++d) v[d] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int jj = 0; jj < D; ++jj) C.a[i][jj] = 0.0f;
+        if (fast) {
+#pragma unroll
+          for (int o = 0; o < S; ++o) g2p_accumulate<D>(o, vt[tb + tile_offset<D>(o)], fx, w, v, C);
+        } else {
+          const int64_t f0 = flat_index<D>(base, N);
+#pragma unroll 1
+          for (int o = 0; o < S; ++o) {
+            const int64_t f = stencil_flat<D>(f0, o, N);
+            float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (f >= 0 && f < P.nodes)
+              g = __ldg(V + f);
+            else
+              atomicOr(err_now, kErrOutOfRange);
+            g2p_accumulate<D>(o, g, fx, w, v, C);
+          }
+        }
+        scale_mat<D>(C, P.cscale);
+#pragma unroll
+        for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];  // advection, src/nclr.h:229
+        Mat<D> F = load_mat<D>(s.F, st, p);
+        float Jp = s.Jp[p];
+        const int material = s.mat ? (int)s.mat[p] : P.model;
+        const Mat<D> R = update_F<D, kRef>(C, F, Jp, material, P.dt);
+#pragma unroll
+        for (int d = 0; d < D; ++d) s.x[(size_t)d * st + p] = x[d];
+        store_mat<D>(s.F, st, p, F);
+        s.Jp[p] = Jp;
+        if (kFinal) {
+#pragma unroll
+          for (int d = 0; d < D; ++d) s.v[(size_t)d * st + p] = v[d];
+          store_mat<D>(s.C, st, p, C);
+        }
+
+        // ---- P2G of the next step: stress, stencil ----
+        m = s.mass[p];
+        A = fused_affine<D>(F, R, C, Jp, m, s.vol[p], material, P);
+#pragma unroll
+        for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
+        stencil<D>(x, P.inv_dx, base, fx_s, w_s);
+        fast_s = true;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          lb[d] = base[d] - org[d];
+          fast_s &= lb[d] >= 0 && lb[d] + 2 < T && base[d] >= 0 && base[d] + 2 < N;
+        }
+        tb_s = tile_index<D>(lb[0], lb[1], lb[2]);
+        if (!fast_s) {  // outside the tile: straight to G
+          const int64_t f0 = flat_index<D>(base, N);
+#pragma unroll 1
+          for (int o = 0; o < S; ++o) {
+            const int64_t f = stencil_flat<D>(f0, o, N);
+            if (f < 0 || f >= P.nodes) {
+              atomicOr(err_next, kErrOutOfRange);
+              continue;
+            }
+            float c[4];
+            p2g_contrib<D>(o, fx_s, w_s, mv, m, A, P.dx, c);
+            red_add_v4(G + f, c[0], c[1], c[2], c[3]);
+          }
+        }
+      }
+      // ---- P2G into this warp's tile.  Shared-memory FP32 atomics are compare-and-swap
+      // loops, so the tile is updated with plain read-modify-writes instead: lanes with the
+      // same stencil base go in separate rounds (rare: consecutive slots are in different
+      // cells), so within a round every lane writes a different node for each
+      // stencil offset; __syncwarp orders the offsets.
+      const bool tile_lane = valid && fast_s;
+      const int key = tile_lane ? tb_s : -1 - lane;
+      const unsigned same = __match_any_sync(0xffffffffu, key);
+      const int rank = __popc(same & ((1u << lane) - 1u));
+      const int rounds = (int)__reduce_max_sync(0xffffffffu, (unsigned)rank) + 1;
+      for (int r = 0; r < rounds; ++r) {
+        const bool act = tile_lane && rank == r;
+#pragma unroll
+        for (int o = 0; o < S; ++o) {
+          if (act) {
+            float c[4];
+            p2g_contrib<D>(o, fx_s, w_s, mv, m, A, P.dx, c);
+            const int ti = tb_s + tile_offset<D>(o);
+            float4 a = mytile[ti];
+            a.x += c[0];
+            a.y += c[1];
+            a.z += c[2];
+            a.w += c[3];
+            mytile[ti] = a;
+          }
+          __syncwarp();
+        }
+      }
+    }
+    __syncthreads();
+
+    for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
+      int g[D], l[3] = {0, 0, 0};
+      bool in = true;
+      int r = t;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        l[d] = r % T;
+        g[d] = org[d] + l[d];
+        r /= T;
+        in &= g[d] >= 0 && g[d] < N;
+      }
+      const int ti = tile_index<D>(l[0], l[1], l[2]);
+      float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int wi = 0; wi < kWarps; ++wi) {
+        const float4 g4 = gt[wi * GS + ti];
+        a[0] += g4.x;
+        a[1] += g4.y;
+        a[2] += g4.z;
+        a[3] += g4.w;
+      }
+      if (a[0] == 0.0f && a[1] == 0.0f && a[2] == 0.0f && a[3] == 0.0f) continue;
+      if (in) red_add_v4(G + flat_index<D>(g, N), a[0], a[1], a[2], a[3]);
+    }
+  }
+}
+
+// Dynamic shared memory of g2p2g: the V tile plus one G tile per warp.
+template <int D>
+constexpr size_t g2p2g_smem_bytes() {
+  return sizeof(float4) * Tiling<D>::SIZE * (1 + kG2P2GThreads / 32);
+}
+
+// ---------------------------------------------------------------------------------------
+// grid() export (src/nclr.h:87): V is already the post-update grid; copy it out.
+// ---------------------------------------------------------------------------------------
+template <int D>
+__global__ void copy_vgrid_kernel(const float4 *__restrict__ V, int64_t nodes,
+                                  float *__restrict__ vel, float *__restrict__ mass) {
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nodes) return;
+  const float4 g = V[f];
+  vel[f * D] = g.x;
+  vel[f * D + 1] = g.y;
+  if (D == 3) vel[f * D + D - 1] = g.z;
+  mass[f] = g.w;
+}
+
+// grid() of an accumulation grid: applies the grid update on the way out.
 template <int D>
 __global__ void export_grid_kernel(const float4 *__restrict__ grid, Params P,
                                    float *__restrict__ vel, float *__restrict__ mass) {
@@ -305,53 +516,61 @@ __global__ void import_particles_kernel(PState s, int n, const float *__restrict
 }
 
 // ---------------------------------------------------------------------------------------
-// Sorting slots by grid cell (a one-digit counting sort over the (res+1)^dim cell keys):
-// keys + ranks, exclusive scan of the per-cell counts, then every field moves to
-// start[key] + rank in the other buffer.
+// Sorting slots by grid block and, inside a block, by cell (a one-digit counting sort over
+// nb^dim * cells-per-block keys): keys + ranks, exclusive scan of the counts, the list of
+// non-empty blocks, then the
+// fields the step reads (x, F, Jp, mass, volume, id, material) move to start[key] + rank in
+// the other buffer.  v and C do not move: they are rewritten by the last step of every
+// advance() call before anyone reads them.
 // ---------------------------------------------------------------------------------------
 template <int D>
-__global__ void sort_keys_kernel(const float *__restrict__ xs, int stride, Params P,
-                                 int *__restrict__ key, int *__restrict__ rank,
-                                 int *__restrict__ count) {
+__global__ void block_keys_kernel(const float *__restrict__ xs, int stride, Params P,
+                                  int *__restrict__ key, int *__restrict__ rank,
+                                  int *__restrict__ count) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P.n) return;
-  int b[D];
+  constexpr int BS = Tiling<D>::BS;
+  int kb = 0, kc = 0;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    const int bd = __float2int_rz(xs[(size_t)d * stride + p] * P.inv_dx - 0.5f);
-    b[d] = min(max(bd, 0), P.N - 1);
+    const int bd = min(max(__float2int_rz(xs[(size_t)d * stride + p] * P.inv_dx - 0.5f), 0), P.N - 1);
+    kb = kb * P.nb + bd / BS;
+    kc = kc * BS + bd % BS;
   }
-  const int k = (int)flat_index<D>(b, P.N);
+  const int k = kb * Tiling<D>::CPB + kc;  // block-major, then the cell inside the block
   key[p] = k;
   rank[p] = atomicAdd(count + k, 1);
 }
 
+// Destination of a particle inside its block: the block's particles are stored cell by cell
+// in rounds -- the first particle of every non-empty cell (cells in x-major order), then the
+// second of every cell that has two, and so on -- so consecutive slots lie in different,
+// neighbouring cells.  Particle `rank` of cell c goes to
+//   start[block] + sum_c' min(count[c'], rank) + #{c' < c : count[c'] > rank}.
 template <int D>
-__global__ void sort_move_kernel(PState src, PState dst, int n, const float4 *__restrict__ pay_src,
-                                 float4 *__restrict__ pay_dst, const int *__restrict__ key,
-                                 const int *__restrict__ rank, const int *__restrict__ start) {
+__global__ void sort_move_kernel(PState src, PState dst, int n, const int *__restrict__ key,
+                                 const int *__restrict__ rank, const int *__restrict__ start,
+                                 const int *__restrict__ count) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  const int q = start[key[p]] + rank[p];
+  constexpr int CPB = Tiling<D>::CPB;
+  const int k = key[p], r = rank[p];
+  const int b0 = k - k % CPB, c = k % CPB;
+  int q = start[b0];
+  for (int cc = 0; cc < CPB; ++cc) {
+    const int m = __ldg(count + b0 + cc);
+    q += min(m, r) + ((cc < c && m > r) ? 1 : 0);
+  }
   const int ss = src.stride, ds = dst.stride;
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    dst.x[(size_t)d * ds + q] = src.x[(size_t)d * ss + p];
-    dst.v[(size_t)d * ds + q] = src.v[(size_t)d * ss + p];
-  }
+  for (int d = 0; d < D; ++d) dst.x[(size_t)d * ds + q] = src.x[(size_t)d * ss + p];
 #pragma unroll
-  for (int c = 0; c < D * D; ++c) {
-    dst.F[(size_t)c * ds + q] = src.F[(size_t)c * ss + p];
-    dst.C[(size_t)c * ds + q] = src.C[(size_t)c * ss + p];
-  }
+  for (int cmp = 0; cmp < D * D; ++cmp) dst.F[(size_t)cmp * ds + q] = src.F[(size_t)cmp * ss + p];
   dst.Jp[q] = src.Jp[p];
   dst.mass[q] = src.mass[p];
   dst.vol[q] = src.vol[p];
   dst.id[q] = src.id[p];
   if (src.mat) dst.mat[q] = src.mat[p];
-  constexpr int R = PayloadRecs<D>::value;
-#pragma unroll
-  for (int r = 0; r < R; ++r) pay_dst[(size_t)q * R + r] = pay_src[(size_t)p * R + r];
 }
 
 // ---------------------------------------------------------------------------------------
@@ -360,33 +579,52 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const float4 *__
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 template <int D>
-void launch_prepare(const PState &s, const Params &P, float4 *pay, bool ref, cudaStream_t st) {
+void launch_p2g_state(const PState &s, const Params &P, float4 *G, int *err, cudaStream_t st) {
   if (P.n == 0) return;
-  if (ref)
-    prepare_payload_kernel<D, true><<<blocks_for(P.n, 256), 256, 0, st>>>(s, P, pay);
-  else
-    prepare_payload_kernel<D, false><<<blocks_for(P.n, 256), 256, 0, st>>>(s, P, pay);
+  p2g_state_kernel<D><<<blocks_for(P.n, 256), 256, 0, st>>>(s, P, G, err);
 }
 
 template <int D>
-void launch_p2g(const float4 *pay, const Params &P, float4 *grid, int *err, int K, cudaStream_t st) {
+void launch_grid_sweep(float4 *G, float4 *V, const Params &P, int *work, int sms, cudaStream_t st) {
+  int64_t blocks = blocks_for(P.nodes, 256);
+  if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
+  if (blocks < 1) blocks = 1;
+  grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, P, work);
+}
+
+template <int D>
+void launch_g2p2g(const PState &s, const Params &P, const float4 *V, float4 *G, const int *blocks,
+                  const int *nactive, const int *bstart, int *work, int *err_now, int *err_next,
+                  bool ref, bool final_step, int ctas, cudaStream_t st) {
   if (P.n == 0) return;
-  const int threads = 128;
-  switch (K) {
-    case 4: p2g_kernel<D, 4><<<blocks_for((P.n + 3) / 4, threads), threads, 0, st>>>(pay, P, grid, err); break;
-    case 16: p2g_kernel<D, 16><<<blocks_for((P.n + 15) / 16, threads), threads, 0, st>>>(pay, P, grid, err); break;
-    default: p2g_kernel<D, 8><<<blocks_for((P.n + 7) / 8, threads), threads, 0, st>>>(pay, P, grid, err); break;
+#define MPM_G2P2G(R, FI)                                                                 \
+  g2p2g_kernel<D, R, FI><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(              \
+      s, P, V, G, blocks, nactive, bstart, work, err_now, err_next)
+  if (ref) {
+    if (final_step) MPM_G2P2G(true, true); else MPM_G2P2G(true, false);
+  } else {
+    if (final_step) MPM_G2P2G(false, true); else MPM_G2P2G(false, false);
   }
+#undef MPM_G2P2G
 }
 
 template <int D>
-void launch_g2p(const PState &s, const Params &P, const float4 *grid, float4 *pay, int *err,
-                bool ref, cudaStream_t st) {
-  if (P.n == 0) return;
-  if (ref)
-    g2p_kernel<D, true><<<blocks_for(P.n, 128), 128, 0, st>>>(s, P, grid, pay, err);
-  else
-    g2p_kernel<D, false><<<blocks_for(P.n, 128), 128, 0, st>>>(s, P, grid, pay, err);
+int g2p2g_ctas_per_sm() {
+  // the tiles exceed the default 48 KB of dynamic shared memory in 3D
+  const int bytes = (int)g2p2g_smem_bytes<D>();
+  cudaFuncSetAttribute(g2p2g_kernel<D, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, g2p2g_kernel<D, true, false>, kG2P2GThreads,
+                                                g2p2g_smem_bytes<D>());
+  return n > 0 ? n : 1;
+}
+
+template <int D>
+void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st) {
+  copy_vgrid_kernel<D><<<blocks_for(nodes, 256), 256, 0, st>>>(V, nodes, vel, mass);
 }
 
 template <int D>
@@ -409,34 +647,36 @@ void launch_import_particles(const PState &s, int n, const float *x, const float
 }
 
 template <int D>
-void launch_sort_keys(const PState &s, const Params &P, int *key, int *rank, int *count, cudaStream_t st) {
+void launch_block_keys(const PState &s, const Params &P, int *key, int *rank, int *count, cudaStream_t st) {
   if (P.n == 0) return;
-  sort_keys_kernel<D><<<blocks_for(P.n, 256), 256, 0, st>>>(s.x, s.stride, P, key, rank, count);
+  block_keys_kernel<D><<<blocks_for(P.n, 256), 256, 0, st>>>(s.x, s.stride, P, key, rank, count);
 }
 
 template <int D>
-void launch_sort_move(const PState &src, const PState &dst, int n, const float4 *pay_src,
-                      float4 *pay_dst, const int *key, const int *rank, const int *start,
-                      cudaStream_t st) {
+void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank,
+                      const int *start, const int *count, cudaStream_t st) {
   if (n == 0) return;
-  sort_move_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, pay_src, pay_dst, key, rank, start);
+  sort_move_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, key, rank, start, count);
 }
 
-#define MPM_INSTANTIATE(D)                                                                      \
-  template void launch_prepare<D>(const PState &, const Params &, float4 *, bool, cudaStream_t); \
-  template void launch_p2g<D>(const float4 *, const Params &, float4 *, int *, int, cudaStream_t); \
-  template void launch_g2p<D>(const PState &, const Params &, const float4 *, float4 *, int *,   \
-                              bool, cudaStream_t);                                              \
-  template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,         \
-                                      cudaStream_t);                                            \
-  template void launch_export_particles<D>(const PState &, int, float *, float *, float *,      \
-                                           float *, float *, cudaStream_t);                     \
-  template void launch_import_particles<D>(const PState &, int, const float *, const float *,   \
-                                           const float *, const float *, const float *,         \
-                                           cudaStream_t);                                       \
-  template void launch_sort_keys<D>(const PState &, const Params &, int *, int *, int *,        \
-                                    cudaStream_t);                                              \
-  template void launch_sort_move<D>(const PState &, const PState &, int, const float4 *,        \
-                                    float4 *, const int *, const int *, const int *, cudaStream_t);
+#define MPM_INSTANTIATE(D)                                                                       \
+  template void launch_p2g_state<D>(const PState &, const Params &, float4 *, int *, cudaStream_t); \
+  template void launch_grid_sweep<D>(float4 *, float4 *, const Params &, int *, int, cudaStream_t); \
+  template void launch_g2p2g<D>(const PState &, const Params &, const float4 *, float4 *,        \
+                                const int *, const int *, const int *, int *, int *, int *, bool, \
+                                bool, int, cudaStream_t);                                        \
+  template int g2p2g_ctas_per_sm<D>();                                                           \
+  template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
+  template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \
+                                      cudaStream_t);                                             \
+  template void launch_export_particles<D>(const PState &, int, float *, float *, float *,       \
+                                           float *, float *, cudaStream_t);                      \
+  template void launch_import_particles<D>(const PState &, int, const float *, const float *,    \
+                                           const float *, const float *, const float *,          \
+                                           cudaStream_t);                                        \
+  template void launch_block_keys<D>(const PState &, const Params &, int *, int *, int *,        \
+                                     cudaStream_t);                                              \
+  template void launch_sort_move<D>(const PState &, const PState &, int, const int *, const int *, \
+                                    const int *, const int *, cudaStream_t);
 
 }  // namespace mpm

@@ -1,8 +1,11 @@
 // Host side of the C ABI in include/nclr_gpu.h: one simulation handle = one CUDA stream, the
-// device-resident particle store (two SoA buffers that the cell sort ping-pongs between),
-// the P2G payload, the dense grid and the sort scratch.  advance() enqueues
-//   [every sort_interval steps: cell keys -> scan -> move]  zero grid -> P2G -> G2P
-// per step, replaying a captured CUDA graph for whole sort intervals.
+// device-resident particle store (two SoA buffers that the block sort ping-pongs between),
+// the two grids (G: the coming step's P2G accumulator; V: the last step's updated grid) and
+// the sort scratch.  advance() enqueues per step
+//   [every sort_interval steps: block keys -> scan -> active-block list -> move]
+//   grid sweep (V = grid_op(G), G = 0) -> g2p2g (G2P of this step + P2G of the next)
+// after a stand-alone P2G when the particle state was just uploaded, replaying a captured
+// CUDA graph for whole sort intervals.  Only the last step of a call writes v and C.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -29,13 +32,21 @@ struct nclr_sim {
 
   void *slab[2] = {nullptr, nullptr};  // particle SoA buffers
   PState ps[2]{};
-  float4 *pay[2] = {nullptr, nullptr};
   int cur = 0;
+  int sms = 1;         // streaming multiprocessors of the device
+  int g2p2g_ctas = 1;  // persistent CTAs of the fused kernel
 
-  float4 *grid = nullptr;
+  float4 *G = nullptr;  // P2G accumulator of the coming step
+  float4 *V = nullptr;  // updated grid of the last step (grid())
   int *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *tile_sums = nullptr;
-  int *err_d = nullptr;
-  int *err_h = nullptr;  // pinned
+  int *blocks = nullptr;  // non-empty blocks of the last sort
+  int *nblocks_active = nullptr;
+  int *work = nullptr;    // fused kernel's block counter
+  int *err_d = nullptr;   // [0]: this call's steps, [1]: the P2G after the call's last step
+  int *err_h = nullptr;   // pinned, 2 ints
+  int deferred_err = 0;   // [1] of the previous call: reported by the next one
+  bool acc_valid = false; // G holds the P2G of the coming step
+  bool need_sort = true;  // the block lists do not describe the particles yet
 
   float *staging = nullptr;       // particle-major transfer buffer (n * row floats)
   float *grid_staging = nullptr;  // grid export buffer (nodes * (dim + 1) floats)
@@ -166,41 +177,51 @@ void collect_profile(nclr_sim *s) {
   s->pending.clear();
 }
 
-// Enqueues one step (optionally preceded by the cell sort) on the handle's stream.
-void enqueue_step(nclr_sim *s, bool sort) {
-  const int64_t nodes = s->P.nodes;
+// Enqueues the block sort of the current buffer into the other one.
+void enqueue_sort(nclr_sim *s) {
+  const int nb = s->P.nblocks;
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
-    if (sort && s->n > 1) {
-      phase(s, NCLR_PHASE_SORT, 5, [&] {
-        cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)nodes, s->stream);
-        mpm::launch_sort_keys<D>(s->ps[s->cur], s->P, s->key, s->rank, s->count, s->stream);
-        mpm::launch_exclusive_scan(s->count, nodes, s->start, s->tile_sums, s->stream);
-        mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->pay[s->cur],
-                                 s->pay[s->cur ^ 1], s->key, s->rank, s->start, s->stream);
-      });
-      s->cur ^= 1;
-      s->launches += 5;  // keys, 3 scan kernels, move
-    }
-    phase(s, NCLR_PHASE_CLEAR, 0, [&] {
-      cudaMemsetAsync(s->grid, 0, sizeof(float4) * (size_t)nodes, s->stream);
+    constexpr int cpb = mpm::Tiling<D>::CPB;
+    const int64_t nkeys = (int64_t)nb * cpb;
+    phase(s, NCLR_PHASE_SORT, 6, [&] {
+      cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)nkeys, s->stream);
+      cudaMemsetAsync(s->nblocks_active, 0, sizeof(int), s->stream);
+      mpm::launch_block_keys<D>(s->ps[s->cur], s->P, s->key, s->rank, s->count, s->stream);
+      mpm::launch_exclusive_scan(s->count, nkeys, s->start, s->tile_sums, s->stream);
+      mpm::launch_compact_blocks(s->start, nb, cpb, s->blocks, s->nblocks_active, s->stream);
+      mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->key, s->rank,
+                               s->start, s->count, s->stream);
     });
+  });
+  s->cur ^= 1;
+  s->launches += 6;  // keys, 3 scan kernels, compaction, move
+}
+
+// Enqueues one step (optionally preceded by the block sort) on the handle's stream.  The
+// last step of a call writes v and C and reports the next step's P2G errors separately.
+void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
+  if (sort && s->n > 0) enqueue_sort(s);
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int D = decltype(dc)::value;
+    phase(s, NCLR_PHASE_GRID, 1, [&] {
+      mpm::launch_grid_sweep<D>(s->G, s->V, s->P, s->work, s->sms, s->stream);
+    });
+    s->launches += 1;
     if (s->n > 0) {
-      phase(s, NCLR_PHASE_P2G, 1, [&] {
-        mpm::launch_p2g<D>(s->pay[s->cur], s->P, s->grid, s->err_d,
-                           s->opt.p2g_particles_per_thread, s->stream);
+      phase(s, NCLR_PHASE_G2P2G, 1, [&] {
+        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P, s->V, s->G, s->blocks, s->nblocks_active,
+                             s->start, s->work, s->err_d, final_step ? s->err_d + 1 : s->err_d,
+                             s->ref, final_step, s->g2p2g_ctas, s->stream);
       });
-      phase(s, NCLR_PHASE_G2P, 1, [&] {
-        mpm::launch_g2p<D>(s->ps[s->cur], s->P, s->grid, s->pay[s->cur], s->err_d, s->ref,
-                           s->stream);
-      });
-      s->launches += 2;
+      s->launches += 1;
     }
   });
 }
 
 bool sort_due(const nclr_sim *s) {
-  return s->opt.sort_interval > 0 && s->steps_since_sort % s->opt.sort_interval == 0;
+  return s->need_sort ||
+         (s->opt.sort_interval > 0 && s->steps_since_sort % s->opt.sort_interval == 0);
 }
 
 int64_t chunk_steps(const nclr_sim *s) { return s->opt.sort_interval > 0 ? s->opt.sort_interval : 16; }
@@ -213,7 +234,7 @@ nclr_status capture_graph(nclr_sim *s, int parity) {
   cudaGraph_t g = nullptr;
   CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const int64_t k = chunk_steps(s);
-  for (int64_t i = 0; i < k; ++i) enqueue_step(s, s->opt.sort_interval > 0 && i == 0);
+  for (int64_t i = 0; i < k; ++i) enqueue_step(s, s->opt.sort_interval > 0 && i == 0, false);
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   s->graph_launches = s->launches - saved_launches;
   s->launches = saved_launches;
@@ -247,16 +268,22 @@ void fill_params(nclr_sim *s, int model, float dt, float E, float nu, float grav
   int64_t nodes = 1;
   for (int d = 0; d < s->dim; ++d) nodes *= P.N;
   P.nodes = nodes;
+  const int bs = (s->dim == 3) ? mpm::Tiling<3>::BS : mpm::Tiling<2>::BS;
+  P.nb = (P.N + bs - 1) / bs;
+  P.nblocks = 1;
+  for (int d = 0; d < s->dim; ++d) P.nblocks *= P.nb;
 }
 
-// Upload of caller-ordered rows that already sit in device memory, then the P2G payload.
+// Upload of caller-ordered rows that already sit in device memory; the next advance() then
+// recomputes the coming P2G from them and re-sorts.
 nclr_status import_rows(nclr_sim *s, const float *x, const float *v, const float *F,
                         const float *C, const float *Jp) {
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     mpm::launch_import_particles<D>(s->ps[s->cur], (int)s->n, x, v, F, C, Jp, s->stream);
-    mpm::launch_prepare<D>(s->ps[s->cur], s->P, s->pay[s->cur], s->ref, s->stream);
   });
+  s->acc_valid = false;  // the coming step's P2G must be recomputed from the new state
+  s->need_sort = true;
   return check_launch(s, "import particles");
 }
 
@@ -288,8 +315,11 @@ void release(nclr_sim *s) {
   for (auto &g : s->graph)
     if (g) cudaGraphExecDestroy(g);
   for (auto p : s->slab) cudaFree(p);
-  for (auto p : s->pay) cudaFree(p);
-  cudaFree(s->grid);
+  cudaFree(s->G);
+  cudaFree(s->V);
+  cudaFree(s->blocks);
+  cudaFree(s->nblocks_active);
+  cudaFree(s->work);
   cudaFree(s->key);
   cudaFree(s->rank);
   cudaFree(s->count);
@@ -382,19 +412,27 @@ nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, cons
   const int64_t nodes = s->P.nodes;
   for (int b = 0; b < 2; ++b)
     if ((st = alloc_particles(s, b)) != NCLR_OK) return bail(st);
-  const int R = (dim == 3) ? 4 : 3;
   const size_t np = (size_t)std::max<int64_t>(n, 1);
-  for (int b = 0; b < 2; ++b) CREATE_TRY(cudaMalloc((void **)&s->pay[b], sizeof(float4) * R * np));
-  CREATE_TRY(cudaMalloc((void **)&s->grid, sizeof(float4) * (size_t)nodes));
+  const size_t nblk = (size_t)s->P.nblocks;
+  const size_t nkeys = nblk * (size_t)(dim == 3 ? mpm::Tiling<3>::CPB : mpm::Tiling<2>::CPB);
+  CREATE_TRY(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
+  s->g2p2g_ctas = s->sms * (dim == 3 ? mpm::g2p2g_ctas_per_sm<3>() : mpm::g2p2g_ctas_per_sm<2>());
+  CREATE_TRY(cudaMalloc((void **)&s->G, sizeof(float4) * (size_t)nodes));
+  CREATE_TRY(cudaMalloc((void **)&s->V, sizeof(float4) * (size_t)nodes));
   CREATE_TRY(cudaMalloc((void **)&s->key, sizeof(int) * np));
   CREATE_TRY(cudaMalloc((void **)&s->rank, sizeof(int) * np));
-  CREATE_TRY(cudaMalloc((void **)&s->count, sizeof(int) * (size_t)nodes));
-  CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (size_t)(nodes + 1)));
-  CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles(nodes), 1)));
-  CREATE_TRY(cudaMalloc((void **)&s->err_d, sizeof(int)));
-  CREATE_TRY(cudaMallocHost((void **)&s->err_h, sizeof(int)));
-  CREATE_TRY(cudaMemsetAsync(s->err_d, 0, sizeof(int), s->stream));
-  CREATE_TRY(cudaMemsetAsync(s->grid, 0, sizeof(float4) * (size_t)nodes, s->stream));
+  CREATE_TRY(cudaMalloc((void **)&s->count, sizeof(int) * nkeys));
+  CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (nkeys + 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles((int64_t)nkeys), 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->blocks, sizeof(int) * nblk));
+  CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, sizeof(int)));
+  CREATE_TRY(cudaMalloc((void **)&s->work, sizeof(int)));
+  CREATE_TRY(cudaMalloc((void **)&s->err_d, 2 * sizeof(int)));
+  CREATE_TRY(cudaMallocHost((void **)&s->err_h, 2 * sizeof(int)));
+  CREATE_TRY(cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int), s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)nodes, s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->V, 0, sizeof(float4) * (size_t)nodes, s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->nblocks_active, 0, sizeof(int), s->stream));
 
   if (n > 0) {
     // Per-particle scalars go straight into the SoA (component stride == n there).
@@ -445,35 +483,53 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
   if (nsteps < 0) return fail(s, NCLR_ERR_INVALID, "nsteps < 0");
   if (nsteps == 0) return NCLR_OK;
   CUDA_TRY(s, cudaSetDevice(s->device));
-  CUDA_TRY(s, cudaMemsetAsync(s->err_d, 0, sizeof(int), s->stream));
+  CUDA_TRY(s, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int), s->stream));
   s->launches = 0;
+  if (!s->acc_valid) {  // the first step's P2G, from the uploaded state
+    s->deferred_err = 0;  // an error of the discarded P2G no longer applies
+    dispatch_dim(s->dim, [&](auto dc) {
+      constexpr int D = decltype(dc)::value;
+      phase(s, NCLR_PHASE_P2G, 1, [&] {
+        mpm::launch_p2g_state<D>(s->ps[s->cur], s->P, s->G, s->err_d, s->stream);
+      });
+    });
+    if (s->n > 0) s->launches += 1;
+    s->acc_valid = true;
+  }
   int64_t left = nsteps;
   const int64_t chunk = chunk_steps(s);
   while (left > 0) {
-    const bool at_boundary = s->opt.sort_interval == 0 || sort_due(s);
-    if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left >= chunk) {
+    const bool sort = sort_due(s);
+    const bool at_boundary = !s->need_sort && (s->opt.sort_interval == 0 || sort);
+    if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left - 1 >= chunk) {
       if (!s->graph[s->cur]) {
         nclr_status st = capture_graph(s, s->cur);
         if (st != NCLR_OK) return st;
       }
       CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur], s->stream));
       s->launches += s->graph_launches;
-      if (s->opt.sort_interval > 0 && s->n > 1) s->cur ^= 1;
+      if (s->opt.sort_interval > 0) s->cur ^= 1;
       s->steps_since_sort += chunk;
       left -= chunk;
       continue;
     }
-    enqueue_step(s, sort_due(s));
+    enqueue_step(s, sort, left == 1);
+    if (sort) {
+      s->need_sort = false;
+      s->steps_since_sort = 0;
+    }
     ++s->steps_since_sort;
     --left;
   }
   nclr_status st = check_launch(s, "advance");
   if (st != NCLR_OK) return st;
   s->stepped = true;
-  CUDA_TRY(s, cudaMemcpyAsync(s->err_h, s->err_d, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaMemcpyAsync(s->err_h, s->err_d, 2 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(s, cudaStreamSynchronize(s->stream));
   collect_profile(s);
-  if (*s->err_h & mpm::kErrOutOfRange)
+  const int errs = s->err_h[0] | s->deferred_err;
+  s->deferred_err = s->err_h[1];
+  if (errs & mpm::kErrOutOfRange)
     return fail(s, NCLR_ERR_OUT_OF_RANGE,
                 "a particle's stencil left the grid (the reference's vector::at throws "
                 "std::out_of_range here)");
@@ -555,7 +611,7 @@ nclr_status nclr_get_grid(nclr_sim *s, float *velocity, float *mass) {
   float *dv = s->grid_staging, *dm = dv + nodes * D;
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int DD = decltype(dc)::value;
-    mpm::launch_export_grid<DD>(s->grid, s->P, dv, dm, s->stream);
+    mpm::launch_copy_vgrid<DD>(s->V, s->P.nodes, dv, dm, s->stream);
   });
   nclr_status st = check_launch(s, "export grid");
   if (st != NCLR_OK) return st;
@@ -591,7 +647,7 @@ nclr_status nclr_count_active_nodes(nclr_sim *s, int64_t *active_nodes) {
   CUDA_TRY(s, cudaSetDevice(s->device));
   if (!s->active_d) CUDA_TRY(s, cudaMalloc((void **)&s->active_d, sizeof(unsigned long long)));
   CUDA_TRY(s, cudaMemsetAsync(s->active_d, 0, sizeof(unsigned long long), s->stream));
-  mpm::launch_count_active(s->grid, s->P.nodes, s->active_d, s->stream);
+  mpm::launch_count_active(s->V, s->P.nodes, s->active_d, s->stream);
   nclr_status st = check_launch(s, "count active nodes");
   if (st != NCLR_OK) return st;
   unsigned long long h = 0;

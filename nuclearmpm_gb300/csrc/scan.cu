@@ -1,4 +1,6 @@
-// Exclusive prefix sum over the per-cell particle counts of the counting sort:
+// Dimension-free helpers of the block sort: the exclusive prefix sum over the per-block
+// particle counts of the counting sort, the compaction of the non-empty blocks and a count of
+// grid nodes holding mass.  The scan:
 // (1) per-tile totals, (2) one block scans the tile totals, (3) each tile scans its counts
 // and adds its tile offset.  Tiles are 2048 counts (256 threads x 8), read as int4 pairs
 // where aligned.
@@ -101,7 +103,29 @@ __global__ void __launch_bounds__(kThreads) count_active_kernel(const float4 *__
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
 }
 
+// The list of non-empty blocks (start[b*cpb] < start[(b+1)*cpb]); one atomic per warp for
+// the append position.
+__global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks, int cpb,
+                                      int *__restrict__ list, int *__restrict__ nlist) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = b < nblocks && start[(int64_t)(b + 1) * cpb] > start[(int64_t)b * cpb];
+  const unsigned mask = __ballot_sync(0xffffffffu, act);
+  if (!mask) return;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(nlist, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (act) list[base + __popc(mask & ((1u << lane) - 1u))] = b;
+}
+
 }  // namespace
+
+void launch_compact_blocks(const int *start, int nblocks, int cpb, int *list, int *nlist,
+                           cudaStream_t st) {
+  if (nblocks <= 0) return;
+  compact_blocks_kernel<<<(unsigned)((nblocks + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+      start, nblocks, cpb, list, nlist);
+}
 
 void launch_count_active(const float4 *grid, int64_t nodes, unsigned long long *out, cudaStream_t st) {
   if (nodes <= 0) return;
