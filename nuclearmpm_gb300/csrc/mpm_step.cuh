@@ -6,7 +6,7 @@
 //   g2p2g:       per block of particles: G2P of step k from a shared-memory tile of V,
 //                F/C/Jp update, then the P2G of step k+1 from the updated particle into a
 //                shared-memory tile of G, flushed once per block with vector reductions.
-// The P2G of the first step after an upload comes from p2g_state.
+// The P2G of the first step after an upload is g2p2g in its P2G-only mode.
 #pragma once
 
 #include "mpm_device.cuh"
@@ -153,63 +153,144 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
   return R;
 }
 
-// ---------------------------------------------------------------------------------------
-// p2g_state: the P2G of the coming step from the stored particle state (after an upload):
-// stress + APIC affine (src/nclr.h:313-337) and the 3^dim contributions, reduced into G.
-// ---------------------------------------------------------------------------------------
+// Grid-block activity flags (one byte per block of BS^dim nodes, the same blocks as the
+// particle blocks): bit 0 = the pending P2G accumulator G has contributions there, bit 1 = V
+// (the last step's grid) may be non-zero there.  Writers of G set bit 0 with a plain
+// read-modify-write (every writer stores the same value, and bit 1 only changes in the
+// sweep); the sweep visits only flagged blocks.
+enum : uint8_t { kPending = 1, kVNonzero = 2 };
+
+// Marks the blocks the stencil at base[] adds to (slow paths).  A stencil whose per-axis
+// index leaves the grid wraps into another row (the reference's flat indexing): then every
+// node's block is marked from its flat index, else the <= 2 blocks per axis.
 template <int D>
-__global__ void __launch_bounds__(256) p2g_state_kernel(PState s, Params P, float4 *__restrict__ G,
-                                                        int *err) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.n) return;
-  const int st = s.stride;
-  float x[D], mv[D];
-  const float m = s.mass[p], vol = s.vol[p];
+__device__ __forceinline__ void mark_node(uint8_t *flags, int64_t f, const Params &P);
+
+template <int D>
+__device__ void mark_stencil(uint8_t *flags, const int base[D], const Params &P) {
+  constexpr int BS = Tiling<D>::BS;
+  bool wraps = false;
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    x[d] = s.x[(size_t)d * st + p];
-    mv[d] = s.v[(size_t)d * st + p] * m;
-  }
-  const Mat<D> F = load_mat<D>(s.F, st, p);
-  const Mat<D> C = load_mat<D>(s.C, st, p);
-  const int material = s.mat ? (int)s.mat[p] : P.model;
-  const Mat<D> A = fused_affine<D>(F, polar_R(F), C, s.Jp[p], m, vol, material, P);
-  int base[D];
-  float fx[D], w[3][D];
-  stencil<D>(x, P.inv_dx, base, fx, w);
-  const int64_t f0 = flat_index<D>(base, P.N);
-  constexpr int S = (D == 3) ? 27 : 9;
-#pragma unroll 1
-  for (int o = 0; o < S; ++o) {
-    const int64_t f = stencil_flat<D>(f0, o, P.N);
-    if (f < 0 || f >= P.nodes) {
-      atomicOr(err, kErrOutOfRange);
-      continue;
+  for (int d = 0; d < D; ++d) wraps |= base[d] < 0 || base[d] + 2 >= P.N;
+  if (wraps) {
+    const int64_t f0 = flat_index<D>(base, P.N);
+    constexpr int S = (D == 3) ? 27 : 9;
+    for (int o = 0; o < S; ++o) {
+      int oi = (D == 3) ? o / 9 : o / 3, oj = (D == 3) ? (o / 3) % 3 : o % 3, ok = (D == 3) ? o % 3 : 0;
+      const int64_t f = (D == 3) ? f0 + ((int64_t)oi * P.N + oj) * P.N + ok : f0 + (int64_t)oi * P.N + oj;
+      if (f >= 0 && f < P.nodes) mark_node<D>(flags, f, P);
     }
-    float c[4];
-    p2g_contrib<D>(o, fx, w, mv, m, A, P.dx, c);
-    red_add_v4(G + f, c[0], c[1], c[2], c[3]);
+    return;
   }
+  const int i0 = base[0] / BS, i1 = (base[0] + 2) / BS;
+  const int j0 = base[1] / BS, j1 = (base[1] + 2) / BS;
+  const int k0 = base[D - 1] / BS, k1 = (base[D - 1] + 2) / BS;
+  for (int i = i0; i <= i1; ++i)
+    for (int j = j0; j <= j1; ++j) {
+      if (D == 2) {
+        flags[i * P.nb + j] |= kPending;
+        continue;
+      }
+      for (int k = k0; k <= k1; ++k) flags[(i * P.nb + j) * P.nb + k] |= kPending;
+    }
+}
+
+// Marks the block of node f.
+template <int D>
+__device__ __forceinline__ void mark_node(uint8_t *flags, int64_t f, const Params &P) {
+  constexpr int BS = Tiling<D>::BS;
+  int idx[D];
+  unflatten<D>(f, P.N, idx);
+  int blk = 0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) blk = blk * P.nb + idx[d] / BS;
+  flags[blk] |= kPending;
 }
 
 // ---------------------------------------------------------------------------------------
-// grid_sweep: grid_op (src/nclr.h:263-310) on every node: V = update(G); then G = 0 for the
-// next P2G.  Also resets the g2p2g work counter.
+// grid_sweep: grid_op (src/nclr.h:263-310) on the flagged blocks: V = update(G), G = 0, and
+// the flags roll over (pending -> V non-zero).  Blocks never flagged hold V = 0 = update(0)
+// (a massless node's velocity is zero and stays zero through the boundary rule).  One warp
+// per block; also resets the g2p2g work counter.
 // ---------------------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
-                                                         float4 *__restrict__ V, Params P,
+                                                         float4 *__restrict__ V,
+                                                         uint8_t *__restrict__ flags, Params P,
                                                          int *__restrict__ work) {
+  constexpr int BS = Tiling<D>::BS;
+  constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;  // nodes per block
   if (blockIdx.x == 0 && threadIdx.x == 0) *work = 0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < P.nodes; f += stride) {
-    const float4 g = G[f];
-    int idx[D];
-    unflatten<D>(f, P.N, idx);
-    float v[D], m;
-    grid_update<D>(g, idx, P, v, m);
-    V[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
-    G[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < P.nblocks; b += warps) {
+    const uint8_t fl = flags[b];
+    if (!fl) continue;
+    int bc[D];
+    {
+      int r = b;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        bc[d] = (r % P.nb) * BS;
+        r /= P.nb;
+      }
+    }
+    for (int t = lane; t < BN; t += 32) {
+      int idx[D];
+      bool in = true;
+      int r = t;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        idx[d] = bc[d] + r % BS;
+        r /= BS;
+        in &= idx[d] < P.N;
+      }
+      if (!in) continue;
+      const int64_t f = flat_index<D>(idx, P.N);
+      const float4 g = G[f];
+      float v[D], m;
+      grid_update<D>(g, idx, P, v, m);
+      V[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
+      G[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (lane == 0) flags[b] = (fl & kPending) ? kVNonzero : 0;
+  }
+}
+
+// Drops the pending accumulation (after the particle state was replaced): G = 0 on the
+// pending blocks, pending flags cleared; V and its flags stay (they are grid()).
+template <int D>
+__global__ void __launch_bounds__(256) discard_pending_kernel(float4 *__restrict__ G,
+                                                              uint8_t *__restrict__ flags, Params P) {
+  constexpr int BS = Tiling<D>::BS;
+  constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < P.nblocks; b += warps) {
+    const uint8_t fl = flags[b];
+    if (!(fl & kPending)) continue;
+    int bc[D];
+    {
+      int r = b;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        bc[d] = (r % P.nb) * BS;
+        r /= P.nb;
+      }
+    }
+    for (int t = lane; t < BN; t += 32) {
+      int idx[D];
+      bool in = true;
+      int r = t;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        idx[d] = bc[d] + r % BS;
+        r /= BS;
+        in &= idx[d] < P.N;
+      }
+      if (in) G[flat_index<D>(idx, P.N)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (lane == 0) flags[b] = fl & (uint8_t)~kPending;
   }
 }
 
@@ -222,10 +303,14 @@ __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
 // of G (again with a global fallback), then flush the tile with one vector reduction per
 // touched node.
 // ---------------------------------------------------------------------------------------
-template <int D, bool kRef, bool kFinal>
+// kMode: kStep (G2P + next P2G), kFinalStep (also writes v and C), kP2GOnly (the P2G of the
+// coming step from the stored state, after an upload; the particles are sorted already).
+enum : int { kStep = kModeStep, kFinalStep = kModeFinalStep, kP2GOnly = kModeP2GOnly };
+
+template <int D, bool kRef, int kMode>
 __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
     PState s, Params P, const float4 *__restrict__ V, float4 *__restrict__ G,
-    const int *__restrict__ blocks, const int *__restrict__ nactive,
+    uint8_t *__restrict__ flags, const int *__restrict__ blocks, const int *__restrict__ nactive,
     const int *__restrict__ bstart, int *__restrict__ work, int *__restrict__ err_now,
     int *__restrict__ err_next) {
   using Tl = Tiling<D>;
@@ -258,19 +343,21 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
         r /= P.nb;
       }
     }
-    for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
-      int g[D], l[3] = {0, 0, 0};
-      bool in = true;
-      int r = t;
+    if (kMode != kP2GOnly) {
+      for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
+        int g[D], l[3] = {0, 0, 0};
+        bool in = true;
+        int r = t;
 #pragma unroll
-      for (int d = D - 1; d >= 0; --d) {
-        l[d] = r % T;
-        g[d] = org[d] + l[d];
-        r /= T;
-        in &= g[d] >= 0 && g[d] < N;
+        for (int d = D - 1; d >= 0; --d) {
+          l[d] = r % T;
+          g[d] = org[d] + l[d];
+          r /= T;
+          in &= g[d] >= 0 && g[d] < N;
+        }
+        vt[tile_index<D>(l[0], l[1], l[2])] =
+            in ? __ldg(V + flat_index<D>(g, N)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
-      vt[tile_index<D>(l[0], l[1], l[2])] =
-          in ? __ldg(V + flat_index<D>(g, N)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
       gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -291,23 +378,31 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
       float fx_s[D], w_s[3][D], mv[D], m = 0.0f;
       Mat<D> A;
       if (valid) {
-        // ---- G2P of this step ----
         float x[D];
+        Mat<D> F, C, R;
+        float v[D], Jp;
+        const int material = s.mat ? (int)s.mat[p] : P.model;
+        int base[D], lb[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < D; ++d) x[d] = s.x[(size_t)d * st + p];
-        int base[D];
+        if (kMode == kP2GOnly) {
+#pragma unroll
+          for (int d = 0; d < D; ++d) v[d] = s.v[(size_t)d * st + p];
+          F = load_mat<D>(s.F, st, p);
+          C = load_mat<D>(s.C, st, p);
+          Jp = s.Jp[p];
+          R = polar_R(F);
+        } else {
+        // ---- G2P of this step ----
         float fx[D], w[3][D];
         stencil<D>(x, P.inv_dx, base, fx, w);
         bool fast = true;
-        int lb[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           lb[d] = base[d] - org[d];
           fast &= lb[d] >= 0 && lb[d] + 2 < T && base[d] >= 0 && base[d] + 2 < N;
         }
         const int tb = tile_index<D>(lb[0], lb[1], lb[2]);
-        float v[D];
-        Mat<D> C;
 #pragma unroll
         for (int d = 0; d < D; ++d) v[d] = 0.0f;
 #pragma unroll
@@ -333,23 +428,24 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
         scale_mat<D>(C, P.cscale);
 #pragma unroll
         for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];  // advection, src/nclr.h:229
-        Mat<D> F = load_mat<D>(s.F, st, p);
-        float Jp = s.Jp[p];
-        const int material = s.mat ? (int)s.mat[p] : P.model;
-        const Mat<D> R = update_F<D, kRef>(C, F, Jp, material, P.dt);
+        F = load_mat<D>(s.F, st, p);
+        Jp = s.Jp[p];
+        R = update_F<D, kRef>(C, F, Jp, material, P.dt);
 #pragma unroll
         for (int d = 0; d < D; ++d) s.x[(size_t)d * st + p] = x[d];
         store_mat<D>(s.F, st, p, F);
         s.Jp[p] = Jp;
-        if (kFinal) {
+        if (kMode == kFinalStep) {
 #pragma unroll
           for (int d = 0; d < D; ++d) s.v[(size_t)d * st + p] = v[d];
           store_mat<D>(s.C, st, p, C);
+        }
         }
 
         // ---- P2G of the next step: stress, stencil ----
         m = s.mass[p];
         A = fused_affine<D>(F, R, C, Jp, m, s.vol[p], material, P);
+        int *err_p2g = (kMode == kP2GOnly) ? err_now : err_next;
 #pragma unroll
         for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
         stencil<D>(x, P.inv_dx, base, fx_s, w_s);
@@ -366,13 +462,14 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
           for (int o = 0; o < S; ++o) {
             const int64_t f = stencil_flat<D>(f0, o, N);
             if (f < 0 || f >= P.nodes) {
-              atomicOr(err_next, kErrOutOfRange);
+              atomicOr(err_p2g, kErrOutOfRange);
               continue;
             }
             float c[4];
             p2g_contrib<D>(o, fx_s, w_s, mv, m, A, P.dx, c);
             red_add_v4(G + f, c[0], c[1], c[2], c[3]);
           }
+          mark_stencil<D>(flags, base, P);
         }
       }
       // ---- P2G into this warp's tile.  Shared-memory FP32 atomics are compare-and-swap
@@ -429,6 +526,21 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
       }
       if (a[0] == 0.0f && a[1] == 0.0f && a[2] == 0.0f && a[3] == 0.0f) continue;
       if (in) red_add_v4(G + flat_index<D>(g, N), a[0], a[1], a[2], a[3]);
+    }
+    // the tile spans node blocks b-1 .. b+1 on every axis
+    if (threadIdx.x < ((D == 3) ? 27 : 9)) {
+      int nbc[3] = {0, 0, 0}, r = b;
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        nbc[d] = r % P.nb;
+        r /= P.nb;
+      }
+      const int t = threadIdx.x;
+      const int di = (D == 3) ? t / 9 - 1 : t / 3 - 1, dj = (D == 3) ? (t / 3) % 3 - 1 : t % 3 - 1;
+      const int dk = (D == 3) ? t % 3 - 1 : 0;
+      const int bi = nbc[0] + di, bj = nbc[1] + dj, bk = nbc[D - 1] + dk;
+      if (bi >= 0 && bi < P.nb && bj >= 0 && bj < P.nb && (D == 2 || (bk >= 0 && bk < P.nb)))
+        flags[(D == 3) ? (bi * P.nb + bj) * P.nb + bk : bi * P.nb + bj] |= kPending;
     }
   }
 }
@@ -550,7 +662,7 @@ __global__ void block_keys_kernel(const float *__restrict__ xs, int stride, Para
 template <int D>
 __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__restrict__ key,
                                  const int *__restrict__ rank, const int *__restrict__ start,
-                                 const int *__restrict__ count) {
+                                 const int *__restrict__ count, int move_vc) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   constexpr int CPB = Tiling<D>::CPB;
@@ -571,6 +683,12 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
   dst.vol[q] = src.vol[p];
   dst.id[q] = src.id[p];
   if (src.mat) dst.mat[q] = src.mat[p];
+  if (move_vc) {  // the next P2G reads v and C (right after an upload)
+#pragma unroll
+    for (int d = 0; d < D; ++d) dst.v[(size_t)d * ds + q] = src.v[(size_t)d * ss + p];
+#pragma unroll
+    for (int cmp = 0; cmp < D * D; ++cmp) dst.C[(size_t)cmp * ds + q] = src.C[(size_t)cmp * ss + p];
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -579,31 +697,39 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 template <int D>
-void launch_p2g_state(const PState &s, const Params &P, float4 *G, int *err, cudaStream_t st) {
-  if (P.n == 0) return;
-  p2g_state_kernel<D><<<blocks_for(P.n, 256), 256, 0, st>>>(s, P, G, err);
-}
-
-template <int D>
-void launch_grid_sweep(float4 *G, float4 *V, const Params &P, int *work, int sms, cudaStream_t st) {
-  int64_t blocks = blocks_for(P.nodes, 256);
+void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Params &P, int *work, int sms,
+                       cudaStream_t st) {
+  int64_t blocks = blocks_for((int64_t)P.nblocks * 32, 256);
   if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
   if (blocks < 1) blocks = 1;
-  grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, P, work);
+  grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, flags, P, work);
 }
 
 template <int D>
-void launch_g2p2g(const PState &s, const Params &P, const float4 *V, float4 *G, const int *blocks,
-                  const int *nactive, const int *bstart, int *work, int *err_now, int *err_next,
-                  bool ref, bool final_step, int ctas, cudaStream_t st) {
+void launch_discard_pending(float4 *G, uint8_t *flags, const Params &P, int sms, cudaStream_t st) {
+  int64_t blocks = blocks_for((int64_t)P.nblocks * 32, 256);
+  if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
+  if (blocks < 1) blocks = 1;
+  discard_pending_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, flags, P);
+}
+
+template <int D>
+void launch_g2p2g(const PState &s, const Params &P, const float4 *V, float4 *G, uint8_t *flags,
+                  const int *blocks, const int *nactive, const int *bstart, int *work,
+                  int *err_now, int *err_next, bool ref, int mode, int ctas,
+                  cudaStream_t st) {
   if (P.n == 0) return;
-#define MPM_G2P2G(R, FI)                                                                 \
-  g2p2g_kernel<D, R, FI><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(              \
-      s, P, V, G, blocks, nactive, bstart, work, err_now, err_next)
+#define MPM_G2P2G(R, MODE)                                                               \
+  g2p2g_kernel<D, R, MODE><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(            \
+      s, P, V, G, flags, blocks, nactive, bstart, work, err_now, err_next)
   if (ref) {
-    if (final_step) MPM_G2P2G(true, true); else MPM_G2P2G(true, false);
+    if (mode == kFinalStep) MPM_G2P2G(true, kFinalStep);
+    else if (mode == kP2GOnly) MPM_G2P2G(true, kP2GOnly);
+    else MPM_G2P2G(true, kStep);
   } else {
-    if (final_step) MPM_G2P2G(false, true); else MPM_G2P2G(false, false);
+    if (mode == kFinalStep) MPM_G2P2G(false, kFinalStep);
+    else if (mode == kP2GOnly) MPM_G2P2G(false, kP2GOnly);
+    else MPM_G2P2G(false, kStep);
   }
 #undef MPM_G2P2G
 }
@@ -612,12 +738,14 @@ template <int D>
 int g2p2g_ctas_per_sm() {
   // the tiles exceed the default 48 KB of dynamic shared memory in 3D
   const int bytes = (int)g2p2g_smem_bytes<D>();
-  cudaFuncSetAttribute(g2p2g_kernel<D, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, true, kStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, true, kFinalStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, true, kP2GOnly>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, false, kStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, false, kFinalStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(g2p2g_kernel<D, false, kP2GOnly>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, g2p2g_kernel<D, true, false>, kG2P2GThreads,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, g2p2g_kernel<D, true, kStep>, kG2P2GThreads,
                                                 g2p2g_smem_bytes<D>());
   return n > 0 ? n : 1;
 }
@@ -654,17 +782,19 @@ void launch_block_keys(const PState &s, const Params &P, int *key, int *rank, in
 
 template <int D>
 void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank,
-                      const int *start, const int *count, cudaStream_t st) {
+                      const int *start, const int *count, bool move_vc, cudaStream_t st) {
   if (n == 0) return;
-  sort_move_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, key, rank, start, count);
+  sort_move_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, key, rank, start, count,
+                                                          move_vc ? 1 : 0);
 }
 
 #define MPM_INSTANTIATE(D)                                                                       \
-  template void launch_p2g_state<D>(const PState &, const Params &, float4 *, int *, cudaStream_t); \
-  template void launch_grid_sweep<D>(float4 *, float4 *, const Params &, int *, int, cudaStream_t); \
+  template void launch_grid_sweep<D>(float4 *, float4 *, uint8_t *, const Params &, int *, int,  \
+                                     cudaStream_t);                                              \
+  template void launch_discard_pending<D>(float4 *, uint8_t *, const Params &, int, cudaStream_t); \
   template void launch_g2p2g<D>(const PState &, const Params &, const float4 *, float4 *,        \
-                                const int *, const int *, const int *, int *, int *, int *, bool, \
-                                bool, int, cudaStream_t);                                        \
+                                uint8_t *, const int *, const int *, const int *, int *, int *,  \
+                                int *, bool, int, int, cudaStream_t);                            \
   template int g2p2g_ctas_per_sm<D>();                                                           \
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \
@@ -677,6 +807,6 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
   template void launch_block_keys<D>(const PState &, const Params &, int *, int *, int *,        \
                                      cudaStream_t);                                              \
   template void launch_sort_move<D>(const PState &, const PState &, int, const int *, const int *, \
-                                    const int *, const int *, cudaStream_t);
+                                    const int *, const int *, bool, cudaStream_t);
 
 }  // namespace mpm

@@ -38,6 +38,7 @@ struct nclr_sim {
 
   float4 *G = nullptr;  // P2G accumulator of the coming step
   float4 *V = nullptr;  // updated grid of the last step (grid())
+  uint8_t *flags = nullptr;  // per grid block: pending contributions in G / non-zero V
   int *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *tile_sums = nullptr;
   int *blocks = nullptr;  // non-empty blocks of the last sort
   int *nblocks_active = nullptr;
@@ -177,8 +178,9 @@ void collect_profile(nclr_sim *s) {
   s->pending.clear();
 }
 
-// Enqueues the block sort of the current buffer into the other one.
-void enqueue_sort(nclr_sim *s) {
+// Enqueues the block sort of the current buffer into the other one (v and C move too when
+// the next P2G reads them, i.e. right after an upload).
+void enqueue_sort(nclr_sim *s, bool move_vc) {
   const int nb = s->P.nblocks;
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
@@ -191,7 +193,7 @@ void enqueue_sort(nclr_sim *s) {
       mpm::launch_exclusive_scan(s->count, nkeys, s->start, s->tile_sums, s->stream);
       mpm::launch_compact_blocks(s->start, nb, cpb, s->blocks, s->nblocks_active, s->stream);
       mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->key, s->rank,
-                               s->start, s->count, s->stream);
+                               s->start, s->count, move_vc, s->stream);
     });
   });
   s->cur ^= 1;
@@ -201,18 +203,19 @@ void enqueue_sort(nclr_sim *s) {
 // Enqueues one step (optionally preceded by the block sort) on the handle's stream.  The
 // last step of a call writes v and C and reports the next step's P2G errors separately.
 void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
-  if (sort && s->n > 0) enqueue_sort(s);
+  if (sort && s->n > 0) enqueue_sort(s, false);
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     phase(s, NCLR_PHASE_GRID, 1, [&] {
-      mpm::launch_grid_sweep<D>(s->G, s->V, s->P, s->work, s->sms, s->stream);
+      mpm::launch_grid_sweep<D>(s->G, s->V, s->flags, s->P, s->work, s->sms, s->stream);
     });
     s->launches += 1;
     if (s->n > 0) {
       phase(s, NCLR_PHASE_G2P2G, 1, [&] {
-        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P, s->V, s->G, s->blocks, s->nblocks_active,
+        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P, s->V, s->G, s->flags, s->blocks, s->nblocks_active,
                              s->start, s->work, s->err_d, final_step ? s->err_d + 1 : s->err_d,
-                             s->ref, final_step, s->g2p2g_ctas, s->stream);
+                             s->ref, final_step ? mpm::kModeFinalStep : mpm::kModeStep,
+                             s->g2p2g_ctas, s->stream);
       });
       s->launches += 1;
     }
@@ -221,7 +224,7 @@ void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
 
 bool sort_due(const nclr_sim *s) {
   return s->need_sort ||
-         (s->opt.sort_interval > 0 && s->steps_since_sort % s->opt.sort_interval == 0);
+         (s->opt.sort_interval > 0 && s->steps_since_sort >= s->opt.sort_interval);
 }
 
 int64_t chunk_steps(const nclr_sim *s) { return s->opt.sort_interval > 0 ? s->opt.sort_interval : 16; }
@@ -317,6 +320,7 @@ void release(nclr_sim *s) {
   for (auto p : s->slab) cudaFree(p);
   cudaFree(s->G);
   cudaFree(s->V);
+  cudaFree(s->flags);
   cudaFree(s->blocks);
   cudaFree(s->nblocks_active);
   cudaFree(s->work);
@@ -419,6 +423,8 @@ nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, cons
   s->g2p2g_ctas = s->sms * (dim == 3 ? mpm::g2p2g_ctas_per_sm<3>() : mpm::g2p2g_ctas_per_sm<2>());
   CREATE_TRY(cudaMalloc((void **)&s->G, sizeof(float4) * (size_t)nodes));
   CREATE_TRY(cudaMalloc((void **)&s->V, sizeof(float4) * (size_t)nodes));
+  CREATE_TRY(cudaMalloc((void **)&s->flags, nblk));
+  CREATE_TRY(cudaMemsetAsync(s->flags, 0, nblk, s->stream));
   CREATE_TRY(cudaMalloc((void **)&s->key, sizeof(int) * np));
   CREATE_TRY(cudaMalloc((void **)&s->rank, sizeof(int) * np));
   CREATE_TRY(cudaMalloc((void **)&s->count, sizeof(int) * nkeys));
@@ -485,22 +491,32 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
   CUDA_TRY(s, cudaSetDevice(s->device));
   CUDA_TRY(s, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int), s->stream));
   s->launches = 0;
+  if (s->need_sort && s->n > 0) {  // the uploaded particles: sort them (with v and C) first
+    enqueue_sort(s, !s->acc_valid);
+    s->need_sort = false;
+    s->steps_since_sort = 0;
+  }
   if (!s->acc_valid) {  // the first step's P2G, from the uploaded state
     s->deferred_err = 0;  // an error of the discarded P2G no longer applies
     dispatch_dim(s->dim, [&](auto dc) {
       constexpr int D = decltype(dc)::value;
-      phase(s, NCLR_PHASE_P2G, 1, [&] {
-        mpm::launch_p2g_state<D>(s->ps[s->cur], s->P, s->G, s->err_d, s->stream);
+      phase(s, NCLR_PHASE_P2G, 3, [&] {
+        mpm::launch_discard_pending<D>(s->G, s->flags, s->P, s->sms, s->stream);
+        // the fused kernel's block counter (before a regular step the sweep resets it)
+        cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
+        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P, s->V, s->G, s->flags, s->blocks,
+                             s->nblocks_active, s->start, s->work, s->err_d, s->err_d, s->ref,
+                             mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
       });
     });
-    if (s->n > 0) s->launches += 1;
+    s->launches += (s->n > 0) ? 2 : 1;
     s->acc_valid = true;
   }
   int64_t left = nsteps;
   const int64_t chunk = chunk_steps(s);
   while (left > 0) {
     const bool sort = sort_due(s);
-    const bool at_boundary = !s->need_sort && (s->opt.sort_interval == 0 || sort);
+    const bool at_boundary = s->opt.sort_interval == 0 || sort;
     if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left - 1 >= chunk) {
       if (!s->graph[s->cur]) {
         nclr_status st = capture_graph(s, s->cur);
@@ -508,16 +524,16 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
       }
       CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur], s->stream));
       s->launches += s->graph_launches;
-      if (s->opt.sort_interval > 0) s->cur ^= 1;
+      if (s->opt.sort_interval > 0) {
+        s->cur ^= 1;
+        s->steps_since_sort = 0;
+      }
       s->steps_since_sort += chunk;
       left -= chunk;
       continue;
     }
     enqueue_step(s, sort, left == 1);
-    if (sort) {
-      s->need_sort = false;
-      s->steps_since_sort = 0;
-    }
+    if (sort) s->steps_since_sort = 0;
     ++s->steps_since_sort;
     --left;
   }
