@@ -46,9 +46,9 @@ WORKLOAD = {"workload": "3D jelly (MaterialModel::kJelly), 4 cubes of 64^3 latti
             "E": 1e4, "nu": 0.2, "gravity": -100.0, "physics": "reference", "seed": 0,
             "l2": "inputs larger than L2 (particle state ~190 MB in HBM)"}
 
-# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each kernel from
-# one ncu capture of this workload (profiles/ holds the summaries); None until captured.
-NCU_TRAFFIC = {"g2p2g": None}
+# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel
+# from one ncu capture of this workload (profiles/g2p2g_jelly3d_1M.md).
+NCU_TRAFFIC = {"g2p2g": 69.006080e6 + 12.848640e6}
 
 
 def peaks():
