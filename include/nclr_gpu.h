@@ -64,6 +64,8 @@ typedef struct nclr_options {
   int use_graphs;          /* capture advance() step sequences in CUDA graphs (default 1) */
   int profile;             /* time every kernel phase of advance() with CUDA events on the
                               handle's stream (direct launches, no graphs; default 0) */
+  int graph_steps;         /* steps per captured CUDA graph, rounded up to a multiple of
+                              sort_interval (0 = one sort interval; default 0) */
 } nclr_options;
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid
@@ -77,6 +79,17 @@ typedef struct nclr_sim nclr_sim;
 /* Fills *opt with the defaults. */
 void nclr_default_options(nclr_options *opt);
 
+/* One scene of a batch: the arguments of nclr_create for one simulation (same layouts, NULL
+ * rules and meaning). */
+typedef struct nclr_scene {
+  int64_t n;
+  const float *x, *v, *F, *C, *Jp, *mass, *volume; /* HOST arrays */
+  const uint8_t *material;                         /* NULL = every particle uses `model` */
+  int model;
+  int res;
+  float dt, E, nu, gravity;
+} nclr_scene;
+
 /* Creates a simulation of n particles (MPMSimulation ctor, src/nclr.h:74-78).  x, v, F, C,
  * Jp, mass, volume are HOST arrays in the layout above; v, C may be NULL (zero), F NULL
  * (diag<dim>(1) of the chosen physics), Jp/mass/volume NULL (1).  material may be NULL
@@ -86,6 +99,23 @@ nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, cons
                         const float *F, const float *C, const float *Jp, const float *mass,
                         const float *volume, const uint8_t *material, int model, int res,
                         float dt, float E, float nu, float gravity, const nclr_options *opt);
+
+/* Batched form (no counterpart in the reference, which runs one simulation per object): one
+ * handle holding `nscenes` independent simulations of uneven particle counts, grid
+ * resolutions, materials and parameters, stepped together -- every kernel of a step covers
+ * all scenes in one launch.  nclr_advance steps every scene (each with its own dt); the
+ * per-scene functions below read and write one scene; nclr_get_particles / nclr_set_particles
+ * address all scenes concatenated in scene order; nclr_get_grid returns scene 0's grid. */
+nclr_status nclr_batch_create(nclr_sim **out, int dim, int nscenes, const nclr_scene *scenes,
+                              const nclr_options *opt);
+int nclr_num_scenes(const nclr_sim *sim);
+nclr_status nclr_scene_get_particles(nclr_sim *sim, int scene, float *x, float *v, float *F,
+                                     float *C, float *Jp);
+nclr_status nclr_scene_set_particles(nclr_sim *sim, int scene, const float *x, const float *v,
+                                     const float *F, const float *C, const float *Jp);
+nclr_status nclr_scene_get_grid(nclr_sim *sim, int scene, float *velocity, float *mass);
+/* NCLR_ERR_OUT_OF_RANGE if a stencil of `scene` left its grid during the last nclr_advance. */
+nclr_status nclr_scene_status(const nclr_sim *sim, int scene);
 
 /* advance() repeated nsteps times (src/nclr.h:80-84).  Returns NCLR_ERR_OUT_OF_RANGE if any
  * stencil left the grid during these steps (the state is then unspecified, as the

@@ -23,7 +23,18 @@ NOALLOC_MAX_NODES = 1 << 20
 class Options(ctypes.Structure):
     _fields_ = [("physics", ctypes.c_int), ("sort_interval", ctypes.c_int),
                 ("p2g_particles_per_thread", ctypes.c_int), ("device", ctypes.c_int),
-                ("use_graphs", ctypes.c_int), ("profile", ctypes.c_int)]
+                ("use_graphs", ctypes.c_int), ("profile", ctypes.c_int),
+                ("graph_steps", ctypes.c_int)]
+
+
+class Scene(ctypes.Structure):
+    """nclr_scene: one simulation of a batch."""
+    _fields_ = [("n", ctypes.c_int64), ("x", ctypes.c_void_p), ("v", ctypes.c_void_p),
+                ("F", ctypes.c_void_p), ("C", ctypes.c_void_p), ("Jp", ctypes.c_void_p),
+                ("mass", ctypes.c_void_p), ("volume", ctypes.c_void_p),
+                ("material", ctypes.c_void_p), ("model", ctypes.c_int), ("res", ctypes.c_int),
+                ("dt", ctypes.c_float), ("E", ctypes.c_float), ("nu", ctypes.c_float),
+                ("gravity", ctypes.c_float)]
 
 
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -39,6 +50,13 @@ SIGNATURES = {
                                    ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                    ctypes.POINTER(Options)]),
     "nclr_advance": (ctypes.c_int, [_h, _i64]),
+    "nclr_batch_create": (ctypes.c_int, [ctypes.POINTER(_h), ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(Scene), ctypes.POINTER(Options)]),
+    "nclr_num_scenes": (ctypes.c_int, [_h]),
+    "nclr_scene_get_particles": (ctypes.c_int, [_h, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "nclr_scene_set_particles": (ctypes.c_int, [_h, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "nclr_scene_get_grid": (ctypes.c_int, [_h, ctypes.c_int, _vp, _vp]),
+    "nclr_scene_status": (ctypes.c_int, [_h, ctypes.c_int]),
     "nclr_get_particles": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp]),
     "nclr_set_particles": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp]),
     "nclr_get_grid": (ctypes.c_int, [_h, _vp, _vp]),

@@ -64,8 +64,20 @@ struct Params {
 struct PState {
   float *x, *v, *F, *C, *Jp, *mass, *vol;  // v and C: see the layout note
   int *id;
-  uint8_t *mat;  // may be null
-  int stride;    // component stride (capacity)
+  uint8_t *mat;     // may be null
+  uint16_t *scene;  // scene of each slot (batched simulations), null for a single scene
+  int stride;       // component stride (capacity)
+};
+
+// One simulation of a batch (a single simulation is a batch of one).  Scenes share the
+// particle store (scene s owns slots [slot_off, slot_off + n)), the grids G and V (scene s owns
+// nodes [node_off, node_off + P.nodes)) and the block key space (blocks [block_off,
+// block_off + P.nblocks)).
+struct Scene {
+  Params P;
+  int64_t node_off;
+  int block_off;
+  int slot_off;
 };
 
 // ---------------------------------------------------------------------------------------

@@ -9,19 +9,31 @@ namespace mpm {
 
 struct Params;
 struct PState;
+struct Scene;
 
-template <int D> void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Params &P, int *work, int sms, cudaStream_t st);
-template <int D> void launch_discard_pending(float4 *G, uint8_t *flags, const Params &P, int sms, cudaStream_t st);
-template <int D> void launch_g2p2g(const PState &s, const Params &P, const float4 *V, float4 *G, uint8_t *flags,
-                                   const int *blocks, const int *nactive, const int *bstart, int *work, int *err_now,
-                                   int *err_next, bool ref, int mode, int ctas, cudaStream_t st);
+template <int D> void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
+                                        const uint16_t *block_scene, int total_blocks, int *work, int sms,
+                                        cudaStream_t st);
+template <int D> void launch_discard_pending(float4 *G, uint8_t *flags, const Scene *scenes,
+                                             const uint16_t *block_scene, int total_blocks, int sms,
+                                             cudaStream_t st);
+// err[2 s] collects scene s's errors of this call, err[2 s + next_slot] those of the P2G that
+// follows the launch (next_slot 0: same call, 1: the next call).
+template <int D> void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes, const uint16_t *block_scene,
+                                   const float4 *V, float4 *G, uint8_t *flags, const int *blocks,
+                                   const int *nactive, const int *bstart, int *work, int *err, int next_slot,
+                                   bool ref, int mode, int ctas, cudaStream_t st);
 template <int D> int g2p2g_ctas_per_sm();
 enum : int { kModeStep = 0, kModeFinalStep = 1, kModeP2GOnly = 2 };  // g2p2g modes
 template <int D> void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st);
 template <int D> void launch_export_grid(const float4 *grid, const Params &P, float *vel, float *mass, cudaStream_t st);
-template <int D> void launch_export_particles(const PState &s, int n, float *x, float *v, float *F, float *C, float *Jp, cudaStream_t st);
-template <int D> void launch_import_particles(const PState &s, int n, const float *x, const float *v, const float *F, const float *C, const float *Jp, cudaStream_t st);
-template <int D> void launch_block_keys(const PState &s, const Params &P, int *key, int *rank, int *count, cudaStream_t st);
+template <int D> void launch_export_particles(const PState &s, int begin, int n, int id_off, float *x, float *v,
+                                              float *F, float *C, float *Jp, cudaStream_t st);
+template <int D> void launch_import_particles(const PState &s, int begin, int n, int id_off, const float *x,
+                                              const float *v, const float *F, const float *C, const float *Jp,
+                                              cudaStream_t st);
+template <int D> void launch_block_keys(const PState &s, int n, const Scene *scenes, int *key, int *rank, int *count,
+                                        cudaStream_t st);
 template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank, const int *start, const int *count, bool move_vc, cudaStream_t st);
 void launch_compact_blocks(const int *start, int nblocks, int cpb, int *list, int *nlist, cudaStream_t st);
 

@@ -213,28 +213,43 @@ __device__ __forceinline__ void mark_node(uint8_t *flags, int64_t f, const Param
 // (a massless node's velocity is zero and stays zero through the boundary rule).  One warp
 // per block; also resets the g2p2g work counter.
 // ---------------------------------------------------------------------------------------
+// Scene of global block gb, and the block's first node per axis inside that scene.
+template <int D>
+__device__ __forceinline__ int block_origin(int gb, const Scene *scenes,
+                                            const uint16_t *block_scene, int bc[D]) {
+  const int sid = block_scene ? (int)block_scene[gb] : 0;
+  int r = gb - scenes[sid].block_off;
+  const int nb = scenes[sid].P.nb;
+#pragma unroll
+  for (int d = D - 1; d >= 0; --d) {
+    bc[d] = (r % nb) * Tiling<D>::BS;
+    r /= nb;
+  }
+  return sid;
+}
+
 template <int D>
 __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
                                                          float4 *__restrict__ V,
-                                                         uint8_t *__restrict__ flags, Params P,
+                                                         uint8_t *__restrict__ flags,
+                                                         const Scene *__restrict__ scenes,
+                                                         const uint16_t *__restrict__ block_scene,
+                                                         int total_blocks,
                                                          int *__restrict__ work) {
   constexpr int BS = Tiling<D>::BS;
   constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;  // nodes per block
   if (blockIdx.x == 0 && threadIdx.x == 0) *work = 0;
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
-  for (int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < P.nblocks; b += warps) {
-    const uint8_t fl = flags[b];
+  for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < total_blocks;
+       gb += warps) {
+    const uint8_t fl = flags[gb];
     if (!fl) continue;
     int bc[D];
-    {
-      int r = b;
-#pragma unroll
-      for (int d = D - 1; d >= 0; --d) {
-        bc[d] = (r % P.nb) * BS;
-        r /= P.nb;
-      }
-    }
+    const int sid = block_origin<D>(gb, scenes, block_scene, bc);
+    const Params P = scenes[sid].P;
+    float4 *Gs = G + scenes[sid].node_off;
+    float4 *Vs = V + scenes[sid].node_off;
     for (int t = lane; t < BN; t += 32) {
       int idx[D];
       bool in = true;
@@ -247,13 +262,13 @@ __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
       }
       if (!in) continue;
       const int64_t f = flat_index<D>(idx, P.N);
-      const float4 g = G[f];
+      const float4 g = Gs[f];
       float v[D], m;
       grid_update<D>(g, idx, P, v, m);
-      V[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
-      G[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      Vs[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
+      Gs[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    if (lane == 0) flags[b] = (fl & kPending) ? kVNonzero : 0;
+    if (lane == 0) flags[gb] = (fl & kPending) ? kVNonzero : 0;
   }
 }
 
@@ -261,23 +276,22 @@ __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
 // pending blocks, pending flags cleared; V and its flags stay (they are grid()).
 template <int D>
 __global__ void __launch_bounds__(256) discard_pending_kernel(float4 *__restrict__ G,
-                                                              uint8_t *__restrict__ flags, Params P) {
+                                                              uint8_t *__restrict__ flags,
+                                                              const Scene *__restrict__ scenes,
+                                                              const uint16_t *__restrict__ block_scene,
+                                                              int total_blocks) {
   constexpr int BS = Tiling<D>::BS;
   constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
-  for (int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < P.nblocks; b += warps) {
-    const uint8_t fl = flags[b];
+  for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < total_blocks;
+       gb += warps) {
+    const uint8_t fl = flags[gb];
     if (!(fl & kPending)) continue;
     int bc[D];
-    {
-      int r = b;
-#pragma unroll
-      for (int d = D - 1; d >= 0; --d) {
-        bc[d] = (r % P.nb) * BS;
-        r /= P.nb;
-      }
-    }
+    const int sid = block_origin<D>(gb, scenes, block_scene, bc);
+    const int N = scenes[sid].P.N;
+    float4 *Gs = G + scenes[sid].node_off;
     for (int t = lane; t < BN; t += 32) {
       int idx[D];
       bool in = true;
@@ -286,11 +300,11 @@ __global__ void __launch_bounds__(256) discard_pending_kernel(float4 *__restrict
       for (int d = D - 1; d >= 0; --d) {
         idx[d] = bc[d] + r % BS;
         r /= BS;
-        in &= idx[d] < P.N;
+        in &= idx[d] < N;
       }
-      if (in) G[flat_index<D>(idx, P.N)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (in) Gs[flat_index<D>(idx, N)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    if (lane == 0) flags[b] = fl & (uint8_t)~kPending;
+    if (lane == 0) flags[gb] = fl & (uint8_t)~kPending;
   }
 }
 
@@ -307,12 +321,15 @@ __global__ void __launch_bounds__(256) discard_pending_kernel(float4 *__restrict
 // coming step from the stored state, after an upload; the particles are sorted already).
 enum : int { kStep = kModeStep, kFinalStep = kModeFinalStep, kP2GOnly = kModeP2GOnly };
 
-template <int D, bool kRef, int kMode>
-__global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
-    PState s, Params P, const float4 *__restrict__ V, float4 *__restrict__ G,
-    uint8_t *__restrict__ flags, const int *__restrict__ blocks, const int *__restrict__ nactive,
-    const int *__restrict__ bstart, int *__restrict__ work, int *__restrict__ err_now,
-    int *__restrict__ err_next) {
+// kBatch: several scenes (per-block parameters from the scene table, staged in shared memory)
+// or one (its parameters are a kernel argument: constant-bank operands, no registers).
+template <int D, bool kRef, int kMode, bool kBatch>
+__global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
+    PState s, Params P0, const Scene *__restrict__ scenes, const uint16_t *__restrict__ block_scene,
+    const float4 *__restrict__ Vall, float4 *__restrict__ Gall, uint8_t *__restrict__ flags_all,
+    const int *__restrict__ blocks, const int *__restrict__ nactive,
+    const int *__restrict__ bstart, int *__restrict__ work, int *__restrict__ err,
+    int next_slot) {
   using Tl = Tiling<D>;
   constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, CPB = Tl::CPB, GS = Tl::SIZE;
   constexpr int S = (D == 3) ? 27 : 9;
@@ -321,7 +338,9 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
   float4 *vt = smem;            // V tile
   float4 *gt = smem + Tl::SIZE;  // kWarps private G tiles: [warp][SIZE]
   __shared__ int s_item;
-  const int N = P.N;
+  __shared__ Params sP;  // the current block's scene (shared: keeps registers for the math)
+  __shared__ int64_t s_node_off;
+  __shared__ int s_block_off;
   const int st = s.stride;
   const int nact = *nactive;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -329,20 +348,39 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
 
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) s_item = atomicAdd(work, 1);
+    if (threadIdx.x == 0) {  // the next block of the list, and its scene
+      const int it = atomicAdd(work, 1);
+      s_item = it;
+      if (kBatch && it < nact) {
+        const int sid0 = (int)block_scene[blocks[it]];
+        sP = scenes[sid0].P;
+        s_node_off = scenes[sid0].node_off;
+        s_block_off = scenes[sid0].block_off;
+      }
+    }
     __syncthreads();
     const int item = s_item;
     if (item >= nact) return;
-    const int b = blocks[item];
+    const int gb = blocks[item];  // global block (scene-major)
+    const int sid = kBatch ? (int)block_scene[gb] : 0;
+    const Params &P = kBatch ? sP : P0;
+    const int64_t node_off = kBatch ? s_node_off : 0;
+    const int block_off = kBatch ? s_block_off : 0;
+    const int N = P.N;
     int org[D];
     {
-      int r = b;
+      int r = gb - block_off;
 #pragma unroll
       for (int d = D - 1; d >= 0; --d) {
         org[d] = (r % P.nb) * BS - 1;
         r /= P.nb;
       }
     }
+    const float4 *__restrict__ V = Vall + node_off;
+    float4 *__restrict__ G = Gall + node_off;
+    uint8_t *__restrict__ flags = flags_all + block_off;
+    const int b = gb - block_off;
+    int *err_now = err + 2 * sid, *err_next = err + 2 * sid + next_slot;
     if (kMode != kP2GOnly) {
       for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
         int g[D], l[3] = {0, 0, 0};
@@ -366,8 +404,8 @@ __global__ void __launch_bounds__(kG2P2GThreads) g2p2g_kernel(
     // The block's particles, stored cell by cell in rounds (see sort_move_kernel), one per
     // thread in slot order.  Every lane of a warp runs the same number of iterations (the
     // warp-wide steps below need them all).
-    const int p0 = bstart[b * CPB];
-    const int np = bstart[(b + 1) * CPB] - p0;
+    const int p0 = bstart[gb * CPB];
+    const int np = bstart[(gb + 1) * CPB] - p0;
     for (int j0 = 0; j0 < np; j0 += kG2P2GThreads) {
       const int j = j0 + threadIdx.x;
       const bool valid = j < np;
@@ -581,15 +619,18 @@ __global__ void export_grid_kernel(const float4 *__restrict__ grid, Params P,
   mass[f] = m;
 }
 
-// particles() export: slot-major SoA -> caller's order, particle-major rows.
+// particles() export: slots [begin, begin + n) (SoA) -> the caller's rows id - id_off
+// (particle-major).  A scene's slots stay inside its own slot range across sorts.
 template <int D>
-__global__ void export_particles_kernel(PState s, int n, float *__restrict__ x,
-                                        float *__restrict__ v, float *__restrict__ F,
-                                        float *__restrict__ C, float *__restrict__ Jp) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
+__global__ void export_particles_kernel(PState s, int begin, int n, int id_off,
+                                        float *__restrict__ x, float *__restrict__ v,
+                                        float *__restrict__ F, float *__restrict__ C,
+                                        float *__restrict__ Jp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = begin + i;
   const int st = s.stride;
-  const int q = s.id[p];
+  const int q = s.id[p] - id_off;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     if (x) x[(size_t)q * D + d] = s.x[(size_t)d * st + p];
@@ -603,17 +644,18 @@ __global__ void export_particles_kernel(PState s, int n, float *__restrict__ x,
   if (Jp) Jp[q] = s.Jp[p];
 }
 
-// Upload: caller's rows -> SoA slots.  Slot p takes caller particle id[p] (the current
-// permutation is kept, so a partial update leaves the other fields in place).
+// Upload: the caller's rows -> slots [begin, begin + n).  Slot p takes row id[p] - id_off
+// (the current permutation is kept, so a partial update leaves the other fields in place).
 template <int D>
-__global__ void import_particles_kernel(PState s, int n, const float *__restrict__ x,
-                                        const float *__restrict__ v, const float *__restrict__ F,
-                                        const float *__restrict__ C,
+__global__ void import_particles_kernel(PState s, int begin, int n, int id_off,
+                                        const float *__restrict__ x, const float *__restrict__ v,
+                                        const float *__restrict__ F, const float *__restrict__ C,
                                         const float *__restrict__ Jp) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = begin + i;
   const int st = s.stride;
-  const int q = s.id[p];
+  const int q = s.id[p] - id_off;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     if (x) s.x[(size_t)d * st + p] = x[(size_t)q * D + d];
@@ -636,12 +678,15 @@ __global__ void import_particles_kernel(PState s, int n, const float *__restrict
 // advance() call before anyone reads them.
 // ---------------------------------------------------------------------------------------
 template <int D>
-__global__ void block_keys_kernel(const float *__restrict__ xs, int stride, Params P,
+__global__ void block_keys_kernel(const float *__restrict__ xs, const uint16_t *__restrict__ pscene,
+                                  int stride, int n, const Scene *__restrict__ scenes,
                                   int *__restrict__ key, int *__restrict__ rank,
                                   int *__restrict__ count) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.n) return;
+  if (p >= n) return;
   constexpr int BS = Tiling<D>::BS;
+  const int sid = pscene ? (int)pscene[p] : 0;
+  const Params &P = scenes[sid].P;
   int kb = 0, kc = 0;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
@@ -649,7 +694,7 @@ __global__ void block_keys_kernel(const float *__restrict__ xs, int stride, Para
     kb = kb * P.nb + bd / BS;
     kc = kc * BS + bd % BS;
   }
-  const int k = kb * Tiling<D>::CPB + kc;  // block-major, then the cell inside the block
+  const int k = (scenes[sid].block_off + kb) * Tiling<D>::CPB + kc;  // block-major, then cell
   key[p] = k;
   rank[p] = atomicAdd(count + k, 1);
 }
@@ -683,6 +728,7 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
   dst.vol[q] = src.vol[p];
   dst.id[q] = src.id[p];
   if (src.mat) dst.mat[q] = src.mat[p];
+  if (src.scene) dst.scene[q] = src.scene[p];
   if (move_vc) {  // the next P2G reads v and C (right after an upload)
 #pragma unroll
     for (int d = 0; d < D; ++d) dst.v[(size_t)d * ds + q] = src.v[(size_t)d * ss + p];
@@ -697,40 +743,51 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 template <int D>
-void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Params &P, int *work, int sms,
+void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
+                       const uint16_t *block_scene, int total_blocks, int *work, int sms,
                        cudaStream_t st) {
-  int64_t blocks = blocks_for((int64_t)P.nblocks * 32, 256);
+  int64_t blocks = blocks_for((int64_t)total_blocks * 32, 256);
   if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
   if (blocks < 1) blocks = 1;
-  grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, flags, P, work);
+  grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, flags, scenes, block_scene,
+                                                          total_blocks, work);
 }
 
 template <int D>
-void launch_discard_pending(float4 *G, uint8_t *flags, const Params &P, int sms, cudaStream_t st) {
-  int64_t blocks = blocks_for((int64_t)P.nblocks * 32, 256);
+void launch_discard_pending(float4 *G, uint8_t *flags, const Scene *scenes,
+                            const uint16_t *block_scene, int total_blocks, int sms,
+                            cudaStream_t st) {
+  int64_t blocks = blocks_for((int64_t)total_blocks * 32, 256);
   if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
   if (blocks < 1) blocks = 1;
-  discard_pending_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, flags, P);
+  discard_pending_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, flags, scenes, block_scene,
+                                                               total_blocks);
 }
 
 template <int D>
-void launch_g2p2g(const PState &s, const Params &P, const float4 *V, float4 *G, uint8_t *flags,
-                  const int *blocks, const int *nactive, const int *bstart, int *work,
-                  int *err_now, int *err_next, bool ref, int mode, int ctas,
-                  cudaStream_t st) {
-  if (P.n == 0) return;
-#define MPM_G2P2G(R, MODE)                                                               \
-  g2p2g_kernel<D, R, MODE><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(            \
-      s, P, V, G, flags, blocks, nactive, bstart, work, err_now, err_next)
-  if (ref) {
-    if (mode == kFinalStep) MPM_G2P2G(true, kFinalStep);
-    else if (mode == kP2GOnly) MPM_G2P2G(true, kP2GOnly);
-    else MPM_G2P2G(true, kStep);
-  } else {
-    if (mode == kFinalStep) MPM_G2P2G(false, kFinalStep);
-    else if (mode == kP2GOnly) MPM_G2P2G(false, kP2GOnly);
-    else MPM_G2P2G(false, kStep);
+void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
+                  const uint16_t *block_scene, const float4 *V, float4 *G, uint8_t *flags,
+                  const int *blocks, const int *nactive, const int *bstart, int *work, int *err,
+                  int next_slot, bool ref, int mode, int ctas, cudaStream_t st) {
+#define MPM_G2P2G(R, MODE, B)                                                            \
+  g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(         \
+      s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart, work, err, next_slot)
+#define MPM_G2P2G_B(R, MODE)          \
+  if (block_scene) {                  \
+    MPM_G2P2G(R, MODE, true);         \
+  } else {                            \
+    MPM_G2P2G(R, MODE, false);        \
   }
+  if (ref) {
+    if (mode == kFinalStep) { MPM_G2P2G_B(true, kFinalStep) }
+    else if (mode == kP2GOnly) { MPM_G2P2G_B(true, kP2GOnly) }
+    else { MPM_G2P2G_B(true, kStep) }
+  } else {
+    if (mode == kFinalStep) { MPM_G2P2G_B(false, kFinalStep) }
+    else if (mode == kP2GOnly) { MPM_G2P2G_B(false, kP2GOnly) }
+    else { MPM_G2P2G_B(false, kStep) }
+  }
+#undef MPM_G2P2G_B
 #undef MPM_G2P2G
 }
 
@@ -738,14 +795,23 @@ template <int D>
 int g2p2g_ctas_per_sm() {
   // the tiles exceed the default 48 KB of dynamic shared memory in 3D
   const int bytes = (int)g2p2g_smem_bytes<D>();
-  cudaFuncSetAttribute(g2p2g_kernel<D, true, kStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, true, kFinalStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, true, kP2GOnly>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, false, kStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, false, kFinalStep>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(g2p2g_kernel<D, false, kP2GOnly>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaFuncSetAttribute(g2p2g_kernel<D, true, kStep, false>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, true, kFinalStep, false>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, true, kP2GOnly, false>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, false, kStep, false>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, false, kFinalStep, false>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, false, kP2GOnly, false>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, true, kStep, true>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, true, kFinalStep, true>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, true, kP2GOnly, true>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, false, kStep, true>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, false, kFinalStep, true>, a, bytes);
+    cudaFuncSetAttribute(g2p2g_kernel<D, false, kP2GOnly, true>, a, bytes);
+  }
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, g2p2g_kernel<D, true, kStep>, kG2P2GThreads,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, g2p2g_kernel<D, true, kStep, true>, kG2P2GThreads,
                                                 g2p2g_smem_bytes<D>());
   return n > 0 ? n : 1;
 }
@@ -761,23 +827,26 @@ void launch_export_grid(const float4 *grid, const Params &P, float *vel, float *
 }
 
 template <int D>
-void launch_export_particles(const PState &s, int n, float *x, float *v, float *F, float *C,
-                             float *Jp, cudaStream_t st) {
+void launch_export_particles(const PState &s, int begin, int n, int id_off, float *x, float *v,
+                             float *F, float *C, float *Jp, cudaStream_t st) {
   if (n == 0) return;
-  export_particles_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, n, x, v, F, C, Jp);
+  export_particles_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, begin, n, id_off, x, v, F, C, Jp);
 }
 
 template <int D>
-void launch_import_particles(const PState &s, int n, const float *x, const float *v,
-                             const float *F, const float *C, const float *Jp, cudaStream_t st) {
+void launch_import_particles(const PState &s, int begin, int n, int id_off, const float *x,
+                             const float *v, const float *F, const float *C, const float *Jp,
+                             cudaStream_t st) {
   if (n == 0) return;
-  import_particles_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, n, x, v, F, C, Jp);
+  import_particles_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, begin, n, id_off, x, v, F, C, Jp);
 }
 
 template <int D>
-void launch_block_keys(const PState &s, const Params &P, int *key, int *rank, int *count, cudaStream_t st) {
-  if (P.n == 0) return;
-  block_keys_kernel<D><<<blocks_for(P.n, 256), 256, 0, st>>>(s.x, s.stride, P, key, rank, count);
+void launch_block_keys(const PState &s, int n, const Scene *scenes, int *key, int *rank, int *count,
+                       cudaStream_t st) {
+  if (n == 0) return;
+  block_keys_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s.x, s.scene, s.stride, n, scenes, key,
+                                                           rank, count);
 }
 
 template <int D>
@@ -789,22 +858,23 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
 }
 
 #define MPM_INSTANTIATE(D)                                                                       \
-  template void launch_grid_sweep<D>(float4 *, float4 *, uint8_t *, const Params &, int *, int,  \
-                                     cudaStream_t);                                              \
-  template void launch_discard_pending<D>(float4 *, uint8_t *, const Params &, int, cudaStream_t); \
-  template void launch_g2p2g<D>(const PState &, const Params &, const float4 *, float4 *,        \
-                                uint8_t *, const int *, const int *, const int *, int *, int *,  \
-                                int *, bool, int, int, cudaStream_t);                            \
+  template void launch_grid_sweep<D>(float4 *, float4 *, uint8_t *, const Scene *,              \
+                                     const uint16_t *, int, int *, int, cudaStream_t);           \
+  template void launch_discard_pending<D>(float4 *, uint8_t *, const Scene *, const uint16_t *,  \
+                                          int, int, cudaStream_t);                               \
+  template void launch_g2p2g<D>(const PState &, const Params &, const Scene *, const uint16_t *, \
+                                const float4 *, float4 *, uint8_t *, const int *, const int *,   \
+                                const int *, int *, int *, int, bool, int, int, cudaStream_t);   \
   template int g2p2g_ctas_per_sm<D>();                                                           \
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \
                                       cudaStream_t);                                             \
-  template void launch_export_particles<D>(const PState &, int, float *, float *, float *,       \
-                                           float *, float *, cudaStream_t);                      \
-  template void launch_import_particles<D>(const PState &, int, const float *, const float *,    \
+  template void launch_export_particles<D>(const PState &, int, int, int, float *, float *,       \
+                                           float *, float *, float *, cudaStream_t);             \
+  template void launch_import_particles<D>(const PState &, int, int, int, const float *,         \
                                            const float *, const float *, const float *,          \
-                                           cudaStream_t);                                        \
-  template void launch_block_keys<D>(const PState &, const Params &, int *, int *, int *,        \
+                                           const float *, cudaStream_t);                         \
+  template void launch_block_keys<D>(const PState &, int, const Scene *, int *, int *, int *,    \
                                      cudaStream_t);                                              \
   template void launch_sort_move<D>(const PState &, const PState &, int, const int *, const int *, \
                                     const int *, const int *, bool, cudaStream_t);

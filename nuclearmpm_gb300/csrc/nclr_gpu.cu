@@ -1,13 +1,16 @@
-// Host side of the C ABI in include/nclr_gpu.h: one simulation handle = one CUDA stream, the
-// device-resident particle store (two SoA buffers that the block sort ping-pongs between),
-// the two grids (G: the coming step's P2G accumulator; V: the last step's updated grid) and
-// the sort scratch.  advance() enqueues per step
+// Host side of the C ABI in include/nclr_gpu.h.  A handle holds one or more scenes (a plain
+// simulation is a batch of one) and owns one CUDA stream; all scenes share one device-resident
+// particle store (two SoA buffers that the block sort ping-pongs between; scene s owns a fixed
+// slot range), the two grids (G: the coming step's P2G accumulator; V: the last step's updated
+// grid; scene s owns a node range of each) and the sort scratch.  advance() enqueues per step
 //   [every sort_interval steps: block keys -> scan -> active-block list -> move]
-//   grid sweep (V = grid_op(G), G = 0) -> g2p2g (G2P of this step + P2G of the next)
-// after a stand-alone P2G when the particle state was just uploaded, replaying a captured
-// CUDA graph for whole sort intervals.  Only the last step of a call writes v and C.
+//   grid sweep (V = grid_op(G), G = 0 on touched blocks) -> g2p2g (G2P + next P2G)
+// for every scene at once, after a P2G-only launch when the particle state was just
+// uploaded, replaying a captured CUDA graph for whole sort intervals.  Only the last step of
+// a call writes v and C.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -20,15 +23,22 @@
 
 using mpm::Params;
 using mpm::PState;
+using mpm::Scene;
 
 struct nclr_sim {
-  int dim = 0, res = 0, device = 0;
-  int64_t n = 0;
+  int dim = 0, device = 0, nscenes = 0;
+  int64_t n = 0;  // particles of all scenes
   nclr_options opt{};
-  Params P{};
   bool ref = true;
   bool has_mat = false;
   cudaStream_t stream = nullptr;
+
+  std::vector<Scene> scenes;   // host copy of the scene table
+  Scene *scenes_d = nullptr;
+  uint16_t *block_scene = nullptr;  // scene of every global block (batches only)
+  int64_t total_nodes = 0;
+  int total_blocks = 0;
+  int64_t nkeys = 0;
 
   void *slab[2] = {nullptr, nullptr};  // particle SoA buffers
   PState ps[2]{};
@@ -36,26 +46,26 @@ struct nclr_sim {
   int sms = 1;         // streaming multiprocessors of the device
   int g2p2g_ctas = 1;  // persistent CTAs of the fused kernel
 
-  float4 *G = nullptr;  // P2G accumulator of the coming step
-  float4 *V = nullptr;  // updated grid of the last step (grid())
-  uint8_t *flags = nullptr;  // per grid block: pending contributions in G / non-zero V
+  float4 *G = nullptr;        // P2G accumulator of the coming step
+  float4 *V = nullptr;        // updated grid of the last step (grid())
+  uint8_t *flags = nullptr;   // per grid block: pending contributions in G / non-zero V
   int *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *tile_sums = nullptr;
-  int *blocks = nullptr;  // non-empty blocks of the last sort
+  int *blocks = nullptr;      // non-empty blocks of the last sort
   int *nblocks_active = nullptr;
-  int *work = nullptr;    // fused kernel's block counter
-  int *err_d = nullptr;   // [0]: this call's steps, [1]: the P2G after the call's last step
-  int *err_h = nullptr;   // pinned, 2 ints
-  int deferred_err = 0;   // [1] of the previous call: reported by the next one
-  bool acc_valid = false; // G holds the P2G of the coming step
-  bool need_sort = true;  // the block lists do not describe the particles yet
+  int *work = nullptr;        // fused kernel's block counter
+  int *err_d = nullptr;       // per scene: [2s] this call's steps, [2s+1] the P2G after them
+  int *err_h = nullptr;       // pinned copy
+  std::vector<int> deferred_err;  // [2s+1] of the previous call, reported by the next one
+  std::vector<int> scene_err;     // the last call's errors per scene
+  bool acc_valid = false;     // G holds the P2G of the coming step
+  bool need_sort = true;      // the block lists do not describe the particles yet
 
   float *staging = nullptr;       // particle-major transfer buffer (n * row floats)
-  float *grid_staging = nullptr;  // grid export buffer (nodes * (dim + 1) floats)
+  float *grid_staging = nullptr;  // grid export buffer (largest scene)
 
   bool stepped = false;  // grid() is empty until the first advance (src/nclr.h:101)
   int64_t steps_since_sort = 0;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  int64_t graph_steps = 0;
+  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parity][final]
   int64_t graph_launches = 0;
   int64_t launches = 0;
   int64_t active_nodes = 0;
@@ -71,6 +81,8 @@ struct nclr_sim {
   double prof_ms[NCLR_NUM_PHASES] = {};
   int64_t prof_launches[NCLR_NUM_PHASES] = {};
   std::string error;
+
+  const Params &P0() const { return scenes[0].P; }
 };
 
 namespace {
@@ -102,7 +114,8 @@ nclr_status alloc_particles(nclr_sim *s, int which) {
   const size_t n = (size_t)std::max<int64_t>(s->n, 1);
   const size_t fbytes = align_up(n * sizeof(float), 256);
   const int nfloat_fields = 2 * D + 2 * D * D + 3;
-  size_t total = fbytes * nfloat_fields + align_up(n * sizeof(int), 256) + align_up(n, 256);
+  const size_t total = fbytes * nfloat_fields + align_up(n * sizeof(int), 256) + align_up(n, 256) +
+                       align_up(n * sizeof(uint16_t), 256);
   char *base = nullptr;
   CUDA_TRY(s, cudaMalloc((void **)&base, total));
   s->slab[which] = base;
@@ -123,6 +136,8 @@ nclr_status alloc_particles(nclr_sim *s, int which) {
   p.id = (int *)(base + off);
   off += align_up(n * sizeof(int), 256);
   p.mat = s->has_mat ? (uint8_t *)(base + off) : nullptr;
+  off += align_up(n, 256);
+  p.scene = s->nscenes > 1 ? (uint16_t *)(base + off) : nullptr;
   p.stride = (int)n;
   return NCLR_OK;
 }
@@ -181,16 +196,16 @@ void collect_profile(nclr_sim *s) {
 // Enqueues the block sort of the current buffer into the other one (v and C move too when
 // the next P2G reads them, i.e. right after an upload).
 void enqueue_sort(nclr_sim *s, bool move_vc) {
-  const int nb = s->P.nblocks;
+  const int nb = s->total_blocks;
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     constexpr int cpb = mpm::Tiling<D>::CPB;
-    const int64_t nkeys = (int64_t)nb * cpb;
     phase(s, NCLR_PHASE_SORT, 6, [&] {
-      cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)nkeys, s->stream);
+      cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)s->nkeys, s->stream);
       cudaMemsetAsync(s->nblocks_active, 0, sizeof(int), s->stream);
-      mpm::launch_block_keys<D>(s->ps[s->cur], s->P, s->key, s->rank, s->count, s->stream);
-      mpm::launch_exclusive_scan(s->count, nkeys, s->start, s->tile_sums, s->stream);
+      mpm::launch_block_keys<D>(s->ps[s->cur], (int)s->n, s->scenes_d, s->key, s->rank, s->count,
+                                s->stream);
+      mpm::launch_exclusive_scan(s->count, s->nkeys, s->start, s->tile_sums, s->stream);
       mpm::launch_compact_blocks(s->start, nb, cpb, s->blocks, s->nblocks_active, s->stream);
       mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->key, s->rank,
                                s->start, s->count, move_vc, s->stream);
@@ -200,22 +215,25 @@ void enqueue_sort(nclr_sim *s, bool move_vc) {
   s->launches += 6;  // keys, 3 scan kernels, compaction, move
 }
 
-// Enqueues one step (optionally preceded by the block sort) on the handle's stream.  The
-// last step of a call writes v and C and reports the next step's P2G errors separately.
+// Enqueues one step of every scene (optionally preceded by the block sort) on the handle's
+// stream.  The last step of a call writes v and C and reports the next step's P2G errors
+// separately.
 void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
   if (sort && s->n > 0) enqueue_sort(s, false);
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     phase(s, NCLR_PHASE_GRID, 1, [&] {
-      mpm::launch_grid_sweep<D>(s->G, s->V, s->flags, s->P, s->work, s->sms, s->stream);
+      mpm::launch_grid_sweep<D>(s->G, s->V, s->flags, s->scenes_d, s->block_scene,
+                                s->total_blocks, s->work, s->sms, s->stream);
     });
     s->launches += 1;
     if (s->n > 0) {
       phase(s, NCLR_PHASE_G2P2G, 1, [&] {
-        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P, s->V, s->G, s->flags, s->blocks, s->nblocks_active,
-                             s->start, s->work, s->err_d, final_step ? s->err_d + 1 : s->err_d,
-                             s->ref, final_step ? mpm::kModeFinalStep : mpm::kModeStep,
-                             s->g2p2g_ctas, s->stream);
+        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
+                             s->flags, s->blocks, s->nblocks_active, s->start, s->work, s->err_d,
+                             final_step ? 1 : 0, s->ref,
+                             final_step ? mpm::kModeFinalStep : mpm::kModeStep, s->g2p2g_ctas,
+                             s->stream);
       });
       s->launches += 1;
     }
@@ -227,38 +245,51 @@ bool sort_due(const nclr_sim *s) {
          (s->opt.sort_interval > 0 && s->steps_since_sort >= s->opt.sort_interval);
 }
 
-int64_t chunk_steps(const nclr_sim *s) { return s->opt.sort_interval > 0 ? s->opt.sort_interval : 16; }
+// Steps per graph: a multiple of the sort interval (the graph starts at a sort boundary).
+int64_t chunk_steps(const nclr_sim *s) {
+  const int64_t si = s->opt.sort_interval;
+  if (s->opt.graph_steps <= 0) return si > 0 ? si : 16;
+  return si > 0 ? (s->opt.graph_steps + si - 1) / si * si : s->opt.graph_steps;
+}
 
-// Captures chunk_steps() steps starting at a sort boundary from buffer parity s->cur.
-nclr_status capture_graph(nclr_sim *s, int parity) {
+// Sorts inside one graph (one at the start of every sort interval).
+int64_t chunk_sorts(const nclr_sim *s) {
+  return s->opt.sort_interval > 0 ? chunk_steps(s) / s->opt.sort_interval : 0;
+}
+
+// Captures chunk_steps() steps starting at a sort boundary from buffer parity `parity`; with
+// `final_chunk` its last step is the call's final step (writes v and C).
+nclr_status capture_graph(nclr_sim *s, int parity, bool final_chunk) {
   const int saved_cur = s->cur;
   const int64_t saved_launches = s->launches;
   s->cur = parity;
   cudaGraph_t g = nullptr;
   CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const int64_t k = chunk_steps(s);
-  for (int64_t i = 0; i < k; ++i) enqueue_step(s, s->opt.sort_interval > 0 && i == 0, false);
+  const int64_t si = s->opt.sort_interval;
+  for (int64_t i = 0; i < k; ++i) enqueue_step(s, si > 0 && i % si == 0, final_chunk && i == k - 1);
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   s->graph_launches = s->launches - saved_launches;
   s->launches = saved_launches;
   s->cur = saved_cur;
   if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&s->graph[parity], g, 0);
+  e = cudaGraphInstantiate(&s->graph[parity][final_chunk ? 1 : 0], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  s->graph_steps = k;
   return NCLR_OK;
 }
 
-void fill_params(nclr_sim *s, int model, float dt, float E, float nu, float gravity) {
-  Params &P = s->P;
-  P.res = s->res;
-  P.N = s->res + 1;
-  P.n = (int)s->n;
+// The step parameters of one scene (the reference's constructor, src/nclr.h:74-78).
+Params scene_params(int dim, int64_t n, int model, int res, float dt, float E, float nu,
+                    float gravity) {
+  Params P{};
+  P.res = res;
+  P.N = res + 1;
+  P.n = (int)n;
   P.model = model;
   P.dt = dt;
   // dx = 1.0 / res in double, narrowed (src/nclr.h:76); inv_dx = 1 / dx in float
-  P.dx = (float)(1.0 / s->res);
+  P.dx = (float)(1.0 / res);
   P.inv_dx = 1.0f / P.dx;
   P.gravity = gravity;
   P.allowed = (float)((double)P.dx * 0.9 / (double)dt);  // src/nclr.h:285
@@ -269,25 +300,38 @@ void fill_params(nclr_sim *s, int model, float dt, float E, float nu, float grav
   P.cscale = 4.0f * P.inv_dx;
   P.dt_gravity = dt * gravity;
   int64_t nodes = 1;
-  for (int d = 0; d < s->dim; ++d) nodes *= P.N;
+  for (int d = 0; d < dim; ++d) nodes *= P.N;
   P.nodes = nodes;
-  const int bs = (s->dim == 3) ? mpm::Tiling<3>::BS : mpm::Tiling<2>::BS;
+  const int bs = (dim == 3) ? mpm::Tiling<3>::BS : mpm::Tiling<2>::BS;
   P.nb = (P.N + bs - 1) / bs;
   P.nblocks = 1;
-  for (int d = 0; d < s->dim; ++d) P.nblocks *= P.nb;
+  for (int d = 0; d < dim; ++d) P.nblocks *= P.nb;
+  return P;
 }
 
-// Upload of caller-ordered rows that already sit in device memory; the next advance() then
-// recomputes the coming P2G from them and re-sorts.
-nclr_status import_rows(nclr_sim *s, const float *x, const float *v, const float *F,
+// Upload of caller-ordered rows (device memory) into the slots of scene `sc` (-1: all); the
+// next advance() then recomputes the coming P2G from them and re-sorts.
+nclr_status import_rows(nclr_sim *s, int sc, const float *x, const float *v, const float *F,
                         const float *C, const float *Jp) {
+  const int begin = sc < 0 ? 0 : s->scenes[sc].slot_off;
+  const int count = sc < 0 ? (int)s->n : s->scenes[sc].P.n;
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
-    mpm::launch_import_particles<D>(s->ps[s->cur], (int)s->n, x, v, F, C, Jp, s->stream);
+    mpm::launch_import_particles<D>(s->ps[s->cur], begin, count, begin, x, v, F, C, Jp, s->stream);
   });
   s->acc_valid = false;  // the coming step's P2G must be recomputed from the new state
   s->need_sort = true;
   return check_launch(s, "import particles");
+}
+
+nclr_status export_rows(nclr_sim *s, int sc, float *x, float *v, float *F, float *C, float *Jp) {
+  const int begin = sc < 0 ? 0 : s->scenes[sc].slot_off;
+  const int count = sc < 0 ? (int)s->n : s->scenes[sc].P.n;
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int D = decltype(dc)::value;
+    mpm::launch_export_particles<D>(s->ps[s->cur], begin, count, begin, x, v, F, C, Jp, s->stream);
+  });
+  return check_launch(s, "export particles");
 }
 
 nclr_status ensure_staging(nclr_sim *s) {
@@ -299,8 +343,7 @@ nclr_status ensure_staging(nclr_sim *s) {
 struct Rows {
   float *x, *v, *F, *C, *Jp;
 };
-Rows staging_rows(nclr_sim *s) {
-  const size_t n = (size_t)s->n;
+Rows staging_rows(nclr_sim *s, int64_t n) {
   const int D = s->dim;
   Rows r;
   r.x = s->staging;
@@ -315,9 +358,12 @@ void release(nclr_sim *s) {
   if (!s) return;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  for (auto &g : s->graph)
-    if (g) cudaGraphExecDestroy(g);
+  for (auto &row : s->graph)
+    for (auto &g : row)
+      if (g) cudaGraphExecDestroy(g);
   for (auto p : s->slab) cudaFree(p);
+  cudaFree(s->scenes_d);
+  cudaFree(s->block_scene);
   cudaFree(s->G);
   cudaFree(s->V);
   cudaFree(s->flags);
@@ -343,55 +389,76 @@ void release(nclr_sim *s) {
   delete s;
 }
 
-}  // namespace
-
-extern "C" {
-
-void nclr_default_options(nclr_options *opt) {
-  if (!opt) return;
-  opt->physics = NCLR_PHYSICS_REFERENCE;
-  opt->sort_interval = 8;
-  opt->p2g_particles_per_thread = 8;
-  opt->device = 0;
-  opt->use_graphs = 1;
-  opt->profile = 0;
+nclr_status validate_scene(const nclr_scene &sc) {
+  if (sc.n < 0 || sc.n > (int64_t)0x7fffffff / 2) return fail(nullptr, NCLR_ERR_INVALID, "bad particle count");
+  if (sc.n > 0 && !sc.x) return fail(nullptr, NCLR_ERR_INVALID, "x is NULL");
+  if (sc.res < 1 || sc.res > 1024) return fail(nullptr, NCLR_ERR_INVALID, "res must be in [1, 1024]");
+  if (sc.model < 0 || sc.model > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material model");
+  if (sc.material)
+    for (int64_t p = 0; p < sc.n; ++p)
+      if (sc.material[p] > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material in material[]");
+  return NCLR_OK;
 }
 
-nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
-                        const float *F, const float *C, const float *Jp, const float *mass,
-                        const float *volume, const uint8_t *material, int model, int res,
-                        float dt, float E, float nu, float gravity, const nclr_options *opt) {
+// Creates a handle of `nscenes` scenes (nclr_create is the one-scene case).
+nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene *descs,
+                          const nclr_options *opt) {
   g_create_error.clear();
   if (!out) return fail(nullptr, NCLR_ERR_INVALID, "out is NULL");
   *out = nullptr;
   if (dim != 2 && dim != 3) return fail(nullptr, NCLR_ERR_INVALID, "dim must be 2 or 3");
-  if (n < 0 || n > (int64_t)0x7fffffff / 2) return fail(nullptr, NCLR_ERR_INVALID, "bad particle count");
-  if (n > 0 && !x) return fail(nullptr, NCLR_ERR_INVALID, "x is NULL");
-  if (res < 1 || res > 1024) return fail(nullptr, NCLR_ERR_INVALID, "res must be in [1, 1024]");
-  if (model < 0 || model > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material model");
-  if (material)
-    for (int64_t p = 0; p < n; ++p)
-      if (material[p] > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material in material[]");
+  if (nscenes < 1 || nscenes > 65535 || !descs) return fail(nullptr, NCLR_ERR_INVALID, "bad scene count");
+  int64_t total_n = 0;
+  bool any_mat = false;
+  for (int i = 0; i < nscenes; ++i) {
+    nclr_status st = validate_scene(descs[i]);
+    if (st != NCLR_OK) return st;
+    total_n += descs[i].n;
+    any_mat |= descs[i].material != nullptr;
+  }
+  if (total_n > (int64_t)0x7fffffff / 2) return fail(nullptr, NCLR_ERR_INVALID, "too many particles");
 
   nclr_sim *s = new (std::nothrow) nclr_sim();
   if (!s) return fail(nullptr, NCLR_ERR_INVALID, "out of host memory");
   nclr_default_options(&s->opt);
   if (opt) s->opt = *opt;
-  if (s->opt.p2g_particles_per_thread != 4 && s->opt.p2g_particles_per_thread != 16)
-    s->opt.p2g_particles_per_thread = 8;
   if (s->opt.sort_interval < 0) s->opt.sort_interval = 0;
   s->dim = dim;
-  s->n = n;
-  s->res = res;
+  s->n = total_n;
+  s->nscenes = nscenes;
   s->device = s->opt.device;
   s->ref = s->opt.physics != NCLR_PHYSICS_CORRECTED;
-  s->has_mat = material != nullptr;
+  s->has_mat = any_mat;
+  s->deferred_err.assign((size_t)nscenes, 0);
+  s->scene_err.assign((size_t)nscenes, 0);
 
+  // scene table: slot, node and block ranges
+  int64_t slot = 0, node = 0, block = 0;
+  for (int i = 0; i < nscenes; ++i) {
+    const nclr_scene &d = descs[i];
+    Scene sc{};
+    sc.P = scene_params(dim, d.n, d.model, d.res, d.dt, d.E, d.nu, d.gravity);
+    sc.slot_off = (int)slot;
+    sc.node_off = node;
+    sc.block_off = (int)std::min<int64_t>(block, 0x7fffffff);
+    slot += d.n;
+    node += sc.P.nodes;
+    block += sc.P.nblocks;
+    s->scenes.push_back(sc);
+  }
+  const int cpb = (dim == 3) ? mpm::Tiling<3>::CPB : mpm::Tiling<2>::CPB;
   auto bail = [&](nclr_status st) {
     g_create_error = s->error;
     release(s);
     return st;
   };
+  if (node > ((int64_t)1 << 34) || block * cpb > 0x7fffffff) {
+    s->error = "grids too large";
+    return bail(NCLR_ERR_INVALID);
+  }
+  s->total_nodes = node;
+  s->total_blocks = (int)block;
+  s->nkeys = block * cpb;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     s->error = "no CUDA device";
@@ -412,75 +479,210 @@ nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, cons
   } while (0)
   CREATE_TRY(cudaSetDevice(s->device));
   CREATE_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-  fill_params(s, model, dt, E, nu, gravity);
-  const int64_t nodes = s->P.nodes;
   for (int b = 0; b < 2; ++b)
     if ((st = alloc_particles(s, b)) != NCLR_OK) return bail(st);
-  const size_t np = (size_t)std::max<int64_t>(n, 1);
-  const size_t nblk = (size_t)s->P.nblocks;
-  const size_t nkeys = nblk * (size_t)(dim == 3 ? mpm::Tiling<3>::CPB : mpm::Tiling<2>::CPB);
+  const size_t np = (size_t)std::max<int64_t>(total_n, 1);
+  const size_t nblk = (size_t)block;
+  const size_t nodes = (size_t)node;
   CREATE_TRY(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
   s->g2p2g_ctas = s->sms * (dim == 3 ? mpm::g2p2g_ctas_per_sm<3>() : mpm::g2p2g_ctas_per_sm<2>());
-  CREATE_TRY(cudaMalloc((void **)&s->G, sizeof(float4) * (size_t)nodes));
-  CREATE_TRY(cudaMalloc((void **)&s->V, sizeof(float4) * (size_t)nodes));
+  CREATE_TRY(cudaMalloc((void **)&s->scenes_d, sizeof(Scene) * (size_t)nscenes));
+  CREATE_TRY(cudaMemcpyAsync(s->scenes_d, s->scenes.data(), sizeof(Scene) * (size_t)nscenes,
+                             cudaMemcpyHostToDevice, s->stream));
+  std::vector<uint16_t> block_scene;
+  if (nscenes > 1) {
+    block_scene.resize(nblk);
+    for (int i = 0; i < nscenes; ++i)
+      std::fill(block_scene.begin() + s->scenes[i].block_off,
+                block_scene.begin() + s->scenes[i].block_off + s->scenes[i].P.nblocks, (uint16_t)i);
+    CREATE_TRY(cudaMalloc((void **)&s->block_scene, sizeof(uint16_t) * nblk));
+    CREATE_TRY(cudaMemcpyAsync(s->block_scene, block_scene.data(), sizeof(uint16_t) * nblk,
+                               cudaMemcpyHostToDevice, s->stream));
+  }
+  CREATE_TRY(cudaMalloc((void **)&s->G, sizeof(float4) * nodes));
+  CREATE_TRY(cudaMalloc((void **)&s->V, sizeof(float4) * nodes));
   CREATE_TRY(cudaMalloc((void **)&s->flags, nblk));
-  CREATE_TRY(cudaMemsetAsync(s->flags, 0, nblk, s->stream));
   CREATE_TRY(cudaMalloc((void **)&s->key, sizeof(int) * np));
   CREATE_TRY(cudaMalloc((void **)&s->rank, sizeof(int) * np));
-  CREATE_TRY(cudaMalloc((void **)&s->count, sizeof(int) * nkeys));
-  CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (nkeys + 1)));
-  CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles((int64_t)nkeys), 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->count, sizeof(int) * (size_t)s->nkeys));
+  CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (size_t)(s->nkeys + 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles(s->nkeys), 1)));
   CREATE_TRY(cudaMalloc((void **)&s->blocks, sizeof(int) * nblk));
   CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, sizeof(int)));
   CREATE_TRY(cudaMalloc((void **)&s->work, sizeof(int)));
-  CREATE_TRY(cudaMalloc((void **)&s->err_d, 2 * sizeof(int)));
-  CREATE_TRY(cudaMallocHost((void **)&s->err_h, 2 * sizeof(int)));
-  CREATE_TRY(cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int), s->stream));
-  CREATE_TRY(cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)nodes, s->stream));
-  CREATE_TRY(cudaMemsetAsync(s->V, 0, sizeof(float4) * (size_t)nodes, s->stream));
+  CREATE_TRY(cudaMalloc((void **)&s->err_d, 2 * sizeof(int) * (size_t)nscenes));
+  CREATE_TRY(cudaMallocHost((void **)&s->err_h, 2 * sizeof(int) * (size_t)nscenes));
+  CREATE_TRY(cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)nscenes, s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->G, 0, sizeof(float4) * nodes, s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->V, 0, sizeof(float4) * nodes, s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->flags, 0, nblk, s->stream));
   CREATE_TRY(cudaMemsetAsync(s->nblocks_active, 0, sizeof(int), s->stream));
 
-  if (n > 0) {
+  if (total_n > 0) {
     // Per-particle scalars go straight into the SoA (component stride == n there).
     PState &p = s->ps[0];
-    std::vector<float> ones((size_t)n, 1.0f);
-    std::vector<int> iota((size_t)n);
-    for (int64_t i = 0; i < n; ++i) iota[(size_t)i] = (int)i;
-    CREATE_TRY(cudaMemcpyAsync(p.mass, mass ? mass : ones.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
-    CREATE_TRY(cudaMemcpyAsync(p.vol, volume ? volume : ones.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
-    CREATE_TRY(cudaMemcpyAsync(p.id, iota.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
-    if (material) CREATE_TRY(cudaMemcpyAsync(p.mat, material, (size_t)n, cudaMemcpyHostToDevice, s->stream));
-
-    // Rows: x, v, F, C, Jp with the constructor's defaults for the NULL ones
-    // (Particle<dim>: v = 0, F = diag<dim>(1), C = 0, Jp = 1; src/nclr.h:46-47).
+    std::vector<float> mass((size_t)total_n, 1.0f), vol((size_t)total_n, 1.0f);
+    std::vector<int> iota((size_t)total_n);
+    std::vector<uint8_t> mat(any_mat ? (size_t)total_n : 0);
+    std::vector<uint16_t> pscene(nscenes > 1 ? (size_t)total_n : 0);
+    std::vector<float> host((size_t)total_n * row_floats(dim), 0.0f);
+    const int64_t N = total_n;
+    float *hx = host.data(), *hv = hx + N * dim, *hF = hv + N * dim, *hC = hF + N * dim * dim,
+          *hJ = hC + N * dim * dim;
+    for (int i = 0; i < nscenes; ++i) {
+      const nclr_scene &d = descs[i];
+      const int64_t o = s->scenes[i].slot_off;
+      for (int64_t q = 0; q < d.n; ++q) {
+        iota[(size_t)(o + q)] = (int)(o + q);
+        if (d.mass) mass[(size_t)(o + q)] = d.mass[q];
+        if (d.volume) vol[(size_t)(o + q)] = d.volume[q];
+        if (any_mat) mat[(size_t)(o + q)] = d.material ? d.material[q] : (uint8_t)d.model;
+        if (nscenes > 1) pscene[(size_t)(o + q)] = (uint16_t)i;
+        hJ[o + q] = d.Jp ? d.Jp[q] : 1.0f;
+      }
+      // Rows: x, v, F, C with the constructor's defaults for the NULL ones
+      // (Particle<dim>: v = 0, F = diag<dim>(1), C = 0, Jp = 1; src/nclr.h:46-47).
+      if (d.n > 0) std::memcpy(hx + o * dim, d.x, sizeof(float) * d.n * dim);
+      if (d.v) std::memcpy(hv + o * dim, d.v, sizeof(float) * d.n * dim);
+      if (d.F) {
+        std::memcpy(hF + o * dim * dim, d.F, sizeof(float) * d.n * dim * dim);
+      } else {
+        for (int64_t q = 0; q < d.n; ++q)
+          for (int k = 0; k < dim; ++k)
+            hF[((o + q) * dim + k) * dim + k] = (k < 2 || !s->ref) ? 1.0f : 0.0f;
+      }
+      if (d.C) std::memcpy(hC + o * dim * dim, d.C, sizeof(float) * d.n * dim * dim);
+    }
+    CREATE_TRY(cudaMemcpyAsync(p.mass, mass.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s->stream));
+    CREATE_TRY(cudaMemcpyAsync(p.vol, vol.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s->stream));
+    CREATE_TRY(cudaMemcpyAsync(p.id, iota.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s->stream));
+    if (any_mat) CREATE_TRY(cudaMemcpyAsync(p.mat, mat.data(), (size_t)N, cudaMemcpyHostToDevice, s->stream));
+    if (nscenes > 1)
+      CREATE_TRY(cudaMemcpyAsync(p.scene, pscene.data(), sizeof(uint16_t) * N, cudaMemcpyHostToDevice, s->stream));
     if ((st = ensure_staging(s)) != NCLR_OK) return bail(st);
-    const Rows r = staging_rows(s);
-    std::vector<float> host((size_t)n * row_floats(dim), 0.0f);
-    float *hx = host.data(), *hv = hx + n * dim, *hF = hv + n * dim, *hC = hF + n * dim * dim,
-          *hJ = hC + n * dim * dim;
-    std::memcpy(hx, x, sizeof(float) * n * dim);
-    if (v) std::memcpy(hv, v, sizeof(float) * n * dim);
-    if (F) {
-      std::memcpy(hF, F, sizeof(float) * n * dim * dim);
-    } else {
-      for (int64_t q = 0; q < n; ++q)
-        for (int d = 0; d < dim; ++d)
-          hF[(q * dim + d) * dim + d] = (d < 2 || !s->ref) ? 1.0f : 0.0f;
-    }
-    if (C) std::memcpy(hC, C, sizeof(float) * n * dim * dim);
-    if (Jp) {
-      std::memcpy(hJ, Jp, sizeof(float) * n);
-    } else {
-      for (int64_t q = 0; q < n; ++q) hJ[q] = 1.0f;
-    }
+    const Rows r = staging_rows(s, N);
     CREATE_TRY(cudaMemcpyAsync(r.x, host.data(), sizeof(float) * host.size(), cudaMemcpyHostToDevice, s->stream));
-    if ((st = import_rows(s, r.x, r.v, r.F, r.C, r.Jp)) != NCLR_OK) return bail(st);
-    CREATE_TRY(cudaStreamSynchronize(s->stream));  // `host` goes out of scope
+    if ((st = import_rows(s, -1, r.x, r.v, r.F, r.C, r.Jp)) != NCLR_OK) return bail(st);
+    CREATE_TRY(cudaStreamSynchronize(s->stream));  // the host vectors go out of scope
   }
   CREATE_TRY(cudaStreamSynchronize(s->stream));
 #undef CREATE_TRY
   *out = s;
   return NCLR_OK;
+}
+
+nclr_status check_scene(nclr_sim *s, int scene) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  if (scene < 0 || scene >= s->nscenes) return fail(s, NCLR_ERR_INVALID, "scene index out of range");
+  return NCLR_OK;
+}
+
+// Host copies of particle fields of scene `sc` (-1: all scenes, caller order throughout).
+nclr_status get_particles_host(nclr_sim *s, int sc, float *x, float *v, float *F, float *C, float *Jp) {
+  const int64_t n = sc < 0 ? s->n : s->scenes[sc].P.n;
+  if (n == 0) return NCLR_OK;
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  nclr_status st = ensure_staging(s);
+  if (st != NCLR_OK) return st;
+  const Rows r = staging_rows(s, n);
+  st = export_rows(s, sc, x ? r.x : nullptr, v ? r.v : nullptr, F ? r.F : nullptr,
+                   C ? r.C : nullptr, Jp ? r.Jp : nullptr);
+  if (st != NCLR_OK) return st;
+  const size_t nn = (size_t)n, D = (size_t)s->dim;
+  if (x) CUDA_TRY(s, cudaMemcpyAsync(x, r.x, sizeof(float) * nn * D, cudaMemcpyDeviceToHost, s->stream));
+  if (v) CUDA_TRY(s, cudaMemcpyAsync(v, r.v, sizeof(float) * nn * D, cudaMemcpyDeviceToHost, s->stream));
+  if (F) CUDA_TRY(s, cudaMemcpyAsync(F, r.F, sizeof(float) * nn * D * D, cudaMemcpyDeviceToHost, s->stream));
+  if (C) CUDA_TRY(s, cudaMemcpyAsync(C, r.C, sizeof(float) * nn * D * D, cudaMemcpyDeviceToHost, s->stream));
+  if (Jp) CUDA_TRY(s, cudaMemcpyAsync(Jp, r.Jp, sizeof(float) * nn, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return NCLR_OK;
+}
+
+nclr_status set_particles_host(nclr_sim *s, int sc, const float *x, const float *v, const float *F,
+                               const float *C, const float *Jp) {
+  const int64_t n = sc < 0 ? s->n : s->scenes[sc].P.n;
+  if (n == 0) return NCLR_OK;
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  nclr_status st = ensure_staging(s);
+  if (st != NCLR_OK) return st;
+  const Rows r = staging_rows(s, n);
+  const size_t nn = (size_t)n, D = (size_t)s->dim;
+  if (x) CUDA_TRY(s, cudaMemcpyAsync(r.x, x, sizeof(float) * nn * D, cudaMemcpyHostToDevice, s->stream));
+  if (v) CUDA_TRY(s, cudaMemcpyAsync(r.v, v, sizeof(float) * nn * D, cudaMemcpyHostToDevice, s->stream));
+  if (F) CUDA_TRY(s, cudaMemcpyAsync(r.F, F, sizeof(float) * nn * D * D, cudaMemcpyHostToDevice, s->stream));
+  if (C) CUDA_TRY(s, cudaMemcpyAsync(r.C, C, sizeof(float) * nn * D * D, cudaMemcpyHostToDevice, s->stream));
+  if (Jp) CUDA_TRY(s, cudaMemcpyAsync(r.Jp, Jp, sizeof(float) * nn, cudaMemcpyHostToDevice, s->stream));
+  st = import_rows(s, sc, x ? r.x : nullptr, v ? r.v : nullptr, F ? r.F : nullptr,
+                   C ? r.C : nullptr, Jp ? r.Jp : nullptr);
+  if (st != NCLR_OK) return st;
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers
+  return NCLR_OK;
+}
+
+nclr_status get_grid_host(nclr_sim *s, int sc, float *velocity, float *mass) {
+  if (!s->stepped) return fail(s, NCLR_ERR_INVALID, "grid() is empty before the first advance()");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  const Scene &S = s->scenes[sc];
+  const size_t nodes = (size_t)S.P.nodes, D = (size_t)s->dim;
+  if (!s->grid_staging) {
+    size_t mx = 0;
+    for (const auto &x : s->scenes) mx = std::max(mx, (size_t)x.P.nodes);
+    CUDA_TRY(s, cudaMalloc((void **)&s->grid_staging, sizeof(float) * mx * (D + 1)));
+  }
+  float *dv = s->grid_staging, *dm = dv + nodes * D;
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    mpm::launch_copy_vgrid<DD>(s->V + S.node_off, S.P.nodes, dv, dm, s->stream);
+  });
+  nclr_status st = check_launch(s, "export grid");
+  if (st != NCLR_OK) return st;
+  if (velocity) CUDA_TRY(s, cudaMemcpyAsync(velocity, dv, sizeof(float) * nodes * D, cudaMemcpyDeviceToHost, s->stream));
+  if (mass) CUDA_TRY(s, cudaMemcpyAsync(mass, dm, sizeof(float) * nodes, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return NCLR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nclr_default_options(nclr_options *opt) {
+  if (!opt) return;
+  opt->physics = NCLR_PHYSICS_REFERENCE;
+  opt->sort_interval = 8;
+  opt->p2g_particles_per_thread = 8;
+  opt->device = 0;
+  opt->use_graphs = 1;
+  opt->profile = 0;
+  opt->graph_steps = 0;
+}
+
+nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
+                        const float *F, const float *C, const float *Jp, const float *mass,
+                        const float *volume, const uint8_t *material, int model, int res,
+                        float dt, float E, float nu, float gravity, const nclr_options *opt) {
+  nclr_scene d{};
+  d.n = n;
+  d.x = x;
+  d.v = v;
+  d.F = F;
+  d.C = C;
+  d.Jp = Jp;
+  d.mass = mass;
+  d.volume = volume;
+  d.material = material;
+  d.model = model;
+  d.res = res;
+  d.dt = dt;
+  d.E = E;
+  d.nu = nu;
+  d.gravity = gravity;
+  return create_scenes(out, dim, 1, &d, opt);
+}
+
+nclr_status nclr_batch_create(nclr_sim **out, int dim, int nscenes, const nclr_scene *scenes,
+                              const nclr_options *opt) {
+  return create_scenes(out, dim, nscenes, scenes, opt);
 }
 
 nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
@@ -489,7 +691,7 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
   if (nsteps < 0) return fail(s, NCLR_ERR_INVALID, "nsteps < 0");
   if (nsteps == 0) return NCLR_OK;
   CUDA_TRY(s, cudaSetDevice(s->device));
-  CUDA_TRY(s, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int), s->stream));
+  CUDA_TRY(s, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)s->nscenes, s->stream));
   s->launches = 0;
   if (s->need_sort && s->n > 0) {  // the uploaded particles: sort them (with v and C) first
     enqueue_sort(s, !s->acc_valid);
@@ -497,16 +699,18 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
     s->steps_since_sort = 0;
   }
   if (!s->acc_valid) {  // the first step's P2G, from the uploaded state
-    s->deferred_err = 0;  // an error of the discarded P2G no longer applies
+    std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // discarded with the P2G
     dispatch_dim(s->dim, [&](auto dc) {
       constexpr int D = decltype(dc)::value;
-      phase(s, NCLR_PHASE_P2G, 3, [&] {
-        mpm::launch_discard_pending<D>(s->G, s->flags, s->P, s->sms, s->stream);
+      phase(s, NCLR_PHASE_P2G, 2, [&] {
+        mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
+                                       s->total_blocks, s->sms, s->stream);
         // the fused kernel's block counter (before a regular step the sweep resets it)
         cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
-        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P, s->V, s->G, s->flags, s->blocks,
-                             s->nblocks_active, s->start, s->work, s->err_d, s->err_d, s->ref,
-                             mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
+        if (s->n > 0)
+          mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
+                               s->flags, s->blocks, s->nblocks_active, s->start, s->work, s->err_d, 0,
+                               s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
       });
     });
     s->launches += (s->n > 0) ? 2 : 1;
@@ -517,18 +721,16 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
   while (left > 0) {
     const bool sort = sort_due(s);
     const bool at_boundary = s->opt.sort_interval == 0 || sort;
-    if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left - 1 >= chunk) {
-      if (!s->graph[s->cur]) {
-        nclr_status st = capture_graph(s, s->cur);
+    if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left >= chunk) {
+      const int fin = (left == chunk) ? 1 : 0;
+      if (!s->graph[s->cur][fin]) {
+        nclr_status st = capture_graph(s, s->cur, fin != 0);
         if (st != NCLR_OK) return st;
       }
-      CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur], s->stream));
+      CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur][fin], s->stream));
       s->launches += s->graph_launches;
-      if (s->opt.sort_interval > 0) {
-        s->cur ^= 1;
-        s->steps_since_sort = 0;
-      }
-      s->steps_since_sort += chunk;
+      if (chunk_sorts(s) & 1) s->cur ^= 1;
+      if (s->opt.sort_interval > 0) s->steps_since_sort = s->opt.sort_interval;
       left -= chunk;
       continue;
     }
@@ -540,15 +742,22 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
   nclr_status st = check_launch(s, "advance");
   if (st != NCLR_OK) return st;
   s->stepped = true;
-  CUDA_TRY(s, cudaMemcpyAsync(s->err_h, s->err_d, 2 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaMemcpyAsync(s->err_h, s->err_d, 2 * sizeof(int) * (size_t)s->nscenes,
+                              cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(s, cudaStreamSynchronize(s->stream));
   collect_profile(s);
-  const int errs = s->err_h[0] | s->deferred_err;
-  s->deferred_err = s->err_h[1];
-  if (errs & mpm::kErrOutOfRange)
+  int first = -1;
+  for (int i = 0; i < s->nscenes; ++i) {
+    const int e = s->err_h[2 * i] | s->deferred_err[(size_t)i];
+    s->deferred_err[(size_t)i] = s->err_h[2 * i + 1];
+    s->scene_err[(size_t)i] = (e & mpm::kErrOutOfRange) ? NCLR_ERR_OUT_OF_RANGE : NCLR_OK;
+    if ((e & mpm::kErrOutOfRange) && first < 0) first = i;
+  }
+  if (first >= 0)
     return fail(s, NCLR_ERR_OUT_OF_RANGE,
                 "a particle's stencil left the grid (the reference's vector::at throws "
-                "std::out_of_range here)");
+                "std::out_of_range here)" +
+                    (s->nscenes > 1 ? std::string(" in scene ") + std::to_string(first) : ""));
   return NCLR_OK;
 }
 
@@ -557,11 +766,7 @@ nclr_status nclr_get_particles_device(nclr_sim *s, float *x, float *v, float *F,
   if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
   s->error.clear();
   CUDA_TRY(s, cudaSetDevice(s->device));
-  dispatch_dim(s->dim, [&](auto dc) {
-    constexpr int D = decltype(dc)::value;
-    mpm::launch_export_particles<D>(s->ps[s->cur], (int)s->n, x, v, F, C, Jp, s->stream);
-  });
-  return check_launch(s, "export particles");
+  return export_rows(s, -1, x, v, F, C, Jp);
 }
 
 nclr_status nclr_set_particles_device(nclr_sim *s, const float *x, const float *v,
@@ -570,84 +775,69 @@ nclr_status nclr_set_particles_device(nclr_sim *s, const float *x, const float *
   s->error.clear();
   CUDA_TRY(s, cudaSetDevice(s->device));
   if (s->n == 0) return NCLR_OK;
-  return import_rows(s, x, v, F, C, Jp);
+  return import_rows(s, -1, x, v, F, C, Jp);
 }
 
 nclr_status nclr_get_particles(nclr_sim *s, float *x, float *v, float *F, float *C, float *Jp) {
   if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
   s->error.clear();
-  if (s->n == 0) return NCLR_OK;
-  CUDA_TRY(s, cudaSetDevice(s->device));
-  nclr_status st = ensure_staging(s);
-  if (st != NCLR_OK) return st;
-  const Rows r = staging_rows(s);
-  st = nclr_get_particles_device(s, x ? r.x : nullptr, v ? r.v : nullptr, F ? r.F : nullptr,
-                                 C ? r.C : nullptr, Jp ? r.Jp : nullptr);
-  if (st != NCLR_OK) return st;
-  const size_t n = (size_t)s->n, D = (size_t)s->dim;
-  if (x) CUDA_TRY(s, cudaMemcpyAsync(x, r.x, sizeof(float) * n * D, cudaMemcpyDeviceToHost, s->stream));
-  if (v) CUDA_TRY(s, cudaMemcpyAsync(v, r.v, sizeof(float) * n * D, cudaMemcpyDeviceToHost, s->stream));
-  if (F) CUDA_TRY(s, cudaMemcpyAsync(F, r.F, sizeof(float) * n * D * D, cudaMemcpyDeviceToHost, s->stream));
-  if (C) CUDA_TRY(s, cudaMemcpyAsync(C, r.C, sizeof(float) * n * D * D, cudaMemcpyDeviceToHost, s->stream));
-  if (Jp) CUDA_TRY(s, cudaMemcpyAsync(Jp, r.Jp, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream));
-  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
-  return NCLR_OK;
+  return get_particles_host(s, -1, x, v, F, C, Jp);
 }
 
 nclr_status nclr_set_particles(nclr_sim *s, const float *x, const float *v, const float *F,
                                const float *C, const float *Jp) {
   if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
   s->error.clear();
-  if (s->n == 0) return NCLR_OK;
-  CUDA_TRY(s, cudaSetDevice(s->device));
-  nclr_status st = ensure_staging(s);
-  if (st != NCLR_OK) return st;
-  const Rows r = staging_rows(s);
-  const size_t n = (size_t)s->n, D = (size_t)s->dim;
-  if (x) CUDA_TRY(s, cudaMemcpyAsync(r.x, x, sizeof(float) * n * D, cudaMemcpyHostToDevice, s->stream));
-  if (v) CUDA_TRY(s, cudaMemcpyAsync(r.v, v, sizeof(float) * n * D, cudaMemcpyHostToDevice, s->stream));
-  if (F) CUDA_TRY(s, cudaMemcpyAsync(r.F, F, sizeof(float) * n * D * D, cudaMemcpyHostToDevice, s->stream));
-  if (C) CUDA_TRY(s, cudaMemcpyAsync(r.C, C, sizeof(float) * n * D * D, cudaMemcpyHostToDevice, s->stream));
-  if (Jp) CUDA_TRY(s, cudaMemcpyAsync(r.Jp, Jp, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
-  st = import_rows(s, x ? r.x : nullptr, v ? r.v : nullptr, F ? r.F : nullptr, C ? r.C : nullptr,
-                   Jp ? r.Jp : nullptr);
-  if (st != NCLR_OK) return st;
-  CUDA_TRY(s, cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers
-  return NCLR_OK;
+  return set_particles_host(s, -1, x, v, F, C, Jp);
 }
 
 nclr_status nclr_get_grid(nclr_sim *s, float *velocity, float *mass) {
   if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
   s->error.clear();
-  if (!s->stepped) return fail(s, NCLR_ERR_INVALID, "grid() is empty before the first advance()");
-  CUDA_TRY(s, cudaSetDevice(s->device));
-  const size_t nodes = (size_t)s->P.nodes, D = (size_t)s->dim;
-  if (!s->grid_staging)
-    CUDA_TRY(s, cudaMalloc((void **)&s->grid_staging, sizeof(float) * nodes * (D + 1)));
-  float *dv = s->grid_staging, *dm = dv + nodes * D;
-  dispatch_dim(s->dim, [&](auto dc) {
-    constexpr int DD = decltype(dc)::value;
-    mpm::launch_copy_vgrid<DD>(s->V, s->P.nodes, dv, dm, s->stream);
-  });
-  nclr_status st = check_launch(s, "export grid");
+  return get_grid_host(s, 0, velocity, mass);
+}
+
+int nclr_num_scenes(const nclr_sim *s) { return s ? s->nscenes : -1; }
+
+nclr_status nclr_scene_get_particles(nclr_sim *s, int scene, float *x, float *v, float *F,
+                                     float *C, float *Jp) {
+  nclr_status st = check_scene(s, scene);
   if (st != NCLR_OK) return st;
-  if (velocity) CUDA_TRY(s, cudaMemcpyAsync(velocity, dv, sizeof(float) * nodes * D, cudaMemcpyDeviceToHost, s->stream));
-  if (mass) CUDA_TRY(s, cudaMemcpyAsync(mass, dm, sizeof(float) * nodes, cudaMemcpyDeviceToHost, s->stream));
-  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
-  return NCLR_OK;
+  s->error.clear();
+  return get_particles_host(s, scene, x, v, F, C, Jp);
+}
+
+nclr_status nclr_scene_set_particles(nclr_sim *s, int scene, const float *x, const float *v,
+                                     const float *F, const float *C, const float *Jp) {
+  nclr_status st = check_scene(s, scene);
+  if (st != NCLR_OK) return st;
+  s->error.clear();
+  return set_particles_host(s, scene, x, v, F, C, Jp);
+}
+
+nclr_status nclr_scene_get_grid(nclr_sim *s, int scene, float *velocity, float *mass) {
+  nclr_status st = check_scene(s, scene);
+  if (st != NCLR_OK) return st;
+  s->error.clear();
+  return get_grid_host(s, scene, velocity, mass);
+}
+
+nclr_status nclr_scene_status(const nclr_sim *s, int scene) {
+  if (!s || scene < 0 || scene >= s->nscenes) return NCLR_ERR_INVALID;
+  return (nclr_status)s->scene_err[(size_t)scene];
 }
 
 nclr_status nclr_get_lame(const nclr_sim *s, float *mu_0, float *lambda_0) {
   if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
-  if (mu_0) *mu_0 = s->P.mu0;
-  if (lambda_0) *lambda_0 = s->P.lambda0;
+  if (mu_0) *mu_0 = s->P0().mu0;
+  if (lambda_0) *lambda_0 = s->P0().lambda0;
   return NCLR_OK;
 }
 
 int64_t nclr_num_particles(const nclr_sim *s) { return s ? s->n : -1; }
 int nclr_dim(const nclr_sim *s) { return s ? s->dim : -1; }
-int nclr_res(const nclr_sim *s) { return s ? s->res : -1; }
-int64_t nclr_num_nodes(const nclr_sim *s) { return s ? s->P.nodes : -1; }
+int nclr_res(const nclr_sim *s) { return s ? s->P0().res : -1; }
+int64_t nclr_num_nodes(const nclr_sim *s) { return s ? s->P0().nodes : -1; }
 void *nclr_stream(nclr_sim *s) { return s ? (void *)s->stream : nullptr; }
 
 nclr_status nclr_stats(const nclr_sim *s, int64_t *kernel_launches, int64_t *active_nodes) {
@@ -663,7 +853,7 @@ nclr_status nclr_count_active_nodes(nclr_sim *s, int64_t *active_nodes) {
   CUDA_TRY(s, cudaSetDevice(s->device));
   if (!s->active_d) CUDA_TRY(s, cudaMalloc((void **)&s->active_d, sizeof(unsigned long long)));
   CUDA_TRY(s, cudaMemsetAsync(s->active_d, 0, sizeof(unsigned long long), s->stream));
-  mpm::launch_count_active(s->V, s->P.nodes, s->active_d, s->stream);
+  mpm::launch_count_active(s->V, s->total_nodes, s->active_d, s->stream);
   nclr_status st = check_launch(s, "count active nodes");
   if (st != NCLR_OK) return st;
   unsigned long long h = 0;

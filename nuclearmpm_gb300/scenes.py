@@ -160,11 +160,31 @@ def random_scene_2d(rng, n: int, res: int, physics: int = REFERENCE) -> dict:
         side = int(np.ceil(np.sqrt(k)))
         spacing = 0.5 * dx
         edge = side * spacing
-        edge_max = 0.8
+        edge_max = 0.7
         if edge > edge_max:
             spacing = edge_max / side
             edge = edge_max
-        lo = rng.uniform(0.1, 0.9 - edge, size=2)
+        lo = rng.uniform(0.1, max(0.1, 0.9 - edge), size=2)
         x = jittered_block(rng, (side, side), spacing, lo, 0.25 * spacing)[:k]
         xs.append(x)
     return particles(np.concatenate(xs), physics=physics)
+
+
+def batched_scenes_2d(seed: int = 0, count: int = 256, n_min: int = 1000, n_max: int = 65536,
+                      physics: int = REFERENCE) -> list:
+    """Independent 2D scenes for the batched form: per scene a particle count log-uniform in
+    [n_min, n_max], grid resolution from {64, 128, 256}, material uniform over {liquid, snow,
+    jelly}, Young's modulus log-uniform in [1e3, 1e5], Poisson ratio uniform in [0.1, 0.4],
+    1-3 jittered cubes; dt = 1e-4."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        res = int(rng.choice([64, 128, 256]))
+        model = int(rng.choice([LIQUID, SNOW, JELLY]))
+        E = float(np.exp(rng.uniform(np.log(1e3), np.log(1e5))))
+        nu = float(rng.uniform(0.1, 0.4))
+        sc = random_scene_2d(rng, n, res, physics=physics)
+        sc.update(model=model, res=res, E=E, nu=nu, dt=1e-4, gravity=-100.0)
+        out.append(sc)
+    return out

@@ -138,7 +138,7 @@ class MPMSimulation:
                  E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, *, dim: int | None = None,
                  material: np.ndarray | None = None, physics: int = capi.PHYSICS_REFERENCE,
                  sort_interval: int = 8, particles_per_thread: int = 8, device: int = 0,
-                 use_graphs: bool = True, profile: bool = False):
+                 use_graphs: bool = True, profile: bool = False, graph_steps: int = 0):
         L = capi.lib()
         self.dim, soa = _soa_from(particles, dim)
         self._c = soa.pop("c")
@@ -150,7 +150,8 @@ class MPMSimulation:
         mat = None if material is None else np.ascontiguousarray(material, dtype=np.uint8)
         opt = capi.default_options(physics=physics, sort_interval=sort_interval,
                                    p2g_particles_per_thread=particles_per_thread, device=device,
-                                   use_graphs=int(use_graphs), profile=int(profile))
+                                   use_graphs=int(use_graphs), profile=int(profile),
+                                   graph_steps=graph_steps)
         h = ctypes.c_void_p()
         st = L.nclr_create(ctypes.byref(h), self.dim, self.n, _ptr(soa["x"]), _ptr(soa["v"]),
                            _ptr(soa["F"]), _ptr(soa["C"]), _ptr(soa["Jp"]), _ptr(soa["mass"]),
@@ -249,3 +250,121 @@ class MPMSimulation:
 
     def __exit__(self, *a):
         self.close()
+
+
+class BatchSimulation:
+    """Many independent simulations stepped together (nclr_batch_create): every kernel of a
+    step covers all scenes in one launch.  `scenes` is a list of dicts with the particle
+    arrays (x, and optionally v, F, C, Jp, mass, volume, material) and the parameters model,
+    res, dt, E, nu, gravity (the MPMSimulation defaults apply to missing ones)."""
+
+    def __init__(self, scenes: list, *, dim: int | None = None,
+                 physics: int = capi.PHYSICS_REFERENCE, sort_interval: int = 8, device: int = 0,
+                 use_graphs: bool = True, graph_steps: int = 0, profile: bool = False):
+        L = capi.lib()
+        if not scenes:
+            raise ValueError("a batch needs at least one scene")
+        self._keep = []
+        descs = (capi.Scene * len(scenes))()
+        self.dims = []
+        self.sizes = []
+        self.res = []
+        for i, sc in enumerate(scenes):
+            d, soa = _soa_from(sc, dim)
+            self.dims.append(d)
+            soa.pop("c")
+            mat = sc.get("material")
+            mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
+            self._keep.append((soa, mat))
+            descs[i].n = soa["x"].shape[0]
+            for k in ("x", "v", "F", "C", "Jp", "mass", "volume"):
+                setattr(descs[i], k, _ptr(soa[k]))
+            descs[i].material = _ptr(mat)
+            descs[i].model = int(sc.get("model", 0))
+            descs[i].res = int(sc.get("res", 64))
+            descs[i].dt = float(sc.get("dt", 1e-4))
+            descs[i].E = float(sc.get("E", 1e4))
+            descs[i].nu = float(sc.get("nu", 0.2))
+            descs[i].gravity = float(sc.get("gravity", -100.0))
+            self.sizes.append(int(descs[i].n))
+            self.res.append(int(descs[i].res))
+        if len(set(self.dims)) != 1:
+            raise ValueError("all scenes of a batch have the same dimension")
+        self.dim = self.dims[0]
+        opt = capi.default_options(physics=physics, sort_interval=sort_interval, device=device,
+                                   use_graphs=int(use_graphs), profile=int(profile),
+                                   graph_steps=graph_steps)
+        h = ctypes.c_void_p()
+        capi.check(L.nclr_batch_create(ctypes.byref(h), self.dim, len(scenes), descs,
+                                       ctypes.byref(opt)), None)
+        self._h = h
+        self._keep = None
+        self._stepped = False
+
+    def __len__(self):
+        return len(self.sizes)
+
+    def advance(self, steps: int = 1) -> None:
+        capi.check(capi.lib().nclr_advance(self._h, int(steps)), self._h)
+        self._stepped = True
+
+    def particles(self, scene: int) -> dict:
+        n, d = self.sizes[scene], self.dim
+        out = {"x": np.empty((n, d), np.float32), "v": np.empty((n, d), np.float32),
+               "F": np.empty((n, d, d), np.float32), "C": np.empty((n, d, d), np.float32),
+               "Jp": np.empty((n,), np.float32)}
+        capi.check(capi.lib().nclr_scene_get_particles(self._h, scene, *(_ptr(out[k]) for k in
+                                                                         ("x", "v", "F", "C", "Jp"))),
+                   self._h)
+        return out
+
+    def set_particles(self, scene: int, x=None, v=None, F=None, C=None, Jp=None) -> None:
+        n, d = self.sizes[scene], self.dim
+        arr = lambda a, s: None if a is None else np.ascontiguousarray(np.asarray(a, np.float32).reshape(s))  # noqa: E731
+        vals = [arr(x, (n, d)), arr(v, (n, d)), arr(F, (n, d, d)), arr(C, (n, d, d)), arr(Jp, (n,))]
+        capi.check(capi.lib().nclr_scene_set_particles(self._h, scene, *(_ptr(a) for a in vals)),
+                   self._h)
+
+    def grid(self, scene: int) -> GridArrays:
+        if not self._stepped:
+            return GridArrays(np.zeros((0, self.dim), np.float32), np.zeros((0,), np.float32))
+        nodes = (self.res[scene] + 1) ** self.dim
+        vel = np.empty((nodes, self.dim), np.float32)
+        mass = np.empty((nodes,), np.float32)
+        capi.check(capi.lib().nclr_scene_get_grid(self._h, scene, _ptr(vel), _ptr(mass)), self._h)
+        return GridArrays(vel, mass)
+
+    def status(self, scene: int) -> int:
+        return int(capi.lib().nclr_scene_status(self._h, scene))
+
+    @property
+    def stream(self) -> int:
+        return int(capi.lib().nclr_stream(self._h) or 0)
+
+    def stats(self) -> tuple[int, int]:
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        capi.check(capi.lib().nclr_stats(self._h, ctypes.byref(a), ctypes.byref(b)), self._h)
+        return int(a.value), int(b.value)
+
+    def profile(self) -> dict:
+        out = {}
+        for i, name in enumerate(capi.PHASE_NAMES):
+            ms, n = ctypes.c_double(), ctypes.c_int64()
+            capi.check(capi.lib().nclr_profile_get(self._h, i, ctypes.byref(ms), ctypes.byref(n)),
+                       self._h)
+            out[name] = (float(ms.value), int(n.value))
+        return out
+
+    def profile_reset(self) -> None:
+        capi.check(capi.lib().nclr_profile_reset(self._h), self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            capi.lib().nclr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
