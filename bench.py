@@ -162,6 +162,53 @@ def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float):
     return m * steps / dt, desc
 
 
+def run_batched(device: int, steps: int = 100) -> dict:
+    """The batched form on 256 independent 2D scenes (particle counts log-uniform in
+    [1,000, 65,536], grids of 64/128/256, mixed materials and moduli; seeded): one
+    BatchSimulation advancing `steps` steps in one CUDA graph, against the same scenes stepped
+    one after another as plain simulations (each `steps` steps with its own graphs).  Both
+    timed with CUDA events on the simulations' streams after a warm-up call."""
+    import torch
+
+    from nuclearmpm_gb300 import BatchSimulation, MPMSimulation, autotune, scenes
+    scs = scenes.batched_scenes_2d(seed=0)
+    total = sum(len(sc["x"]) for sc in scs)
+    tuned = autotune.tune(lambda **o: BatchSimulation(scs, device=device, **o), key=None,
+                          steps=16, repeats=2, cache_path=None)
+    batch = BatchSimulation(scs, device=device, graph_steps=steps, **tuned)
+    batch.advance(steps)  # warm-up: sort, first P2G, graph capture
+    stream = torch.cuda.ExternalStream(batch.stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    batch.advance(steps)
+    b.record(stream)
+    b.synchronize()
+    t_batch = a.elapsed_time(b) / 1e3
+    launches = batch.stats()[0]
+    batch.close()
+    t_seq = 0.0
+    for sc in scs:
+        sim = MPMSimulation({k: sc[k] for k in ("x", "v", "F", "C", "Jp", "mass", "volume")},
+                            sc["model"], res=sc["res"], dt=sc["dt"], E=sc["E"], nu=sc["nu"],
+                            gravity=sc["gravity"], device=device)
+        sim.advance(steps)
+        st = torch.cuda.ExternalStream(sim.stream)
+        a.record(st)
+        sim.advance(steps)
+        b.record(st)
+        b.synchronize()
+        t_seq += a.elapsed_time(b) / 1e3
+        sim.close()
+    return {"value": total * steps / t_batch, "unit": UNIT, "scenes": len(scs),
+            "particles": total, "steps": steps, "ms_per_step": t_batch / steps * 1e3,
+            "gpu_launches": launches, "tuned": tuned,
+            "sequential_value": total * steps / t_seq, "speedup_vs_sequential": t_seq / t_batch,
+            "config": "256 2D scenes, n log-uniform [1e3, 65536], res {64,128,256}, "
+                      "materials uniform, E log-uniform [1e3,1e5], nu uniform [0.1,0.4], "
+                      "dt 1e-4, one CUDA graph per 100 steps; sequential = the same scenes as "
+                      "plain simulations one after another"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -278,6 +325,10 @@ def run_ours(args):
            "d2h_bytes_per_step": n * row,
            "path": "nclr_set_particles (pinned host) + nclr_advance(1) + nclr_get_particles"}
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(local)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, desc = cpu_reference_run(scene, steps=args.cpu_steps, warmup=1, budget_s=20.0)
@@ -291,7 +342,7 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded scene with the workload's shapes and distributions)",
                 "config": dict(WORKLOAD, parallelism=f"replicas x{world}"),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
                 "gpu_launches": launches_total, "clocks": clk}
         print(json.dumps(line), flush=True)
     sim.close()
@@ -308,6 +359,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1,0 +1,71 @@
+"""Autotuner for the runtime knobs of a simulation (plain or batched): the block re-sort
+interval and the number of steps per captured CUDA graph.
+
+The tile and block sizes of the kernels (4^3 cells in 3D, 8^2 in 2D, 8^3 / 12^2 node tiles,
+256-thread CTAs) are compile-time constants fixed by the shared-memory layout; the knobs that
+trade work against locality at run time are tuned here by timing short runs of the workload
+itself through the public API, and the winner is cached per workload signature.
+
+    from nuclearmpm_gb300 import autotune
+    best = autotune.tune(lambda **opt: BatchSimulation(scenes, **opt), key="batch256")
+    sim = BatchSimulation(scenes, **best)
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+
+DEFAULT_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32]}
+CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
+
+
+def _load(path: str) -> dict:
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _time(sim, steps: int, repeats: int) -> float:
+    sim.advance(steps)  # warm-up: sort, first P2G, graph capture
+    best = float("inf")
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        sim.advance(steps)  # synchronises at its end
+        best = min(best, time.perf_counter() - t0)
+    return best
+
+
+def tune(make_sim, *, key: str | None = None, candidates: dict | None = None, steps: int = 32,
+         repeats: int = 3, cache_path: str | None = CACHE, graph_steps: int | None = None) -> dict:
+    """Returns the fastest option set {knob: value}; `make_sim(**options)` builds the
+    simulation.  Knobs are tuned one after another (coordinate descent from the defaults).
+    With `key`, results are cached in `cache_path` and reused."""
+    cands = dict(DEFAULT_CANDIDATES if candidates is None else candidates)
+    cache = _load(cache_path) if (key and cache_path) else {}
+    if key and key in cache:
+        return dict(cache[key]["best"])
+    best: dict = {}
+    if graph_steps is not None:
+        best["graph_steps"] = graph_steps
+    timings = {}
+    for knob, values in cands.items():
+        scored = []
+        for v in values:
+            opts = dict(best, **{knob: v})
+            sim = make_sim(**opts)
+            try:
+                t = _time(sim, steps, repeats)
+            finally:
+                sim.close()
+            scored.append((t, v))
+            timings[f"{knob}={v}"] = t
+        best[knob] = min(scored)[1]
+    if key and cache_path:
+        os.makedirs(os.path.dirname(cache_path), exist_ok=True)
+        cache[key] = {"best": best, "seconds": timings, "steps": steps}
+        with open(cache_path, "w") as f:
+            json.dump(cache, f, indent=1)
+    return best
