@@ -337,7 +337,7 @@ class Simulation {
   const std::vector<Cell<T, D>> &grid() const { return cells_; }
   Counters counters;
 
- private:
+  // Internals are public: the adjoint restatement (nclr_adjoint.h) steps the phases itself.
   const Model model_;
   const Physics mode_;
   const int res_;
@@ -394,7 +394,6 @@ class Simulation {
     return {mu_0 * e, lambda_0 * e};
   }
 
- public:
   // first_piola_kirchoff_stress, src/nclr.h:313-337.
   Mat<T, D> affine(const Particle<T, D> &p) const {
     const auto [mu, lambda] = hardening(p);
@@ -417,7 +416,6 @@ class Simulation {
     return out;
   }
 
- private:
   // p2g + compute_fused_momentum, src/nclr.h:104-165.
   void p2g() {
     cells_.assign((size_t)num_nodes(), Cell<T, D>{Vec<T, D>::constant(T(0)), T(0)});

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <vector>
 
+#include "nclr_adjoint.h"
 #include "nclr_oracle.h"
 
 using namespace oracle;
@@ -97,9 +98,99 @@ void polar(int physics, const double *A, double *R) {
     for (int j = 0; j < D; ++j) R[i * D + j] = (double)r(i, j);
 }
 
+template <int D>
+int adjoint(int physics, int64_t n, const double *x0, const double *v0, const double *F0,
+            const double *C0, const double *mass, const double *volume, int res, double dt,
+            double E, double nu, double gravity, int nsteps, double *xT, double *vT, double *FT,
+            double *CT, const double *gx, const double *gv, const double *gF, const double *gC,
+            double *gx0, double *gv0, double *gF0, double *gC0, double *gmu_glambda) {
+  using T = double;
+  std::vector<Particle<T, D>> ps((size_t)n);
+  for (int64_t p = 0; p < n; ++p) {
+    auto &q = ps[(size_t)p];
+    for (int d = 0; d < D; ++d) {
+      q.x[d] = x0[p * D + d];
+      q.v[d] = v0[p * D + d];
+    }
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j < D; ++j) {
+        q.F(i, j) = F0[p * D * D + i * D + j];
+        q.C(i, j) = C0[p * D * D + i * D + j];
+      }
+    q.Jp = 1;
+    q.mass = mass[p];
+    q.volume = volume[p];
+  }
+  try {
+    Adjoint<T, D> adj(std::move(ps), Model::kJelly, res, dt, E, nu, gravity, (Physics)physics,
+                      nsteps);
+    const auto &fin = adj.final_state();
+    StepAdjoint<T, D> seed;
+    seed.x.resize((size_t)n);
+    seed.v.resize((size_t)n);
+    seed.F.resize((size_t)n);
+    seed.C.resize((size_t)n);
+    for (int64_t p = 0; p < n; ++p) {
+      const auto &q = fin[(size_t)p];
+      for (int d = 0; d < D; ++d) {
+        xT[p * D + d] = q.x[d];
+        vT[p * D + d] = q.v[d];
+        seed.x[(size_t)p][d] = gx ? gx[p * D + d] : 0.0;
+        seed.v[(size_t)p][d] = gv ? gv[p * D + d] : 0.0;
+      }
+      for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) {
+          FT[p * D * D + i * D + j] = q.F(i, j);
+          CT[p * D * D + i * D + j] = q.C(i, j);
+          seed.F[(size_t)p](i, j) = gF ? gF[p * D * D + i * D + j] : 0.0;
+          seed.C[(size_t)p](i, j) = gC ? gC[p * D * D + i * D + j] : 0.0;
+        }
+    }
+    T gmu = 0, glam = 0;
+    const StepAdjoint<T, D> out = adj.backward(seed, gmu, glam);
+    for (int64_t p = 0; p < n; ++p) {
+      for (int d = 0; d < D; ++d) {
+        gx0[p * D + d] = out.x[(size_t)p][d];
+        gv0[p * D + d] = out.v[(size_t)p][d];
+      }
+      for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) {
+          gF0[p * D * D + i * D + j] = out.F[(size_t)p](i, j);
+          gC0[p * D * D + i * D + j] = out.C[(size_t)p](i, j);
+        }
+    }
+    gmu_glambda[0] = gmu;
+    gmu_glambda[1] = glam;
+  } catch (const std::out_of_range &) {
+    return 2;
+  }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+// FP64 reverse pass of an `nsteps` jelly rollout (nclr_adjoint.h): the forward final state
+// into xT/vT/FT/CT, the adjoint of the initial state (given the final state's adjoint
+// gx/gv/gF/gC, any may be NULL = 0) into gx0/gv0/gF0/gC0, and the adjoints of mu_0 and
+// lambda_0 into gmu_glambda[0..1].  Returns 0, 2 (a stencil left the grid) or 1.
+int oracle_adjoint(int dim, int physics, int64_t n, const double *x0, const double *v0,
+                   const double *F0, const double *C0, const double *mass, const double *volume,
+                   int res, double dt, double E, double nu, double gravity, int nsteps,
+                   double *xT, double *vT, double *FT, double *CT, const double *gx,
+                   const double *gv, const double *gF, const double *gC, double *gx0,
+                   double *gv0, double *gF0, double *gC0, double *gmu_glambda) {
+  if (n < 0 || res < 1 || nsteps < 0) return 1;
+  if (dim == 2)
+    return adjoint<2>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda);
+  if (dim == 3)
+    return adjoint<3>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda);
+  return 1;
+}
+
 
 // Runs `nsteps` calls of advance() on the given state, in place.  Returns 0, or 2 when a
 // grid index went out of range (the reference's std::out_of_range), or 1 on bad arguments.

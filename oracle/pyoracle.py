@@ -41,6 +41,10 @@ def _load(name: str, sub: str) -> ctypes.CDLL:
             lib.oracle_polar.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]
             lib.oracle_linspaced.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                              ctypes.POINTER(ctypes.c_float)]
+            lib.oracle_adjoint.restype = ctypes.c_int
+            lib.oracle_adjoint.argtypes = ([ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [_dp] * 6 +
+                                           [ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int] +
+                                           [_dp] * 13)
         else:
             lib.ref_advance.restype = ctypes.c_int
             lib.ref_advance.argtypes = [ctypes.c_int, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -139,3 +143,36 @@ def ref_cube(dim: int, n: int, lo: float, hi: float) -> np.ndarray:
     out = np.zeros((n ** dim, dim), dtype=np.float32)
     ref_lib().ref_cube(dim, n, lo, hi, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
     return out
+
+
+def lame(E: float, nu: float):
+    """mu_0, lambda_0 (src/nclr.h:77-78) and their derivatives with respect to E and nu."""
+    mu = E / (2 * (1 + nu))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    dmu = (1 / (2 * (1 + nu)), -E / (2 * (1 + nu) ** 2))
+    dlam = (nu / ((1 + nu) * (1 - 2 * nu)), E * (1 + 2 * nu ** 2) / ((1 + nu) * (1 - 2 * nu)) ** 2)
+    return mu, lam, dmu, dlam
+
+
+def adjoint(state: dict, *, dim: int, res: int, steps: int, dt: float = 1e-4, E: float = 1e4,
+            nu: float = 0.2, gravity: float = -100.0, physics: int = REFERENCE, seed: dict):
+    """FP64 jelly rollout and its reverse pass.  `seed` holds the final state's adjoint (keys
+    among x, v, F, C).  Returns (final state, adjoint of the initial state incl. 'E' and 'nu')."""
+    n, s = _prep(state, dim)
+    out = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C")}
+    g = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C")}
+    sd = {k: (np.ascontiguousarray(seed[k], dtype=np.float64) if k in seed else None)
+          for k in ("x", "v", "F", "C")}
+    ml = np.zeros(2)
+    st = oracle_lib().oracle_adjoint(
+        dim, physics, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]), _p(s["mass"]),
+        _p(s["volume"]), res, dt, E, nu, gravity, steps, _p(out["x"]), _p(out["v"]),
+        _p(out["F"]), _p(out["C"]), *(None if sd[k] is None else _p(sd[k]) for k in ("x", "v", "F", "C")),
+        _p(g["x"]), _p(g["v"]), _p(g["F"]), _p(g["C"]), _p(ml))
+    if st != 0:
+        raise RuntimeError(f"oracle adjoint failed ({st})")
+    _, _, dmu, dlam = lame(E, nu)
+    g["mu0"], g["lambda0"] = float(ml[0]), float(ml[1])
+    g["E"] = ml[0] * dmu[0] + ml[1] * dlam[0]
+    g["nu"] = ml[0] * dmu[1] + ml[1] * dlam[1]
+    return out, g

@@ -1,0 +1,79 @@
+"""The FP64 CPU adjoint of a jelly rollout (oracle/nclr_adjoint.h) against FP64 central finite
+differences.  Loss 1 = |centre of mass of the final positions - target|^2 (gradients with
+respect to initial velocities, positions and deformation gradients); internal forces conserve
+momentum, so away from the boundary this loss does not depend on the material and its E / nu
+gradients vanish -- loss 2 = sum_p m_p |x_p - target_p|^2 over the final positions depends on
+the deformation and checks the Young's modulus and Poisson ratio gradients."""
+import numpy as np
+import pytest
+
+from nuclearmpm_gb300 import scenes
+
+CASES = [(2, 32, 50, 1024), (3, 16, 10, 216)]  # dim, res, steps, particles
+
+
+def setup(dim, res, n, physics, seed=0):
+    rng = np.random.default_rng(seed)
+    side = round(n ** (1 / dim))
+    x = scenes.jittered_block(rng, (side,) * dim, 0.5 / res, (0.35,) * dim, 0.25 / res)
+    s = scenes.particles(x.astype(np.float64), rng.normal(0, 0.5, size=x.shape), physics=physics)
+    s = {k: np.asarray(v, np.float64) for k, v in s.items()}
+    s["F"] = s["F"] + rng.normal(0, 0.01, size=s["F"].shape)
+    target = rng.uniform(0.4, 0.6, size=dim)
+    return s, target
+
+
+def loss_and_seed(xT, mass, target):
+    com = (xT * mass[:, None]).sum(0) / mass.sum()
+    d = com - target
+    return float(d @ d), (2 * d[None, :] * mass[:, None] / mass.sum())
+
+
+def pointwise(xT, mass, targets):
+    d = xT - targets
+    return float((mass[:, None] * d * d).sum()), 2 * mass[:, None] * d
+
+
+def forward_loss(oracle, s, target, dim, res, steps, physics, E=1e4, nu=0.2, loss=loss_and_seed):
+    out, _, st, _ = oracle.advance(s, dim=dim, model=scenes.JELLY, res=res, steps=steps, fp64=True,
+                                   physics=physics, E=E, nu=nu, want_grid=False)
+    assert st == 0
+    return loss(out["x"], s["mass"], target)[0]
+
+
+@pytest.mark.parametrize("dim,res,steps,n", CASES)
+@pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
+def test_oracle_adjoint_matches_finite_differences(oracle, dim, res, steps, n, physics):
+    s, target = setup(dim, res, n, physics)
+    out, _ = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={})
+    _, seed = loss_and_seed(out["x"], s["mass"], target)
+    _, g = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={"x": seed})
+    rng = np.random.default_rng(1)
+    checks = []
+    for _ in range(4):
+        p, d = int(rng.integers(n)), int(rng.integers(dim))
+        checks.append(("v", (p, d), 1e-5))
+        checks.append(("x", (p, d), 1e-7))
+    checks.append(("F", (int(rng.integers(n)), 0, 1), 1e-6))
+    for field, idx, h in checks:
+        sp = {k: v.copy() for k, v in s.items()}
+        sm = {k: v.copy() for k, v in s.items()}
+        sp[field][idx] += h
+        sm[field][idx] -= h
+        fd = (forward_loss(oracle, sp, target, dim, res, steps, physics) -
+              forward_loss(oracle, sm, target, dim, res, steps, physics)) / (2 * h)
+        ad = g[field][idx]
+        assert abs(ad - fd) <= 1e-6 * max(1.0, abs(fd)) + 1e-4 * abs(fd), (field, idx, ad, fd)
+    assert abs(g["E"]) < 1e-15 and abs(g["nu"]) < 1e-12  # momentum conservation
+    targets = out["x"] + np.random.default_rng(2).normal(0, 1e-3, size=out["x"].shape)
+    _, seed2 = pointwise(out["x"], s["mass"], targets)
+    _, g2 = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={"x": seed2})
+    for name, h in (("E", 1.0), ("nu", 1e-5)):
+        kp = {"E": 1e4, "nu": 0.2}
+        km = dict(kp)
+        kp[name] += h
+        km[name] -= h
+        fd = (forward_loss(oracle, s, targets, dim, res, steps, physics, loss=pointwise, **kp) -
+              forward_loss(oracle, s, targets, dim, res, steps, physics, loss=pointwise, **km)) / (2 * h)
+        assert abs(fd) > 0
+        assert abs(g2[name] - fd) <= 1e-4 * abs(fd), (name, g2[name], fd)
