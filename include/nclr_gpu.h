@@ -174,6 +174,40 @@ const char *nclr_last_error(const nclr_sim *sim);
 void nclr_destroy(nclr_sim *sim);
 
 /* ---------------------------------------------------------------------------------------
+ * Differentiable rollouts (no counterpart in the reference).  A rollout is `nsteps` jelly
+ * steps (src/nclr.h:80-337, MaterialModel::kJelly) from a given state; the reverse pass is a
+ * hand-written adjoint of the whole step (G2P, grid update with its clamp and boundary masks,
+ * P2G, the fixed-corotated stress and its polar rotation) run backwards through the rollout,
+ * recomputing each segment of `checkpoint_every` steps from a checkpoint.
+ *
+ * All state arrays are DEVICE pointers in the host layout above (caller order, rows).
+ * nclr_rollout_create takes the particle count, initial positions (HOST, used only to size and
+ * place the simulation), mass and volume (HOST, NULL = 1) and the step constants;
+ * nclr_rollout_forward runs from (x0, v0, F0, C0) with the given E and nu (Jp = 1) and writes
+ * the final state (any output may be NULL); nclr_rollout_backward takes the adjoint of the
+ * final state (NULL = 0) and writes the adjoint of the initial state (outputs may be NULL) and
+ * of E and nu.  Calls are ordered on the rollout's stream and synchronise it before
+ * returning. */
+typedef struct nclr_rollout nclr_rollout;
+nclr_status nclr_rollout_create(nclr_rollout **out, int dim, int64_t n, const float *x0,
+                                const float *mass, const float *volume, int res, float dt,
+                                float gravity, int64_t nsteps, int checkpoint_every,
+                                const nclr_options *opt);
+nclr_status nclr_rollout_forward(nclr_rollout *r, const float *x0, const float *v0, const float *F0,
+                                 const float *C0, float E, float nu, float *xT, float *vT,
+                                 float *FT, float *CT);
+nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float *gvT,
+                                  const float *gFT, const float *gCT, float *gx0, float *gv0,
+                                  float *gF0, float *gC0, double *gE, double *gnu);
+/* Device time (ms, CUDA events on the rollout's stream) of the last forward and backward. */
+nclr_status nclr_rollout_timing(const nclr_rollout *r, double *forward_ms, double *backward_ms);
+void *nclr_rollout_stream(nclr_rollout *r);
+/* Message of the rollout's last failed call; with r == NULL the last nclr_rollout_create
+ * failure of this thread. */
+const char *nclr_rollout_error(const nclr_rollout *r);
+void nclr_rollout_destroy(nclr_rollout *r);
+
+/* ---------------------------------------------------------------------------------------
  * Particle-to-grid transfer without any allocation.  No counterpart in the reference: it is
  * an addition for callers that cannot call cudaMalloc while they run -- applications whose
  * own allocator already holds the device's memory, real-time loops where allocating (and the

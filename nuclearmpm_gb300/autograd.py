@@ -1,0 +1,127 @@
+"""Differentiable MPM rollouts for PyTorch: a torch.autograd.Function over the hand-written
+adjoint of the step (nclr_rollout_* in include/nclr_gpu.h).
+
+    roll = Rollout(x0, res=64, steps=2000, checkpoint_every=50)      # jelly
+    xT, vT = roll(x0, v0, E, nu)           # CUDA tensors in, CUDA tensors out
+    loss = ((xT.mean(0) - target) ** 2).sum()
+    loss.backward()                        # gradients of x0, v0, E, nu
+
+The forward pass runs the GPU step kernels and keeps a checkpoint every `checkpoint_every`
+steps; the backward pass recomputes each segment from its checkpoint and runs the adjoint
+kernels back through it.  Only the jelly material is covered (the rollout has no plasticity).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import capi
+
+
+def _dp(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+class Rollout:
+    """A differentiable `steps`-step jelly rollout of `n` particles (positions x0 only size and
+    place the simulation; mass / volume default to 1, as Particle<dim> does)."""
+
+    def __init__(self, x0, *, res: int = 64, steps: int = 100, checkpoint_every: int = 50,
+                 dt: float = 1e-4, gravity: float = -100.0, mass=None, volume=None,
+                 physics: int = capi.PHYSICS_REFERENCE, device: int = 0, sort_interval: int = 8):
+        x = np.ascontiguousarray(torch.as_tensor(x0).detach().cpu().numpy(), dtype=np.float32)
+        self.n, self.dim = x.shape
+        self.steps = int(steps)
+        m = None if mass is None else np.ascontiguousarray(mass, dtype=np.float32)
+        vo = None if volume is None else np.ascontiguousarray(volume, dtype=np.float32)
+        opt = capi.default_options(physics=physics, device=device, sort_interval=sort_interval)
+        h = ctypes.c_void_p()
+        L = capi.lib()
+        st = L.nclr_rollout_create(ctypes.byref(h), self.dim, self.n, x.ctypes.data,
+                                   None if m is None else m.ctypes.data,
+                                   None if vo is None else vo.ctypes.data, int(res), float(dt),
+                                   float(gravity), self.steps, int(checkpoint_every),
+                                   ctypes.byref(opt))
+        if st != 0:
+            raise capi.NclrError(st, (L.nclr_rollout_error(None) or b"").decode())
+        self._h = h
+        self.device = torch.device("cuda", device)
+        self.corrected = physics == capi.PHYSICS_CORRECTED
+
+    def _check(self, st):
+        if st != 0:
+            msg = (capi.lib().nclr_rollout_error(self._h) or b"").decode()
+            if st == capi.NCLR_ERR_OUT_OF_RANGE:
+                raise capi.OutOfRange(st, msg)
+            raise capi.NclrError(st, msg)
+
+    def __call__(self, x0, v0, E, nu, F0=None, C0=None):
+        return RolloutFunction.apply(self, x0, v0, E, nu, F0, C0)
+
+    def timing(self) -> tuple[float, float]:
+        f, b = ctypes.c_double(), ctypes.c_double()
+        capi.lib().nclr_rollout_timing(self._h, ctypes.byref(f), ctypes.byref(b))
+        return f.value, b.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().nclr_rollout_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RolloutFunction(torch.autograd.Function):
+    """(x0, v0, E, nu[, F0, C0]) -> (x_T, v_T); backward via the adjoint rollout."""
+
+    @staticmethod
+    def forward(ctx, roll: Rollout, x0, v0, E, nu, F0=None, C0=None):
+        dev = roll.device
+        n, d = roll.n, roll.dim
+        f32 = dict(dtype=torch.float32, device=dev)
+        x0c = x0.detach().to(**f32).contiguous()
+        v0c = v0.detach().to(**f32).contiguous()
+        if F0 is None:  # Particle<dim>'s F = diag<dim>(1): diag(1,1,0) in 3D (src/nclr_math.h:13-19)
+            F0c = torch.eye(d, **f32).expand(n, d, d).contiguous()
+            if d == 3 and not roll.corrected:
+                F0c[:, 2, 2] = 0.0
+        else:
+            F0c = F0.detach().to(**f32).contiguous()
+        C0c = torch.zeros(n, d, d, **f32) if C0 is None else C0.detach().to(**f32).contiguous()
+        xT = torch.empty(n, d, **f32)
+        vT = torch.empty(n, d, **f32)
+        Ef, nuf = float(E), float(nu)
+        torch.cuda.synchronize(dev)
+        roll._check(capi.lib().nclr_rollout_forward(roll._h, _dp(x0c), _dp(v0c), _dp(F0c), _dp(C0c),
+                                                     Ef, nuf, _dp(xT), _dp(vT), None, None))
+        ctx.roll = roll
+        ctx.params = [(t.dtype, t.device) if torch.is_tensor(t) else None for t in (E, nu)]
+        return xT, vT
+
+    @staticmethod
+    def backward(ctx, gxT, gvT):
+        roll = ctx.roll
+        dev = roll.device
+        n, d = roll.n, roll.dim
+        f32 = dict(dtype=torch.float32, device=dev)
+        gx = None if gxT is None else gxT.to(**f32).contiguous()
+        gv = None if gvT is None else gvT.to(**f32).contiguous()
+        gx0 = torch.empty(n, d, **f32)
+        gv0 = torch.empty(n, d, **f32)
+        gF0 = torch.empty(n, d, d, **f32)
+        gC0 = torch.empty(n, d, d, **f32)
+        gE, gnu = ctypes.c_double(), ctypes.c_double()
+        torch.cuda.synchronize(dev)
+        roll._check(capi.lib().nclr_rollout_backward(roll._h, _dp(gx), _dp(gv), None, None,
+                                                      _dp(gx0), _dp(gv0), _dp(gF0), _dp(gC0),
+                                                      ctypes.byref(gE), ctypes.byref(gnu)))
+        out = []
+        for val, spec in ((gE.value, ctx.params[0]), (gnu.value, ctx.params[1])):
+            out.append(None if spec is None else torch.tensor(val, dtype=spec[0], device=spec[1]))
+        return None, gx0, gv0, out[0], out[1], gF0, gC0

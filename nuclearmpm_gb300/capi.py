@@ -75,6 +75,19 @@ SIGNATURES = {
     "nclr_profile_reset": (ctypes.c_int, [_h]),
     "nclr_last_error": (ctypes.c_char_p, [_h]),
     "nclr_destroy": (None, [_h]),
+    "nclr_rollout_create": (ctypes.c_int, [ctypes.POINTER(_h), ctypes.c_int, _i64, _vp, _vp, _vp,
+                                           ctypes.c_int, ctypes.c_float, ctypes.c_float, _i64,
+                                           ctypes.c_int, ctypes.POINTER(Options)]),
+    "nclr_rollout_forward": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
+                                            _vp, _vp, _vp, _vp]),
+    "nclr_rollout_backward": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                             ctypes.POINTER(ctypes.c_double),
+                                             ctypes.POINTER(ctypes.c_double)]),
+    "nclr_rollout_timing": (ctypes.c_int, [_h, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double)]),
+    "nclr_rollout_stream": (_vp, [_h]),
+    "nclr_rollout_error": (ctypes.c_char_p, [_h]),
+    "nclr_rollout_destroy": (None, [_h]),
     "nclr_grid_transfer_noalloc": (ctypes.c_int, [ctypes.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
                                                   _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                   ctypes.c_float, ctypes.c_float, ctypes.c_float,

@@ -1,0 +1,471 @@
+// Reverse-mode kernels of one jelly step (the adjoint of MPMSimulation<dim>::advance(),
+// src/nclr.h:80-337 without plasticity).  A step maps s_t = (x, v, F, C) to s_{t+1}; given the
+// adjoint of s_{t+1} these kernels produce the adjoint of s_t and accumulate the adjoints of
+// mu_0 and lambda_0:
+//   adj_g2p   per particle: reverse of the G2P gather, F update and advection; scatters the
+//             adjoint of the updated grid velocity to the nodes;
+//   adj_grid  per node: reverse of the grid update (v = clamp(mv / m + dt g)); clamped
+//             components and stuck or empty nodes pass nothing;
+//   adj_p2g   per particle: gathers the node adjoints, reverses the P2G scatter, the APIC +
+//             fixed-corotated stress term and the polar rotation.
+// All arrays are particle-major rows in the caller's order (the layout of the C ABI) and the
+// updated grid V_t of the step is the float4 {v, m} grid the forward step produced.
+#include <cuda_runtime.h>
+
+#include "mpm_device.cuh"
+#include "mpm_launch.h"
+
+namespace mpm {
+
+namespace {
+
+template <int D>
+struct Stencil {
+  int base[D];
+  float fx[D], w[3][D], dw[3][D];
+};
+
+template <int D>
+__device__ __forceinline__ Stencil<D> make_stencil(const float x[D], float inv_dx) {
+  Stencil<D> s;
+  stencil<D>(x, inv_dx, s.base, s.fx, s.w);
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const float f = s.fx[d];
+    s.dw[0][d] = f - 1.5f;
+    s.dw[1][d] = -2.0f * (f - 1.0f);
+    s.dw[2][d] = f - 0.5f;
+  }
+  return s;
+}
+
+template <int D>
+__device__ __forceinline__ void offs(int o, int oo[3]) {
+  oo[0] = (D == 3) ? o / 9 : o / 3;
+  oo[1] = (D == 3) ? (o / 3) % 3 : o % 3;
+  oo[2] = (D == 3) ? o % 3 : 0;
+}
+
+template <int D>
+__device__ __forceinline__ float wprod(const Stencil<D> &s, const int oo[3]) {
+  float w = s.w[oo[0]][0] * s.w[oo[1]][1];
+  if (D == 3) w *= s.w[oo[2]][D - 1];
+  return w;
+}
+
+// d fx from the adjoints of the stencil weights W_o = prod_d w_d(o_d).
+template <int D>
+__device__ __forceinline__ void weight_backward(const Stencil<D> &s, const float *Wbar, float gfx[D]) {
+  constexpr int S = (D == 3) ? 27 : 9;
+#pragma unroll
+  for (int o = 0; o < S; ++o) {
+    int oo[3];
+    offs<D>(o, oo);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      float other = 1.0f;
+#pragma unroll
+      for (int e = 0; e < D; ++e)
+        if (e != d) other *= s.w[oo[e]][e];
+      gfx[d] += Wbar[o] * other * s.dw[oo[d]][d];
+    }
+  }
+}
+
+template <int D>
+__device__ __forceinline__ Mat<D> load_row_mat(const float *a, int p) {
+  Mat<D> m;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) m.a[i][j] = a[((size_t)p * D + i) * D + j];
+  return m;
+}
+
+template <int D>
+__device__ __forceinline__ void store_row_mat(float *a, int p, const Mat<D> &m) {
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) a[((size_t)p * D + i) * D + j] = m.a[i][j];
+}
+
+template <int D>
+__device__ __forceinline__ Mat<D> row_mat_or_zero(const float *a, int p) {
+  Mat<D> m;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) m.a[i][j] = a ? a[((size_t)p * D + i) * D + j] : 0.0f;
+  return m;
+}
+
+__device__ __forceinline__ Mat<2> cofactor(const Mat<2> &a) {
+  Mat<2> c;
+  c.a[0][0] = a.a[1][1];
+  c.a[0][1] = -a.a[1][0];
+  c.a[1][0] = -a.a[0][1];
+  c.a[1][1] = a.a[0][0];
+  return c;
+}
+__device__ __forceinline__ Mat<3> cofactor(const Mat<3> &a) {
+  Mat<3> c;
+  c.a[0][0] = a.a[1][1] * a.a[2][2] - a.a[1][2] * a.a[2][1];
+  c.a[0][1] = a.a[1][2] * a.a[2][0] - a.a[1][0] * a.a[2][2];
+  c.a[0][2] = a.a[1][0] * a.a[2][1] - a.a[1][1] * a.a[2][0];
+  c.a[1][0] = a.a[0][2] * a.a[2][1] - a.a[0][1] * a.a[2][2];
+  c.a[1][1] = a.a[0][0] * a.a[2][2] - a.a[0][2] * a.a[2][0];
+  c.a[1][2] = a.a[0][1] * a.a[2][0] - a.a[0][0] * a.a[2][1];
+  c.a[2][0] = a.a[0][1] * a.a[1][2] - a.a[0][2] * a.a[1][1];
+  c.a[2][1] = a.a[0][2] * a.a[1][0] - a.a[0][0] * a.a[1][2];
+  c.a[2][2] = a.a[0][0] * a.a[1][1] - a.a[0][1] * a.a[1][0];
+  return c;
+}
+
+// Adjoint of the polar rotation: 2D closed form (src/nclr_math.h:80-89); 3D with F = U S V^T,
+// R = U V^T: F_bar = U Z V^T, Z_ij = (P_ij - P_ji) / (s_i + s_j), P = U^T R_bar V.
+__device__ __forceinline__ Mat<2> polar_backward(const Mat<2> &F, const Mat<2> &Rb) {
+  const float a = F.a[0][0] + F.a[1][1], b = F.a[1][0] - F.a[0][1];
+  const float r2 = a * a + b * b;
+  const float inv_r3 = 1.0f / (r2 * sqrtf(r2));
+  const float cb = Rb.a[0][0] + Rb.a[1][1], sb = Rb.a[1][0] - Rb.a[0][1];
+  const float ab = (cb * b * b - sb * a * b) * inv_r3;
+  const float bb = (-cb * a * b + sb * a * a) * inv_r3;
+  Mat<2> out;
+  out.a[0][0] = ab;
+  out.a[1][1] = ab;
+  out.a[1][0] = bb;
+  out.a[0][1] = -bb;
+  return out;
+}
+__device__ __forceinline__ Mat<3> polar_backward(const Mat<3> &F, const Mat<3> &Rb) {
+  Mat<3> U, V;
+  float sg[3];
+  svd3(F, U, sg, V);
+  // P = U^T Rb V
+  Mat<3> UtR;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      UtR.a[i][j] = U.a[0][i] * Rb.a[0][j] + U.a[1][i] * Rb.a[1][j] + U.a[2][i] * Rb.a[2][j];
+  const Mat<3> Pm = mat_mul<3>(UtR, V);
+  Mat<3> Z;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float sden = sg[i] + sg[j];
+      Z.a[i][j] = (i != j && fabsf(sden) > 1e-30f) ? (Pm.a[i][j] - Pm.a[j][i]) / sden : 0.0f;
+    }
+  return mat_mul_t<3>(mat_mul<3>(U, Z), V);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// adj_g2p: reverse of x' = x + dt v', v' = sum W vg, C' = 4 inv_dx sum W vg (o - fx)^T,
+// F' = (I + dt C') F.  Writes the adjoint of x and F (partial; adj_p2g adds the P2G part)
+// and scatters the adjoint of the updated grid velocity into VB.
+// ---------------------------------------------------------------------------------------
+template <int D, bool kRef>
+__global__ void __launch_bounds__(128) adj_g2p_kernel(
+    int n, const float *__restrict__ x, const float *__restrict__ F,
+    const float *__restrict__ Cn, const float4 *__restrict__ V, Params P,
+    const float *__restrict__ gx, const float *__restrict__ gv, const float *__restrict__ gF,
+    const float *__restrict__ gC, float *__restrict__ ox, float *__restrict__ oF,
+    float *__restrict__ VB, int *err) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  constexpr int S = (D == 3) ? 27 : 9;
+  float xp[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) xp[d] = x[(size_t)p * D + d];
+  const Stencil<D> st = make_stencil<D>(xp, P.inv_dx);
+  const Mat<D> Fm = load_row_mat<D>(F, p);
+  const Mat<D> Cm = load_row_mat<D>(Cn, p);
+  const Mat<D> gFn = row_mat_or_zero<D>(gF, p);
+  Mat<D> gCt = row_mat_or_zero<D>(gC, p);
+  Mat<D> M;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) M.a[i][j] = diag_one<D, kRef>(i, j) + P.dt * Cm.a[i][j];
+  // F_bar = M^T gF'
+  Mat<D> gFp;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.0f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s += M.a[k][i] * gFn.a[k][j];
+      gFp.a[i][j] = s;
+    }
+  store_row_mat<D>(oF, p, gFp);
+  const Mat<D> gFFt = mat_mul_t<D>(gFn, Fm);
+  float gvt[D], gxp[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) gCt.a[i][j] += P.dt * gFFt.a[i][j];
+    gxp[i] = gx ? gx[(size_t)p * D + i] : 0.0f;
+    gvt[i] = (gv ? gv[(size_t)p * D + i] : 0.0f) + P.dt * gxp[i];
+  }
+  const float cs = P.cscale;
+  float Wbar[S], gfx[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) gfx[d] = 0.0f;
+  const int64_t f0 = flat_index<D>(st.base, P.N);
+#pragma unroll
+  for (int o = 0; o < S; ++o) {
+    int oo[3];
+    offs<D>(o, oo);
+    const int64_t f = (D == 3) ? f0 + ((int64_t)oo[0] * P.N + oo[1]) * P.N + oo[2]
+                               : f0 + (int64_t)oo[0] * P.N + oo[1];
+    Wbar[o] = 0.0f;
+    if (f < 0 || f >= P.nodes) {
+      atomicOr(err, kErrOutOfRange);
+      continue;
+    }
+    const float4 g4 = __ldg(V + f);
+    const float vg[3] = {g4.x, g4.y, g4.z};
+    const float W = wprod<D>(st, oo);
+    float du[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) du[d] = (float)oo[d] - st.fx[d];
+    float wb = 0.0f;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      float gcdu = 0.0f;
+#pragma unroll
+      for (int b = 0; b < D; ++b) gcdu += gCt.a[a][b] * du[b];
+      atomicAdd(VB + f * 4 + a, W * gvt[a] + cs * W * gcdu);
+      wb += gvt[a] * vg[a] + cs * vg[a] * gcdu;
+    }
+    Wbar[o] = wb;
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      float gctv = 0.0f;
+#pragma unroll
+      for (int a = 0; a < D; ++a) gctv += gCt.a[a][b] * vg[a];
+      gfx[b] -= cs * W * gctv;
+    }
+  }
+  weight_backward<D>(st, Wbar, gfx);
+#pragma unroll
+  for (int d = 0; d < D; ++d) ox[(size_t)p * D + d] = gxp[d] + P.inv_dx * gfx[d];
+}
+
+// ---------------------------------------------------------------------------------------
+// adj_grid: reverse of vg = clamp(mv / m + dt g e_y) (src/nclr.h:284-298) from the updated
+// grid V (its m is 0 where the node was empty or stuck).  VB is cleared for the next step.
+// ---------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(256) adj_grid_kernel(const float4 *__restrict__ V,
+                                                       float *__restrict__ VB,
+                                                       float4 *__restrict__ GB, Params P) {
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= P.nodes) return;
+  const float4 g4 = V[f];
+  const float vg[3] = {g4.x, g4.y, g4.z};
+  const float m = g4.w;
+  float gmv[3] = {0.0f, 0.0f, 0.0f}, gm = 0.0f;
+  if (m > 0.0f) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float u = VB[f * 4 + d];
+      if (fabsf(vg[d]) >= P.allowed) continue;  // clamped
+      const float raw = vg[d] - (d == 1 ? P.dt_gravity : 0.0f);
+      gmv[d] = u / m;
+      gm -= u * raw / m;
+    }
+  }
+  GB[f] = make_float4(gmv[0], gmv[1], gmv[2], gm);
+  reinterpret_cast<float4 *>(VB)[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// ---------------------------------------------------------------------------------------
+// adj_p2g: reverse of mv_i += W (m v + A dpos), m_i += W m, with the fused APIC + stress
+// A = -(dt vol Dinv)(2 mu (F - R) F^T + lambda (J - 1) J 1) + m C (jelly: mu = 0.3 mu_0,
+// lambda = 0.3 lambda_0).  Adds to the adjoints of x and F, writes those of v and C, and
+// accumulates the adjoints of mu_0 and lambda_0 into gml[0..1].
+// ---------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(128) adj_p2g_kernel(
+    int n, const float *__restrict__ x, const float *__restrict__ v, const float *__restrict__ F,
+    const float *__restrict__ C, const float *__restrict__ mass, const float *__restrict__ vol,
+    const float4 *__restrict__ GB, Params P, float *__restrict__ ox, float *__restrict__ ov,
+    float *__restrict__ oF, float *__restrict__ oC, double *gml, int *err) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int S = (D == 3) ? 27 : 9;
+  float gmu = 0.0f, glam = 0.0f;
+  if (p < n) {
+    float xp[D], vp[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      xp[d] = x[(size_t)p * D + d];
+      vp[d] = v[(size_t)p * D + d];
+    }
+    const Stencil<D> st = make_stencil<D>(xp, P.inv_dx);
+    const Mat<D> Fm = load_row_mat<D>(F, p);
+    const Mat<D> Cm = load_row_mat<D>(C, p);
+    const float m = mass[p], vo = vol[p];
+    const Mat<D> R = polar_R(Fm);
+    const Mat<D> A = fused_affine<D>(Fm, R, Cm, 1.0f, m, vo, kJelly, P);
+    Mat<D> gA;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) gA.a[i][j] = 0.0f;
+    float gvp[D], gfx[D], Wbar[S];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      gvp[d] = 0.0f;
+      gfx[d] = 0.0f;
+    }
+    const int64_t f0 = flat_index<D>(st.base, P.N);
+#pragma unroll
+    for (int o = 0; o < S; ++o) {
+      int oo[3];
+      offs<D>(o, oo);
+      const int64_t f = (D == 3) ? f0 + ((int64_t)oo[0] * P.N + oo[1]) * P.N + oo[2]
+                                 : f0 + (int64_t)oo[0] * P.N + oo[1];
+      Wbar[o] = 0.0f;
+      if (f < 0 || f >= P.nodes) {
+        atomicOr(err, kErrOutOfRange);
+        continue;
+      }
+      const float4 g4 = __ldg(GB + f);
+      const float g[3] = {g4.x, g4.y, g4.z};
+      const float W = wprod<D>(st, oo);
+      float dpos[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) dpos[d] = ((float)oo[d] - st.fx[d]) * P.dx;
+      float wb = g4.w * m;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        float ad = 0.0f;
+#pragma unroll
+        for (int b = 0; b < D; ++b) {
+          ad += A.a[a][b] * dpos[b];
+          gA.a[a][b] += W * g[a] * dpos[b];
+        }
+        gvp[a] += W * m * g[a];
+        wb += g[a] * (m * vp[a] + ad);
+      }
+      Wbar[o] = wb;
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        float atg = 0.0f;
+#pragma unroll
+        for (int a = 0; a < D; ++a) atg += A.a[a][b] * g[a];
+        gfx[b] -= P.dx * W * atg;
+      }
+    }
+    weight_backward<D>(st, Wbar, gfx);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      ox[(size_t)p * D + d] += P.inv_dx * gfx[d];
+      ov[(size_t)p * D + d] = gvp[d];
+    }
+    Mat<D> gC;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) gC.a[i][j] = m * gA.a[i][j];
+    store_row_mat<D>(oC, p, gC);
+    // stress
+    const float kappa = P.dt * vo * P.Dinv;
+    const float mu = P.mu0 * 0.3f, lam = P.lambda0 * 0.3f;
+    const float J = det(Fm);
+    Mat<D> X, G;
+    float sbar = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        X.a[i][j] = Fm.a[i][j] - R.a[i][j];
+        G.a[i][j] = -kappa * gA.a[i][j];
+        sbar += G.a[i][j];
+      }
+    const Mat<D> Q = mat_mul_t<D>(X, Fm);
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) gmu += 2.0f * G.a[i][j] * Q.a[i][j];
+    glam = sbar * (J - 1.0f) * J;
+    Mat<D> Qb;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) Qb.a[i][j] = 2.0f * mu * G.a[i][j];
+    const Mat<D> Xb = mat_mul<D>(Qb, Fm);
+    Mat<D> Rb, FQ;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        Rb.a[i][j] = -Xb.a[i][j];
+        float s = 0.0f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) s += Qb.a[k][i] * X.a[k][j];
+        FQ.a[i][j] = s;
+      }
+    const Mat<D> Fp = polar_backward(Fm, Rb);
+    const Mat<D> cof = cofactor(Fm);
+    const float dJ = sbar * lam * (2.0f * J - 1.0f);
+    Mat<D> gF = load_row_mat<D>(oF, p);
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) gF.a[i][j] += FQ.a[i][j] + Xb.a[i][j] + Fp.a[i][j] + dJ * cof.a[i][j];
+    store_row_mat<D>(oF, p, gF);
+    gmu *= 0.3f;  // jelly hardening (src/nclr.h:362-364)
+    glam *= 0.3f;
+  }
+  // block reduction of the parameter adjoints, one double atomic per warp
+  double a = gmu, b = glam;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (a != 0.0 || b != 0.0)) {
+    atomicAdd(gml, a);
+    atomicAdd(gml + 1, b);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+template <int D>
+void launch_adjoint_step(int n, const float *x, const float *v, const float *F, const float *C,
+                         const float *Cn, const float *mass, const float *vol, const float4 *V,
+                         const Params &P, bool ref, const float *gx, const float *gv,
+                         const float *gF, const float *gC, float *ox, float *ov, float *oF,
+                         float *oC, float *VB, float4 *GB, double *gml, int *err,
+                         cudaStream_t st) {
+  const unsigned pb = (unsigned)((n + 127) / 128);
+  if (n > 0) {
+    if (ref)
+      adj_g2p_kernel<D, true><<<pb, 128, 0, st>>>(n, x, F, Cn, V, P, gx, gv, gF, gC, ox, oF, VB, err);
+    else
+      adj_g2p_kernel<D, false><<<pb, 128, 0, st>>>(n, x, F, Cn, V, P, gx, gv, gF, gC, ox, oF, VB, err);
+  }
+  adj_grid_kernel<D><<<(unsigned)((P.nodes + 255) / 256), 256, 0, st>>>(V, VB, GB, P);
+  if (n > 0)
+    adj_p2g_kernel<D><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF, oC, gml, err);
+}
+
+template void launch_adjoint_step<2>(int, const float *, const float *, const float *, const float *,
+                                     const float *, const float *, const float *, const float4 *,
+                                     const Params &, bool, const float *, const float *,
+                                     const float *, const float *, float *, float *, float *,
+                                     float *, float *, float4 *, double *, int *, cudaStream_t);
+template void launch_adjoint_step<3>(int, const float *, const float *, const float *, const float *,
+                                     const float *, const float *, const float *, const float4 *,
+                                     const Params &, bool, const float *, const float *,
+                                     const float *, const float *, float *, float *, float *,
+                                     float *, float *, float4 *, double *, int *, cudaStream_t);
+
+}  // namespace mpm

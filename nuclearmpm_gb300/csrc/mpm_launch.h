@@ -37,6 +37,18 @@ template <int D> void launch_block_keys(const PState &s, int n, const Scene *sce
 template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank, const int *start, const int *count, bool move_vc, cudaStream_t st);
 void launch_compact_blocks(const int *start, int nblocks, int cpb, int *list, int *nlist, cudaStream_t st);
 
+// Reverse of one jelly step (adjoint.cu): adjoint of s_{t+1} (gx, gv, gF, gC; NULL = 0) ->
+// adjoint of s_t (ox, ov, oF, oC), mu_0 / lambda_0 adjoints added to gml[0..1].  States are
+// caller-order rows; V is the step's updated grid; VB (4 floats per node) must be zero on
+// entry and is zero again on exit; GB holds nodes float4.
+template <int D>
+void launch_adjoint_step(int n, const float *x, const float *v, const float *F, const float *C,
+                         const float *Cn, const float *mass, const float *vol, const float4 *V,
+                         const Params &P, bool ref, const float *gx, const float *gv,
+                         const float *gF, const float *gC, float *ox, float *ov, float *oF,
+                         float *oC, float *VB, float4 *GB, double *gml, int *err,
+                         cudaStream_t st);
+
 // Exclusive prefix sum of count[0..n) into start[0..n]; tile_sums must hold
 // scan_tiles(n) ints.  Three launches.
 int64_t scan_tiles(int64_t n);

@@ -888,3 +888,290 @@ const char *nclr_last_error(const nclr_sim *s) {
 void nclr_destroy(nclr_sim *s) { release(s); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Differentiable rollouts: nsteps jelly steps from a given state, keeping a checkpoint every
+// `every` steps; the reverse pass recomputes each segment's states and grids forward (the
+// regular step kernels) and runs the adjoint kernels (adjoint.cu) backwards through it.
+// ---------------------------------------------------------------------------------------
+struct nclr_rollout {
+  nclr_sim *sim = nullptr;
+  int dim = 0;
+  int64_t n = 0, nsteps = 0, nodes = 0;
+  int every = 0, nseg = 0;
+  float E = 0.0f, nu = 0.0f;
+  size_t rowf = 0;            // floats of one state: x, v, F, C rows
+  float *ckpt = nullptr;      // nseg states
+  float *seg = nullptr;       // every + 1 states of the segment being reversed
+  float4 *grids = nullptr;    // `every` updated grids of that segment
+  float *adj[2] = {nullptr, nullptr};
+  float *VB = nullptr;
+  float4 *GB = nullptr;
+  double *gml = nullptr;      // adjoints of mu_0, lambda_0
+  int *err = nullptr;
+  float *mass = nullptr, *vol = nullptr, *ones = nullptr;
+  bool have_forward = false;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  float fwd_ms = 0.0f, bwd_ms = 0.0f;
+  std::string error;
+
+  float *x(float *st) const { return st; }
+  float *v(float *st) const { return st + n * dim; }
+  float *F(float *st) const { return st + 2 * n * dim; }
+  float *C(float *st) const { return st + 2 * n * dim + n * dim * dim; }
+  float *state(float *base, int64_t i) const { return base + (size_t)i * rowf; }
+};
+
+namespace {
+
+nclr_status rfail(nclr_rollout *r, nclr_status st, const std::string &m) {
+  if (r) r->error = m;
+  return st;
+}
+
+#define R_TRY(r, call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return rfail((r), NCLR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define R_SIM(r, call)                                                     \
+  do {                                                                     \
+    nclr_status st_ = (call);                                              \
+    if (st_ != NCLR_OK) return rfail((r), st_, nclr_last_error((r)->sim)); \
+  } while (0)
+
+void rollout_release(nclr_rollout *r) {
+  if (!r) return;
+  if (r->sim) {
+    cudaSetDevice(r->sim->device);
+    cudaStreamSynchronize(r->sim->stream);
+  }
+  cudaFree(r->ckpt);
+  cudaFree(r->seg);
+  cudaFree(r->grids);
+  cudaFree(r->adj[0]);
+  cudaFree(r->adj[1]);
+  cudaFree(r->VB);
+  cudaFree(r->GB);
+  cudaFree(r->gml);
+  cudaFree(r->err);
+  cudaFree(r->mass);
+  cudaFree(r->vol);
+  cudaFree(r->ones);
+  for (auto e : r->ev)
+    if (e) cudaEventDestroy(e);
+  if (r->sim) nclr_destroy(r->sim);
+  delete r;
+}
+
+// New Young's modulus / Poisson ratio for the (single) scene: host and device tables; the
+// captured graphs hold the old parameters and are dropped.
+void set_material(nclr_sim *s, float E, float nu) {
+  Params &P = s->scenes[0].P;
+  P.mu0 = E / (2.0f * (1.0f + nu));
+  P.lambda0 = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+  cudaMemcpyAsync(s->scenes_d, s->scenes.data(), sizeof(Scene), cudaMemcpyHostToDevice, s->stream);
+  for (auto &row : s->graph)
+    for (auto &g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+}
+
+// Loads a state (rows) into the simulation; the next advance() starts from it.
+nclr_status load_state(nclr_rollout *r, float *st) {
+  R_SIM(r, nclr_set_particles_device(r->sim, r->x(st), r->v(st), r->F(st), r->C(st), r->ones));
+  return NCLR_OK;
+}
+
+nclr_status save_state(nclr_rollout *r, float *st) {
+  R_SIM(r, nclr_get_particles_device(r->sim, r->x(st), r->v(st), r->F(st), r->C(st), nullptr));
+  return NCLR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nclr_status nclr_rollout_create(nclr_rollout **out, int dim, int64_t n, const float *x0,
+                                const float *mass, const float *volume, int res, float dt,
+                                float gravity, int64_t nsteps, int checkpoint_every,
+                                const nclr_options *opt) {
+  if (!out) return NCLR_ERR_INVALID;
+  *out = nullptr;
+  g_create_error.clear();
+  if (nsteps < 1 || checkpoint_every < 1) return fail(nullptr, NCLR_ERR_INVALID, "nsteps and checkpoint_every must be >= 1");
+  if (n < 1 || !x0) return fail(nullptr, NCLR_ERR_INVALID, "a rollout needs particles");
+  nclr_rollout *r = new (std::nothrow) nclr_rollout();
+  if (!r) return fail(nullptr, NCLR_ERR_INVALID, "out of host memory");
+  nclr_status st = nclr_create(&r->sim, dim, n, x0, nullptr, nullptr, nullptr, nullptr, mass, volume,
+                               nullptr, NCLR_JELLY, res, dt, 1e4f, 0.2f, gravity, opt);
+  if (st != NCLR_OK) {
+    delete r;
+    return st;
+  }
+  nclr_sim *s = r->sim;
+  r->dim = dim;
+  r->n = n;
+  r->nsteps = nsteps;
+  r->every = (int)std::min<int64_t>(checkpoint_every, nsteps);
+  r->nseg = (int)((nsteps + r->every - 1) / r->every);
+  r->nodes = s->P0().nodes;
+  r->rowf = (size_t)n * (2 * dim + 2 * dim * dim);
+  auto bail = [&](const std::string &m) {
+    g_create_error = m;
+    rollout_release(r);
+    return NCLR_ERR_CUDA;
+  };
+#define RC(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return bail(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+  RC(cudaSetDevice(s->device));
+  RC(cudaMalloc((void **)&r->ckpt, sizeof(float) * r->rowf * (size_t)r->nseg));
+  RC(cudaMalloc((void **)&r->seg, sizeof(float) * r->rowf * (size_t)(r->every + 1)));
+  RC(cudaMalloc((void **)&r->grids, sizeof(float4) * (size_t)r->nodes * (size_t)r->every));
+  for (auto &a : r->adj) RC(cudaMalloc((void **)&a, sizeof(float) * r->rowf));
+  RC(cudaMalloc((void **)&r->VB, sizeof(float4) * (size_t)r->nodes));
+  RC(cudaMalloc((void **)&r->GB, sizeof(float4) * (size_t)r->nodes));
+  RC(cudaMalloc((void **)&r->gml, 2 * sizeof(double)));
+  RC(cudaMalloc((void **)&r->err, sizeof(int)));
+  RC(cudaMalloc((void **)&r->mass, sizeof(float) * (size_t)n));
+  RC(cudaMalloc((void **)&r->vol, sizeof(float) * (size_t)n));
+  RC(cudaMalloc((void **)&r->ones, sizeof(float) * (size_t)n));
+  std::vector<float> ones((size_t)n, 1.0f);
+  RC(cudaMemcpy(r->mass, mass ? mass : ones.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  RC(cudaMemcpy(r->vol, volume ? volume : ones.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  RC(cudaMemcpy(r->ones, ones.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  RC(cudaMemset(r->VB, 0, sizeof(float4) * (size_t)r->nodes));
+  for (auto &e : r->ev) RC(cudaEventCreate(&e));
+#undef RC
+  *out = r;
+  return NCLR_OK;
+}
+
+nclr_status nclr_rollout_forward(nclr_rollout *r, const float *x0, const float *v0, const float *F0,
+                                 const float *C0, float E, float nu, float *xT, float *vT,
+                                 float *FT, float *CT) {
+  if (!r || !x0 || !v0 || !F0 || !C0) return rfail(r, NCLR_ERR_INVALID, "NULL argument");
+  nclr_sim *s = r->sim;
+  R_TRY(r, cudaSetDevice(s->device));
+  r->E = E;
+  r->nu = nu;
+  set_material(s, E, nu);
+  float *c0 = r->state(r->ckpt, 0);
+  const size_t vec = sizeof(float) * (size_t)r->n * r->dim, mat = vec * r->dim;
+  R_TRY(r, cudaMemcpyAsync(r->x(c0), x0, vec, cudaMemcpyDeviceToDevice, s->stream));
+  R_TRY(r, cudaMemcpyAsync(r->v(c0), v0, vec, cudaMemcpyDeviceToDevice, s->stream));
+  R_TRY(r, cudaMemcpyAsync(r->F(c0), F0, mat, cudaMemcpyDeviceToDevice, s->stream));
+  R_TRY(r, cudaMemcpyAsync(r->C(c0), C0, mat, cudaMemcpyDeviceToDevice, s->stream));
+  R_TRY(r, cudaEventRecord(r->ev[0], s->stream));
+  nclr_status st = load_state(r, c0);
+  if (st != NCLR_OK) return st;
+  for (int k = 1; k < r->nseg; ++k) {
+    R_SIM(r, nclr_advance(s, r->every));
+    if ((st = save_state(r, r->state(r->ckpt, k))) != NCLR_OK) return st;
+  }
+  R_SIM(r, nclr_advance(s, r->nsteps - (int64_t)(r->nseg - 1) * r->every));
+  R_SIM(r, nclr_get_particles_device(s, xT, vT, FT, CT, nullptr));
+  R_TRY(r, cudaEventRecord(r->ev[1], s->stream));
+  R_TRY(r, cudaEventSynchronize(r->ev[1]));
+  cudaEventElapsedTime(&r->fwd_ms, r->ev[0], r->ev[1]);
+  r->have_forward = true;
+  return NCLR_OK;
+}
+
+nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float *gvT,
+                                  const float *gFT, const float *gCT, float *gx0, float *gv0,
+                                  float *gF0, float *gC0, double *gE, double *gnu) {
+  if (!r) return NCLR_ERR_INVALID;
+  if (!r->have_forward) return rfail(r, NCLR_ERR_INVALID, "backward before forward");
+  nclr_sim *s = r->sim;
+  R_TRY(r, cudaSetDevice(s->device));
+  const int D = r->dim;
+  const int n = (int)r->n;
+  const size_t vec = sizeof(float) * (size_t)n * D, mat = vec * D;
+  R_TRY(r, cudaEventRecord(r->ev[0], s->stream));
+  float *a = r->adj[0], *b = r->adj[1];
+  auto seed = [&](float *dst, const float *src, size_t bytes) -> cudaError_t {
+    return src ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s->stream)
+               : cudaMemsetAsync(dst, 0, bytes, s->stream);
+  };
+  R_TRY(r, seed(r->x(a), gxT, vec));
+  R_TRY(r, seed(r->v(a), gvT, vec));
+  R_TRY(r, seed(r->F(a), gFT, mat));
+  R_TRY(r, seed(r->C(a), gCT, mat));
+  R_TRY(r, cudaMemsetAsync(r->gml, 0, 2 * sizeof(double), s->stream));
+  R_TRY(r, cudaMemsetAsync(r->err, 0, sizeof(int), s->stream));
+  const Params &P = s->P0();
+  for (int sg = r->nseg - 1; sg >= 0; --sg) {
+    const int64_t t0 = (int64_t)sg * r->every;
+    const int L = (int)std::min<int64_t>(r->every, r->nsteps - t0);
+    // recompute the segment: states s_t0..s_t0+L and the grids of its steps
+    float *first = r->state(r->seg, 0);
+    R_TRY(r, cudaMemcpyAsync(first, r->state(r->ckpt, sg), sizeof(float) * r->rowf,
+                             cudaMemcpyDeviceToDevice, s->stream));
+    nclr_status st = load_state(r, first);
+    if (st != NCLR_OK) return st;
+    for (int i = 0; i < L; ++i) {
+      R_SIM(r, nclr_advance(s, 1));
+      R_TRY(r, cudaMemcpyAsync(r->grids + (size_t)i * r->nodes, s->V, sizeof(float4) * (size_t)r->nodes,
+                               cudaMemcpyDeviceToDevice, s->stream));
+      if ((st = save_state(r, r->state(r->seg, i + 1))) != NCLR_OK) return st;
+    }
+    for (int i = L - 1; i >= 0; --i) {
+      float *st_t = r->state(r->seg, i), *st_n = r->state(r->seg, i + 1);
+      dispatch_dim(D, [&](auto dc) {
+        constexpr int DD = decltype(dc)::value;
+        mpm::launch_adjoint_step<DD>(n, r->x(st_t), r->v(st_t), r->F(st_t), r->C(st_t), r->C(st_n),
+                                     r->mass, r->vol, r->grids + (size_t)i * r->nodes, P, s->ref,
+                                     r->x(a), r->v(a), r->F(a), r->C(a), r->x(b), r->v(b),
+                                     r->F(b), r->C(b), r->VB, r->GB, r->gml, r->err, s->stream);
+      });
+      std::swap(a, b);
+    }
+    nclr_status cst = check_launch(s, "adjoint step");
+    if (cst != NCLR_OK) return rfail(r, cst, s->error);
+  }
+  if (gx0) R_TRY(r, cudaMemcpyAsync(gx0, r->x(a), vec, cudaMemcpyDeviceToDevice, s->stream));
+  if (gv0) R_TRY(r, cudaMemcpyAsync(gv0, r->v(a), vec, cudaMemcpyDeviceToDevice, s->stream));
+  if (gF0) R_TRY(r, cudaMemcpyAsync(gF0, r->F(a), mat, cudaMemcpyDeviceToDevice, s->stream));
+  if (gC0) R_TRY(r, cudaMemcpyAsync(gC0, r->C(a), mat, cudaMemcpyDeviceToDevice, s->stream));
+  double gml[2] = {0.0, 0.0};
+  int err = 0;
+  R_TRY(r, cudaMemcpyAsync(gml, r->gml, sizeof(gml), cudaMemcpyDeviceToHost, s->stream));
+  R_TRY(r, cudaMemcpyAsync(&err, r->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  R_TRY(r, cudaEventRecord(r->ev[1], s->stream));
+  R_TRY(r, cudaEventSynchronize(r->ev[1]));
+  cudaEventElapsedTime(&r->bwd_ms, r->ev[0], r->ev[1]);
+  // mu_0 = E / (2 (1 + nu)), lambda_0 = E nu / ((1 + nu)(1 - 2 nu)) (src/nclr.h:77-78)
+  const double E = r->E, nu = r->nu;
+  const double dmu_dE = 1.0 / (2.0 * (1.0 + nu)), dmu_dnu = -E / (2.0 * (1.0 + nu) * (1.0 + nu));
+  const double q = (1.0 + nu) * (1.0 - 2.0 * nu);
+  const double dl_dE = nu / q, dl_dnu = E * (1.0 + 2.0 * nu * nu) / (q * q);
+  if (gE) *gE = gml[0] * dmu_dE + gml[1] * dl_dE;
+  if (gnu) *gnu = gml[0] * dmu_dnu + gml[1] * dl_dnu;
+  if (err & mpm::kErrOutOfRange) return rfail(r, NCLR_ERR_OUT_OF_RANGE, "a stencil left the grid");
+  return NCLR_OK;
+}
+
+nclr_status nclr_rollout_timing(const nclr_rollout *r, double *forward_ms, double *backward_ms) {
+  if (!r) return NCLR_ERR_INVALID;
+  if (forward_ms) *forward_ms = r->fwd_ms;
+  if (backward_ms) *backward_ms = r->bwd_ms;
+  return NCLR_OK;
+}
+
+void *nclr_rollout_stream(nclr_rollout *r) { return r ? (void *)r->sim->stream : nullptr; }
+
+const char *nclr_rollout_error(const nclr_rollout *r) {
+  return r ? r->error.c_str() : g_create_error.c_str();
+}
+
+void nclr_rollout_destroy(nclr_rollout *r) { rollout_release(r); }
+
+}  // extern "C"

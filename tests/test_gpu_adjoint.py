@@ -1,0 +1,117 @@
+"""GPU adjoint of jelly rollouts (nclr_rollout_* / nuclearmpm_gb300.autograd) against the FP64
+CPU adjoint of the oracle and FP64 finite differences of the oracle's forward step.
+
+Bounds: the GPU runs FP32 forward and FP32 adjoint kernels (FP64 only for the E / nu sums),
+so its gradients sit within 1e-3 (normwise, relative to each field's largest entry) of the
+FP64 adjoint, and directional derivatives within 1e-3 of central differences in FP64."""
+import numpy as np
+import pytest
+
+from nuclearmpm_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+GRAD_TOL = 1e-3
+
+
+def setup(dim, res, n, physics, seed=0):
+    rng = np.random.default_rng(seed)
+    side = round(n ** (1 / dim))
+    x = scenes.jittered_block(rng, (side,) * dim, 0.5 / res, (0.35,) * dim, 0.25 / res)
+    s = scenes.particles(x, rng.normal(0, 0.5, size=x.shape).astype(np.float32), physics=physics)
+    s["F"] = (s["F"] + rng.normal(0, 0.01, size=s["F"].shape)).astype(np.float32)
+    return s
+
+
+def gpu_grads(s, dim, res, steps, physics, every, seed_fn, E=1e4, nu=0.2):
+    from nuclearmpm_gb300.autograd import Rollout
+    roll = Rollout(s["x"], res=res, steps=steps, checkpoint_every=every, physics=physics)
+    dev = torch.device("cuda", 0)
+    x0 = torch.tensor(s["x"], device=dev, requires_grad=True)
+    v0 = torch.tensor(s["v"], device=dev, requires_grad=True)
+    F0 = torch.tensor(s["F"], device=dev, requires_grad=True)
+    C0 = torch.tensor(s["C"], device=dev, requires_grad=True)
+    Et = torch.tensor(E, dtype=torch.float64, requires_grad=True)
+    nut = torch.tensor(nu, dtype=torch.float64, requires_grad=True)
+    xT, vT = roll(x0, v0, Et, nut, F0, C0)
+    loss = seed_fn(xT)
+    loss.backward()
+    out = {"x": x0.grad.cpu().numpy(), "v": v0.grad.cpu().numpy(), "F": F0.grad.cpu().numpy(),
+           "C": C0.grad.cpu().numpy(), "E": float(Et.grad), "nu": float(nut.grad),
+           "xT": xT.detach().cpu().numpy(), "loss": float(loss.detach())}
+    out["timing"] = roll.timing()
+    roll.close()
+    return out
+
+
+def com_loss(target):
+    t = torch.tensor(target, dtype=torch.float32, device="cuda")
+    return lambda xT: ((xT.mean(0) - t) ** 2).sum()
+
+
+def point_loss(targets):
+    t = torch.tensor(targets, dtype=torch.float32, device="cuda")
+    return lambda xT: ((xT - t) ** 2).sum()
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+@pytest.mark.parametrize("dim,res,steps,n", [(2, 32, 50, 1024), (3, 16, 10, 512)])
+@pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
+def test_gpu_adjoint_matches_fp64_adjoint(oracle, dim, res, steps, n, physics):
+    s = setup(dim, res, n, physics)
+    rng = np.random.default_rng(3)
+    # pointwise loss: depends on the deformation (E / nu gradients non-zero)
+    fwd, _ = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={})
+    targets = (fwd["x"] + rng.normal(0, 1e-3, size=fwd["x"].shape)).astype(np.float32)
+    g = gpu_grads(s, dim, res, steps, physics, every=7, seed_fn=point_loss(targets))
+    seed = 2 * (g["xT"].astype(np.float64) - targets)  # the GPU's own final state
+    _, o = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={"x": seed})
+    for f in ("x", "v", "F", "C"):
+        assert rel(g[f], o[f]) <= GRAD_TOL, (f, rel(g[f], o[f]))
+    for p in ("E", "nu"):
+        assert abs(g[p] - o[p]) <= GRAD_TOL * abs(o[p]), (p, g[p], o[p])
+
+
+def test_gpu_gradients_match_finite_differences(oracle):
+    """The reduced 2D case: 1,024 particles, 32^2 grid, 50 steps, loss = |COM - target|^2."""
+    dim, res, steps, n = 2, 32, 50, 1024
+    s = setup(dim, res, n, scenes.CORRECTED, seed=9)
+    target = np.array([0.45, 0.4])
+    g = gpu_grads(s, dim, res, steps, scenes.CORRECTED, every=50, seed_fn=com_loss(target))
+
+    def loss64(st):
+        out, _, status, _ = oracle.advance(st, dim=dim, model=scenes.JELLY, res=res, steps=steps,
+                                           fp64=True, physics=scenes.CORRECTED, want_grid=False)
+        assert status == 0
+        d = out["x"].mean(0) - target
+        return float(d @ d)
+
+    rng = np.random.default_rng(11)
+    s64 = {k: np.asarray(v, np.float64) for k, v in s.items()}
+    for field, h in (("v", 1e-4), ("x", 1e-6)):
+        for _ in range(3):
+            dirn = rng.normal(size=s64[field].shape)
+            sp = dict(s64)
+            sm = dict(s64)
+            sp[field] = s64[field] + h * dirn
+            sm[field] = s64[field] - h * dirn
+            fd = (loss64(sp) - loss64(sm)) / (2 * h)
+            ad = float((g[field].astype(np.float64) * dirn).sum())
+            assert abs(ad - fd) <= GRAD_TOL * abs(fd), (field, ad, fd)
+
+
+def test_checkpoint_interval_does_not_change_gradients():
+    """Recomputing from checkpoints every 3 steps or once: same gradients (a loss on every
+    particle's position, so that no field's gradient vanishes by momentum conservation)."""
+    dim, res, steps, n = 2, 32, 40, 1024
+    s = setup(dim, res, n, scenes.REFERENCE, seed=4)
+    loss = point_loss(s["x"] + np.float32(0.01))
+    a = gpu_grads(s, dim, res, steps, scenes.REFERENCE, every=40, seed_fn=loss)
+    b = gpu_grads(s, dim, res, steps, scenes.REFERENCE, every=3, seed_fn=loss)
+    for f in ("x", "v", "F", "C"):
+        assert rel(a[f], b[f]) <= GRAD_TOL, f
