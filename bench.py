@@ -209,6 +209,47 @@ def run_batched(device: int, steps: int = 100) -> dict:
                       "plain simulations one after another"}
 
 
+def run_adjoint(device: int, steps: int = 2000, every: int = 50) -> dict:
+    """The differentiable form: 3D jelly, 64^3 grid, one 64x64x32 jittered lattice (131,072
+    particles, seeded), `steps` steps with a checkpoint every `every`; loss = squared distance
+    of the final centre of mass from a seeded target; gradients with respect to the initial
+    velocities, Young's modulus and Poisson ratio through nuclearmpm_gb300.autograd.  Device
+    times of the forward and of the backward (which recomputes every segment) from CUDA
+    events on the rollout's stream."""
+    import torch
+
+    from nuclearmpm_gb300 import scenes
+    from nuclearmpm_gb300.autograd import Rollout
+    sc = scenes.jelly_block_3d(seed=0, res=64, shape=(64, 64, 32))
+    n = len(sc["x"])
+    rng = np.random.default_rng(0)
+    dev = torch.device("cuda", device)
+    roll = Rollout(sc["x"], res=64, steps=steps, checkpoint_every=every, device=device)
+    x0 = torch.tensor(sc["x"], device=dev)
+    v0 = torch.tensor(rng.normal(0, 0.5, size=(n, 3)).astype(np.float32), device=dev,
+                      requires_grad=True)
+    E = torch.tensor(1e4, dtype=torch.float64, requires_grad=True)
+    nu = torch.tensor(0.2, dtype=torch.float64, requires_grad=True)
+    target = torch.tensor(rng.uniform(0.3, 0.7, size=3).astype(np.float32), device=dev)
+    for _ in range(2):  # the second iteration is the measured one
+        v0.grad = None
+        E.grad = None
+        nu.grad = None
+        xT, vT = roll(x0, v0, E, nu)
+        loss = ((xT.mean(0) - target) ** 2).sum()
+        loss.backward()
+    fwd_ms, bwd_ms = roll.timing()
+    roll.close()
+    return {"value": n * steps / ((fwd_ms + bwd_ms) / 1e3), "unit": UNIT,
+            "metric": "fwd+adjoint particle-steps/s", "particles": n, "steps": steps,
+            "checkpoint_every": every, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+            "backward_over_forward": bwd_ms / fwd_ms,
+            "forward_value": n * steps / (fwd_ms / 1e3),
+            "grad_norms": {"v0": float(v0.grad.norm()), "E": float(E.grad), "nu": float(nu.grad)},
+            "config": "3D jelly, 64^3 grid, 64x64x32 jittered lattice, dt 1e-4, loss |COM - "
+                      "target|^2, gradients w.r.t. v0, E, nu"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -328,6 +369,9 @@ def run_ours(args):
     batched = None
     if not args.no_batched:
         batched = run_batched(local)
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = run_adjoint(local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -343,6 +387,7 @@ def run_ours(args):
                 "data": "synthetic (seeded scene with the workload's shapes and distributions)",
                 "config": dict(WORKLOAD, parallelism=f"replicas x{world}"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
+                "adjoint": adjoint,
                 "gpu_launches": launches_total, "clocks": clk}
         print(json.dumps(line), flush=True)
     sim.close()
@@ -360,6 +405,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

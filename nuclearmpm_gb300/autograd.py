@@ -102,6 +102,7 @@ class RolloutFunction(torch.autograd.Function):
                                                      Ef, nuf, _dp(xT), _dp(vT), None, None))
         ctx.roll = roll
         ctx.params = [(t.dtype, t.device) if torch.is_tensor(t) else None for t in (E, nu)]
+        ctx.given = (F0 is not None, C0 is not None)
         return xT, vT
 
     @staticmethod
@@ -124,4 +125,5 @@ class RolloutFunction(torch.autograd.Function):
         out = []
         for val, spec in ((gE.value, ctx.params[0]), (gnu.value, ctx.params[1])):
             out.append(None if spec is None else torch.tensor(val, dtype=spec[0], device=spec[1]))
-        return None, gx0, gv0, out[0], out[1], gF0, gC0
+        return (None, gx0, gv0, out[0], out[1], gF0 if ctx.given[0] else None,
+                gC0 if ctx.given[1] else None)

@@ -138,10 +138,9 @@ __device__ __forceinline__ Mat<2> polar_backward(const Mat<2> &F, const Mat<2> &
   out.a[0][1] = -bb;
   return out;
 }
-__device__ __forceinline__ Mat<3> polar_backward(const Mat<3> &F, const Mat<3> &Rb) {
-  Mat<3> U, V;
-  float sg[3];
-  svd3(F, U, sg, V);
+// With the SVD of F already at hand (R = U V^T).
+__device__ __forceinline__ Mat<3> polar_backward_svd(const Mat<3> &U, const float sg[3],
+                                                     const Mat<3> &V, const Mat<3> &Rb) {
   // P = U^T Rb V
   Mat<3> UtR;
 #pragma unroll
@@ -160,6 +159,30 @@ __device__ __forceinline__ Mat<3> polar_backward(const Mat<3> &F, const Mat<3> &
     }
   return mat_mul_t<3>(mat_mul<3>(U, Z), V);
 }
+
+// The polar rotation of F and what its adjoint needs: 3D keeps the SVD, 2D nothing.
+template <int D>
+struct Polar;
+template <>
+struct Polar<2> {
+  Mat<2> R;
+  __device__ __forceinline__ explicit Polar(const Mat<2> &F) : R(polar_rotation(F)) {}
+  __device__ __forceinline__ Mat<2> backward(const Mat<2> &F, const Mat<2> &Rb) const {
+    return polar_backward(F, Rb);
+  }
+};
+template <>
+struct Polar<3> {
+  Mat<3> U, V, R;
+  float sg[3];
+  __device__ __forceinline__ explicit Polar(const Mat<3> &F) {
+    svd3(F, U, sg, V);
+    R = uvt<3>(U, V);
+  }
+  __device__ __forceinline__ Mat<3> backward(const Mat<3> &, const Mat<3> &Rb) const {
+    return polar_backward_svd(U, sg, V, Rb);
+  }
+};
 
 }  // namespace
 
@@ -234,15 +257,16 @@ __global__ void __launch_bounds__(128) adj_g2p_kernel(
     float du[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) du[d] = (float)oo[d] - st.fx[d];
-    float wb = 0.0f;
+    float wb = 0.0f, add[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       float gcdu = 0.0f;
 #pragma unroll
       for (int b = 0; b < D; ++b) gcdu += gCt.a[a][b] * du[b];
-      atomicAdd(VB + f * 4 + a, W * gvt[a] + cs * W * gcdu);
+      add[a] = W * gvt[a] + cs * W * gcdu;
       wb += gvt[a] * vg[a] + cs * vg[a] * gcdu;
     }
+    red_add_v4(reinterpret_cast<float4 *>(VB) + f, add[0], add[1], add[2], 0.0f);
     Wbar[o] = wb;
 #pragma unroll
     for (int b = 0; b < D; ++b) {
@@ -311,7 +335,8 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     const Mat<D> Fm = load_row_mat<D>(F, p);
     const Mat<D> Cm = load_row_mat<D>(C, p);
     const float m = mass[p], vo = vol[p];
-    const Mat<D> R = polar_R(Fm);
+    const Polar<D> pol(Fm);
+    const Mat<D> &R = pol.R;
     const Mat<D> A = fused_affine<D>(Fm, R, Cm, 1.0f, m, vo, kJelly, P);
     Mat<D> gA;
 #pragma unroll
@@ -412,7 +437,7 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
         for (int k = 0; k < D; ++k) s += Qb.a[k][i] * X.a[k][j];
         FQ.a[i][j] = s;
       }
-    const Mat<D> Fp = polar_backward(Fm, Rb);
+    const Mat<D> Fp = pol.backward(Fm, Rb);
     const Mat<D> cof = cofactor(Fm);
     const float dJ = sbar * lam * (2.0f * J - 1.0f);
     Mat<D> gF = load_row_mat<D>(oF, p);

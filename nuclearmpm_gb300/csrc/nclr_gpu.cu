@@ -992,6 +992,49 @@ nclr_status save_state(nclr_rollout *r, float *st) {
   return NCLR_OK;
 }
 
+// Steps the simulation L times from the loaded state, recording after step i the state
+// (into r->seg state i + 1, caller order) and the step's updated grid (r->grids[i]); one
+// synchronisation at the end.  Every step writes v and C (they are part of the record).
+nclr_status record_segment(nclr_rollout *r, int L) {
+  nclr_sim *s = r->sim;
+  R_TRY(r, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)s->nscenes, s->stream));
+  if (s->need_sort) {
+    enqueue_sort(s, !s->acc_valid);
+    s->need_sort = false;
+    s->steps_since_sort = 0;
+  }
+  if (!s->acc_valid) {
+    dispatch_dim(s->dim, [&](auto dc) {
+      constexpr int D = decltype(dc)::value;
+      mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
+                                     s->total_blocks, s->sms, s->stream);
+      cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
+      mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
+                           s->flags, s->blocks, s->nblocks_active, s->start, s->work, s->err_d, 0,
+                           s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
+    });
+    s->acc_valid = true;
+  }
+  for (int i = 0; i < L; ++i) {
+    const bool sort = sort_due(s);
+    enqueue_step(s, sort, true);
+    if (sort) s->steps_since_sort = 0;
+    ++s->steps_since_sort;
+    R_TRY(r, cudaMemcpyAsync(r->grids + (size_t)i * r->nodes, s->V, sizeof(float4) * (size_t)r->nodes,
+                             cudaMemcpyDeviceToDevice, s->stream));
+    float *st = r->state(r->seg, i + 1);
+    nclr_status e = export_rows(s, -1, r->x(st), r->v(st), r->F(st), r->C(st), nullptr);
+    if (e != NCLR_OK) return rfail(r, e, s->error);
+  }
+  s->stepped = true;
+  R_TRY(r, cudaMemcpyAsync(s->err_h, s->err_d, 2 * sizeof(int) * (size_t)s->nscenes,
+                           cudaMemcpyDeviceToHost, s->stream));
+  R_TRY(r, cudaStreamSynchronize(s->stream));
+  if ((s->err_h[0] | s->err_h[1]) & mpm::kErrOutOfRange)
+    return rfail(r, NCLR_ERR_OUT_OF_RANGE, "a stencil left the grid during the recomputation");
+  return NCLR_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1117,12 +1160,7 @@ nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float
                              cudaMemcpyDeviceToDevice, s->stream));
     nclr_status st = load_state(r, first);
     if (st != NCLR_OK) return st;
-    for (int i = 0; i < L; ++i) {
-      R_SIM(r, nclr_advance(s, 1));
-      R_TRY(r, cudaMemcpyAsync(r->grids + (size_t)i * r->nodes, s->V, sizeof(float4) * (size_t)r->nodes,
-                               cudaMemcpyDeviceToDevice, s->stream));
-      if ((st = save_state(r, r->state(r->seg, i + 1))) != NCLR_OK) return st;
-    }
+    if ((st = record_segment(r, L)) != NCLR_OK) return st;
     for (int i = L - 1; i >= 0; --i) {
       float *st_t = r->state(r->seg, i), *st_n = r->state(r->seg, i + 1);
       dispatch_dim(D, [&](auto dc) {
