@@ -176,7 +176,7 @@ struct Polar<3> {
   Mat<3> U, V, R;
   float sg[3];
   __device__ __forceinline__ explicit Polar(const Mat<3> &F) {
-    svd3(F, U, sg, V);
+    svd3<false>(F, U, sg, V);  // the same factorisation as the forward stress (polar_R)
     R = uvt<3>(U, V);
   }
   __device__ __forceinline__ Mat<3> backward(const Mat<3> &, const Mat<3> &Rb) const {

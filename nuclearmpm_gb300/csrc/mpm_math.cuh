@@ -137,13 +137,19 @@ namespace detail {
 // Conjugate symmetric S (stored full) by the Jacobi rotation in the (p,q) plane that zeroes
 // S_pq (the symmetric Schur rotation of Golub & Van Loan, Alg. 8.4.2, in the numerically
 // stable small-angle form); accumulate it into V (V <- V Q).
-template <int P, int Q>
+// kExact: the rotation's cosine (here and in qr_givens) is correctly rounded rather than from
+// the approximate reciprocal square root, so a rotation by a rounding-level angle is exactly
+// the identity and the singular values of a matrix that is the identity to within rounding
+// come out exactly 1.  Plasticity needs that (the liquid's J = prod sigma enters the
+// pressure lambda (J - 1) J on every entry; snow recomposes F from the clamped sigma); the
+// polar rotation of the stress does not.
+template <int P, int Q, bool kExact>
 MPM_HD void jacobi_rotate(float S[3][3], float V[3][3]) {
   const float app = S[P][P], aqq = S[Q][Q], apq = S[P][Q];
   if (apq == 0.0f) return;
   const float tau = (aqq - app) / (2.0f * apq);
   const float t = copysignf(1.0f, tau) / (fabsf(tau) + sqrtf(1.0f + tau * tau));
-  const float c = rsqrt_(1.0f + t * t), s = t * c;
+  const float c = kExact ? 1.0f / sqrtf(1.0f + t * t) : rsqrt_(1.0f + t * t), s = t * c;
   // S <- Q^T S Q with Q = I except Q_pp = c, Q_pq = s, Q_qp = -s, Q_qq = c
 #pragma unroll
   for (int k = 0; k < 3; ++k) {  // columns: S Q
@@ -188,15 +194,21 @@ MPM_HD void cond_swap(float B[3][3], float V[3][3], float rho[3]) {
 }
 
 // Givens rotation on rows (P,Q) of B zeroing B[Q][COL]; accumulates U <- U G.
-template <int P, int Q, int COL>
+template <int P, int Q, int COL, bool kExact>
 MPM_HD void qr_givens(float B[3][3], float U[3][3]) {
   const float a1 = B[P][COL], a2 = B[Q][COL];
   const float n2 = a1 * a1 + a2 * a2;
   float c = 1.0f, s = 0.0f;
   if (n2 > 1e-38f) {
-    const float inv = rsqrt_(n2);
-    c = a1 * inv;
-    s = a2 * inv;
+    if constexpr (kExact) {  // c = +-1, s = 0 exactly when a2 is negligible against a1
+      const float r = sqrtf(n2);
+      c = a1 / r;
+      s = a2 / r;
+    } else {
+      const float inv = rsqrt_(n2);
+      c = a1 * inv;
+      s = a2 * inv;
+    }
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {  // rows: G^T B with G = [[c,-s],[s,c]] in (P,Q)
@@ -216,6 +228,7 @@ MPM_HD void qr_givens(float B[3][3], float U[3][3]) {
 
 constexpr int kJacobiSweeps = 4;
 
+template <bool kExact = true>
 MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
   using namespace detail;
   float S[3][3], V[3][3];
@@ -228,9 +241,9 @@ MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
     }
 #pragma unroll 1
   for (int sweep = 0; sweep < kJacobiSweeps; ++sweep) {
-    jacobi_rotate<0, 1>(S, V);
-    jacobi_rotate<1, 2>(S, V);
-    jacobi_rotate<0, 2>(S, V);
+    jacobi_rotate<0, 1, kExact>(S, V);
+    jacobi_rotate<1, 2, kExact>(S, V);
+    jacobi_rotate<0, 2, kExact>(S, V);
   }
   float B[3][3];
 #pragma unroll
@@ -244,9 +257,9 @@ MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
   cond_swap<0, 2>(B, V, rho);
   cond_swap<1, 2>(B, V, rho);
   float U[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
-  qr_givens<0, 1, 0>(B, U);
-  qr_givens<0, 2, 0>(B, U);
-  qr_givens<1, 2, 1>(B, U);
+  qr_givens<0, 1, 0, kExact>(B, U);
+  qr_givens<0, 2, 0, kExact>(B, U);
+  qr_givens<1, 2, 1, kExact>(B, U);
   sig[0] = B[0][0];
   sig[1] = B[1][1];
   sig[2] = B[2][2];
@@ -281,7 +294,7 @@ MPM_HD Mat<2> polar_R(const Mat<2> &F) { return polar_rotation(F); }
 MPM_HD Mat<3> polar_R(const Mat<3> &F) {
   Mat<3> U, V;
   float s[3];
-  svd3(F, U, s, V);
+  svd3<false>(F, U, s, V);
   return uvt<3>(U, V);
 }
 

@@ -106,17 +106,21 @@ def jelly_cubes_3d(seed: int = 0, res: int = 128, cubes: int = 4, side: int = 64
 
 
 def liquid_snow_boxes_3d(seed: int = 0, res: int = 256, boxes: int = 16,
-                         total: int = 4_194_304, physics: int = REFERENCE):
+                         total: int = 4_194_304, physics: int = REFERENCE, margin: float = 0.05):
     """3D mixed liquid + snow: `boxes` axis-aligned boxes with sides uniform in [0.05, 0.2]
-    in the upper half of the domain, filled with jittered lattices whose common spacing makes
-    the particle count `total` (the largest boxes are trimmed to hit it exactly); half the
-    boxes liquid, half snow, shuffled.  Returns (scene, material per particle)."""
+    in the upper half of the domain, at least `margin` from the walls, filled with jittered
+    lattices whose common spacing makes the particle count `total` (the largest boxes are
+    trimmed to hit it exactly); half the boxes liquid, half snow, shuffled.  Returns (scene,
+    material per particle).  (A box reaching into the 3-node sticky border, where the
+    boundary rule tests the sign of an exactly-zero velocity component, makes the step
+    discontinuous in its input: keep `margin` above (3 + 2) / res.)"""
     rng = np.random.default_rng(seed)
     dx = 1.0 / res
     sides = rng.uniform(0.05, 0.2, size=(boxes, 3))
-    lo = np.column_stack([rng.uniform(0.05, 0.95 - sides[:, 0]),
-                          rng.uniform(0.5, 0.95 - sides[:, 1]),
-                          rng.uniform(0.05, 0.95 - sides[:, 2])])
+    hi = 1.0 - margin
+    lo = np.column_stack([rng.uniform(margin, hi - sides[:, 0]),
+                          rng.uniform(0.5, hi - sides[:, 1]),
+                          rng.uniform(margin, hi - sides[:, 2])])
     vol = np.prod(sides, axis=1).sum()
     spacing = (vol / total) ** (1.0 / 3.0)
     counts = [np.maximum(1, np.round(s / spacing)).astype(int) for s in sides]

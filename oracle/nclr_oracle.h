@@ -298,6 +298,7 @@ struct Particle {
   Vec<T, D> x, v;
   Mat<T, D> F, C;
   T Jp, mass, volume;
+  int material = -1;  // per-particle material (an extension); -1: the simulation's model
 };
 
 // Cell<dim>, src/nclr.h:50-55.
@@ -381,11 +382,17 @@ class Simulation {
       return (int64_t)(base[0] + o[0]) * N + (base[1] + o[1]);
   }
 
+  // The material of particle p: the simulation's model (src/nclr.h:90) unless the particle
+  // carries its own (the mixed-material extension).
+  Model model_of(const Particle<T, D> &p) const {
+    return p.material < 0 ? model_ : (Model)p.material;
+  }
+
   // hardening, src/nclr.h:351-372.  Snow: e = exp(10*(1.0 - Jp)) in double, narrowed to
   // the scalar (constant_hardening takes `real`); jelly 0.3; liquid 1.0.
   std::pair<T, T> hardening(const Particle<T, D> &p) const {
     T e;
-    switch (model_) {
+    switch (model_of(p)) {
       case Model::kSnow: e = (T)std::exp((double)T(10.0) * (1.0 - (double)p.Jp)); break;
       case Model::kJelly: e = T(0.3); break;
       case Model::kLiquid: e = T(1.0); break;
@@ -502,14 +509,15 @@ class Simulation {
       for (int i = 0; i < D; ++i)
         for (int j = 0; j < D; ++j) M(i, j) = I(i, j) + dt_ * p.C(i, j);
       Mat<T, D> Fh = mul(M, p.F);
-      if (model_ == Model::kJelly) {
+      const Model model = model_of(p);
+      if (model == Model::kJelly) {
         p.F = Fh;
         continue;
       }
       Mat<T, D> U, sig, V;
       nclr_svd<T, D>(Fh, U, sig, V, mode_);
       if (det(Fh) < T(0)) ++counters.inverted_svd;  // the 2D sign-fix ambiguity only bites here
-      if (model_ == Model::kSnow) {
+      if (model == Model::kSnow) {
         for (int d = 0; d < D; ++d)
           sig(d, d) = std::clamp(sig(d, d), T(1.0 - 2.5e-2), T(1.0 + 4.5e-3));
         const T old_J = det(Fh);

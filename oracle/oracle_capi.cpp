@@ -20,7 +20,7 @@ template <typename T, int D>
 int run(int physics, int64_t n, double *x, double *v, double *F, double *C, double *Jp,
         const double *mass, const double *volume, int model, int res, double dt, double E,
         double nu, double gravity, int nsteps, double *grid_vel, double *grid_mass,
-        int64_t *counters) {
+        int64_t *counters, const uint8_t *material) {
   std::vector<Particle<T, D>> ps((size_t)n);
   for (int64_t p = 0; p < n; ++p) {
     auto &q = ps[(size_t)p];
@@ -36,6 +36,7 @@ int run(int physics, int64_t n, double *x, double *v, double *F, double *C, doub
     q.Jp = (T)Jp[p];
     q.mass = (T)mass[p];
     q.volume = (T)volume[p];
+    q.material = material ? (int)material[p] : -1;
   }
   Simulation<T, D> sim(std::move(ps), (Model)model, res, (T)dt, (T)E, (T)nu, (T)gravity,
                        (Physics)physics);
@@ -194,14 +195,16 @@ int oracle_adjoint(int dim, int physics, int64_t n, const double *x0, const doub
 
 // Runs `nsteps` calls of advance() on the given state, in place.  Returns 0, or 2 when a
 // grid index went out of range (the reference's std::out_of_range), or 1 on bad arguments.
+// `material` (may be NULL): one MaterialModel per particle, the mixed-material extension.
 int oracle_advance(int dim, int fp64, int physics, int64_t n, double *x, double *v, double *F,
                    double *C, double *Jp, const double *mass, const double *volume, int model,
                    int res, double dt, double E, double nu, double gravity, int nsteps,
-                   double *grid_vel, double *grid_mass, int64_t *counters) {
+                   double *grid_vel, double *grid_mass, int64_t *counters,
+                   const uint8_t *material) {
   if (n < 0 || res < 1 || (dim != 2 && dim != 3) || model < 0 || model > 2) return 1;
 #define ORACLE_RUN(T, D)                                                                   \
   return run<T, D>(physics, n, x, v, F, C, Jp, mass, volume, model, res, dt, E, nu, gravity, \
-                   nsteps, grid_vel, grid_mass, counters)
+                   nsteps, grid_vel, grid_mass, counters, material)
   if (dim == 2) {
     if (fp64) ORACLE_RUN(double, 2);
     ORACLE_RUN(float, 2);

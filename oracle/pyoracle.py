@@ -36,7 +36,7 @@ def _load(name: str, sub: str) -> ctypes.CDLL:
                                            _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp,
-                                           _dp, _ip]
+                                           _dp, _ip, ctypes.c_void_p]
             lib.oracle_svd.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp]
             lib.oracle_polar.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]
             lib.oracle_linspaced.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float,
@@ -85,13 +85,14 @@ def _prep(state: dict, dim: int):
 def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-4,
             E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, steps: int = 1,
             fp64: bool = False, physics: int = REFERENCE, fast: bool = False,
-            want_grid: bool = True):
+            want_grid: bool = True, material=None):
     """Runs `steps` reference steps on a copy of `state`; returns (state, grid, status, counters).
 
     grid = (velocity (nodes, dim), mass (nodes,)) of the last step, post grid update.
     status 0 = ok, 2 = a grid index left the grid (the reference throws std::out_of_range).
     """
     n, s = _prep(state, dim)
+    mat = None if material is None else np.ascontiguousarray(material, dtype=np.uint8)
     nodes = (res + 1) ** dim
     gv = np.zeros((nodes, dim)) if want_grid else None
     gm = np.zeros((nodes,)) if want_grid else None
@@ -100,7 +101,7 @@ def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-
         dim, int(fp64), physics, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]), _p(s["Jp"]),
         _p(s["mass"]), _p(s["volume"]), model, res, dt, E, nu, gravity, steps,
         _p(gv) if want_grid else None, _p(gm) if want_grid else None,
-        counters.ctypes.data_as(_ip))
+        counters.ctypes.data_as(_ip), mat.ctypes.data if mat is not None else None)
     return s, ((gv, gm) if want_grid else None), st, counters
 
 

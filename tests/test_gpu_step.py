@@ -217,3 +217,21 @@ def test_lame_constants():
     assert abs(sim.mu_0 - 1e4 / 2.4) < 1e-2
     assert abs(sim.lambda_0 - 1e4 * 0.2 / (1.2 * 0.6)) < 1e-2
     sim.close()
+
+
+@pytest.mark.parametrize("physics,steps", [(scenes.CORRECTED, 1), (scenes.CORRECTED, 5),
+                                           (scenes.REFERENCE, 1)])
+def test_mixed_liquid_snow_matches_oracle(oracle, physics, steps):
+    """The mixed-material extension (one material per particle; the reference has one per
+    simulation): boxes of liquid and snow in one 3D domain, against the oracle given the same
+    per-particle materials."""
+    s, mat = scenes.liquid_snow_boxes_3d(seed=3, res=32, boxes=6, total=12_000, physics=physics,
+                                         margin=6 / 32)
+    out, grid = run_gpu(s, dict(model=scenes.SNOW, res=32, dt=1e-4, E=1e4, nu=0.2,
+                                gravity=-100.0), steps, physics=physics, material=mat)
+    o, og, st, _ = oracle.advance(s, dim=3, model=scenes.SNOW, res=32, steps=steps,
+                                  physics=physics, material=mat)
+    assert st == 0
+    tol = ONE_STEP if steps == 1 else DRIFT
+    for f in FIELDS:
+        assert field_err(out[f], o[f], f) <= tol[f], f
