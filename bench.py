@@ -162,7 +162,7 @@ def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float):
     return m * steps / dt, desc
 
 
-def run_batched(device: int, steps: int = 100) -> dict:
+def run_batched(device: int, steps: int = 100, sequential: bool = True) -> dict:
     """The batched form on 256 independent 2D scenes (particle counts log-uniform in
     [1,000, 65,536], grids of 64/128/256, mixed materials and moduli; seeded): one
     BatchSimulation advancing `steps` steps in one CUDA graph, against the same scenes stepped
@@ -187,7 +187,7 @@ def run_batched(device: int, steps: int = 100) -> dict:
     launches = batch.stats()[0]
     batch.close()
     t_seq = 0.0
-    for sc in scs:
+    for sc in (scs if sequential else []):
         sim = MPMSimulation({k: sc[k] for k in ("x", "v", "F", "C", "Jp", "mass", "volume")},
                             sc["model"], res=sc["res"], dt=sc["dt"], E=sc["E"], nu=sc["nu"],
                             gravity=sc["gravity"], device=device)
@@ -202,7 +202,8 @@ def run_batched(device: int, steps: int = 100) -> dict:
     return {"value": total * steps / t_batch, "unit": UNIT, "scenes": len(scs),
             "particles": total, "steps": steps, "ms_per_step": t_batch / steps * 1e3,
             "gpu_launches": launches, "tuned": tuned,
-            "sequential_value": total * steps / t_seq, "speedup_vs_sequential": t_seq / t_batch,
+            "sequential_value": total * steps / t_seq if sequential else None,
+            "speedup_vs_sequential": t_seq / t_batch if sequential else None,
             "config": "256 2D scenes, n log-uniform [1e3, 65536], res {64,128,256}, "
                       "materials uniform, E log-uniform [1e3,1e5], nu uniform [0.1,0.4], "
                       "dt 1e-4, one CUDA graph per 100 steps; sequential = the same scenes as "
@@ -275,6 +276,57 @@ def run_mixed(device: int, steps: int = 100) -> dict:
             "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
             "config": "3D liquid + snow, 256^3 grid, 16 boxes (sides U[0.05,0.2]), per-particle "
                       "material, dt 1e-4, reference physics"}
+
+
+def run_snow(device: int, steps: int = 100) -> dict:
+    """3D snow on the headline geometry: the four jittered 64^3 lattices of the 1M-particle
+    jelly scene (128^3 grid, same seed) with MaterialModel::kSnow, reference physics; `steps`
+    steps timed with CUDA events on the simulation's stream after warm-up, with the fused
+    kernel's per-launch device time and its fraction of the HBM roofline."""
+    import torch
+
+    from nuclearmpm_gb300 import MPMSimulation, scenes
+    sc = make_scene()
+    n = len(sc["x"])
+    sim = MPMSimulation(dict(sc), scenes.SNOW, res=128, profile=True, device=device)
+    sim.advance(10)
+    sim.profile_reset()
+    st = torch.cuda.ExternalStream(sim.stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    sim.advance(steps)
+    b.record(st)
+    b.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    prof = sim.profile()
+    active = sim.active_nodes()
+    launches = sim.stats()[0]
+    sim.close()
+    g_ms = prof["g2p2g"][0] / max(prof["g2p2g"][1], 1)
+    alg = algorithmic_bytes(3, n, active)["g2p2g"]
+    peak, kind = peaks()
+    return {"value": n * steps / t, "unit": UNIT, "particles": n, "steps": steps,
+            "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
+            "g2p2g_avg_ms": g_ms, "g2p2g_gbs": alg / (g_ms / 1e3) / 1e9,
+            "g2p2g_frac": alg / (g_ms / 1e3) / 1e9 / peak, "peak_source": kind,
+            "config": "3D snow (MaterialModel::kSnow), the 1M-particle scene above, 128^3 grid, "
+                      "dt 1e-4, reference physics"}
+
+
+FORMS = {"batched": run_batched, "adjoint": run_adjoint, "mixed": run_mixed, "snow": run_snow}
+
+
+def run_form(args):
+    """One form alone (for profiling): its JSON object on one line, `--form-steps` steps."""
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    kw = {} if args.form_steps is None else {"steps": args.form_steps}
+    if args.only == "batched" and args.no_sequential:
+        kw["sequential"] = False
+    out = FORMS[args.only](local, **kw)
+    print(json.dumps({"form": args.only, **out}), flush=True)
+    return 0
 
 
 def run_reference(args):
@@ -402,6 +454,9 @@ def run_ours(args):
     mixed = None
     if not args.no_mixed:
         mixed = run_mixed(local)
+    snow = None
+    if not args.no_snow:
+        snow = run_snow(local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -417,7 +472,7 @@ def run_ours(args):
                 "data": "synthetic (seeded scene with the workload's shapes and distributions)",
                 "config": dict(WORKLOAD, parallelism=f"replicas x{world}"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
-                "adjoint": adjoint, "mixed": mixed,
+                "adjoint": adjoint, "mixed": mixed, "snow": snow,
                 "gpu_launches": launches_total, "clocks": clk}
         print(json.dumps(line), flush=True)
     sim.close()
@@ -437,11 +492,19 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-snow", action="store_true")
+    ap.add_argument("--only", choices=sorted(FORMS), default=None,
+                    help="run one of the other forms alone and print its object")
+    ap.add_argument("--form-steps", type=int, default=None)
+    ap.add_argument("--no-sequential", action="store_true",
+                    help="with --only batched: skip stepping the scenes one by one")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.only is not None:
+        return run_form(args)
     return run_ours(args)
 
 

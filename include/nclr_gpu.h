@@ -66,6 +66,11 @@ typedef struct nclr_options {
                               handle's stream (direct launches, no graphs; default 0) */
   int graph_steps;         /* steps per captured CUDA graph, rounded up to a multiple of
                               sort_interval (0 = one sort interval; default 0) */
+  int sparse_block_max;    /* grid blocks holding fewer particles than this (at the last sort)
+                              are stepped particle by particle, gathering from and scattering
+                              into the grid directly instead of through a shared-memory tile;
+                              0 = never, -1 = the default for the dimension (default -1);
+                              single simulations only, batches ignore it */
 } nclr_options;
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid

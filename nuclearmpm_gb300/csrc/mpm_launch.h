@@ -21,8 +21,8 @@ template <int D> void launch_discard_pending(float4 *G, uint8_t *flags, const Sc
 // follows the launch (next_slot 0: same call, 1: the next call).
 template <int D> void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes, const uint16_t *block_scene,
                                    const float4 *V, float4 *G, uint8_t *flags, const int *blocks,
-                                   const int *nactive, const int *bstart, int *work, int *err, int next_slot,
-                                   bool ref, int mode, int ctas, cudaStream_t st);
+                                   const int *nactive, const int *bstart, const int *sparse, int *work,
+                                   int *err, int next_slot, bool ref, int mode, int ctas, cudaStream_t st);
 template <int D> int g2p2g_ctas_per_sm();
 enum : int { kModeStep = 0, kModeFinalStep = 1, kModeP2GOnly = 2 };  // g2p2g modes
 template <int D> void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st);
@@ -35,7 +35,11 @@ template <int D> void launch_import_particles(const PState &s, int begin, int n,
 template <int D> void launch_block_keys(const PState &s, int n, const Scene *scenes, int *key, int *rank, int *count,
                                         cudaStream_t st);
 template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank, const int *start, const int *count, bool move_vc, cudaStream_t st);
-void launch_compact_blocks(const int *start, int nblocks, int cpb, int *list, int *nlist, cudaStream_t st);
+// The non-empty blocks of the sort: those with at least sparse_max particles (all of them when
+// sparse_max <= 0) into list / nlist[0]; the particle slots of the others, block by block,
+// into sparse / nlist[1].  nlist[0..1] must be zero on entry.
+void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int *list,
+                           int *nlist, int *sparse, cudaStream_t st);
 
 // Reverse of one jelly step (adjoint.cu): adjoint of s_{t+1} (gx, gv, gF, gC; NULL = 0) ->
 // adjoint of s_t (ox, ov, oF, oC), mu_0 / lambda_0 adjoints added to gml[0..1].  States are

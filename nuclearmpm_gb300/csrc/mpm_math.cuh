@@ -227,6 +227,7 @@ MPM_HD void qr_givens(float B[3][3], float U[3][3]) {
 }  // namespace detail
 
 constexpr int kJacobiSweeps = 4;
+constexpr float kJacobiDone = 2.3e-13f;  // (4.8e-7)^2
 
 template <bool kExact = true>
 MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
@@ -241,6 +242,14 @@ MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
     }
 #pragma unroll 1
   for (int sweep = 0; sweep < kJacobiSweeps; ++sweep) {
+    // Done once every off-diagonal S_pq is below 4.8e-7 sqrt(S_pp S_qq) (the 2 epsilon
+    // relative threshold of a two-sided Jacobi SVD such as Eigen's JacobiSVD, on A^T A);
+    // tested before the first sweep as well, so an input that is diagonal to within rounding
+    // is not rotated at all and keeps its diagonal exactly.
+    if (S[0][1] * S[0][1] <= kJacobiDone * fabsf(S[0][0] * S[1][1]) &&
+        S[0][2] * S[0][2] <= kJacobiDone * fabsf(S[0][0] * S[2][2]) &&
+        S[1][2] * S[1][2] <= kJacobiDone * fabsf(S[1][1] * S[2][2]))
+      break;
     jacobi_rotate<0, 1, kExact>(S, V);
     jacobi_rotate<1, 2, kExact>(S, V);
     jacobi_rotate<0, 2, kExact>(S, V);

@@ -328,8 +328,8 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
     PState s, Params P0, const Scene *__restrict__ scenes, const uint16_t *__restrict__ block_scene,
     const float4 *__restrict__ Vall, float4 *__restrict__ Gall, uint8_t *__restrict__ flags_all,
     const int *__restrict__ blocks, const int *__restrict__ nactive,
-    const int *__restrict__ bstart, int *__restrict__ work, int *__restrict__ err,
-    int next_slot) {
+    const int *__restrict__ bstart, const int *__restrict__ sparse, int *__restrict__ work,
+    int *__restrict__ err, int next_slot) {
   using Tl = Tiling<D>;
   constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, CPB = Tl::CPB, GS = Tl::SIZE;
   constexpr int S = (D == 3) ? 27 : 9;
@@ -342,7 +342,11 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
   __shared__ int64_t s_node_off;
   __shared__ int s_block_off;
   const int st = s.stride;
-  const int nact = *nactive;
+  // work items: the dense blocks of the list, then chunks of kG2P2GThreads particles of the
+  // sparse blocks (single simulations only; see compact_blocks_kernel)
+  const int nact = nactive[0];
+  const int nsp = kBatch ? 0 : nactive[1];
+  const int nitems = nact + (nsp + kG2P2GThreads - 1) / kG2P2GThreads;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float4 *mytile = gt + warp * GS;
 
@@ -360,8 +364,11 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
     }
     __syncthreads();
     const int item = s_item;
-    if (item >= nact) return;
-    const int gb = blocks[item];  // global block (scene-major)
+    if (item >= nitems) return;
+    // a sparse chunk: particles of blocks too thin for the tile to pay, one per thread,
+    // gathered from V and scattered into G directly (CTA-uniform)
+    const bool chunk = !kBatch && item >= nact;
+    const int gb = chunk ? 0 : blocks[item];  // global block (scene-major)
     const int sid = kBatch ? (int)block_scene[gb] : 0;
     const Params &P = kBatch ? sP : P0;
     const int64_t node_off = kBatch ? s_node_off : 0;
@@ -381,7 +388,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
     uint8_t *__restrict__ flags = flags_all + block_off;
     const int b = gb - block_off;
     int *err_now = err + 2 * sid, *err_next = err + 2 * sid + next_slot;
-    if (kMode != kP2GOnly) {
+    if (kMode != kP2GOnly && !chunk) {
       for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
         int g[D], l[3] = {0, 0, 0};
         bool in = true;
@@ -397,19 +404,21 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
             in ? __ldg(V + flat_index<D>(g, N)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
     }
-    for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
-      gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (!chunk)
+      for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
+        gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     __syncthreads();
 
     // The block's particles, stored cell by cell in rounds (see sort_move_kernel), one per
     // thread in slot order.  Every lane of a warp runs the same number of iterations (the
     // warp-wide steps below need them all).
-    const int p0 = bstart[gb * CPB];
-    const int np = bstart[(gb + 1) * CPB] - p0;
+    const int c0 = (item - nact) * kG2P2GThreads;
+    const int p0 = chunk ? 0 : bstart[gb * CPB];
+    const int np = chunk ? min(kG2P2GThreads, nsp - c0) : bstart[(gb + 1) * CPB] - p0;
     for (int j0 = 0; j0 < np; j0 += kG2P2GThreads) {
       const int j = j0 + threadIdx.x;
       const bool valid = j < np;
-      const int p = p0 + j;
+      const int p = chunk ? (valid ? sparse[c0 + j] : 0) : p0 + j;
       // what the particle contributes to the next P2G
       bool fast_s = false;
       int tb_s = 0;
@@ -434,7 +443,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
         // ---- G2P of this step ----
         float fx[D], w[3][D];
         stencil<D>(x, P.inv_dx, base, fx, w);
-        bool fast = true;
+        bool fast = !chunk;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           lb[d] = base[d] - org[d];
@@ -487,7 +496,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
 #pragma unroll
         for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
         stencil<D>(x, P.inv_dx, base, fx_s, w_s);
-        fast_s = true;
+        fast_s = !chunk;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           lb[d] = base[d] - org[d];
@@ -515,6 +524,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
       // same stencil base go in separate rounds (rare: consecutive slots are in different
       // cells), so within a round every lane writes a different node for each
       // stencil offset; __syncwarp orders the offsets.
+      if (chunk) continue;  // nothing for the tile
       const bool tile_lane = valid && fast_s;
       const int key = tile_lane ? tb_s : -1 - lane;
       const unsigned same = __match_any_sync(0xffffffffu, key);
@@ -539,6 +549,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
         }
       }
     }
+    if (chunk) continue;  // its P2G went straight to G (and the flags)
     __syncthreads();
 
     for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
@@ -767,11 +778,13 @@ void launch_discard_pending(float4 *G, uint8_t *flags, const Scene *scenes,
 template <int D>
 void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                   const uint16_t *block_scene, const float4 *V, float4 *G, uint8_t *flags,
-                  const int *blocks, const int *nactive, const int *bstart, int *work, int *err,
-                  int next_slot, bool ref, int mode, int ctas, cudaStream_t st) {
+                  const int *blocks, const int *nactive, const int *bstart, const int *sparse,
+                  int *work, int *err, int next_slot, bool ref, int mode, int ctas,
+                  cudaStream_t st) {
 #define MPM_G2P2G(R, MODE, B)                                                            \
   g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(         \
-      s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart, work, err, next_slot)
+      s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart, sparse, work, err,  \
+      next_slot)
 #define MPM_G2P2G_B(R, MODE)          \
   if (block_scene) {                  \
     MPM_G2P2G(R, MODE, true);         \
@@ -864,7 +877,8 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
                                           int, int, cudaStream_t);                               \
   template void launch_g2p2g<D>(const PState &, const Params &, const Scene *, const uint16_t *, \
                                 const float4 *, float4 *, uint8_t *, const int *, const int *,   \
-                                const int *, int *, int *, int, bool, int, int, cudaStream_t);   \
+                                const int *, const int *, int *, int *, int, bool, int, int,     \
+                                cudaStream_t);                                                   \
   template int g2p2g_ctas_per_sm<D>();                                                           \
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \

@@ -50,8 +50,10 @@ struct nclr_sim {
   float4 *V = nullptr;        // updated grid of the last step (grid())
   uint8_t *flags = nullptr;   // per grid block: pending contributions in G / non-zero V
   int *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *tile_sums = nullptr;
-  int *blocks = nullptr;      // non-empty blocks of the last sort
-  int *nblocks_active = nullptr;
+  int *blocks = nullptr;      // non-empty blocks of the last sort (the dense ones)
+  int *nblocks_active = nullptr;  // [0] dense blocks in `blocks`, [1] slots in `sparse`
+  int *sparse = nullptr;      // particle slots of the thin blocks (stepped without a tile)
+  int sparse_max = 0;         // blocks with fewer particles than this are thin
   int *work = nullptr;        // fused kernel's block counter
   int *err_d = nullptr;       // per scene: [2s] this call's steps, [2s+1] the P2G after them
   int *err_h = nullptr;       // pinned copy
@@ -88,6 +90,12 @@ struct nclr_sim {
 namespace {
 
 thread_local std::string g_create_error;
+
+// Default thin-block thresholds (particles per block at the last sort): below them the
+// shared-memory tile of a block (load, clear, flush of 8^3 nodes in 3D, 12^2 in 2D) costs more
+// than the block's particles gathering and scattering through L2 directly.
+constexpr int kSparseMax3 = 64;
+constexpr int kSparseMax2 = 32;
 
 int row_floats(int dim) { return 2 * dim + 2 * dim * dim + 1; }  // x, v, F, C, Jp
 
@@ -202,11 +210,12 @@ void enqueue_sort(nclr_sim *s, bool move_vc) {
     constexpr int cpb = mpm::Tiling<D>::CPB;
     phase(s, NCLR_PHASE_SORT, 6, [&] {
       cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)s->nkeys, s->stream);
-      cudaMemsetAsync(s->nblocks_active, 0, sizeof(int), s->stream);
+      cudaMemsetAsync(s->nblocks_active, 0, 2 * sizeof(int), s->stream);
       mpm::launch_block_keys<D>(s->ps[s->cur], (int)s->n, s->scenes_d, s->key, s->rank, s->count,
                                 s->stream);
       mpm::launch_exclusive_scan(s->count, s->nkeys, s->start, s->tile_sums, s->stream);
-      mpm::launch_compact_blocks(s->start, nb, cpb, s->blocks, s->nblocks_active, s->stream);
+      mpm::launch_compact_blocks(s->start, nb, cpb, s->sparse_max, s->blocks, s->nblocks_active,
+                                 s->sparse, s->stream);
       mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->key, s->rank,
                                s->start, s->count, move_vc, s->stream);
     });
@@ -230,7 +239,7 @@ void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
     if (s->n > 0) {
       phase(s, NCLR_PHASE_G2P2G, 1, [&] {
         mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
-                             s->flags, s->blocks, s->nblocks_active, s->start, s->work, s->err_d,
+                             s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d,
                              final_step ? 1 : 0, s->ref,
                              final_step ? mpm::kModeFinalStep : mpm::kModeStep, s->g2p2g_ctas,
                              s->stream);
@@ -369,6 +378,7 @@ void release(nclr_sim *s) {
   cudaFree(s->flags);
   cudaFree(s->blocks);
   cudaFree(s->nblocks_active);
+  cudaFree(s->sparse);
   cudaFree(s->work);
   cudaFree(s->key);
   cudaFree(s->rank);
@@ -429,6 +439,10 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   s->device = s->opt.device;
   s->ref = s->opt.physics != NCLR_PHYSICS_CORRECTED;
   s->has_mat = any_mat;
+  // thin blocks are a single-simulation path (a batch's fused kernel reads its scene per block)
+  s->sparse_max = nscenes > 1 ? 0
+                  : s->opt.sparse_block_max < 0 ? (dim == 3 ? kSparseMax3 : kSparseMax2)
+                                                : s->opt.sparse_block_max;
   s->deferred_err.assign((size_t)nscenes, 0);
   s->scene_err.assign((size_t)nscenes, 0);
 
@@ -508,7 +522,8 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (size_t)(s->nkeys + 1)));
   CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles(s->nkeys), 1)));
   CREATE_TRY(cudaMalloc((void **)&s->blocks, sizeof(int) * nblk));
-  CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, sizeof(int)));
+  CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, 2 * sizeof(int)));
+  CREATE_TRY(cudaMalloc((void **)&s->sparse, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->work, sizeof(int)));
   CREATE_TRY(cudaMalloc((void **)&s->err_d, 2 * sizeof(int) * (size_t)nscenes));
   CREATE_TRY(cudaMallocHost((void **)&s->err_h, 2 * sizeof(int) * (size_t)nscenes));
@@ -516,7 +531,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMemsetAsync(s->G, 0, sizeof(float4) * nodes, s->stream));
   CREATE_TRY(cudaMemsetAsync(s->V, 0, sizeof(float4) * nodes, s->stream));
   CREATE_TRY(cudaMemsetAsync(s->flags, 0, nblk, s->stream));
-  CREATE_TRY(cudaMemsetAsync(s->nblocks_active, 0, sizeof(int), s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->nblocks_active, 0, 2 * sizeof(int), s->stream));
 
   if (total_n > 0) {
     // Per-particle scalars go straight into the SoA (component stride == n there).
@@ -655,6 +670,7 @@ void nclr_default_options(nclr_options *opt) {
   opt->use_graphs = 1;
   opt->profile = 0;
   opt->graph_steps = 0;
+  opt->sparse_block_max = -1;
 }
 
 nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
@@ -709,7 +725,7 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
         cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
         if (s->n > 0)
           mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
-                               s->flags, s->blocks, s->nblocks_active, s->start, s->work, s->err_d, 0,
+                               s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d, 0,
                                s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
       });
     });
@@ -1010,7 +1026,7 @@ nclr_status record_segment(nclr_rollout *r, int L) {
                                      s->total_blocks, s->sms, s->stream);
       cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
       mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
-                           s->flags, s->blocks, s->nblocks_active, s->start, s->work, s->err_d, 0,
+                           s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d, 0,
                            s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
     });
     s->acc_valid = true;

@@ -103,28 +103,47 @@ __global__ void __launch_bounds__(kThreads) count_active_kernel(const float4 *__
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
 }
 
-// The list of non-empty blocks (start[b*cpb] < start[(b+1)*cpb]); one atomic per warp for
-// the append position.
+// The non-empty blocks (start[b*cpb] < start[(b+1)*cpb]): those with at least sparse_max
+// particles go to the block list, the particle slots of the thinner ones to the sparse list
+// (stepped particle by particle).  One atomic per warp and list for the append position, so
+// the sparse slots stay in block order within each warp's run of 32 blocks.
 __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks, int cpb,
-                                      int *__restrict__ list, int *__restrict__ nlist) {
+                                      int sparse_max, int *__restrict__ list,
+                                      int *__restrict__ nlist, int *__restrict__ sparse) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool act = b < nblocks && start[(int64_t)(b + 1) * cpb] > start[(int64_t)b * cpb];
-  const unsigned mask = __ballot_sync(0xffffffffu, act);
-  if (!mask) return;
+  int s0 = 0, np = 0;
+  if (b < nblocks) {
+    s0 = start[(int64_t)b * cpb];
+    np = start[(int64_t)(b + 1) * cpb] - s0;
+  }
+  const bool thin = np > 0 && np < sparse_max;
+  const bool act = np > 0 && !thin;
   const int lane = threadIdx.x & 31;
-  int base = 0;
-  if (lane == 0) base = atomicAdd(nlist, __popc(mask));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (act) list[base + __popc(mask & ((1u << lane) - 1u))] = b;
+  const unsigned mask = __ballot_sync(0xffffffffu, act);
+  if (mask) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(nlist, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (act) list[base + __popc(mask & ((1u << lane) - 1u))] = b;
+  }
+  const int cnt = thin ? np : 0;
+  const int inc = warp_inclusive(cnt);
+  const int tot = __shfl_sync(0xffffffffu, inc, 31);
+  if (tot) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(nlist + 1, tot);
+    base = __shfl_sync(0xffffffffu, base, 0) + inc - cnt;
+    for (int i = 0; i < cnt; ++i) sparse[base + i] = s0 + i;
+  }
 }
 
 }  // namespace
 
-void launch_compact_blocks(const int *start, int nblocks, int cpb, int *list, int *nlist,
-                           cudaStream_t st) {
+void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int *list,
+                           int *nlist, int *sparse, cudaStream_t st) {
   if (nblocks <= 0) return;
   compact_blocks_kernel<<<(unsigned)((nblocks + kThreads - 1) / kThreads), kThreads, 0, st>>>(
-      start, nblocks, cpb, list, nlist);
+      start, nblocks, cpb, sparse_max, list, nlist, sparse);
 }
 
 void launch_count_active(const float4 *grid, int64_t nodes, unsigned long long *out, cudaStream_t st) {

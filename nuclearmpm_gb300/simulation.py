@@ -138,7 +138,8 @@ class MPMSimulation:
                  E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, *, dim: int | None = None,
                  material: np.ndarray | None = None, physics: int = capi.PHYSICS_REFERENCE,
                  sort_interval: int = 8, particles_per_thread: int = 8, device: int = 0,
-                 use_graphs: bool = True, profile: bool = False, graph_steps: int = 0):
+                 use_graphs: bool = True, profile: bool = False, graph_steps: int = 0,
+                 sparse_block_max: int = -1):
         L = capi.lib()
         self.dim, soa = _soa_from(particles, dim)
         self._c = soa.pop("c")
@@ -151,7 +152,7 @@ class MPMSimulation:
         opt = capi.default_options(physics=physics, sort_interval=sort_interval,
                                    p2g_particles_per_thread=particles_per_thread, device=device,
                                    use_graphs=int(use_graphs), profile=int(profile),
-                                   graph_steps=graph_steps)
+                                   graph_steps=graph_steps, sparse_block_max=sparse_block_max)
         h = ctypes.c_void_p()
         st = L.nclr_create(ctypes.byref(h), self.dim, self.n, _ptr(soa["x"]), _ptr(soa["v"]),
                            _ptr(soa["F"]), _ptr(soa["C"]), _ptr(soa["Jp"]), _ptr(soa["mass"]),

@@ -81,9 +81,12 @@ def _random_state(rng, dim, n, res, physics):
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("model", [scenes.SNOW, scenes.JELLY, scenes.LIQUID])
 @pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
-def test_one_step_vs_oracle_random(oracle, dim, model, physics):
+@pytest.mark.parametrize("thin", [0, 8, 1 << 30])
+def test_one_step_vs_oracle_random(oracle, dim, model, physics, thin):
     """Seeded random states (non-trivial F, C, Jp, mass, volume): one GPU step vs the FP32
-    oracle within the one-step bounds, and the FP64 oracle's error reported alongside."""
+    oracle within the one-step bounds, and the FP64 oracle's error reported alongside.  `thin`
+    is the sparse-block threshold: every block through the shared-memory tile (0), about half
+    of them stepped particle by particle (8), all of them particle by particle."""
     if dim == 3 and model == scenes.LIQUID and physics == scenes.REFERENCE:
         pytest.skip("3D liquid under the reference physics has F = diag(J,1,0): its polar "
                     "rotation is not unique, so parity there is implementation-defined")
@@ -91,7 +94,7 @@ def test_one_step_vs_oracle_random(oracle, dim, model, physics):
     res = 32
     s = _random_state(rng, dim, 2000 if dim == 2 else 4000, res, physics)
     out, grid = run_gpu(s, dict(model=model, res=res, dt=1e-4, E=1e4, nu=0.2, gravity=-100.0), 1,
-                        physics=physics)
+                        physics=physics, sparse_block_max=thin)
     o32, og, st, _ = oracle.advance(s, dim=dim, model=model, res=res, steps=1, physics=physics)
     o64, og64, _, _ = oracle.advance(s, dim=dim, model=model, res=res, steps=1, physics=physics,
                                      fp64=True)
@@ -107,14 +110,16 @@ def test_one_step_vs_oracle_random(oracle, dim, model, physics):
 
 
 def test_sort_graph_and_threading_options_agree():
-    """Cell sort on/off, graphs on/off and particles-per-thread change only the summation
-    order: the results agree to FP32 rounding."""
+    """Cell sort on/off, graphs on/off, particles-per-thread and the sparse-block threshold
+    change only the summation order: the results agree to FP32 rounding."""
     z, state, params, _ = load_golden("block3d_jelly")
     runs = []
     for kw in (dict(sort_interval=0, use_graphs=False, particles_per_thread=4),
                dict(sort_interval=1, use_graphs=True, particles_per_thread=8),
                dict(sort_interval=3, use_graphs=True, particles_per_thread=16),
-               dict(sort_interval=8, use_graphs=False, particles_per_thread=8)):
+               dict(sort_interval=8, use_graphs=False, particles_per_thread=8),
+               dict(sort_interval=2, sparse_block_max=0),
+               dict(sort_interval=2, sparse_block_max=1 << 30)):
         runs.append(run_gpu(state, params, 20, **kw)[0])
     for r in runs[1:]:
         for f in FIELDS:
