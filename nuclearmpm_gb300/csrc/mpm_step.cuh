@@ -324,7 +324,9 @@ enum : int { kStep = kModeStep, kFinalStep = kModeFinalStep, kP2GOnly = kModeP2G
 // kBatch: several scenes (per-block parameters from the scene table, staged in shared memory)
 // or one (its parameters are a kernel argument: constant-bank operands, no registers).
 template <int D, bool kRef, int kMode, bool kBatch>
-__global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
+// 3D: two CTAs per SM (the tiles take 106 KB of shared memory each); 2D: four, which keeps
+// the 2D kernel within 64 registers without spills.
+__global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
     PState s, Params P0, const Scene *__restrict__ scenes, const uint16_t *__restrict__ block_scene,
     const float4 *__restrict__ Vall, float4 *__restrict__ Gall, uint8_t *__restrict__ flags_all,
     const int *__restrict__ blocks, const int *__restrict__ nactive,
@@ -461,7 +463,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
           for (int o = 0; o < S; ++o) g2p_accumulate<D>(o, vt[tb + tile_offset<D>(o)], fx, w, v, C);
         } else {
           const int64_t f0 = flat_index<D>(base, N);
-#pragma unroll 1
+#pragma unroll  // constant offsets keep w[][] in registers (and the gathers independent)
           for (int o = 0; o < S; ++o) {
             const int64_t f = stencil_flat<D>(f0, o, N);
             float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -505,7 +507,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, 2) g2p2g_kernel(
         tb_s = tile_index<D>(lb[0], lb[1], lb[2]);
         if (!fast_s) {  // outside the tile: straight to G
           const int64_t f0 = flat_index<D>(base, N);
-#pragma unroll 1
+#pragma unroll
           for (int o = 0; o < S; ++o) {
             const int64_t f = stencil_flat<D>(f0, o, N);
             if (f < 0 || f >= P.nodes) {
