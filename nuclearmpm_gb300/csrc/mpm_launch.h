@@ -11,6 +11,13 @@ struct Params;
 struct PState;
 struct Scene;
 
+// Caller-order copies of the state after a final-mode step (rows of x, v: dim floats; F, C:
+// dim*dim floats), written by the fused kernel for the adjoint's recorded segments; all null
+// when not recording (single simulations only).
+struct Record {
+  float *x, *v, *F, *C;
+};
+
 template <int D> void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
                                         const uint16_t *block_scene, int total_blocks, int *work, int sms,
                                         cudaStream_t st);
@@ -22,7 +29,8 @@ template <int D> void launch_discard_pending(float4 *G, uint8_t *flags, const Sc
 template <int D> void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes, const uint16_t *block_scene,
                                    const float4 *V, float4 *G, uint8_t *flags, const int *blocks,
                                    const int *nactive, const int *bstart, const int *sparse, int *work,
-                                   int *err, int next_slot, bool ref, int mode, int ctas, cudaStream_t st);
+                                   int *err, int next_slot, bool ref, int mode, int ctas, cudaStream_t st,
+                                   const Record &rec = Record{});
 template <int D> int g2p2g_ctas_per_sm();
 enum : int { kModeStep = 0, kModeFinalStep = 1, kModeP2GOnly = 2 };  // g2p2g modes
 template <int D> void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st);

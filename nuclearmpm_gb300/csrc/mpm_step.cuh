@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
     const float4 *__restrict__ Vall, float4 *__restrict__ Gall, uint8_t *__restrict__ flags_all,
     const int *__restrict__ blocks, const int *__restrict__ nactive,
     const int *__restrict__ bstart, const int *__restrict__ sparse, int *__restrict__ work,
-    int *__restrict__ err, int next_slot) {
+    int *__restrict__ err, int next_slot, Record rec) {
   using Tl = Tiling<D>;
   constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, CPB = Tl::CPB, GS = Tl::SIZE;
   constexpr int S = (D == 3) ? 27 : 9;
@@ -488,6 +488,21 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
 #pragma unroll
           for (int d = 0; d < D; ++d) s.v[(size_t)d * st + p] = v[d];
           store_mat<D>(s.C, st, p, C);
+          if (!kBatch && rec.x) {  // the recorded state, in the caller's order
+            const size_t q = (size_t)s.id[p];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              rec.x[q * D + d] = x[d];
+              rec.v[q * D + d] = v[d];
+            }
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+#pragma unroll
+              for (int jj = 0; jj < D; ++jj) {
+                rec.F[(q * D + i) * D + jj] = F.a[i][jj];
+                rec.C[(q * D + i) * D + jj] = C.a[i][jj];
+              }
+          }
         }
         }
 
@@ -782,11 +797,11 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                   const uint16_t *block_scene, const float4 *V, float4 *G, uint8_t *flags,
                   const int *blocks, const int *nactive, const int *bstart, const int *sparse,
                   int *work, int *err, int next_slot, bool ref, int mode, int ctas,
-                  cudaStream_t st) {
+                  cudaStream_t st, const Record &rec) {
 #define MPM_G2P2G(R, MODE, B)                                                            \
   g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(         \
       s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart, sparse, work, err,  \
-      next_slot)
+      next_slot, rec)
 #define MPM_G2P2G_B(R, MODE)          \
   if (block_scene) {                  \
     MPM_G2P2G(R, MODE, true);         \
@@ -880,7 +895,7 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
   template void launch_g2p2g<D>(const PState &, const Params &, const Scene *, const uint16_t *, \
                                 const float4 *, float4 *, uint8_t *, const int *, const int *,   \
                                 const int *, const int *, int *, int *, int, bool, int, int,     \
-                                cudaStream_t);                                                   \
+                                cudaStream_t, const Record &);                                   \
   template int g2p2g_ctas_per_sm<D>();                                                           \
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \

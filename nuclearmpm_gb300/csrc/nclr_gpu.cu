@@ -54,6 +54,7 @@ struct nclr_sim {
   int *nblocks_active = nullptr;  // [0] dense blocks in `blocks`, [1] slots in `sparse`
   int *sparse = nullptr;      // particle slots of the thin blocks (stepped without a tile)
   int sparse_max = 0;         // blocks with fewer particles than this are thin
+  mpm::Record record{};       // where final-mode steps also write the caller-order state
   int *work = nullptr;        // fused kernel's block counter
   int *err_d = nullptr;       // per scene: [2s] this call's steps, [2s+1] the P2G after them
   int *err_h = nullptr;       // pinned copy
@@ -242,7 +243,7 @@ void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
                              s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d,
                              final_step ? 1 : 0, s->ref,
                              final_step ? mpm::kModeFinalStep : mpm::kModeStep, s->g2p2g_ctas,
-                             s->stream);
+                             s->stream, s->record);
       });
       s->launches += 1;
     }
@@ -908,7 +909,10 @@ void nclr_destroy(nclr_sim *s) { release(s); }
 // ---------------------------------------------------------------------------------------
 // Differentiable rollouts: nsteps jelly steps from a given state, keeping a checkpoint every
 // `every` steps; the reverse pass recomputes each segment's states and grids forward (the
-// regular step kernels) and runs the adjoint kernels (adjoint.cu) backwards through it.
+// regular step kernels) and runs the adjoint kernels (adjoint.cu) backwards through it.  The
+// segment records are double-buffered: the recomputation of segment k-1 (the simulation's
+// stream) runs while the adjoint of segment k (the rollout's reverse stream) consumes the
+// other buffer; events order each buffer's writer and reader.
 // ---------------------------------------------------------------------------------------
 struct nclr_rollout {
   nclr_sim *sim = nullptr;
@@ -918,8 +922,10 @@ struct nclr_rollout {
   float E = 0.0f, nu = 0.0f;
   size_t rowf = 0;            // floats of one state: x, v, F, C rows
   float *ckpt = nullptr;      // nseg states
-  float *seg = nullptr;       // every + 1 states of the segment being reversed
-  float4 *grids = nullptr;    // `every` updated grids of that segment
+  float *seg[2] = {nullptr, nullptr};     // every + 1 states of a recorded segment
+  float4 *grids[2] = {nullptr, nullptr};  // `every` updated grids of that segment
+  cudaStream_t rev = nullptr;             // the adjoint steps
+  cudaEvent_t recorded[2] = {nullptr, nullptr}, reversed[2] = {nullptr, nullptr};
   float *adj[2] = {nullptr, nullptr};
   float *VB = nullptr;
   float4 *GB = nullptr;
@@ -964,9 +970,15 @@ void rollout_release(nclr_rollout *r) {
     cudaSetDevice(r->sim->device);
     cudaStreamSynchronize(r->sim->stream);
   }
+  if (r->rev) cudaStreamSynchronize(r->rev);
   cudaFree(r->ckpt);
-  cudaFree(r->seg);
-  cudaFree(r->grids);
+  for (int b = 0; b < 2; ++b) {
+    cudaFree(r->seg[b]);
+    cudaFree(r->grids[b]);
+    if (r->recorded[b]) cudaEventDestroy(r->recorded[b]);
+    if (r->reversed[b]) cudaEventDestroy(r->reversed[b]);
+  }
+  if (r->rev) cudaStreamDestroy(r->rev);
   cudaFree(r->adj[0]);
   cudaFree(r->adj[1]);
   cudaFree(r->VB);
@@ -1008,12 +1020,13 @@ nclr_status save_state(nclr_rollout *r, float *st) {
   return NCLR_OK;
 }
 
-// Steps the simulation L times from the loaded state, recording after step i the state
-// (into r->seg state i + 1, caller order) and the step's updated grid (r->grids[i]); one
-// synchronisation at the end.  Every step writes v and C (they are part of the record).
-nclr_status record_segment(nclr_rollout *r, int L) {
+// Enqueues L steps of the simulation from the loaded state, recording after step i the state
+// (into r->seg[buf] state i + 1, caller order, written by the fused kernel) and the step's
+// updated grid (r->grids[buf][i]).  Every step writes v and C (they are part of the record).
+// No synchronisation: stencil errors accumulate in the simulation's flags, which the caller
+// cleared and reads once at the end.
+nclr_status record_segment(nclr_rollout *r, int L, int buf) {
   nclr_sim *s = r->sim;
-  R_TRY(r, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)s->nscenes, s->stream));
   if (s->need_sort) {
     enqueue_sort(s, !s->acc_valid);
     s->need_sort = false;
@@ -1033,22 +1046,19 @@ nclr_status record_segment(nclr_rollout *r, int L) {
   }
   for (int i = 0; i < L; ++i) {
     const bool sort = sort_due(s);
+    float *st = r->state(r->seg[buf], i + 1);
+    s->record = mpm::Record{r->x(st), r->v(st), r->F(st), r->C(st)};  // written by the step
     enqueue_step(s, sort, true);
+    s->record = mpm::Record{};
     if (sort) s->steps_since_sort = 0;
     ++s->steps_since_sort;
-    R_TRY(r, cudaMemcpyAsync(r->grids + (size_t)i * r->nodes, s->V, sizeof(float4) * (size_t)r->nodes,
-                             cudaMemcpyDeviceToDevice, s->stream));
-    float *st = r->state(r->seg, i + 1);
-    nclr_status e = export_rows(s, -1, r->x(st), r->v(st), r->F(st), r->C(st), nullptr);
-    if (e != NCLR_OK) return rfail(r, e, s->error);
+    R_TRY(r, cudaMemcpyAsync(r->grids[buf] + (size_t)i * r->nodes, s->V,
+                             sizeof(float4) * (size_t)r->nodes, cudaMemcpyDeviceToDevice,
+                             s->stream));
   }
   s->stepped = true;
-  R_TRY(r, cudaMemcpyAsync(s->err_h, s->err_d, 2 * sizeof(int) * (size_t)s->nscenes,
-                           cudaMemcpyDeviceToHost, s->stream));
-  R_TRY(r, cudaStreamSynchronize(s->stream));
-  if ((s->err_h[0] | s->err_h[1]) & mpm::kErrOutOfRange)
-    return rfail(r, NCLR_ERR_OUT_OF_RANGE, "a stencil left the grid during the recomputation");
-  return NCLR_OK;
+  const nclr_status st = check_launch(s, "segment recomputation");
+  return st == NCLR_OK ? st : rfail(r, st, s->error);
 }
 
 }  // namespace
@@ -1092,8 +1102,13 @@ nclr_status nclr_rollout_create(nclr_rollout **out, int dim, int64_t n, const fl
   } while (0)
   RC(cudaSetDevice(s->device));
   RC(cudaMalloc((void **)&r->ckpt, sizeof(float) * r->rowf * (size_t)r->nseg));
-  RC(cudaMalloc((void **)&r->seg, sizeof(float) * r->rowf * (size_t)(r->every + 1)));
-  RC(cudaMalloc((void **)&r->grids, sizeof(float4) * (size_t)r->nodes * (size_t)r->every));
+  for (int b = 0; b < 2; ++b) {
+    RC(cudaMalloc((void **)&r->seg[b], sizeof(float) * r->rowf * (size_t)(r->every + 1)));
+    RC(cudaMalloc((void **)&r->grids[b], sizeof(float4) * (size_t)r->nodes * (size_t)r->every));
+    RC(cudaEventCreateWithFlags(&r->recorded[b], cudaEventDisableTiming));
+    RC(cudaEventCreateWithFlags(&r->reversed[b], cudaEventDisableTiming));
+  }
+  RC(cudaStreamCreateWithFlags(&r->rev, cudaStreamNonBlocking));
   for (auto &a : r->adj) RC(cudaMalloc((void **)&a, sizeof(float) * r->rowf));
   RC(cudaMalloc((void **)&r->VB, sizeof(float4) * (size_t)r->nodes));
   RC(cudaMalloc((void **)&r->GB, sizeof(float4) * (size_t)r->nodes));
@@ -1166,31 +1181,46 @@ nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float
   R_TRY(r, seed(r->C(a), gCT, mat));
   R_TRY(r, cudaMemsetAsync(r->gml, 0, 2 * sizeof(double), s->stream));
   R_TRY(r, cudaMemsetAsync(r->err, 0, sizeof(int), s->stream));
+  R_TRY(r, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)s->nscenes, s->stream));
   const Params &P = s->P0();
+  bool used[2] = {false, false};
   for (int sg = r->nseg - 1; sg >= 0; --sg) {
     const int64_t t0 = (int64_t)sg * r->every;
     const int L = (int)std::min<int64_t>(r->every, r->nsteps - t0);
-    // recompute the segment: states s_t0..s_t0+L and the grids of its steps
-    float *first = r->state(r->seg, 0);
+    const int buf = sg & 1;
+    // recompute the segment into buffer `buf` (once the adjoint of the segment that used it
+    // last is done): states s_t0..s_t0+L and the grids of its steps
+    if (used[buf]) R_TRY(r, cudaStreamWaitEvent(s->stream, r->reversed[buf], 0));
+    float *first = r->state(r->seg[buf], 0);
     R_TRY(r, cudaMemcpyAsync(first, r->state(r->ckpt, sg), sizeof(float) * r->rowf,
                              cudaMemcpyDeviceToDevice, s->stream));
     nclr_status st = load_state(r, first);
     if (st != NCLR_OK) return st;
-    if ((st = record_segment(r, L)) != NCLR_OK) return st;
+    if ((st = record_segment(r, L, buf)) != NCLR_OK) return st;
+    R_TRY(r, cudaEventRecord(r->recorded[buf], s->stream));
+    // its adjoint on the reverse stream, overlapping the next recomputation
+    R_TRY(r, cudaStreamWaitEvent(r->rev, r->recorded[buf], 0));
     for (int i = L - 1; i >= 0; --i) {
-      float *st_t = r->state(r->seg, i), *st_n = r->state(r->seg, i + 1);
+      float *st_t = r->state(r->seg[buf], i), *st_n = r->state(r->seg[buf], i + 1);
       dispatch_dim(D, [&](auto dc) {
         constexpr int DD = decltype(dc)::value;
         mpm::launch_adjoint_step<DD>(n, r->x(st_t), r->v(st_t), r->F(st_t), r->C(st_t), r->C(st_n),
-                                     r->mass, r->vol, r->grids + (size_t)i * r->nodes, P, s->ref,
-                                     r->x(a), r->v(a), r->F(a), r->C(a), r->x(b), r->v(b),
-                                     r->F(b), r->C(b), r->VB, r->GB, r->gml, r->err, s->stream);
+                                     r->mass, r->vol, r->grids[buf] + (size_t)i * r->nodes, P,
+                                     s->ref, r->x(a), r->v(a), r->F(a), r->C(a), r->x(b), r->v(b),
+                                     r->F(b), r->C(b), r->VB, r->GB, r->gml, r->err, r->rev);
       });
       std::swap(a, b);
     }
+    R_TRY(r, cudaEventRecord(r->reversed[buf], r->rev));
+    used[buf] = true;
     nclr_status cst = check_launch(s, "adjoint step");
     if (cst != NCLR_OK) return rfail(r, cst, s->error);
   }
+  // join the reverse stream back into the simulation's stream
+  for (int b2 = 0; b2 < 2; ++b2)
+    if (used[b2]) R_TRY(r, cudaStreamWaitEvent(s->stream, r->reversed[b2], 0));
+  int serr[2] = {0, 0};
+  R_TRY(r, cudaMemcpyAsync(serr, s->err_d, 2 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   if (gx0) R_TRY(r, cudaMemcpyAsync(gx0, r->x(a), vec, cudaMemcpyDeviceToDevice, s->stream));
   if (gv0) R_TRY(r, cudaMemcpyAsync(gv0, r->v(a), vec, cudaMemcpyDeviceToDevice, s->stream));
   if (gF0) R_TRY(r, cudaMemcpyAsync(gF0, r->F(a), mat, cudaMemcpyDeviceToDevice, s->stream));
@@ -1209,6 +1239,8 @@ nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float
   const double dl_dE = nu / q, dl_dnu = E * (1.0 + 2.0 * nu * nu) / (q * q);
   if (gE) *gE = gml[0] * dmu_dE + gml[1] * dl_dE;
   if (gnu) *gnu = gml[0] * dmu_dnu + gml[1] * dl_dnu;
+  if ((serr[0] | serr[1]) & mpm::kErrOutOfRange)
+    return rfail(r, NCLR_ERR_OUT_OF_RANGE, "a stencil left the grid during the recomputation");
   if (err & mpm::kErrOutOfRange) return rfail(r, NCLR_ERR_OUT_OF_RANGE, "a stencil left the grid");
   return NCLR_OK;
 }
