@@ -48,7 +48,7 @@ WORKLOAD = {"workload": "3D jelly (MaterialModel::kJelly), 4 cubes of 64^3 latti
 
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel
 # from one ncu capture of this workload (profiles/g2p2g_jelly3d_1M.md).
-NCU_TRAFFIC = {"g2p2g": 69.006080e6 + 12.848640e6}
+NCU_TRAFFIC = {"g2p2g": 68.746752e6 + 6.398208e6}
 
 
 def peaks():
@@ -431,19 +431,21 @@ def run_ours(args):
         capi.check(L.nclr_get_particles(h, _ptr(ox), _ptr(ov), _ptr(oF), _ptr(oC), _ptr(oJ)), h)
         return launches
 
-    for _ in range(max(args.warmup, 1)):
-        e2e_step()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        launches_total += e2e_step() + 2  # + the import/prepare and export kernels
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    barrier()
-    row = 4 * (2 * 3 + 2 * 9 + 1)
-    e2e = {"value": world * n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * row,
-           "d2h_bytes_per_step": n * row,
-           "path": "nclr_set_particles (pinned host) + nclr_advance(1) + nclr_get_particles"}
+    e2e = None
+    if not args.no_e2e:
+        for _ in range(max(args.warmup, 1)):
+            e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            launches_total += e2e_step() + 2  # + the import/prepare and export kernels
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+        barrier()
+        row = 4 * (2 * 3 + 2 * 9 + 1)
+        e2e = {"value": world * n * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": n * row, "d2h_bytes_per_step": n * row,
+               "path": "nclr_set_particles (pinned host) + nclr_advance(1) + nclr_get_particles"}
 
     batched = None
     if not args.no_batched:
@@ -493,6 +495,9 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-snow", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the end-to-end (host buffers) measurement, e.g. for a launch list "
+                         "of the device-resident steps alone")
     ap.add_argument("--only", choices=sorted(FORMS), default=None,
                     help="run one of the other forms alone and print its object")
     ap.add_argument("--form-steps", type=int, default=None)
