@@ -1,5 +1,6 @@
 """Autotuner for the runtime knobs of a simulation (plain or batched): the block re-sort
-interval and the number of steps per captured CUDA graph.
+interval, the number of steps per captured CUDA graph and, for single simulations, the
+thin-block threshold below which a block's particles skip the shared-memory tile.
 
 The tile and block sizes of the kernels (4^3 cells in 3D, 8^2 in 2D, 8^3 / 12^2 node tiles,
 256-thread CTAs) are compile-time constants fixed by the shared-memory layout; the knobs that
@@ -9,6 +10,9 @@ itself through the public API, and the winner is cached per workload signature.
     from nuclearmpm_gb300 import autotune
     best = autotune.tune(lambda **opt: BatchSimulation(scenes, **opt), key="batch256")
     sim = BatchSimulation(scenes, **best)
+
+    best = autotune.tune(lambda **opt: MPMSimulation(state, model, res=res, **opt),
+                         key="snow1M", candidates=autotune.PLAIN_CANDIDATES)
 """
 from __future__ import annotations
 
@@ -17,6 +21,9 @@ import os
 import time
 
 DEFAULT_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32]}
+# single simulations: also the thin-block threshold (particles per block; 0 = every block
+# through the tile); batches ignore it
+PLAIN_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32], "sparse_block_max": [0, 32, 64, 128, 256]}
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 
