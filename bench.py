@@ -313,7 +313,40 @@ def run_snow(device: int, steps: int = 100) -> dict:
                       "dt 1e-4, reference physics"}
 
 
-FORMS = {"batched": run_batched, "adjoint": run_adjoint, "mixed": run_mixed, "snow": run_snow}
+def run_readme(device: int, steps: int = 4000, cpu_steps: int = 400) -> dict:
+    """The README scene (2D snow, two cube<2>(50, 0.4, 0.6) lattices, 5,000 particles, res 64,
+    dt 1e-4): `steps` steps timed with CUDA events on the simulation's stream (CUDA graphs),
+    and the CPU oracle (-Ofast, one thread) timed on `cpu_steps` steps of the same scene."""
+    import torch
+
+    from oracle import pyoracle as po
+    from nuclearmpm_gb300 import MPMSimulation, scenes
+    sc = scenes.readme_scene()
+    n = len(sc["x"])
+    sim = MPMSimulation(dict(sc), scenes.SNOW, res=64, graph_steps=200, device=device)
+    sim.advance(200)
+    st = torch.cuda.ExternalStream(sim.stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    sim.advance(steps)
+    b.record(st)
+    b.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    launches = sim.stats()[0]
+    sim.close()
+    t0 = time.perf_counter()
+    po.advance(sc, dim=2, model=scenes.SNOW, res=64, steps=cpu_steps, fast=True, want_grid=False)
+    tc = time.perf_counter() - t0
+    return {"value": n * steps / t, "unit": UNIT, "particles": n, "steps": steps,
+            "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
+            "cpu_value": n * cpu_steps / tc, "cpu_sample": f"{cpu_steps} steps of the same scene, "
+            "oracle -Ofast, one thread", "speedup_vs_cpu": (n * steps / t) / (n * cpu_steps / tc),
+            "config": "README scene: 2D snow, 5,000 particles, res 64, dt 1e-4, reference "
+                      "physics, CUDA graphs of 200 steps"}
+
+
+FORMS = {"batched": run_batched, "adjoint": run_adjoint, "mixed": run_mixed, "snow": run_snow,
+         "readme": run_readme}
 
 
 def run_form(args):
@@ -459,6 +492,9 @@ def run_ours(args):
     snow = None
     if not args.no_snow:
         snow = run_snow(local)
+    readme = None
+    if not args.no_readme and rank == 0:
+        readme = run_readme(local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -474,7 +510,7 @@ def run_ours(args):
                 "data": "synthetic (seeded scene with the workload's shapes and distributions)",
                 "config": dict(WORKLOAD, parallelism=f"replicas x{world}"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
-                "adjoint": adjoint, "mixed": mixed, "snow": snow,
+                "adjoint": adjoint, "mixed": mixed, "snow": snow, "readme": readme,
                 "gpu_launches": launches_total, "clocks": clk}
         print(json.dumps(line), flush=True)
     sim.close()
@@ -495,6 +531,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-snow", action="store_true")
+    ap.add_argument("--no-readme", action="store_true")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the end-to-end (host buffers) measurement, e.g. for a launch list "
                          "of the device-resident steps alone")

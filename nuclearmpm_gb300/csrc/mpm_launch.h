@@ -35,14 +35,20 @@ template <int D> int g2p2g_ctas_per_sm();
 enum : int { kModeStep = 0, kModeFinalStep = 1, kModeP2GOnly = 2 };  // g2p2g modes
 template <int D> void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st);
 template <int D> void launch_export_grid(const float4 *grid, const Params &P, float *vel, float *mass, cudaStream_t st);
-template <int D> void launch_export_particles(const PState &s, int begin, int n, int id_off, float *x, float *v,
-                                              float *F, float *C, float *Jp, cudaStream_t st);
-template <int D> void launch_import_particles(const PState &s, int begin, int n, int id_off, const float *x,
-                                              const float *v, const float *F, const float *C, const float *Jp,
-                                              cudaStream_t st);
+// Caller rows [0, n) of the scene whose global ids (and slots) start at id_off <-> their
+// slots: the export runs per caller row through inv (global id -> slot), the import per slot
+// through id.  The import counts, into *moved (when non-null), the rows that left their
+// slot's grid block.
+template <int D> void launch_export_rows(const PState &s, const int *inv, int id_off, int n, float *x, float *v,
+                                         float *F, float *C, float *Jp, cudaStream_t st);
+template <int D> void launch_import_rows(const PState &s, int id_off, int n, const float *x,
+                                         const float *v, const float *F, const float *C, const float *Jp,
+                                         const Scene *scenes, const int *slot_block, int *moved,
+                                         cudaStream_t st);
 template <int D> void launch_block_keys(const PState &s, int n, const Scene *scenes, int *key, int *rank, int *count,
                                         cudaStream_t st);
-template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank, const int *start, const int *count, bool move_vc, cudaStream_t st);
+// Also records inv[id] = new slot and slot_block[new slot] = its grid block.
+template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank, const int *start, const int *count, bool move_vc, int *inv, int *slot_block, cudaStream_t st);
 // The non-empty blocks of the sort: those with at least sparse_max particles (all of them when
 // sparse_max <= 0) into list / nlist[0]; the particle slots of the others, block by block,
 // into sparse / nlist[1].  nlist[0..1] must be zero on entry.

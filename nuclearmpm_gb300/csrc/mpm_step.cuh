@@ -647,18 +647,36 @@ __global__ void export_grid_kernel(const float4 *__restrict__ grid, Params P,
   mass[f] = m;
 }
 
-// particles() export: slots [begin, begin + n) (SoA) -> the caller's rows id - id_off
-// (particle-major).  A scene's slots stay inside its own slot range across sorts.
+// Grid block (global, scene-major) and cell within it of a position: the sort key of
+// block_keys_kernel (stencil base clamped into the grid, as the sort needs a bucket even for a
+// particle that is about to raise the out-of-range error).
 template <int D>
-__global__ void export_particles_kernel(PState s, int begin, int n, int id_off,
-                                        float *__restrict__ x, float *__restrict__ v,
-                                        float *__restrict__ F, float *__restrict__ C,
-                                        float *__restrict__ Jp) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int p = begin + i;
+__device__ __forceinline__ void block_of(const float x[D], const Params &P, int block_off, int &kb,
+                                         int &kc) {
+  constexpr int BS = Tiling<D>::BS;
+  kb = 0;
+  kc = 0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int bd = min(max(__float2int_rz(x[d] * P.inv_dx - 0.5f), 0), P.N - 1);
+    kb = kb * P.nb + bd / BS;
+    kc = kc * BS + bd % BS;
+  }
+  kb += block_off;
+}
+
+// particles() export, one thread per caller row: row q of the scene whose rows start at
+// global id id_off lives in slot inv[id_off + q].  Rows are written in order (coalesced on the
+// caller's side, which may be mapped host memory); slots are read where the sort put them.
+template <int D>
+__global__ void export_rows_kernel(PState s, const int *__restrict__ inv, int id_off, int n,
+                                   float *__restrict__ x, float *__restrict__ v,
+                                   float *__restrict__ F, float *__restrict__ C,
+                                   float *__restrict__ Jp) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int p = inv[id_off + q];
   const int st = s.stride;
-  const int q = s.id[p] - id_off;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     if (x) x[(size_t)q * D + d] = s.x[(size_t)d * st + p];
@@ -672,29 +690,49 @@ __global__ void export_particles_kernel(PState s, int begin, int n, int id_off,
   if (Jp) Jp[q] = s.Jp[p];
 }
 
-// Upload: the caller's rows -> slots [begin, begin + n).  Slot p takes row id[p] - id_off
-// (the current permutation is kept, so a partial update leaves the other fields in place).
+// Upload, one thread per slot of the scene (slots [id_off, id_off + n); slot p takes caller
+// row id[p] - id_off, so the slot-major writes stay coalesced and a partial update leaves the
+// other fields in place).  With `moved`, counts the rows whose new position lies in another
+// grid block than the one their slot was sorted into (slot_block, from the last sort): zero
+// means the block lists still describe the particles and no re-sort is needed.
 template <int D>
-__global__ void import_particles_kernel(PState s, int begin, int n, int id_off,
-                                        const float *__restrict__ x, const float *__restrict__ v,
-                                        const float *__restrict__ F, const float *__restrict__ C,
-                                        const float *__restrict__ Jp) {
+__global__ void import_rows_kernel(PState s, int id_off, int n, const float *__restrict__ x,
+                                   const float *__restrict__ v, const float *__restrict__ F,
+                                   const float *__restrict__ C, const float *__restrict__ Jp,
+                                   const Scene *__restrict__ scenes,
+                                   const int *__restrict__ slot_block, int *moved) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int p = begin + i;
-  const int st = s.stride;
-  const int q = s.id[p] - id_off;
+  bool off_block = false;
+  if (i < n) {
+    const int p = id_off + i;
+    const int q = s.id[p] - id_off;
+    const int st = s.stride;
+    float xp[D];
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    if (x) s.x[(size_t)d * st + p] = x[(size_t)q * D + d];
-    if (v) s.v[(size_t)d * st + p] = v[(size_t)q * D + d];
-  }
+    for (int d = 0; d < D; ++d) {
+      if (x) {
+        xp[d] = x[(size_t)q * D + d];
+        s.x[(size_t)d * st + p] = xp[d];
+      }
+      if (v) s.v[(size_t)d * st + p] = v[(size_t)q * D + d];
+    }
 #pragma unroll
-  for (int c = 0; c < D * D; ++c) {
-    if (F) s.F[(size_t)c * st + p] = F[(size_t)q * D * D + c];
-    if (C) s.C[(size_t)c * st + p] = C[(size_t)q * D * D + c];
+    for (int c = 0; c < D * D; ++c) {
+      if (F) s.F[(size_t)c * st + p] = F[(size_t)q * D * D + c];
+      if (C) s.C[(size_t)c * st + p] = C[(size_t)q * D * D + c];
+    }
+    if (Jp) s.Jp[p] = Jp[q];
+    if (moved && x) {
+      const Scene &sc = scenes[s.scene ? (int)s.scene[p] : 0];
+      int kb, kc;
+      block_of<D>(xp, sc.P, sc.block_off, kb, kc);
+      off_block = kb != slot_block[p];
+    }
   }
-  if (Jp) s.Jp[p] = Jp[q];
+  if (moved) {  // one atomic per warp (every lane reaches this point)
+    const unsigned b = __ballot_sync(0xffffffffu, off_block);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(moved, __popc(b));
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -712,17 +750,13 @@ __global__ void block_keys_kernel(const float *__restrict__ xs, const uint16_t *
                                   int *__restrict__ count) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  constexpr int BS = Tiling<D>::BS;
   const int sid = pscene ? (int)pscene[p] : 0;
-  const Params &P = scenes[sid].P;
-  int kb = 0, kc = 0;
+  float x[D];
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const int bd = min(max(__float2int_rz(xs[(size_t)d * stride + p] * P.inv_dx - 0.5f), 0), P.N - 1);
-    kb = kb * P.nb + bd / BS;
-    kc = kc * BS + bd % BS;
-  }
-  const int k = (scenes[sid].block_off + kb) * Tiling<D>::CPB + kc;  // block-major, then cell
+  for (int d = 0; d < D; ++d) x[d] = xs[(size_t)d * stride + p];
+  int kb, kc;
+  block_of<D>(x, scenes[sid].P, scenes[sid].block_off, kb, kc);
+  const int k = kb * Tiling<D>::CPB + kc;  // block-major, then cell
   key[p] = k;
   rank[p] = atomicAdd(count + k, 1);
 }
@@ -735,7 +769,8 @@ __global__ void block_keys_kernel(const float *__restrict__ xs, const uint16_t *
 template <int D>
 __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__restrict__ key,
                                  const int *__restrict__ rank, const int *__restrict__ start,
-                                 const int *__restrict__ count, int move_vc) {
+                                 const int *__restrict__ count, int move_vc, int *__restrict__ inv,
+                                 int *__restrict__ slot_block) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   constexpr int CPB = Tiling<D>::CPB;
@@ -754,7 +789,10 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
   dst.Jp[q] = src.Jp[p];
   dst.mass[q] = src.mass[p];
   dst.vol[q] = src.vol[p];
-  dst.id[q] = src.id[p];
+  const int id = src.id[p];
+  dst.id[q] = id;
+  inv[id] = q;                     // caller row -> slot
+  slot_block[q] = k / CPB;         // the block this slot now belongs to
   if (src.mat) dst.mat[q] = src.mat[p];
   if (src.scene) dst.scene[q] = src.scene[p];
   if (move_vc) {  // the next P2G reads v and C (right after an upload)
@@ -857,18 +895,19 @@ void launch_export_grid(const float4 *grid, const Params &P, float *vel, float *
 }
 
 template <int D>
-void launch_export_particles(const PState &s, int begin, int n, int id_off, float *x, float *v,
-                             float *F, float *C, float *Jp, cudaStream_t st) {
+void launch_export_rows(const PState &s, const int *inv, int id_off, int n, float *x, float *v,
+                        float *F, float *C, float *Jp, cudaStream_t st) {
   if (n == 0) return;
-  export_particles_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, begin, n, id_off, x, v, F, C, Jp);
+  export_rows_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, inv, id_off, n, x, v, F, C, Jp);
 }
 
 template <int D>
-void launch_import_particles(const PState &s, int begin, int n, int id_off, const float *x,
-                             const float *v, const float *F, const float *C, const float *Jp,
-                             cudaStream_t st) {
+void launch_import_rows(const PState &s, int id_off, int n, const float *x,
+                        const float *v, const float *F, const float *C, const float *Jp,
+                        const Scene *scenes, const int *slot_block, int *moved, cudaStream_t st) {
   if (n == 0) return;
-  import_particles_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, begin, n, id_off, x, v, F, C, Jp);
+  import_rows_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(s, id_off, n, x, v, F, C, Jp, scenes,
+                                                            slot_block, moved);
 }
 
 template <int D>
@@ -881,10 +920,11 @@ void launch_block_keys(const PState &s, int n, const Scene *scenes, int *key, in
 
 template <int D>
 void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank,
-                      const int *start, const int *count, bool move_vc, cudaStream_t st) {
+                      const int *start, const int *count, bool move_vc, int *inv, int *slot_block,
+                      cudaStream_t st) {
   if (n == 0) return;
   sort_move_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, key, rank, start, count,
-                                                          move_vc ? 1 : 0);
+                                                          move_vc ? 1 : 0, inv, slot_block);
 }
 
 #define MPM_INSTANTIATE(D)                                                                       \
@@ -900,14 +940,15 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \
                                       cudaStream_t);                                             \
-  template void launch_export_particles<D>(const PState &, int, int, int, float *, float *,       \
-                                           float *, float *, float *, cudaStream_t);             \
-  template void launch_import_particles<D>(const PState &, int, int, int, const float *,         \
-                                           const float *, const float *, const float *,          \
-                                           const float *, cudaStream_t);                         \
+  template void launch_export_rows<D>(const PState &, const int *, int, int, float *, float *,    \
+                                      float *, float *, float *, cudaStream_t);                  \
+  template void launch_import_rows<D>(const PState &, int, int, const float *,                   \
+                                      const float *, const float *, const float *,               \
+                                      const float *, const Scene *, const int *, int *,          \
+                                      cudaStream_t);                                             \
   template void launch_block_keys<D>(const PState &, int, const Scene *, int *, int *, int *,    \
                                      cudaStream_t);                                              \
   template void launch_sort_move<D>(const PState &, const PState &, int, const int *, const int *, \
-                                    const int *, const int *, bool, cudaStream_t);
+                                    const int *, const int *, bool, int *, int *, cudaStream_t);
 
 }  // namespace mpm

@@ -172,6 +172,71 @@ def test_advance_after_set_particles_matches_fresh_simulation():
         assert field_err(getattr(pa, f), getattr(pb, f), f) <= 1e-5, f
 
 
+def _pinned(a):
+    """A pinned (page-locked, device-mapped) host copy of `a`."""
+    torch = pytest.importorskip("torch")
+    t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+    t.numpy()[...] = a
+    return t
+
+
+def test_pinned_and_pageable_buffers_agree():
+    """Uploads and downloads through pinned and through pageable host buffers give the same
+    results up to the order of the grid's atomic sums, including an upload that keeps the
+    positions (no re-sort) and one that moves them.  Without stepping, the transfers are
+    exact."""
+    z, state, params, steps = load_golden("block3d_jelly")
+    kw = dict(res=params["res"], dt=params["dt"], E=params["E"], nu=params["nu"],
+              gravity=params["gravity"])
+    runs = []
+    for pinned in (False, True):
+        sim = MPMSimulation(dict(state), params["model"], **kw)
+        sim.advance(4)
+        p = sim.particles()
+        wrap = (lambda a: _pinned(a).numpy()) if pinned else (lambda a: np.ascontiguousarray(a))
+        v2 = wrap(p.v * np.float32(0.5))
+        sim.set_particles(v=v2)               # same positions: no re-sort
+        assert np.array_equal(sim.particles().v, v2)
+        sim.advance(3)
+        q = sim.particles()
+        x3 = wrap(q.x + np.float32(0.3 / params["res"]))
+        sim.set_particles(x=x3)               # moved positions: re-sorted
+        sim.advance(2)
+        n, d = sim.n, sim.dim
+        bufs = {f: wrap(np.zeros(shape, np.float32)) for f, shape in
+                (("x", (n, d)), ("v", (n, d)), ("F", (n, d, d)), ("C", (n, d, d)), ("Jp", (n,)))}
+        from nuclearmpm_gb300.simulation import _ptr
+        from nuclearmpm_gb300 import capi
+        capi.check(capi.lib().nclr_get_particles(sim._h, *(_ptr(bufs[f]) for f in FIELDS)), sim._h)
+        runs.append({f: np.array(bufs[f]) for f in FIELDS})
+        sim.close()
+    for f in FIELDS:  # the grid sums are FP32 atomics: equal up to their order
+        assert field_err(runs[1][f], runs[0][f], f) <= DRIFT[f], f
+
+
+def test_upload_keeping_positions_matches_fresh_simulation():
+    """An upload whose particles all stay in their grid blocks skips the re-sort; stepping on
+    equals a fresh simulation created from the same state, up to summation order."""
+    z, state, params, steps = load_golden("block3d_snow")
+    kw = dict(res=params["res"], dt=params["dt"], E=params["E"], nu=params["nu"],
+              gravity=params["gravity"])
+    a = MPMSimulation(dict(state), params["model"], **kw)
+    a.advance(3)
+    p = a.particles()
+    v = p.v + np.float32(0.01)
+    a.set_particles(x=p.x, v=v, F=p.F, C=p.C, Jp=p.Jp)
+    a.advance(2)
+    pa = a.particles()
+    a.close()
+    b = MPMSimulation(dict(x=p.x, v=v, F=p.F, C=p.C, Jp=p.Jp, mass=state["mass"],
+                           volume=state["volume"]), params["model"], **kw)
+    b.advance(2)
+    pb = b.particles()
+    b.close()
+    for f in FIELDS:
+        assert field_err(getattr(pa, f), getattr(pb, f), f) <= 1e-5, f
+
+
 def test_empty_scene_and_empty_grid_before_advance():
     sim = MPMSimulation([], scenes.SNOW, res=16, dim=2)
     assert len(sim.grid()) == 0  # the reference's grid() is empty before the first step
