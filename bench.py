@@ -127,6 +127,32 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def host_cpu() -> dict:
+    """The host the CPU legs run on: online cores and the CPU model (Arm machines report no
+    "model name"; their implementer/part codes and /proc/device-tree model stand in)."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read()
+        for key in ("model name", "Model", "CPU part"):
+            for line in info.splitlines():
+                if line.split(":")[0].strip() == key:
+                    model = line.split(":", 1)[1].strip()
+                    break
+            if model:
+                break
+    except OSError:
+        pass
+    try:
+        with open("/proc/device-tree/model") as f:
+            model = (model + " / " if model else "") + f.read().strip("\x00\n ")
+    except OSError:
+        pass
+    import platform
+    return {"nproc": os.cpu_count(), "cpu": model or platform.processor() or platform.machine(),
+            "arch": platform.machine()}
+
+
 def make_scene():
     from nuclearmpm_gb300 import scenes
     return scenes.jelly_cubes_3d(seed=0, res=128)
@@ -373,6 +399,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": dict(WORKLOAD), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                             "host": host_cpu(),
                              "sample": desc + "; the reference's step restated in C++ "
                              "(oracle/, -Ofast like the reference build), single thread as "
                              "the reference runs (its OpenMP pragmas are inert)"},
@@ -499,7 +526,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, desc = cpu_reference_run(scene, steps=args.cpu_steps, warmup=1, budget_s=20.0)
-        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
                "sample": desc + "; the reference's step restated in C++ (oracle/, -Ofast like "
                                 "the reference build), one thread"}
 

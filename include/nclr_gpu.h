@@ -105,6 +105,25 @@ nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, cons
                         const float *volume, const uint8_t *material, int model, int res,
                         float dt, float E, float nu, float gravity, const nclr_options *opt);
 
+/* nclr_create with DEVICE arrays (same layouts and NULL rules): scenes built or kept on the
+ * GPU are not staged through the host.  An extension. */
+nclr_status nclr_create_device(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
+                               const float *F, const float *C, const float *Jp, const float *mass,
+                               const float *volume, const uint8_t *material, int model, int res,
+                               float dt, float E, float nu, float gravity,
+                               const nclr_options *opt);
+
+/* Scene builders on the device.  nclr_cube_device writes cube<dim>(res, lo, hi)
+ * (src/nclr_math.h:100-129: res^dim lattice points over [lo, hi]^dim from Eigen's
+ * LinSpaced, x outermost) as res^dim rows of dim floats into the DEVICE array x, bit-equal
+ * to the host builder.  nclr_cubes_device writes ncubes such lattices one after another,
+ * cube c over [lo[c], hi[c]] (HOST arrays) -- the headless solver's generate_cubes
+ * (src/solver.cpp:133-149).  Both run on `stream` (a cudaStream_t, NULL = default) and
+ * synchronise it. */
+nclr_status nclr_cube_device(int dim, int res, float lo, float hi, float *x, void *stream);
+nclr_status nclr_cubes_device(int dim, int ncubes, int res, const float *lo, const float *hi,
+                              float *x, void *stream);
+
 /* Batched form (no counterpart in the reference, which runs one simulation per object): one
  * handle holding `nscenes` independent simulations of uneven particle counts, grid
  * resolutions, materials and parameters, stepped together -- every kernel of a step covers

@@ -19,7 +19,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libnclr_gpu.so")
-SOURCES = ["nclr_gpu.cu", "step2d.cu", "step3d.cu", "scan.cu", "noalloc.cu", "adjoint.cu"]
+SOURCES = ["nclr_gpu.cu", "step2d.cu", "step3d.cu", "scan.cu", "noalloc.cu", "adjoint.cu",
+           "scene_build.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -49,6 +49,14 @@ SIGNATURES = {
                                    _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                    ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                    ctypes.POINTER(Options)]),
+    "nclr_create_device": (ctypes.c_int, [ctypes.POINTER(_h), ctypes.c_int, _i64, _vp, _vp, _vp,
+                                          _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                          ctypes.c_float, ctypes.POINTER(Options)]),
+    "nclr_cube_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                        _vp, _vp]),
+    "nclr_cubes_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp,
+                                         _vp]),
     "nclr_advance": (ctypes.c_int, [_h, _i64]),
     "nclr_batch_create": (ctypes.c_int, [ctypes.POINTER(_h), ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(Scene), ctypes.POINTER(Options)]),

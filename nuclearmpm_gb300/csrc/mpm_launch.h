@@ -55,6 +55,10 @@ template <int D> void launch_sort_move(const PState &src, const PState &dst, int
 void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int *list,
                            int *nlist, int *sparse, cudaStream_t st);
 
+// Counts material[] entries above NCLR_LIQUID into *out (host); synchronises `st`
+// (scene_build.cu).
+cudaError_t count_bad_materials(const uint8_t *mat, int64_t n, int *scratch, int *out, cudaStream_t st);
+
 // Reverse of one jelly step (adjoint.cu): adjoint of s_{t+1} (gx, gv, gF, gC; NULL = 0) ->
 // adjoint of s_t (ox, ov, oF, oC), mu_0 / lambda_0 adjoints added to gml[0..1].  States are
 // caller-order rows; V is the step's updated grid; VB (4 floats per node) must be zero on

@@ -430,20 +430,23 @@ void release(nclr_sim *s) {
   delete s;
 }
 
-nclr_status validate_scene(const nclr_scene &sc) {
+nclr_status validate_scene(const nclr_scene &sc, bool device_arrays) {
   if (sc.n < 0 || sc.n > (int64_t)0x7fffffff / 2) return fail(nullptr, NCLR_ERR_INVALID, "bad particle count");
   if (sc.n > 0 && !sc.x) return fail(nullptr, NCLR_ERR_INVALID, "x is NULL");
   if (sc.res < 1 || sc.res > 1024) return fail(nullptr, NCLR_ERR_INVALID, "res must be in [1, 1024]");
   if (sc.model < 0 || sc.model > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material model");
-  if (sc.material)
+  if (sc.material && !device_arrays)  // device arrays are checked on the device after the copy
     for (int64_t p = 0; p < sc.n; ++p)
       if (sc.material[p] > 2) return fail(nullptr, NCLR_ERR_INVALID, "unknown material in material[]");
   return NCLR_OK;
 }
 
-// Creates a handle of `nscenes` scenes (nclr_create is the one-scene case).
+// Creates a handle of `nscenes` scenes (nclr_create is the one-scene case).  With
+// device_arrays, the scenes' particle arrays are device pointers (nclr_create_device): the
+// defaults are staged from the host as usual and the given arrays are copied over them on
+// the device.
 nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene *descs,
-                          const nclr_options *opt) {
+                          const nclr_options *opt, bool device_arrays = false) {
   g_create_error.clear();
   if (!out) return fail(nullptr, NCLR_ERR_INVALID, "out is NULL");
   *out = nullptr;
@@ -452,7 +455,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   int64_t total_n = 0;
   bool any_mat = false;
   for (int i = 0; i < nscenes; ++i) {
-    nclr_status st = validate_scene(descs[i]);
+    nclr_status st = validate_scene(descs[i], device_arrays);
     if (st != NCLR_OK) return st;
     total_n += descs[i].n;
     any_mat |= descs[i].material != nullptr;
@@ -584,26 +587,27 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
     for (int i = 0; i < nscenes; ++i) {
       const nclr_scene &d = descs[i];
       const int64_t o = s->scenes[i].slot_off;
+      const bool h = !device_arrays;  // host arrays may be read here
       for (int64_t q = 0; q < d.n; ++q) {
         iota[(size_t)(o + q)] = (int)(o + q);
-        if (d.mass) mass[(size_t)(o + q)] = d.mass[q];
-        if (d.volume) vol[(size_t)(o + q)] = d.volume[q];
-        if (any_mat) mat[(size_t)(o + q)] = d.material ? d.material[q] : (uint8_t)d.model;
+        if (h && d.mass) mass[(size_t)(o + q)] = d.mass[q];
+        if (h && d.volume) vol[(size_t)(o + q)] = d.volume[q];
+        if (any_mat) mat[(size_t)(o + q)] = (h && d.material) ? d.material[q] : (uint8_t)d.model;
         if (nscenes > 1) pscene[(size_t)(o + q)] = (uint16_t)i;
-        hJ[o + q] = d.Jp ? d.Jp[q] : 1.0f;
+        hJ[o + q] = (h && d.Jp) ? d.Jp[q] : 1.0f;
       }
       // Rows: x, v, F, C with the constructor's defaults for the NULL ones
       // (Particle<dim>: v = 0, F = diag<dim>(1), C = 0, Jp = 1; src/nclr.h:46-47).
-      if (d.n > 0) std::memcpy(hx + o * dim, d.x, sizeof(float) * d.n * dim);
-      if (d.v) std::memcpy(hv + o * dim, d.v, sizeof(float) * d.n * dim);
-      if (d.F) {
+      if (h && d.n > 0) std::memcpy(hx + o * dim, d.x, sizeof(float) * d.n * dim);
+      if (h && d.v) std::memcpy(hv + o * dim, d.v, sizeof(float) * d.n * dim);
+      if (h && d.F) {
         std::memcpy(hF + o * dim * dim, d.F, sizeof(float) * d.n * dim * dim);
       } else {
         for (int64_t q = 0; q < d.n; ++q)
           for (int k = 0; k < dim; ++k)
             hF[((o + q) * dim + k) * dim + k] = (k < 2 || !s->ref) ? 1.0f : 0.0f;
       }
-      if (d.C) std::memcpy(hC + o * dim * dim, d.C, sizeof(float) * d.n * dim * dim);
+      if (h && d.C) std::memcpy(hC + o * dim * dim, d.C, sizeof(float) * d.n * dim * dim);
     }
     CREATE_TRY(cudaMemcpyAsync(p.mass, mass.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s->stream));
     CREATE_TRY(cudaMemcpyAsync(p.vol, vol.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s->stream));
@@ -615,6 +619,30 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
     if ((st = ensure_staging(s)) != NCLR_OK) return bail(st);
     const Rows r = staging_rows(s, N);
     CREATE_TRY(cudaMemcpyAsync(r.x, host.data(), sizeof(float) * host.size(), cudaMemcpyHostToDevice, s->stream));
+    if (device_arrays) {  // the caller's device arrays over the staged defaults
+      const auto d2d = cudaMemcpyDeviceToDevice;
+      for (int i = 0; i < nscenes; ++i) {
+        const nclr_scene &d = descs[i];
+        const int64_t o = s->scenes[i].slot_off, q = d.n, dd = dim * dim;
+        if (q == 0) continue;
+        CREATE_TRY(cudaMemcpyAsync(r.x + o * dim, d.x, sizeof(float) * q * dim, d2d, s->stream));
+        if (d.v) CREATE_TRY(cudaMemcpyAsync(r.v + o * dim, d.v, sizeof(float) * q * dim, d2d, s->stream));
+        if (d.F) CREATE_TRY(cudaMemcpyAsync(r.F + o * dd, d.F, sizeof(float) * q * dd, d2d, s->stream));
+        if (d.C) CREATE_TRY(cudaMemcpyAsync(r.C + o * dd, d.C, sizeof(float) * q * dd, d2d, s->stream));
+        if (d.Jp) CREATE_TRY(cudaMemcpyAsync(r.Jp + o, d.Jp, sizeof(float) * q, d2d, s->stream));
+        if (d.mass) CREATE_TRY(cudaMemcpyAsync(p.mass + o, d.mass, sizeof(float) * q, d2d, s->stream));
+        if (d.volume) CREATE_TRY(cudaMemcpyAsync(p.vol + o, d.volume, sizeof(float) * q, d2d, s->stream));
+        if (d.material) {
+          CREATE_TRY(cudaMemcpyAsync(p.mat + o, d.material, (size_t)q, d2d, s->stream));
+          int bad = 0;
+          CREATE_TRY(mpm::count_bad_materials(p.mat + o, q, s->moved_d, &bad, s->stream));
+          if (bad) {
+            s->error = "unknown material in material[]";
+            return bail(NCLR_ERR_INVALID);
+          }
+        }
+      }
+    }
     if ((st = import_rows(s, -1, r.x, r.v, r.F, r.C, r.Jp)) != NCLR_OK) return bail(st);
     CREATE_TRY(cudaStreamSynchronize(s->stream));  // the host vectors go out of scope
   }
@@ -753,6 +781,30 @@ nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, cons
   d.nu = nu;
   d.gravity = gravity;
   return create_scenes(out, dim, 1, &d, opt);
+}
+
+nclr_status nclr_create_device(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
+                               const float *F, const float *C, const float *Jp, const float *mass,
+                               const float *volume, const uint8_t *material, int model, int res,
+                               float dt, float E, float nu, float gravity,
+                               const nclr_options *opt) {
+  nclr_scene d{};
+  d.n = n;
+  d.x = x;
+  d.v = v;
+  d.F = F;
+  d.C = C;
+  d.Jp = Jp;
+  d.mass = mass;
+  d.volume = volume;
+  d.material = material;
+  d.model = model;
+  d.res = res;
+  d.dt = dt;
+  d.E = E;
+  d.nu = nu;
+  d.gravity = gravity;
+  return create_scenes(out, dim, 1, &d, opt, true);
 }
 
 nclr_status nclr_batch_create(nclr_sim **out, int dim, int nscenes, const nclr_scene *scenes,

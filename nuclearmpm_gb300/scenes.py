@@ -39,6 +39,31 @@ def cube(dim: int, n: int, lo: float, hi: float) -> np.ndarray:
     return np.stack([g.reshape(-1) for g in grids], axis=1).astype(np.float32)
 
 
+def cubes_device(dim: int, res: int, los, his, device: int = 0):
+    """ncubes lattices cube<dim>(res, lo[c], hi[c]) built on the GPU (nclr_cubes_device), one
+    after another: the headless solver's generate_cubes (src/solver.cpp:133-149) without a
+    host round trip.  Returns a CUDA tensor (ncubes * res^dim, dim), bit-equal to `cube`."""
+    import ctypes
+
+    import torch
+
+    from . import capi
+    los = np.ascontiguousarray(np.atleast_1d(los), dtype=np.float32)
+    his = np.ascontiguousarray(np.atleast_1d(his), dtype=np.float32)
+    if los.shape != his.shape:
+        raise ValueError("one (lo, hi) pair per cube")
+    out = torch.empty((len(los) * res ** dim, dim), dtype=torch.float32,
+                      device=torch.device("cuda", device))
+    with torch.cuda.device(device):
+        stream = torch.cuda.current_stream().cuda_stream
+        capi.check(capi.lib().nclr_cubes_device(dim, len(los), res,
+                                                los.ctypes.data_as(ctypes.c_void_p),
+                                                his.ctypes.data_as(ctypes.c_void_p),
+                                                ctypes.c_void_p(out.data_ptr()),
+                                                ctypes.c_void_p(stream)), None)
+    return out
+
+
 def initial_identity(dim: int, physics: int = REFERENCE) -> np.ndarray:
     """Particle<dim>'s initial F = diag<dim>(1) (src/nclr.h:47): diag(1,1,0) in 3D for the
     reference physics (src/nclr_math.h:13-19), the true identity for the corrected physics."""

@@ -165,6 +165,54 @@ class MPMSimulation:
         self.mu_0, self.lambda_0 = float(mu.value), float(lam.value)
         self._stepped = False
 
+    @classmethod
+    def from_device(cls, x, model: MaterialModel | int, res: int = 64, dt: float = 1e-4,
+                    E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, *, v=None, F=None,
+                    C=None, Jp=None, mass=None, volume=None, material=None,
+                    physics: int = capi.PHYSICS_REFERENCE, sort_interval: int = 8,
+                    device: int | None = None, use_graphs: bool = True, profile: bool = False,
+                    graph_steps: int = 0, sparse_block_max: int = -1) -> "MPMSimulation":
+        """A simulation created from CUDA tensors (nclr_create_device): x (n, dim) and the
+        optional fields in the layouts of the constructor, already on the GPU (e.g. from
+        scenes.cubes_device), never staged through the host."""
+        import torch
+        L = capi.lib()
+        if not (isinstance(x, torch.Tensor) and x.is_cuda):
+            raise TypeError("from_device takes CUDA tensors")
+        n, dim = x.shape
+        dev = x.device.index if device is None else device
+
+        def ptr(t, dtype=torch.float32):
+            if t is None:
+                return None
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dtype and t.is_contiguous()):
+                raise TypeError("device arrays must be contiguous CUDA tensors of the field's type")
+            return ctypes.c_void_p(t.data_ptr())
+        self = cls.__new__(cls)
+        self.dim, self.n, self.res = int(dim), int(n), int(res)
+        self.model = MaterialModel(int(model))
+        self._c = np.zeros(n, np.int32)
+        self._mass = (mass.cpu().numpy().astype(np.float32) if mass is not None
+                      else np.ones(n, np.float32))
+        self._volume = (volume.cpu().numpy().astype(np.float32) if volume is not None
+                        else np.ones(n, np.float32))
+        opt = capi.default_options(physics=physics, sort_interval=sort_interval, device=dev,
+                                   use_graphs=int(use_graphs), profile=int(profile),
+                                   graph_steps=graph_steps, sparse_block_max=sparse_block_max)
+        h = ctypes.c_void_p()
+        st = L.nclr_create_device(ctypes.byref(h), self.dim, self.n, ptr(x.contiguous()), ptr(v),
+                                  ptr(F), ptr(C), ptr(Jp), ptr(mass), ptr(volume),
+                                  ptr(material, torch.uint8), int(self.model), self.res,
+                                  float(dt), float(E), float(nu), float(gravity),
+                                  ctypes.byref(opt))
+        capi.check(st, None)
+        self._h = h
+        mu, lam = ctypes.c_float(), ctypes.c_float()
+        capi.check(L.nclr_get_lame(h, ctypes.byref(mu), ctypes.byref(lam)), h)
+        self.mu_0, self.lambda_0 = float(mu.value), float(lam.value)
+        self._stepped = False
+        return self
+
     # -- the reference's API ------------------------------------------------------------
     def advance(self, steps: int = 1) -> None:
         """advance() (src/nclr.h:80-84), `steps` times."""

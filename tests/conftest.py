@@ -13,6 +13,9 @@ FIELDS = ("x", "v", "F", "C", "Jp")
 # Error of a field = max|a - b| / max(max|b|, floor); floors are in the field's natural units
 # (positions in the unit box, velocities of one gravity step, F and Jp near 1, C of order 1)
 # so that a field that is zero up to rounding does not produce a meaningless ratio.
+# Drift over many steps: the GPU's atomic summation order and its register SVD differ from the
+# reference in the last bits; the stress term amplifies those differences step by step.
+DRIFT = {"x": 2e-5, "v": 3e-3, "F": 3e-4, "C": 1e-2, "Jp": 3e-4}
 FLOORS = {"x": 1.0, "v": 1e-2, "F": 1.0, "C": 1.0, "Jp": 1.0, "grid_v": 1e-2, "grid_m": 1e-3}
 
 

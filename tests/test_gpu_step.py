@@ -14,7 +14,7 @@ Tolerances (FP32; error = max|gpu - ref| / max(max|ref|, floor), floors in conft
 import numpy as np
 import pytest
 
-from conftest import FIELDS, field_err, golden_names, load_golden, state_at
+from conftest import DRIFT, FIELDS, field_err, golden_names, load_golden, state_at
 from nuclearmpm_gb300 import MPMSimulation, OutOfRange, scenes
 
 pytestmark = pytest.mark.gpu
@@ -27,9 +27,6 @@ GRID_ONE_STEP = {"grid_v": 1e-5, "grid_m": 1e-5}
 MIDRUN = {"x": 1e-5, "v": 3e-5, "F": 1e-5, "C": 3e-5, "Jp": 1e-5}
 RANDOM_VS_FP32 = 5e-5
 RANDOM_FP64_FACTOR = 2.5
-# Drift over many steps: the GPU's atomic summation order and its register SVD differ from the
-# reference in the last bits; the stress term amplifies those differences step by step.
-DRIFT = {"x": 2e-5, "v": 3e-3, "F": 3e-4, "C": 1e-2, "Jp": 3e-4}
 
 
 def run_gpu(state, params, steps, **kw):
