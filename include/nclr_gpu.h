@@ -166,6 +166,18 @@ nclr_status nclr_get_particles_device(nclr_sim *sim, float *x, float *v, float *
                                       float *Jp);
 nclr_status nclr_set_particles_device(nclr_sim *sim, const float *x, const float *v,
                                       const float *F, const float *C, const float *Jp);
+/* grid() into device arrays (scene 0), ordered on the handle's stream. */
+nclr_status nclr_get_grid_device(nclr_sim *sim, float *velocity, float *mass);
+
+/* Headless renderer (replaces the reference's X11 canvas, src/solver.cpp:184-201): draws
+ * n particles (DEVICE rows x of dim floats; 3D is drawn in the x-y plane) as discs of
+ * `radius` pixels over the canvas background and boundary box into the DEVICE array rgba
+ * (width*height 0xRRGGBB values, row 0 at the top, y up in the scene).  colors (DEVICE, one
+ * per particle, the Particle's c) may be NULL: every particle then takes `color`.  Particles
+ * are painted in index order.  Ordered on `stream` (a cudaStream_t, NULL = default). */
+nclr_status nclr_render_device(const float *x, int64_t n, int dim, const uint32_t *colors,
+                               uint32_t color, int width, int height, float radius,
+                               uint32_t *rgba, void *stream);
 
 /* Public constants of the simulation (src/nclr.h:66-72). */
 nclr_status nclr_get_lame(const nclr_sim *sim, float *mu_0, float *lambda_0);

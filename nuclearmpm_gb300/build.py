@@ -2,7 +2,8 @@
 
 Each translation unit is compiled in parallel, then linked into
 nuclearmpm_gb300/_build/libnclr_gpu.so (git-ignored; rebuilt on every machine, since the
-library is architecture-specific host code plus sm_103a device code).
+library is architecture-specific host code plus sm_103a device code); the headless solver
+nuclearmpm_gb300/_build/nclr_solver is linked against it.
 
     python -m nuclearmpm_gb300.build [-v]
 """
@@ -19,8 +20,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libnclr_gpu.so")
+SOLVER = os.path.join(OUT_DIR, "nclr_solver")  # the headless solver (cli/nclr_solver.cpp)
 SOURCES = ["nclr_gpu.cu", "step2d.cu", "step3d.cu", "scan.cu", "noalloc.cu", "adjoint.cu",
-           "scene_build.cu"]
+           "scene_build.cu", "render.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -57,6 +59,10 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     tmp = LIB + ".tmp"
     run([cc] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB)
+    # the headless solver (cli/nclr_solver.cpp), linked against the library next to it
+    run([cc, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+         os.path.join(HERE, "cli", "nclr_solver.cpp"), "-o", SOLVER, "-L", OUT_DIR, "-lnclr_gpu",
+         "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"])
     return LIB
 
 

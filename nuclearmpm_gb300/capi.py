@@ -57,6 +57,9 @@ SIGNATURES = {
                                         _vp, _vp]),
     "nclr_cubes_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp,
                                          _vp]),
+    "nclr_get_grid_device": (ctypes.c_int, [_h, _vp, _vp]),
+    "nclr_render_device": (ctypes.c_int, [_vp, _i64, ctypes.c_int, _vp, ctypes.c_uint32,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_float, _vp, _vp]),
     "nclr_advance": (ctypes.c_int, [_h, _i64]),
     "nclr_batch_create": (ctypes.c_int, [ctypes.POINTER(_h), ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(Scene), ctypes.POINTER(Options)]),

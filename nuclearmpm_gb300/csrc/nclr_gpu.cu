@@ -924,6 +924,26 @@ nclr_status nclr_get_grid(nclr_sim *s, float *velocity, float *mass) {
   return get_grid_host(s, 0, velocity, mass);
 }
 
+nclr_status nclr_get_grid_device(nclr_sim *s, float *velocity, float *mass) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  if (!s->stepped) return fail(s, NCLR_ERR_INVALID, "grid() is empty before the first advance()");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  const Scene &S = s->scenes[0];
+  const size_t nodes = (size_t)S.P.nodes, D = (size_t)s->dim;
+  if (!velocity || !mass) {  // the kernel writes both: stage what the caller does not want
+    if (!s->grid_staging)
+      CUDA_TRY(s, cudaMalloc((void **)&s->grid_staging, sizeof(float) * nodes * (D + 1)));
+    if (!velocity) velocity = s->grid_staging;
+    if (!mass) mass = s->grid_staging + nodes * D;
+  }
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    mpm::launch_copy_vgrid<DD>(s->V + S.node_off, S.P.nodes, velocity, mass, s->stream);
+  });
+  return check_launch(s, "export grid");
+}
+
 int nclr_num_scenes(const nclr_sim *s) { return s ? s->nscenes : -1; }
 
 nclr_status nclr_scene_get_particles(nclr_sim *s, int scene, float *x, float *v, float *F,
