@@ -47,53 +47,108 @@ __device__ __forceinline__ int tile_offset(int o) {
   return tile_index<D>(oi, oj, ok);
 }
 
-// One node's contribution of the reference's compute_fused_momentum (src/nclr.h:160-165):
-// weight * (m v + A dpos) and weight * m, with dpos = (o - fx) dx.
+// The reference's compute_fused_momentum (src/nclr.h:160-165) gives node o
+//   weight_o * (m v + A dpos_o) and weight_o * m,   dpos_o = (o - fx) dx.
+// p2g_terms rewrites a particle's m v and A once into q0 = m v - A fx dx (the bracket at
+// o = 0) and A dx, so that a node's bracket is q0 + sum_d o_d (A dx)[:, d] with constant o_d:
+// a few adds per node instead of a matrix-vector product (the two differ only in rounding).
 template <int D>
-__device__ __forceinline__ void p2g_contrib(int o, const float fx[D], const float w[3][D],
-                                            const float mv[D], float m, const Mat<D> &A, float dx,
-                                            float c[4]) {
+__device__ __forceinline__ void p2g_terms(const float fx[D], float dx, float mv[D], Mat<D> &A) {
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float afx = A.a[r][0] * fx[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) afx += A.a[r][k] * fx[k];
+    mv[r] -= afx * dx;  // q0
+#pragma unroll
+    for (int k = 0; k < D; ++k) A.a[r][k] *= dx;  // A dx
+  }
+}
+
+// One node's contribution from the terms of p2g_terms: c[0..D) the momentum, c[3] the mass.
+template <int D>
+__device__ __forceinline__ void p2g_contrib(int o, const float w[3][D], const float q0[D], float m,
+                                            const Mat<D> &Adx, float c[4]) {
   int oi, oj, ok;
   stencil_offset<D>(o, oi, oj, ok);
   const int oo[3] = {oi, oj, ok};
-  float dpos[D];
-#pragma unroll
-  for (int d = 0; d < D; ++d) dpos[d] = ((float)oo[d] - fx[d]) * dx;
   float weight = w[oi][0] * w[oj][1];
   if (D == 3) weight = weight * w[ok][D - 1];
   c[2] = 0.0f;
 #pragma unroll
   for (int r = 0; r < D; ++r) {
-    float ad = A.a[r][0] * dpos[0];
+    float q = q0[r];
 #pragma unroll
-    for (int k = 1; k < D; ++k) ad = ad + A.a[r][k] * dpos[k];
-    c[r] = weight * (mv[r] + ad);
+    for (int k = 0; k < D; ++k) {
+      if (oo[k] == 1) q += Adx.a[r][k];
+      if (oo[k] == 2) q += 2.0f * Adx.a[r][k];
+    }
+    c[r] = weight * q;
   }
   c[3] = weight * m;
 }
 
-// One node's part of the G2P gather (src/nclr.h:197-225): v += w gv and
-// C += (w gv) dpos^T with dpos = o - fx; the caller scales C by 4 inv_dx once at the end
-// (the reference scales every term; the two differ only in rounding).
-template <int D>
-__device__ __forceinline__ void g2p_accumulate(int o, const float4 g, const float fx[D],
-                                               const float w[3][D], float v[D], Mat<D> &C) {
-  int oi, oj, ok;
-  stencil_offset<D>(o, oi, oj, ok);
-  const int oo[3] = {oi, oj, ok};
-  float weight = w[oi][0] * w[oj][1];
-  if (D == 3) weight = weight * w[ok][D - 1];
-  const float gv[3] = {g.x, g.y, g.z};
-  float wgv[D];
+// The G2P gather (src/nclr.h:197-225) over the 3^dim stencil nodes:
+//   v += sum_o W_o g_o,   C += sum_o W_o g_o (o - fx)^T,   W_o = prod_d w[o_d][d],
+// factored by axis -- sums over the last axis first, then the middle one, then the first --
+// which is the same algebra in about half the multiply-adds of the node-by-node form (the
+// two differ only in rounding).  load(o) returns node o's {v, m}; the caller scales C by
+// 4 inv_dx once at the end (the reference scales every term).
+template <int D, class Load>
+__device__ __forceinline__ void g2p_gather(const Load &load, const float fx[D],
+                                           const float w[3][D], float v[D], Mat<D> &C) {
+  float wl[3], wld[3];  // last axis: weight, and weight times the node's distance
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    wgv[d] = weight * gv[d];
-    v[d] += wgv[d];
+  for (int k = 0; k < 3; ++k) {
+    wl[k] = w[k][D - 1];
+    wld[k] = w[k][D - 1] * ((float)k - fx[D - 1]);
   }
 #pragma unroll
-  for (int i = 0; i < D; ++i)
+  for (int i = 0; i < 3; ++i) {
+    float a[3] = {0.0f, 0.0f, 0.0f}, bl[3] = {0.0f, 0.0f, 0.0f}, bm[3] = {0.0f, 0.0f, 0.0f};
+    if constexpr (D == 3) {
 #pragma unroll
-    for (int j = 0; j < D; ++j) C.a[i][j] += wgv[i] * ((float)oo[j] - fx[j]);
+      for (int j = 0; j < 3; ++j) {
+        float aj[3] = {0.0f, 0.0f, 0.0f}, bj[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float4 g = load(i * 9 + j * 3 + k);
+          const float gv[3] = {g.x, g.y, g.z};
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            aj[c] += wl[k] * gv[c];
+            bj[c] += wld[k] * gv[c];
+          }
+        }
+        const float wm = w[j][1], wmd = w[j][1] * ((float)j - fx[1]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          a[c] += wm * aj[c];
+          bm[c] += wmd * aj[c];
+          bl[c] += wm * bj[c];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float4 g = load(i * 3 + j);
+        const float gv[2] = {g.x, g.y};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          a[c] += wl[j] * gv[c];
+          bl[c] += wld[j] * gv[c];
+        }
+      }
+    }
+    const float wf = w[i][0], wfd = w[i][0] * ((float)i - fx[0]);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      v[c] += wf * a[c];
+      C.a[c][0] += wfd * a[c];
+      if constexpr (D == 3) C.a[c][1] += wf * bm[c];
+      C.a[c][D - 1] += wf * bl[c];
+    }
+  }
 }
 
 template <int D>
@@ -459,20 +514,17 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
 #pragma unroll
           for (int jj = 0; jj < D; ++jj) C.a[i][jj] = 0.0f;
         if (fast) {
-#pragma unroll
-          for (int o = 0; o < S; ++o) g2p_accumulate<D>(o, vt[tb + tile_offset<D>(o)], fx, w, v, C);
-        } else {
+          g2p_gather<D>([&](int o) { return vt[tb + tile_offset<D>(o)]; }, fx, w, v, C);
+        } else {  // outside the tile: straight from V, each node range-checked
           const int64_t f0 = flat_index<D>(base, N);
-#pragma unroll  // constant offsets keep w[][] in registers (and the gathers independent)
-          for (int o = 0; o < S; ++o) {
-            const int64_t f = stencil_flat<D>(f0, o, N);
-            float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (f >= 0 && f < P.nodes)
-              g = __ldg(V + f);
-            else
-              atomicOr(err_now, kErrOutOfRange);
-            g2p_accumulate<D>(o, g, fx, w, v, C);
-          }
+          g2p_gather<D>(
+              [&](int o) {
+                const int64_t f = stencil_flat<D>(f0, o, N);
+                if (f >= 0 && f < P.nodes) return __ldg(V + f);
+                atomicOr(err_now, kErrOutOfRange);
+                return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+              },
+              fx, w, v, C);
         }
         scale_mat<D>(C, P.cscale);
 #pragma unroll
@@ -513,6 +565,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
 #pragma unroll
         for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
         stencil<D>(x, P.inv_dx, base, fx_s, w_s);
+        p2g_terms<D>(fx_s, P.dx, mv, A);  // mv, A now hold q0 and A dx
         fast_s = !chunk;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
@@ -530,7 +583,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
               continue;
             }
             float c[4];
-            p2g_contrib<D>(o, fx_s, w_s, mv, m, A, P.dx, c);
+            p2g_contrib<D>(o, w_s, mv, m, A, c);
             red_add_v4(G + f, c[0], c[1], c[2], c[3]);
           }
           mark_stencil<D>(flags, base, P);
@@ -553,7 +606,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
         for (int o = 0; o < S; ++o) {
           if (act) {
             float c[4];
-            p2g_contrib<D>(o, fx_s, w_s, mv, m, A, P.dx, c);
+            p2g_contrib<D>(o, w_s, mv, m, A, c);
             const int ti = tb_s + tile_offset<D>(o);
             float4 a = mytile[ti];
             a.x += c[0];
