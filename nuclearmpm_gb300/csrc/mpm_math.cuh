@@ -21,6 +21,15 @@
 
 namespace mpm {
 
+// a / b with the fast reciprocal on the device (no special-value path; |b| < 2^126)
+MPM_HD float fast_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
 MPM_HD float rsqrt_(float x) {
 #ifdef __CUDA_ARCH__
   return rsqrtf(x);
@@ -147,8 +156,10 @@ template <int P, int Q, bool kExact>
 MPM_HD void jacobi_rotate(float S[3][3], float V[3][3]) {
   const float app = S[P][P], aqq = S[Q][Q], apq = S[P][Q];
   if (apq == 0.0f) return;
-  const float tau = (aqq - app) / (2.0f * apq);
-  const float t = copysignf(1.0f, tau) / (fabsf(tau) + sqrtf(1.0f + tau * tau));
+  // tau and t only choose the angle; c and s below are formed from t consistently, so the
+  // fast reciprocal does here (|tau| -> inf gives t = 0, the identity)
+  const float tau = fast_div(aqq - app, 2.0f * apq);
+  const float t = fast_div(copysignf(1.0f, tau), fabsf(tau) + sqrtf(1.0f + tau * tau));
   const float c = kExact ? 1.0f / sqrtf(1.0f + t * t) : rsqrt_(1.0f + t * t), s = t * c;
   // S <- Q^T S Q with Q = I except Q_pp = c, Q_pq = s, Q_qp = -s, Q_qq = c
 #pragma unroll
