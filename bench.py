@@ -149,8 +149,21 @@ def host_cpu() -> dict:
     except OSError:
         pass
     import platform
+    arm_parts = {"0xd4f": "Arm Neoverse-V2 (Grace)", "0xd40": "Arm Neoverse-V1",
+                 "0xd0c": "Arm Neoverse-N1", "0xd8e": "Arm Neoverse-N3"}
+    if model in arm_parts:
+        model = arm_parts[model]
     return {"nproc": os.cpu_count(), "cpu": model or platform.processor() or platform.machine(),
             "arch": platform.machine()}
+
+
+def tune_plain(state: dict, model: int, res: int, device: int) -> dict:
+    """The project's autotuner (nuclearmpm_gb300.autotune) on this workload: re-sort interval
+    and thin-block threshold, from short timed runs of the simulation itself."""
+    from nuclearmpm_gb300 import MPMSimulation, autotune
+    return autotune.tune(lambda **o: MPMSimulation(dict(state), model, res=res, device=device, **o),
+                         key=None, candidates=autotune.PLAIN_CANDIDATES, steps=16, repeats=2,
+                         cache_path=None)
 
 
 def make_scene():
@@ -314,7 +327,8 @@ def run_snow(device: int, steps: int = 100) -> dict:
     from nuclearmpm_gb300 import MPMSimulation, scenes
     sc = make_scene()
     n = len(sc["x"])
-    sim = MPMSimulation(dict(sc), scenes.SNOW, res=128, profile=True, device=device)
+    tuned = tune_plain(sc, scenes.SNOW, 128, device)
+    sim = MPMSimulation(dict(sc), scenes.SNOW, res=128, profile=True, device=device, **tuned)
     sim.advance(10)
     sim.profile_reset()
     st = torch.cuda.ExternalStream(sim.stream)
@@ -334,7 +348,7 @@ def run_snow(device: int, steps: int = 100) -> dict:
     return {"value": n * steps / t, "unit": UNIT, "particles": n, "steps": steps,
             "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
             "g2p2g_avg_ms": g_ms, "g2p2g_gbs": alg / (g_ms / 1e3) / 1e9,
-            "g2p2g_frac": alg / (g_ms / 1e3) / 1e9 / peak, "peak_source": kind,
+            "g2p2g_frac": alg / (g_ms / 1e3) / 1e9 / peak, "peak_source": kind, "tuned": tuned,
             "config": "3D snow (MaterialModel::kSnow), the 1M-particle scene above, 128^3 grid, "
                       "dt 1e-4, reference physics"}
 
@@ -436,7 +450,8 @@ def run_ours(args):
 
     scene = make_scene()
     n = len(scene["x"])
-    sim = MPMSimulation(dict(scene), scenes.JELLY, res=128, device=local, profile=True)
+    tuned = tune_plain(scene, scenes.JELLY, 128, local)
+    sim = MPMSimulation(dict(scene), scenes.JELLY, res=128, device=local, profile=True, **tuned)
     stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
 
     # ---- device-resident throughput ---------------------------------------------------
@@ -535,7 +550,7 @@ def run_ours(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded scene with the workload's shapes and distributions)",
-                "config": dict(WORKLOAD, parallelism=f"replicas x{world}"),
+                "config": dict(WORKLOAD, parallelism=f"replicas x{world}", tuned=tuned),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
                 "adjoint": adjoint, "mixed": mixed, "snow": snow, "readme": readme,
                 "gpu_launches": launches_total, "clocks": clk}
