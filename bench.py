@@ -171,16 +171,17 @@ def make_scene():
     return scenes.jelly_cubes_3d(seed=0, res=128)
 
 
-def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float):
-    """The CPU oracle (-Ofast build, one thread) on the workload: `warmup` untimed steps, then
-    `steps` timed steps, on the full scene if that fits `budget_s`, else on the first
-    particles of the scene (same per-particle work) so that it does."""
+def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float, threads: int = 1):
+    """The CPU oracle (-Ofast build; one thread, or `threads` for the multi-threaded port of
+    oracle/nclr_oracle_mt.h) on the workload: `warmup` untimed steps, then `steps` timed
+    steps, on the full scene if that fits `budget_s`, else on the first particles of the scene
+    (same per-particle work) so that it does."""
     from oracle import pyoracle as po
     from nuclearmpm_gb300 import scenes
     n = len(scene["x"])
     t0 = time.perf_counter()
     state, _, st, _ = po.advance(scene, dim=3, model=scenes.JELLY, res=128, steps=1, fast=True,
-                                 want_grid=False)
+                                 want_grid=False, threads=threads)
     one = time.perf_counter() - t0
     total = max(1, steps + max(warmup - 1, 0))
     frac = min(1.0, budget_s / max(one * total, 1e-9))
@@ -189,10 +190,11 @@ def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float):
               for k, v in state.items()}
     if warmup > 1:
         sample, _, st, _ = po.advance(sample, dim=3, model=scenes.JELLY, res=128,
-                                      steps=warmup - 1, fast=True, want_grid=False)
+                                      steps=warmup - 1, fast=True, want_grid=False,
+                                      threads=threads)
     t0 = time.perf_counter()
     _, _, st, _ = po.advance(sample, dim=3, model=scenes.JELLY, res=128, steps=steps, fast=True,
-                             want_grid=False)
+                             want_grid=False, threads=threads)
     dt = time.perf_counter() - t0
     if st != 0:
         raise RuntimeError("CPU oracle reported an out-of-range stencil")
@@ -538,12 +540,19 @@ def run_ours(args):
     if not args.no_readme and rank == 0:
         readme = run_readme(local)
 
-    cpu = None
+    cpu = cpu_mt = None
     if rank == 0 and not args.no_cpu_baseline:
         v, desc = cpu_reference_run(scene, steps=args.cpu_steps, warmup=1, budget_s=20.0)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
                "sample": desc + "; the reference's step restated in C++ (oracle/, -Ofast like "
                                 "the reference build), one thread"}
+        nt = os.cpu_count() or 1
+        v, desc = cpu_reference_run(scene, steps=args.cpu_steps, warmup=1, budget_s=15.0,
+                                    threads=nt)
+        cpu_mt = {"value": v, "unit": UNIT, "cores": nt, "kind": "port",
+                  "sample": desc + f"; the same port on {nt} threads, race-free (P2G over two "
+                                   "colours of x-slabs, oracle/nclr_oracle_mt.h); the "
+                                   "reference itself runs on one thread"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -551,7 +560,8 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded scene with the workload's shapes and distributions)",
                 "config": dict(WORKLOAD, parallelism=f"replicas x{world}", tuned=tuned),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
+                "roofline": roofline, "cpu_baseline": cpu, "cpu_baseline_mt": cpu_mt,
+                "e2e": e2e, "batched": batched,
                 "adjoint": adjoint, "mixed": mixed, "snow": snow, "readme": readme,
                 "gpu_launches": launches_total, "clocks": clk}
         print(json.dumps(line), flush=True)

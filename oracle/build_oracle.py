@@ -22,7 +22,7 @@ REFERENCE_SRC = "/root/reference/src"
 
 def _cmds():
     cxx = os.environ.get("CXX", "g++")
-    common = [cxx, "-std=c++17", "-fPIC", "-shared", "-w"]
+    common = [cxx, "-std=c++17", "-fPIC", "-shared", "-w", "-pthread"]
     src = os.path.join(HERE, "oracle_capi.cpp")
     out = [
         (common + ["-O2", "-ffp-contract=off", src, "-o",

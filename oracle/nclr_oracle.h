@@ -26,6 +26,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <limits>
@@ -308,9 +309,9 @@ struct Cell {
   T mass;
 };
 
-struct Counters {
-  int64_t inverted_svd = 0;  // G2P SVDs of an inverted element (det F_hat < 0)
-  int64_t out_of_range = 0;  // node indices outside the grid (reference: vector::at throws)
+struct Counters {  // atomic: the multi-threaded baseline (nclr_oracle_mt.h) shares them
+  std::atomic<int64_t> inverted_svd{0};  // G2P SVDs of an inverted element (det F_hat < 0)
+  std::atomic<int64_t> out_of_range{0};  // node indices outside the grid (vector::at throws)
 };
 
 // MPMSimulation<dim>, src/nclr.h:63-384.
@@ -426,110 +427,119 @@ class Simulation {
   // p2g + compute_fused_momentum, src/nclr.h:104-165.
   void p2g() {
     cells_.assign((size_t)num_nodes(), Cell<T, D>{Vec<T, D>::constant(T(0)), T(0)});
-    for (auto &p : particles_) {
-      int base[D];
-      Vec<T, D> fx, w[3];
-      kernel(p.x, base, fx, w);
-      const Mat<T, D> A = affine(p);
-      Vec<T, D> mv;
-      for (int d = 0; d < D; ++d) mv[d] = p.v[d] * p.mass;
-      int o[3] = {0, 0, 0};
-      for (o[0] = 0; o[0] < 3; ++o[0])
-        for (o[1] = 0; o[1] < 3; ++o[1])
-          for (o[2] = 0; o[2] < (D == 3 ? 3 : 1); ++o[2]) {
-            Vec<T, D> dpos;
-            for (int d = 0; d < D; ++d) dpos[d] = ((T)o[d] - fx[d]) * dx_;
-            T weight = w[o[0]][0] * w[o[1]][1];
-            if constexpr (D == 3) weight = weight * w[o[2]][2];
-            Cell<T, D> &cell = at(flat(base, o));
-            const Vec<T, D> Ad = mul(A, dpos);
-            for (int d = 0; d < D; ++d) cell.velocity[d] += weight * (mv[d] + Ad[d]);
-            cell.mass += weight * p.mass;
-          }
-    }
+    for (auto &p : particles_) p2g_particle(p);
+  }
+
+  // One particle's scatter of p2g (the loop body of src/nclr.h:111-165).
+  void p2g_particle(const Particle<T, D> &p) {
+    int base[D];
+    Vec<T, D> fx, w[3];
+    kernel(p.x, base, fx, w);
+    const Mat<T, D> A = affine(p);
+    Vec<T, D> mv;
+    for (int d = 0; d < D; ++d) mv[d] = p.v[d] * p.mass;
+    int o[3] = {0, 0, 0};
+    for (o[0] = 0; o[0] < 3; ++o[0])
+      for (o[1] = 0; o[1] < 3; ++o[1])
+        for (o[2] = 0; o[2] < (D == 3 ? 3 : 1); ++o[2]) {
+          Vec<T, D> dpos;
+          for (int d = 0; d < D; ++d) dpos[d] = ((T)o[d] - fx[d]) * dx_;
+          T weight = w[o[0]][0] * w[o[1]][1];
+          if constexpr (D == 3) weight = weight * w[o[2]][2];
+          Cell<T, D> &cell = at(flat(base, o));
+          const Vec<T, D> Ad = mul(A, dpos);
+          for (int d = 0; d < D; ++d) cell.velocity[d] += weight * (mv[d] + Ad[d]);
+          cell.mass += weight * p.mass;
+        }
   }
 
   // grid_op + grid_normalization + sticky_boundary, src/nclr.h:263-310.
   void grid_op() {
+    const int64_t total = num_nodes();
+    for (int64_t index = 0; index < total; ++index) grid_node(index);
+  }
+
+  // One node of grid_op (the loop body of src/nclr.h:264-309).
+  void grid_node(int64_t index) {
     // allowed_velocity = dx*0.9/dt evaluated in double, stored in the scalar (src/nclr.h:285)
     const T allowed = (T)((double)dx_ * 0.9 / (double)dt_);
     const int N = res_ + 1;
-    const int64_t total = num_nodes();
-    for (int64_t index = 0; index < total; ++index) {
-      int idx[D];
-      int64_t rem = index;
-      for (int d = D - 1; d >= 0; --d) {
-        idx[d] = (int)(rem % N);
-        rem /= N;
-      }
-      Cell<T, D> &g = cells_[index];
-      if (g.mass > T(0)) {
-        for (int d = 0; d < D; ++d) g.velocity[d] = g.velocity[d] / g.mass;
-        g.velocity[1] += dt_ * gravity_;
-        for (int d = 0; d < D; ++d) g.velocity[d] = std::clamp(g.velocity[d], -allowed, allowed);
-      }
-      for (int d = 0; d < D; ++d) {
-        if ((idx[d] < 3 && g.velocity[d] < T(0)) || (idx[d] >= N - 3 && g.velocity[d] > T(0))) {
-          g.velocity = Vec<T, D>::constant(T(0));
-          g.mass = T(0);
-        }
+    int idx[D];
+    int64_t rem = index;
+    for (int d = D - 1; d >= 0; --d) {
+      idx[d] = (int)(rem % N);
+      rem /= N;
+    }
+    Cell<T, D> &g = cells_[index];
+    if (g.mass > T(0)) {
+      for (int d = 0; d < D; ++d) g.velocity[d] = g.velocity[d] / g.mass;
+      g.velocity[1] += dt_ * gravity_;
+      for (int d = 0; d < D; ++d) g.velocity[d] = std::clamp(g.velocity[d], -allowed, allowed);
+    }
+    for (int d = 0; d < D; ++d) {
+      if ((idx[d] < 3 && g.velocity[d] < T(0)) || (idx[d] >= N - 3 && g.velocity[d] > T(0))) {
+        g.velocity = Vec<T, D>::constant(T(0));
+        g.mass = T(0);
       }
     }
   }
 
   // g2p, src/nclr.h:167-261.
   void g2p() {
+    for (auto &p : particles_) g2p_particle(p);
+  }
+
+  // One particle of g2p (the loop body of src/nclr.h:168-260).
+  void g2p_particle(Particle<T, D> &p) {
     const Mat<T, D> I = diag_of<T, D>(T(1), mode_);
     const T cscale = T(4) * inv_dx_;
-    for (auto &p : particles_) {
-      int base[D];
-      Vec<T, D> fx, w[3];
-      kernel(p.x, base, fx, w);
-      p.C = Mat<T, D>::constant(T(0));
-      p.v = Vec<T, D>::constant(T(0));
-      int o[3] = {0, 0, 0};
-      for (o[0] = 0; o[0] < 3; ++o[0])
-        for (o[1] = 0; o[1] < 3; ++o[1])
-          for (o[2] = 0; o[2] < (D == 3 ? 3 : 1); ++o[2]) {
-            Vec<T, D> dpos;
-            for (int d = 0; d < D; ++d) dpos[d] = (T)o[d] - fx[d];
-            const Vec<T, D> gv = at(flat(base, o)).velocity;
-            T weight = w[o[0]][0] * w[o[1]][1];
-            if constexpr (D == 3) weight = weight * w[o[2]][2];
-            Vec<T, D> wgv;
-            for (int d = 0; d < D; ++d) {
-              wgv[d] = weight * gv[d];
-              p.v[d] += wgv[d];
-            }
-            for (int i = 0; i < D; ++i)
-              for (int j = 0; j < D; ++j) p.C(i, j) += (cscale * wgv[i]) * dpos[j];
+    int base[D];
+    Vec<T, D> fx, w[3];
+    kernel(p.x, base, fx, w);
+    p.C = Mat<T, D>::constant(T(0));
+    p.v = Vec<T, D>::constant(T(0));
+    int o[3] = {0, 0, 0};
+    for (o[0] = 0; o[0] < 3; ++o[0])
+      for (o[1] = 0; o[1] < 3; ++o[1])
+        for (o[2] = 0; o[2] < (D == 3 ? 3 : 1); ++o[2]) {
+          Vec<T, D> dpos;
+          for (int d = 0; d < D; ++d) dpos[d] = (T)o[d] - fx[d];
+          const Vec<T, D> gv = at(flat(base, o)).velocity;
+          T weight = w[o[0]][0] * w[o[1]][1];
+          if constexpr (D == 3) weight = weight * w[o[2]][2];
+          Vec<T, D> wgv;
+          for (int d = 0; d < D; ++d) {
+            wgv[d] = weight * gv[d];
+            p.v[d] += wgv[d];
           }
-      for (int d = 0; d < D; ++d) p.x[d] += dt_ * p.v[d];
-      Mat<T, D> M;
-      for (int i = 0; i < D; ++i)
-        for (int j = 0; j < D; ++j) M(i, j) = I(i, j) + dt_ * p.C(i, j);
-      Mat<T, D> Fh = mul(M, p.F);
-      const Model model = model_of(p);
-      if (model == Model::kJelly) {
-        p.F = Fh;
-        continue;
-      }
-      Mat<T, D> U, sig, V;
-      nclr_svd<T, D>(Fh, U, sig, V, mode_);
-      if (det(Fh) < T(0)) ++counters.inverted_svd;  // the 2D sign-fix ambiguity only bites here
-      if (model == Model::kSnow) {
-        for (int d = 0; d < D; ++d)
-          sig(d, d) = std::clamp(sig(d, d), T(1.0 - 2.5e-2), T(1.0 + 4.5e-3));
-        const T old_J = det(Fh);
-        Fh = mul(mul(U, sig), transpose(V));
-        p.Jp = std::clamp(p.Jp * old_J / det(Fh), T(0.6), T(20.0));
-        p.F = Fh;
-      } else {  // kLiquid: J accumulated in double, src/nclr.h:253-257
-        double J = 1.0;
-        for (int d = 0; d < D; ++d) J *= (double)sig(d, d);
-        p.F = diag_of<T, D>(T(1.0), mode_);
-        p.F(0, 0) = (T)J;
-      }
+          for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j) p.C(i, j) += (cscale * wgv[i]) * dpos[j];
+        }
+    for (int d = 0; d < D; ++d) p.x[d] += dt_ * p.v[d];
+    Mat<T, D> M;
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j < D; ++j) M(i, j) = I(i, j) + dt_ * p.C(i, j);
+    Mat<T, D> Fh = mul(M, p.F);
+    const Model model = model_of(p);
+    if (model == Model::kJelly) {
+      p.F = Fh;
+      return;
+    }
+    Mat<T, D> U, sig, V;
+    nclr_svd<T, D>(Fh, U, sig, V, mode_);
+    if (det(Fh) < T(0)) ++counters.inverted_svd;  // the 2D sign-fix ambiguity only bites here
+    if (model == Model::kSnow) {
+      for (int d = 0; d < D; ++d)
+        sig(d, d) = std::clamp(sig(d, d), T(1.0 - 2.5e-2), T(1.0 + 4.5e-3));
+      const T old_J = det(Fh);
+      Fh = mul(mul(U, sig), transpose(V));
+      p.Jp = std::clamp(p.Jp * old_J / det(Fh), T(0.6), T(20.0));
+      p.F = Fh;
+    } else {  // kLiquid: J accumulated in double, src/nclr.h:253-257
+      double J = 1.0;
+      for (int d = 0; d < D; ++d) J *= (double)sig(d, d);
+      p.F = diag_of<T, D>(T(1.0), mode_);
+      p.F(0, 0) = (T)J;
     }
   }
 };

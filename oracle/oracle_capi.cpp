@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "nclr_adjoint.h"
+#include "nclr_oracle_mt.h"
 #include "nclr_oracle.h"
 
 using namespace oracle;
@@ -20,7 +21,7 @@ template <typename T, int D>
 int run(int physics, int64_t n, double *x, double *v, double *F, double *C, double *Jp,
         const double *mass, const double *volume, int model, int res, double dt, double E,
         double nu, double gravity, int nsteps, double *grid_vel, double *grid_mass,
-        int64_t *counters, const uint8_t *material) {
+        int64_t *counters, const uint8_t *material, int threads = 1) {
   std::vector<Particle<T, D>> ps((size_t)n);
   for (int64_t p = 0; p < n; ++p) {
     auto &q = ps[(size_t)p];
@@ -42,7 +43,12 @@ int run(int physics, int64_t n, double *x, double *v, double *F, double *C, doub
                        (Physics)physics);
   int status = 0;
   try {
-    for (int s = 0; s < nsteps; ++s) sim.advance();
+    for (int s = 0; s < nsteps; ++s) {
+      if (threads > 1)
+        advance_threads(sim, threads);
+      else
+        sim.advance();
+    }
   } catch (const std::out_of_range &) {
     status = 2;
   }
@@ -205,6 +211,27 @@ int oracle_advance(int dim, int fp64, int physics, int64_t n, double *x, double 
 #define ORACLE_RUN(T, D)                                                                   \
   return run<T, D>(physics, n, x, v, F, C, Jp, mass, volume, model, res, dt, E, nu, gravity, \
                    nsteps, grid_vel, grid_mass, counters, material)
+  if (dim == 2) {
+    if (fp64) ORACLE_RUN(double, 2);
+    ORACLE_RUN(float, 2);
+  }
+  if (fp64) ORACLE_RUN(double, 3);
+  ORACLE_RUN(float, 3);
+#undef ORACLE_RUN
+}
+
+// oracle_advance on `threads` host threads (nclr_oracle_mt.h): the multi-threaded CPU
+// baseline.  Same arguments and results up to the FP32 summation order of the grid.
+int oracle_advance_threads(int dim, int fp64, int physics, int64_t n, double *x, double *v,
+                           double *F, double *C, double *Jp, const double *mass,
+                           const double *volume, int model, int res, double dt, double E,
+                           double nu, double gravity, int nsteps, double *grid_vel,
+                           double *grid_mass, int64_t *counters, const uint8_t *material,
+                           int threads) {
+  if (n < 0 || res < 1 || (dim != 2 && dim != 3) || model < 0 || model > 2 || threads < 1) return 1;
+#define ORACLE_RUN(T, D)                                                                   \
+  return run<T, D>(physics, n, x, v, F, C, Jp, mass, volume, model, res, dt, E, nu, gravity, \
+                   nsteps, grid_vel, grid_mass, counters, material, threads)
   if (dim == 2) {
     if (fp64) ORACLE_RUN(double, 2);
     ORACLE_RUN(float, 2);

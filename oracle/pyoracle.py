@@ -37,6 +37,8 @@ def _load(name: str, sub: str) -> ctypes.CDLL:
                                            ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp,
                                            _dp, _ip, ctypes.c_void_p]
+            lib.oracle_advance_threads.restype = ctypes.c_int
+            lib.oracle_advance_threads.argtypes = lib.oracle_advance.argtypes + [ctypes.c_int]
             lib.oracle_svd.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp]
             lib.oracle_polar.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]
             lib.oracle_linspaced.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float,
@@ -85,11 +87,13 @@ def _prep(state: dict, dim: int):
 def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-4,
             E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, steps: int = 1,
             fp64: bool = False, physics: int = REFERENCE, fast: bool = False,
-            want_grid: bool = True, material=None):
+            want_grid: bool = True, material=None, threads: int = 1):
     """Runs `steps` reference steps on a copy of `state`; returns (state, grid, status, counters).
 
     grid = (velocity (nodes, dim), mass (nodes,)) of the last step, post grid update.
     status 0 = ok, 2 = a grid index left the grid (the reference throws std::out_of_range).
+    threads > 1 runs the multi-threaded baseline (nclr_oracle_mt.h): the same step up to the
+    FP32 summation order of the grid.
     """
     n, s = _prep(state, dim)
     mat = None if material is None else np.ascontiguousarray(material, dtype=np.uint8)
@@ -97,11 +101,12 @@ def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-
     gv = np.zeros((nodes, dim)) if want_grid else None
     gm = np.zeros((nodes,)) if want_grid else None
     counters = np.zeros(2, dtype=np.int64)
-    st = oracle_lib(fast).oracle_advance(
-        dim, int(fp64), physics, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]), _p(s["Jp"]),
-        _p(s["mass"]), _p(s["volume"]), model, res, dt, E, nu, gravity, steps,
-        _p(gv) if want_grid else None, _p(gm) if want_grid else None,
-        counters.ctypes.data_as(_ip), mat.ctypes.data if mat is not None else None)
+    args = (dim, int(fp64), physics, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]),
+            _p(s["Jp"]), _p(s["mass"]), _p(s["volume"]), model, res, dt, E, nu, gravity, steps,
+            _p(gv) if want_grid else None, _p(gm) if want_grid else None,
+            counters.ctypes.data_as(_ip), mat.ctypes.data if mat is not None else None)
+    lib = oracle_lib(fast)
+    st = lib.oracle_advance_threads(*args, threads) if threads > 1 else lib.oracle_advance(*args)
     return s, ((gv, gm) if want_grid else None), st, counters
 
 

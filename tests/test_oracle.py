@@ -3,7 +3,7 @@ code, and checked against the analytic invariants of the MLS-MPM step."""
 import numpy as np
 import pytest
 
-from conftest import FIELDS, field_err, golden_names, load_golden, state_at
+from conftest import DRIFT, FIELDS, field_err, golden_names, load_golden, state_at
 from nuclearmpm_gb300 import scenes
 
 # Drift bound over 100 steps (oracle FP32 vs the reference's own FP32 run): the two differ
@@ -186,4 +186,26 @@ def test_out_of_range_is_reported(oracle):
     vector::at (src/nclr.h:163); the oracle reports status 2."""
     s = scenes.particles(np.array([[0.5, 0.5], [-0.2, 0.5]], dtype=np.float32))
     _, _, status, counters = oracle.advance(s, dim=2, model=scenes.JELLY, steps=1)
+    assert status == 2 and counters[1] >= 1
+
+
+@pytest.mark.parametrize("name", ["readme_snow", "block3d_jelly", "block3d_snow"])
+def test_threaded_baseline_matches_serial_oracle(oracle, name):
+    """The multi-threaded CPU baseline (oracle/nclr_oracle_mt.h: P2G over two colours of
+    x-slabs, G2P and the grid update split by range) is the serial step up to the FP32
+    summation order of the grid."""
+    z, state, params, steps = load_golden(name)
+    kw = dict(dim=params["dim"], model=params["model"], res=params["res"], dt=params["dt"],
+              E=params["E"], nu=params["nu"], gravity=params["gravity"], steps=steps[0] + 4)
+    a, ga, sa, _ = oracle.advance(state, **kw)
+    b, gb, sb, _ = oracle.advance(state, threads=4, **kw)
+    assert sa == sb == 0
+    for f in FIELDS:  # summation order, amplified over the steps like any drift
+        assert field_err(b[f], a[f], f) <= DRIFT[f], f
+    assert field_err(gb[1], ga[1], "grid_m") <= 1e-4
+
+
+def test_threaded_baseline_reports_out_of_range(oracle):
+    s = scenes.particles(np.array([[0.5, 0.5], [-0.2, 0.5]] * 40, dtype=np.float32))
+    _, _, status, counters = oracle.advance(s, dim=2, model=scenes.JELLY, steps=1, threads=3)
     assert status == 2 and counters[1] >= 1
