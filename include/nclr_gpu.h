@@ -71,6 +71,11 @@ typedef struct nclr_options {
                               into the grid directly instead of through a shared-memory tile;
                               0 = never, -1 = the default for the dimension (default -1);
                               single simulations only, batches ignore it */
+  int small_scene_max;     /* single simulations of at most this many particles run all the
+                              steps of an advance() call in one cooperative kernel launch
+                              (reference order p2g / grid_op / g2p, grid-wide barriers)
+                              instead of two launches per step; 0 = never, -1 = the default
+                              (default -1) */
 } nclr_options;
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid

@@ -26,7 +26,7 @@
 namespace mpm {
 
 enum : int { kSnow = 0, kJelly = 1, kLiquid = 2 };
-enum : int { kErrOutOfRange = 1 };
+enum : int { kErrOutOfRange = 1, kErrBarrier = 2 };  // error flag bits
 
 // Block tiling of the grid (see the layout note above).  Particles are sorted by block and,
 // inside a block, stored cell by cell in rounds (the first particle of every cell in x-major

@@ -857,6 +857,142 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
 }
 
 // ---------------------------------------------------------------------------------------
+// Small scenes: all k steps in one cooperative launch, in the reference's order -- p2g,
+// grid_op, g2p (src/nclr.h:80-84) -- one particle per thread straight from global memory
+// (the grid of a small scene stays in L2), with a grid-wide barrier after the P2G and after
+// the grid update.  A thread keeps the same particles in every phase, so only V and G
+// cross threads; they are read through L2 (__ldcg), since other SMs rewrite them during
+// the launch.  Replaces 2 launches per step (whose fixed cost dominates a scene of a few
+// thousand particles) by one per advance() call.
+// ---------------------------------------------------------------------------------------
+constexpr int kSmallThreads = 256;
+constexpr unsigned kBarrierSpins = 1u << 24;  // x ~64 ns: about a second, then an error
+
+// Barrier of all CTAs of a cooperative launch (every CTA is resident): bar[0] counts
+// arrivals, bar[1] is the generation.  A wait that runs out sets kErrBarrier and every CTA
+// returns false (and leaves the kernel); nothing waits without a bound.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();  // this CTA's writes before its arrival
+    int ok = 1;
+    if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+      atomicExch(bar, 0u);  // reset for the next barrier, before the release
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned spins = 0;
+      while (*gen == g) {
+        if (++spins > kBarrierSpins) {
+          atomicOr(err, kErrBarrier);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok && !(*(volatile int *)err & kErrBarrier);
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <int D, bool kRef>
+__global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Params P,
+                                                                    float4 *__restrict__ G,
+                                                                    float4 *__restrict__ V,
+                                                                    int steps, int *err,
+                                                                    unsigned *bar) {
+  constexpr int S = (D == 3) ? 27 : 9;
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int st = s.stride, N = P.N;
+  for (int step = 0; step < steps; ++step) {
+    // ---- p2g (src/nclr.h:104-165) ----
+    for (int p = tid; p < P.n; p += stride) {
+      float x[D], mv[D], fx[D], w[3][D];
+      int base[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) x[d] = s.x[(size_t)d * st + p];
+      const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
+      const float m = s.mass[p];
+      const int material = s.mat ? (int)s.mat[p] : P.model;
+      Mat<D> A = fused_affine<D>(F, polar_R(F), C, s.Jp[p], m, s.vol[p], material, P);
+#pragma unroll
+      for (int d = 0; d < D; ++d) mv[d] = s.v[(size_t)d * st + p] * m;
+      stencil<D>(x, P.inv_dx, base, fx, w);
+      p2g_terms<D>(fx, P.dx, mv, A);
+      const int64_t f0 = flat_index<D>(base, N);
+#pragma unroll
+      for (int o = 0; o < S; ++o) {
+        const int64_t f = stencil_flat<D>(f0, o, N);
+        if (f < 0 || f >= P.nodes) {
+          atomicOr(err, kErrOutOfRange);
+          continue;
+        }
+        float c[4];
+        p2g_contrib<D>(o, w, mv, m, A, c);
+        red_add_v4(G + f, c[0], c[1], c[2], c[3]);
+      }
+    }
+    if (!grid_barrier(bar, err)) return;
+    // ---- grid_op (src/nclr.h:263-310): V = op(G), and G cleared for the next p2g ----
+    for (int64_t i = tid; i < P.nodes; i += stride) {
+      int idx[D];
+      unflatten<D>(i, N, idx);
+      float v[D], m;
+      grid_update<D>(__ldcg(G + i), idx, P, v, m);
+      V[i] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
+      G[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (!grid_barrier(bar, err)) return;
+    // ---- g2p (src/nclr.h:167-261) ----
+    for (int p = tid; p < P.n; p += stride) {
+      float x[D], v[D], fx[D], w[3][D];
+      int base[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        x[d] = s.x[(size_t)d * st + p];
+        v[d] = 0.0f;
+      }
+      Mat<D> C;
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) C.a[i][j] = 0.0f;
+      stencil<D>(x, P.inv_dx, base, fx, w);
+      const int64_t f0 = flat_index<D>(base, N);
+      g2p_gather<D>(
+          [&](int o) {
+            const int64_t f = stencil_flat<D>(f0, o, N);
+            if (f >= 0 && f < P.nodes) return __ldcg(V + f);
+            atomicOr(err, kErrOutOfRange);
+            return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          },
+          fx, w, v, C);
+      scale_mat<D>(C, P.cscale);
+#pragma unroll
+      for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];
+      Mat<D> F = load_mat<D>(s.F, st, p);
+      float Jp = s.Jp[p];
+      update_F<D, kRef>(C, F, Jp, s.mat ? (int)s.mat[p] : P.model, P.dt);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        s.x[(size_t)d * st + p] = x[d];
+        s.v[(size_t)d * st + p] = v[d];
+      }
+      store_mat<D>(s.F, st, p, F);
+      store_mat<D>(s.C, st, p, C);
+      s.Jp[p] = Jp;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------------------
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
@@ -910,6 +1046,26 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
   }
 #undef MPM_G2P2G_B
 #undef MPM_G2P2G
+}
+
+// The small-scene launch: `ctas` CTAs, all resident (cooperative launch), `steps` steps.
+// bar (2 unsigned) must be zero.  Returns the launch error (e.g. too many CTAs).
+template <int D>
+cudaError_t launch_small_steps(const PState &s, const Params &P, float4 *G, float4 *V, int steps,
+                               int *err, unsigned *bar, bool ref, int ctas, cudaStream_t st) {
+  PState sv = s;
+  Params Pv = P;
+  void *args[] = {&sv, &Pv, &G, &V, &steps, &err, &bar};
+  const void *fn = ref ? (const void *)small_steps_kernel<D, true> : (const void *)small_steps_kernel<D, false>;
+  return cudaLaunchCooperativeKernel(fn, dim3((unsigned)ctas), dim3(kSmallThreads), args, 0, st);
+}
+
+template <int D>
+int small_ctas_per_sm(bool ref) {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &n, ref ? small_steps_kernel<D, true> : small_steps_kernel<D, false>, kSmallThreads, 0);
+  return n;
 }
 
 template <int D>
@@ -990,6 +1146,9 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
                                 const int *, const int *, int *, int *, int, bool, int, int,     \
                                 cudaStream_t, const Record &);                                   \
   template int g2p2g_ctas_per_sm<D>();                                                           \
+  template cudaError_t launch_small_steps<D>(const PState &, const Params &, float4 *, float4 *,   \
+                                             int, int *, unsigned *, bool, int, cudaStream_t);  \
+  template int small_ctas_per_sm<D>(bool);                                                       \
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \
                                       cudaStream_t);                                             \

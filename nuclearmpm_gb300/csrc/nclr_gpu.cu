@@ -61,6 +61,9 @@ struct nclr_sim {
   int *moved_h = nullptr;     // pinned copy
   bool sorted_once = false;   // slot_block is valid
   cudaStream_t copy_stream = nullptr;  // host transfers, pipelined field by field
+  unsigned *bar = nullptr;    // the small-scene kernel's grid barrier (2 counters)
+  int small_max = 0;          // particles up to which advance() uses the small-scene kernel
+  int small_ctas = 0;         // its CTAs that fit on the device at once (0: no cooperative launch)
   cudaEvent_t field_ev[5] = {};        // x, v, F, C, Jp ready (staged / imported)
   int *work = nullptr;        // fused kernel's block counter
   int *err_d = nullptr;       // per scene: [2s] this call's steps, [2s+1] the P2G after them
@@ -104,6 +107,10 @@ thread_local std::string g_create_error;
 // than the block's particles gathering and scattering through L2 directly.
 constexpr int kSparseMax3 = 64;
 constexpr int kSparseMax2 = 32;
+// Default small-scene limits (particles): up to them one persistent launch per advance() call
+// beats two launches per step (measured on GB300: 2D up to 64k particles, 3D up to 32k).
+constexpr int kSmallMax2 = 65536;
+constexpr int kSmallMax3 = 32768;
 
 int row_floats(int dim) { return 2 * dim + 2 * dim * dim + 1; }  // x, v, F, C, Jp
 
@@ -400,6 +407,7 @@ void release(nclr_sim *s) {
   cudaFree(s->blocks);
   cudaFree(s->nblocks_active);
   cudaFree(s->sparse);
+  cudaFree(s->bar);
   cudaFree(s->inv);
   cudaFree(s->slot_block);
   cudaFree(s->moved_d);
@@ -536,6 +544,17 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   const size_t nodes = (size_t)node;
   CREATE_TRY(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
   s->g2p2g_ctas = s->sms * (dim == 3 ? mpm::g2p2g_ctas_per_sm<3>() : mpm::g2p2g_ctas_per_sm<2>());
+  {
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
+    const bool ref = s->opt.physics != NCLR_PHYSICS_CORRECTED;
+    s->small_ctas = coop ? s->sms * (dim == 3 ? mpm::small_ctas_per_sm<3>(ref)
+                                             : mpm::small_ctas_per_sm<2>(ref))
+                         : 0;
+    s->small_max = nscenes > 1 ? 0
+                   : s->opt.small_scene_max < 0 ? (dim == 3 ? kSmallMax3 : kSmallMax2)
+                                                : s->opt.small_scene_max;
+  }
   CREATE_TRY(cudaMalloc((void **)&s->scenes_d, sizeof(Scene) * (size_t)nscenes));
   CREATE_TRY(cudaMemcpyAsync(s->scenes_d, s->scenes.data(), sizeof(Scene) * (size_t)nscenes,
                              cudaMemcpyHostToDevice, s->stream));
@@ -560,6 +579,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMalloc((void **)&s->blocks, sizeof(int) * nblk));
   CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, 2 * sizeof(int)));
   CREATE_TRY(cudaMalloc((void **)&s->sparse, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->bar, 2 * sizeof(unsigned)));
   CREATE_TRY(cudaMalloc((void **)&s->inv, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->slot_block, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->moved_d, sizeof(int)));
@@ -744,6 +764,89 @@ nclr_status get_grid_host(nclr_sim *s, int sc, float *velocity, float *mass) {
   return NCLR_OK;
 }
 
+// The steps of nclr_advance on the regular path: block sort, fused G2P2G, graphs.
+nclr_status advance_regular(nclr_sim *s, int64_t nsteps) {
+  if (s->need_sort && s->n > 0) {  // the uploaded particles: sort them (with v and C) first
+    enqueue_sort(s, !s->acc_valid);
+    s->need_sort = false;
+    s->steps_since_sort = 0;
+  }
+  if (!s->acc_valid) {  // the first step's P2G, from the uploaded state
+    std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // discarded with the P2G
+    dispatch_dim(s->dim, [&](auto dc) {
+      constexpr int D = decltype(dc)::value;
+      phase(s, NCLR_PHASE_P2G, 2, [&] {
+        mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
+                                       s->total_blocks, s->sms, s->stream);
+        // the fused kernel's block counter (before a regular step the sweep resets it)
+        cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
+        if (s->n > 0)
+          mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
+                               s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d, 0,
+                               s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
+      });
+    });
+    s->launches += (s->n > 0) ? 2 : 1;
+    s->acc_valid = true;
+  }
+  int64_t left = nsteps;
+  const int64_t chunk = chunk_steps(s);
+  while (left > 0) {
+    const bool sort = sort_due(s);
+    const bool at_boundary = s->opt.sort_interval == 0 || sort;
+    if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left >= chunk) {
+      const int fin = (left == chunk) ? 1 : 0;
+      if (!s->graph[s->cur][fin]) {
+        nclr_status st = capture_graph(s, s->cur, fin != 0);
+        if (st != NCLR_OK) return st;
+      }
+      CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur][fin], s->stream));
+      s->launches += s->graph_launches;
+      if (chunk_sorts(s) & 1) s->cur ^= 1;
+      if (s->opt.sort_interval > 0) s->steps_since_sort = s->opt.sort_interval;
+      left -= chunk;
+      continue;
+    }
+    enqueue_step(s, sort, left == 1);
+    if (sort) s->steps_since_sort = 0;
+    ++s->steps_since_sort;
+    --left;
+  }
+  return NCLR_OK;
+}
+
+// The steps of nclr_advance for a small scene: one cooperative launch per 2^30 steps.
+nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
+  const int ctas = (int)std::min<int64_t>((s->n + mpm::kSmallThreadsPerCta - 1) / mpm::kSmallThreadsPerCta,
+                                          s->small_ctas);
+  std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // a pending P2G is redone
+  if (s->acc_valid)  // drop the regular path's pending P2G: the kernel starts with its own
+    CUDA_TRY(s, cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)s->total_nodes, s->stream));
+  for (int64_t left = nsteps; left > 0;) {
+    const int k = (int)std::min<int64_t>(left, (int64_t)1 << 30);
+    CUDA_TRY(s, cudaMemsetAsync(s->bar, 0, 2 * sizeof(unsigned), s->stream));
+    cudaError_t e = cudaSuccess;
+    dispatch_dim(s->dim, [&](auto dc) {
+      constexpr int D = decltype(dc)::value;
+      phase(s, NCLR_PHASE_G2P2G, 1, [&] {
+        e = mpm::launch_small_steps<D>(s->ps[s->cur], s->P0(), s->G, s->V, k, s->err_d, s->bar,
+                                       s->ref, ctas, s->stream);
+      });
+    });
+    if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("small-scene launch: ") + cudaGetErrorString(e));
+    s->launches += 1;
+    left -= k;
+  }
+  s->acc_valid = false;  // G is clear: the regular path recomputes its P2G if it takes over
+  // V was rewritten everywhere: the next regular sweep visits every block
+  CUDA_TRY(s, cudaMemsetAsync(s->flags, mpm::kFlagVNonzeroBit, (size_t)s->total_blocks, s->stream));
+  return NCLR_OK;
+}
+
+bool small_scene(const nclr_sim *s) {
+  return s->n > 0 && s->n <= s->small_max && s->small_ctas > 0 && s->nscenes == 1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -758,6 +861,7 @@ void nclr_default_options(nclr_options *opt) {
   opt->profile = 0;
   opt->graph_steps = 0;
   opt->sparse_block_max = -1;
+  opt->small_scene_max = -1;
 }
 
 nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
@@ -820,52 +924,8 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
   CUDA_TRY(s, cudaSetDevice(s->device));
   CUDA_TRY(s, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)s->nscenes, s->stream));
   s->launches = 0;
-  if (s->need_sort && s->n > 0) {  // the uploaded particles: sort them (with v and C) first
-    enqueue_sort(s, !s->acc_valid);
-    s->need_sort = false;
-    s->steps_since_sort = 0;
-  }
-  if (!s->acc_valid) {  // the first step's P2G, from the uploaded state
-    std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // discarded with the P2G
-    dispatch_dim(s->dim, [&](auto dc) {
-      constexpr int D = decltype(dc)::value;
-      phase(s, NCLR_PHASE_P2G, 2, [&] {
-        mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
-                                       s->total_blocks, s->sms, s->stream);
-        // the fused kernel's block counter (before a regular step the sweep resets it)
-        cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
-        if (s->n > 0)
-          mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
-                               s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d, 0,
-                               s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
-      });
-    });
-    s->launches += (s->n > 0) ? 2 : 1;
-    s->acc_valid = true;
-  }
-  int64_t left = nsteps;
-  const int64_t chunk = chunk_steps(s);
-  while (left > 0) {
-    const bool sort = sort_due(s);
-    const bool at_boundary = s->opt.sort_interval == 0 || sort;
-    if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left >= chunk) {
-      const int fin = (left == chunk) ? 1 : 0;
-      if (!s->graph[s->cur][fin]) {
-        nclr_status st = capture_graph(s, s->cur, fin != 0);
-        if (st != NCLR_OK) return st;
-      }
-      CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur][fin], s->stream));
-      s->launches += s->graph_launches;
-      if (chunk_sorts(s) & 1) s->cur ^= 1;
-      if (s->opt.sort_interval > 0) s->steps_since_sort = s->opt.sort_interval;
-      left -= chunk;
-      continue;
-    }
-    enqueue_step(s, sort, left == 1);
-    if (sort) s->steps_since_sort = 0;
-    ++s->steps_since_sort;
-    --left;
-  }
+  const nclr_status path = small_scene(s) ? advance_small(s, nsteps) : advance_regular(s, nsteps);
+  if (path != NCLR_OK) return path;
   nclr_status st = check_launch(s, "advance");
   if (st != NCLR_OK) return st;
   s->stepped = true;
@@ -880,6 +940,8 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
     s->scene_err[(size_t)i] = (e & mpm::kErrOutOfRange) ? NCLR_ERR_OUT_OF_RANGE : NCLR_OK;
     if ((e & mpm::kErrOutOfRange) && first < 0) first = i;
   }
+  if (s->err_h[0] & mpm::kErrBarrier)
+    return fail(s, NCLR_ERR_CUDA, "the small-scene kernel's grid barrier ran out of time");
   if (first >= 0)
     return fail(s, NCLR_ERR_OUT_OF_RANGE,
                 "a particle's stencil left the grid (the reference's vector::at throws "

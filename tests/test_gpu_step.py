@@ -40,17 +40,23 @@ def run_gpu(state, params, steps, **kw):
     return out, g
 
 
+# The two step paths of a single simulation: "small" runs every step of a call in one
+# cooperative launch (the default for scenes this size), "tile" the block-sorted fused kernel.
+PATHS = {"small": {}, "tile": {"small_scene_max": 0}}
+
+
+@pytest.mark.parametrize("path", sorted(PATHS))
 @pytest.mark.parametrize("name", golden_names())
-def test_matches_reference_goldens(name):
+def test_matches_reference_goldens(name, path):
     z, state, params, steps = load_golden(name)
     first = steps[0]
-    out, grid = run_gpu(state, params, first)
+    out, grid = run_gpu(state, params, first, **PATHS[path])
     for f in FIELDS:
         assert field_err(out[f], z[f"{f}@{first}"], f) <= ONE_STEP[f], f
     assert field_err(grid.velocity, z["grid_v"], "grid_v") <= GRID_ONE_STEP["grid_v"]
     assert field_err(grid.mass, z["grid_m"], "grid_m") <= GRID_ONE_STEP["grid_m"]
     for k in steps[1:]:
-        out, _ = run_gpu(state, params, k)
+        out, _ = run_gpu(state, params, k, **PATHS[path])
         for f in FIELDS:
             assert field_err(out[f], z[f"{f}@{k}"], f) <= DRIFT[f], (k, f)
 
@@ -78,20 +84,22 @@ def _random_state(rng, dim, n, res, physics):
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("model", [scenes.SNOW, scenes.JELLY, scenes.LIQUID])
 @pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
-@pytest.mark.parametrize("thin", [0, 8, 1 << 30])
+@pytest.mark.parametrize("thin", [-2, 0, 8, 1 << 30])
 def test_one_step_vs_oracle_random(oracle, dim, model, physics, thin):
     """Seeded random states (non-trivial F, C, Jp, mass, volume): one GPU step vs the FP32
     oracle within the one-step bounds, and the FP64 oracle's error reported alongside.  `thin`
-    is the sparse-block threshold: every block through the shared-memory tile (0), about half
-    of them stepped particle by particle (8), all of them particle by particle."""
+    is the sparse-block threshold of the tile path: every block through the shared-memory tile
+    (0), about half of them stepped particle by particle (8), all of them particle by particle;
+    -2 runs the small-scene kernel instead."""
     if dim == 3 and model == scenes.LIQUID and physics == scenes.REFERENCE:
         pytest.skip("3D liquid under the reference physics has F = diag(J,1,0): its polar "
                     "rotation is not unique, so parity there is implementation-defined")
     rng = np.random.default_rng(100 * dim + 10 * model + physics)
     res = 32
     s = _random_state(rng, dim, 2000 if dim == 2 else 4000, res, physics)
+    path = dict(small_scene_max=-1) if thin == -2 else dict(small_scene_max=0, sparse_block_max=thin)
     out, grid = run_gpu(s, dict(model=model, res=res, dt=1e-4, E=1e4, nu=0.2, gravity=-100.0), 1,
-                        physics=physics, sparse_block_max=thin)
+                        physics=physics, **path)
     o32, og, st, _ = oracle.advance(s, dim=dim, model=model, res=res, steps=1, physics=physics)
     o64, og64, _, _ = oracle.advance(s, dim=dim, model=model, res=res, steps=1, physics=physics,
                                      fp64=True)
@@ -107,16 +115,19 @@ def test_one_step_vs_oracle_random(oracle, dim, model, physics, thin):
 
 
 def test_sort_graph_and_threading_options_agree():
-    """Cell sort on/off, graphs on/off, particles-per-thread and the sparse-block threshold
-    change only the summation order: the results agree to FP32 rounding."""
+    """Cell sort on/off, graphs on/off, particles-per-thread, the sparse-block threshold and
+    the small-scene kernel change only the summation order: the results agree to FP32
+    rounding."""
     z, state, params, _ = load_golden("block3d_jelly")
     runs = []
-    for kw in (dict(sort_interval=0, use_graphs=False, particles_per_thread=4),
-               dict(sort_interval=1, use_graphs=True, particles_per_thread=8),
-               dict(sort_interval=3, use_graphs=True, particles_per_thread=16),
-               dict(sort_interval=8, use_graphs=False, particles_per_thread=8),
-               dict(sort_interval=2, sparse_block_max=0),
-               dict(sort_interval=2, sparse_block_max=1 << 30)):
+    tile = dict(small_scene_max=0)  # these options belong to the tile path
+    for kw in (dict(sort_interval=0, use_graphs=False, particles_per_thread=4, **tile),
+               dict(sort_interval=1, use_graphs=True, particles_per_thread=8, **tile),
+               dict(sort_interval=3, use_graphs=True, particles_per_thread=16, **tile),
+               dict(sort_interval=8, use_graphs=False, particles_per_thread=8, **tile),
+               dict(sort_interval=2, sparse_block_max=0, **tile),
+               dict(sort_interval=2, sparse_block_max=1 << 30, **tile),
+               dict(small_scene_max=1 << 30)):
         runs.append(run_gpu(state, params, 20, **kw)[0])
     for r in runs[1:]:
         for f in FIELDS:
@@ -148,20 +159,21 @@ def test_set_and_get_round_trip():
     sim.close()
 
 
-def test_advance_after_set_particles_matches_fresh_simulation():
+@pytest.mark.parametrize("path", sorted(PATHS))
+def test_advance_after_set_particles_matches_fresh_simulation(path):
     """Replacing the state between steps discards the pending particle-to-grid sums: stepping
     on from the new state equals a fresh simulation created from it."""
     z, state, params, steps = load_golden("block3d_snow")
     mid = state_at(z, steps[1])
     kw = dict(res=params["res"], dt=params["dt"], E=params["E"], nu=params["nu"],
               gravity=params["gravity"])
-    a = MPMSimulation(dict(state), params["model"], **kw)
+    a = MPMSimulation(dict(state), params["model"], **kw, **PATHS[path])
     a.advance(5)
     a.set_particles(x=mid["x"], v=mid["v"], F=mid["F"], C=mid["C"], Jp=mid["Jp"])
     a.advance(3)
     pa = a.particles()
     a.close()
-    b = MPMSimulation(dict(mid), params["model"], **kw)
+    b = MPMSimulation(dict(mid), params["model"], **kw, **PATHS[path])
     b.advance(3)
     pb = b.particles()
     b.close()
@@ -187,7 +199,7 @@ def test_pinned_and_pageable_buffers_agree():
               gravity=params["gravity"])
     runs = []
     for pinned in (False, True):
-        sim = MPMSimulation(dict(state), params["model"], **kw)
+        sim = MPMSimulation(dict(state), params["model"], small_scene_max=0, **kw)  # tile path
         sim.advance(4)
         p = sim.particles()
         wrap = (lambda a: _pinned(a).numpy()) if pinned else (lambda a: np.ascontiguousarray(a))
@@ -217,7 +229,7 @@ def test_upload_keeping_positions_matches_fresh_simulation():
     z, state, params, steps = load_golden("block3d_snow")
     kw = dict(res=params["res"], dt=params["dt"], E=params["E"], nu=params["nu"],
               gravity=params["gravity"])
-    a = MPMSimulation(dict(state), params["model"], **kw)
+    a = MPMSimulation(dict(state), params["model"], small_scene_max=0, **kw)  # tile path: the sort
     a.advance(3)
     p = a.particles()
     v = p.v + np.float32(0.01)
@@ -226,7 +238,7 @@ def test_upload_keeping_positions_matches_fresh_simulation():
     pa = a.particles()
     a.close()
     b = MPMSimulation(dict(x=p.x, v=v, F=p.F, C=p.C, Jp=p.Jp, mass=state["mass"],
-                           volume=state["volume"]), params["model"], **kw)
+                           volume=state["volume"]), params["model"], small_scene_max=0, **kw)
     b.advance(2)
     pb = b.particles()
     b.close()
@@ -286,16 +298,18 @@ def test_lame_constants():
     sim.close()
 
 
+@pytest.mark.parametrize("path", sorted(PATHS))
 @pytest.mark.parametrize("physics,steps", [(scenes.CORRECTED, 1), (scenes.CORRECTED, 5),
                                            (scenes.REFERENCE, 1)])
-def test_mixed_liquid_snow_matches_oracle(oracle, physics, steps):
+def test_mixed_liquid_snow_matches_oracle(oracle, physics, steps, path):
     """The mixed-material extension (one material per particle; the reference has one per
     simulation): boxes of liquid and snow in one 3D domain, against the oracle given the same
     per-particle materials."""
     s, mat = scenes.liquid_snow_boxes_3d(seed=3, res=32, boxes=6, total=12_000, physics=physics,
                                          margin=6 / 32)
     out, grid = run_gpu(s, dict(model=scenes.SNOW, res=32, dt=1e-4, E=1e4, nu=0.2,
-                                gravity=-100.0), steps, physics=physics, material=mat)
+                                gravity=-100.0), steps, physics=physics, material=mat,
+                       **PATHS[path])
     o, og, st, _ = oracle.advance(s, dim=3, model=scenes.SNOW, res=32, steps=steps,
                                   physics=physics, material=mat)
     assert st == 0
