@@ -59,7 +59,9 @@ typedef struct nclr_options {
   int physics;             /* NCLR_PHYSICS_* (default REFERENCE) */
   int sort_interval;       /* re-sort particles by grid block every this many steps (0 = only
                               after an upload; default 8) */
-  int p2g_particles_per_thread; /* reserved (ignored) */
+  int p2g_particles_per_thread; /* particles per thread of the small-scene kernel (it launches
+                              ceil(n / (256 * this)) CTAs; default 1); the tile path steps one
+                              particle per thread */
   int device;              /* CUDA device ordinal (default 0) */
   int use_graphs;          /* capture advance() step sequences in CUDA graphs (default 1) */
   int profile;             /* time every kernel phase of advance() with CUDA events on the

@@ -24,6 +24,8 @@ DEFAULT_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32]}
 # single simulations: also the thin-block threshold (particles per block; 0 = every block
 # through the tile); batches ignore it
 PLAIN_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32], "sparse_block_max": [0, 32, 64, 128, 256]}
+# single simulations small enough for the small-scene kernel: its particles per thread
+SMALL_CANDIDATES = {"particles_per_thread": [1, 2, 4]}
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 

@@ -817,8 +817,8 @@ nclr_status advance_regular(nclr_sim *s, int64_t nsteps) {
 
 // The steps of nclr_advance for a small scene: one cooperative launch per 2^30 steps.
 nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
-  const int ctas = (int)std::min<int64_t>((s->n + mpm::kSmallThreadsPerCta - 1) / mpm::kSmallThreadsPerCta,
-                                          s->small_ctas);
+  const int64_t per_cta = (int64_t)mpm::kSmallThreadsPerCta * std::max(1, s->opt.p2g_particles_per_thread);
+  const int ctas = (int)std::min<int64_t>((s->n + per_cta - 1) / per_cta, s->small_ctas);
   std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // a pending P2G is redone
   if (s->acc_valid)  // drop the regular path's pending P2G: the kernel starts with its own
     CUDA_TRY(s, cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)s->total_nodes, s->stream));
@@ -855,7 +855,7 @@ void nclr_default_options(nclr_options *opt) {
   if (!opt) return;
   opt->physics = NCLR_PHYSICS_REFERENCE;
   opt->sort_interval = 8;
-  opt->p2g_particles_per_thread = 8;
+  opt->p2g_particles_per_thread = 1;
   opt->device = 0;
   opt->use_graphs = 1;
   opt->profile = 0;

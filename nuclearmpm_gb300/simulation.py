@@ -137,7 +137,7 @@ class MPMSimulation:
     def __init__(self, particles, model: MaterialModel | int, res: int = 64, dt: float = 1e-4,
                  E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, *, dim: int | None = None,
                  material: np.ndarray | None = None, physics: int = capi.PHYSICS_REFERENCE,
-                 sort_interval: int = 8, particles_per_thread: int = 8, device: int = 0,
+                 sort_interval: int = 8, particles_per_thread: int = 1, device: int = 0,
                  use_graphs: bool = True, profile: bool = False, graph_steps: int = 0,
                  sparse_block_max: int = -1, small_scene_max: int = -1):
         L = capi.lib()

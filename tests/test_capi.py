@@ -28,7 +28,8 @@ def test_every_declared_symbol_is_exported_and_bound():
 
 def test_default_options():
     o = capi.default_options()
-    assert (o.physics, o.sort_interval, o.p2g_particles_per_thread, o.device, o.use_graphs) == (0, 8, 8, 0, 1)
+    assert (o.physics, o.sort_interval, o.p2g_particles_per_thread, o.device, o.use_graphs) == (0, 8, 1, 0, 1)
+    assert (o.sparse_block_max, o.small_scene_max) == (-1, -1)
 
 
 def test_invalid_arguments_are_rejected_before_touching_a_device():

@@ -127,7 +127,8 @@ def test_sort_graph_and_threading_options_agree():
                dict(sort_interval=8, use_graphs=False, particles_per_thread=8, **tile),
                dict(sort_interval=2, sparse_block_max=0, **tile),
                dict(sort_interval=2, sparse_block_max=1 << 30, **tile),
-               dict(small_scene_max=1 << 30)):
+               dict(small_scene_max=1 << 30),
+               dict(small_scene_max=1 << 30, particles_per_thread=3)):
         runs.append(run_gpu(state, params, 20, **kw)[0])
     for r in runs[1:]:
         for f in FIELDS:
