@@ -73,11 +73,13 @@ typedef struct nclr_options {
                               into the grid directly instead of through a shared-memory tile;
                               0 = never, -1 = the default for the dimension (default -1);
                               single simulations only, batches ignore it */
-  int small_scene_max;     /* single simulations of at most this many particles run all the
-                              steps of an advance() call in one cooperative kernel launch
-                              (reference order p2g / grid_op / g2p, grid-wide barriers)
-                              instead of two launches per step; 0 = never, -1 = the default
-                              (default -1) */
+  int small_scene_max;     /* simulations of at most this many particles (per scene) run all
+                              the steps of an advance() call in one cooperative kernel launch
+                              (reference order p2g / grid_op / g2p, grid-wide barriers; a
+                              batch gives each scene its own group of CTAs) instead of two
+                              launches per step; 0 = never, -1 = the default (default -1:
+                              65,536 particles in 2D and 32,768 in 3D for one scene, never for
+                              a batch, where the tile path is faster) */
 } nclr_options;
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid

@@ -38,6 +38,13 @@ template <int D> cudaError_t launch_small_steps(const PState &s, const Params &P
                                                int steps, int *err, unsigned *bar, bool ref, int ctas,
                                                cudaStream_t st);
 template <int D> int small_ctas_per_sm(bool ref);
+// The same for a batch: CTA c works on scene cta_scene[c]; scene s owns CTAs
+// [group_first[s], group_first[s+1]) and the barrier bars[2s..2s+1] (zeroed).
+template <int D> cudaError_t launch_small_batch(const PState &s, const Scene *scenes, const uint16_t *cta_scene,
+                                               const int *group_first, float4 *G, float4 *V, uint8_t *flags,
+                                               int steps, int *err, unsigned *bars, bool ref, int ctas,
+                                               cudaStream_t st);
+template <int D> int small_batch_ctas_per_sm(bool ref);
 constexpr int kSmallThreadsPerCta = 256;
 constexpr uint8_t kFlagVNonzeroBit = 2;  // mpm_step.cuh's kVNonzero: V may be non-zero there
 enum : int { kModeStep = 0, kModeFinalStep = 1, kModeP2GOnly = 2 };  // g2p2g modes

@@ -868,10 +868,10 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
 constexpr int kSmallThreads = 256;
 constexpr unsigned kBarrierSpins = 1u << 24;  // x ~64 ns: about a second, then an error
 
-// Barrier of all CTAs of a cooperative launch (every CTA is resident): bar[0] counts
+// Barrier of `ctas` CTAs of a cooperative launch (every CTA is resident): bar[0] counts
 // arrivals, bar[1] is the generation.  A wait that runs out sets kErrBarrier and every CTA
 // returns false (and leaves the kernel); nothing waits without a bound.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned ctas) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -879,7 +879,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
     const unsigned g = *gen;
     __threadfence();  // this CTA's writes before its arrival
     int ok = 1;
-    if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+    if (atomicAdd(bar, 1u) + 1u == ctas) {
       atomicExch(bar, 0u);  // reset for the next barrier, before the release
       __threadfence();
       atomicAdd(bar + 1, 1u);
@@ -939,7 +939,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
         red_add_v4(G + f, c[0], c[1], c[2], c[3]);
       }
     }
-    if (!grid_barrier(bar, err)) return;
+    if (!grid_barrier(bar, err, gridDim.x)) return;
     // ---- grid_op (src/nclr.h:263-310): V = op(G), and G cleared for the next p2g ----
     for (int64_t i = tid; i < P.nodes; i += stride) {
       int idx[D];
@@ -949,9 +949,153 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
       V[i] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
       G[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    if (!grid_barrier(bar, err)) return;
+    if (!grid_barrier(bar, err, gridDim.x)) return;
     // ---- g2p (src/nclr.h:167-261) ----
     for (int p = tid; p < P.n; p += stride) {
+      float x[D], v[D], fx[D], w[3][D];
+      int base[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        x[d] = s.x[(size_t)d * st + p];
+        v[d] = 0.0f;
+      }
+      Mat<D> C;
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) C.a[i][j] = 0.0f;
+      stencil<D>(x, P.inv_dx, base, fx, w);
+      const int64_t f0 = flat_index<D>(base, N);
+      g2p_gather<D>(
+          [&](int o) {
+            const int64_t f = stencil_flat<D>(f0, o, N);
+            if (f >= 0 && f < P.nodes) return __ldcg(V + f);
+            atomicOr(err, kErrOutOfRange);
+            return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          },
+          fx, w, v, C);
+      scale_mat<D>(C, P.cscale);
+#pragma unroll
+      for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];
+      Mat<D> F = load_mat<D>(s.F, st, p);
+      float Jp = s.Jp[p];
+      update_F<D, kRef>(C, F, Jp, s.mat ? (int)s.mat[p] : P.model, P.dt);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        s.x[(size_t)d * st + p] = x[d];
+        s.v[(size_t)d * st + p] = v[d];
+      }
+      store_mat<D>(s.F, st, p, F);
+      store_mat<D>(s.C, st, p, C);
+      s.Jp[p] = Jp;
+    }
+  }
+}
+
+// The small-scene kernel for a batch: one cooperative launch for every scene, each scene
+// owning a group of CTAs (cta_scene, group_first) with a barrier of its own, so scenes never
+// wait for one another.  The grid update visits the scene's flagged blocks only (the
+// batch's grids are large in total): P2G marks the blocks its stencils touch, and the sweep
+// rolls the flags over as grid_sweep_kernel does, so the tile path finds the usual state.
+template <int D, bool kRef>
+__global__ void __launch_bounds__(kSmallThreads) small_batch_kernel(
+    PState s, const Scene *__restrict__ scenes, const uint16_t *__restrict__ cta_scene,
+    const int *__restrict__ group_first, float4 *__restrict__ Gall, float4 *__restrict__ Vall,
+    uint8_t *__restrict__ flags_all, int steps, int *err_all, unsigned *bars) {
+  constexpr int S = (D == 3) ? 27 : 9;
+  constexpr int BS = Tiling<D>::BS;
+  constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;
+  __shared__ Params sP;
+  __shared__ int64_t s_node_off;
+  __shared__ int s_block_off, s_slot_off, s_first, s_ctas;
+  const int sid = (int)cta_scene[blockIdx.x];
+  if (threadIdx.x == 0) {
+    sP = scenes[sid].P;
+    s_node_off = scenes[sid].node_off;
+    s_block_off = scenes[sid].block_off;
+    s_slot_off = scenes[sid].slot_off;
+    s_first = group_first[sid];
+    s_ctas = group_first[sid + 1] - group_first[sid];
+  }
+  __syncthreads();
+  const Params &P = sP;
+  float4 *__restrict__ G = Gall + s_node_off;
+  float4 *__restrict__ V = Vall + s_node_off;
+  uint8_t *__restrict__ flags = flags_all + s_block_off;
+  int *err = err_all + 2 * sid;
+  unsigned *bar = bars + 2 * sid;
+  const unsigned ctas = (unsigned)s_ctas;
+  const int stride = s_ctas * blockDim.x;
+  const int tid = (blockIdx.x - s_first) * blockDim.x + threadIdx.x;
+  const int warps = s_ctas * (blockDim.x >> 5), warp = tid >> 5, lane = threadIdx.x & 31;
+  const int st = s.stride, N = P.N, p0 = s_slot_off;
+  for (int step = 0; step < steps; ++step) {
+    // ---- p2g (src/nclr.h:104-165), marking the touched blocks ----
+    for (int q = tid; q < P.n; q += stride) {
+      const int p = p0 + q;
+      float x[D], mv[D], fx[D], w[3][D];
+      int base[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) x[d] = s.x[(size_t)d * st + p];
+      const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
+      const float m = s.mass[p];
+      const int material = s.mat ? (int)s.mat[p] : P.model;
+      Mat<D> A = fused_affine<D>(F, polar_R(F), C, s.Jp[p], m, s.vol[p], material, P);
+#pragma unroll
+      for (int d = 0; d < D; ++d) mv[d] = s.v[(size_t)d * st + p] * m;
+      stencil<D>(x, P.inv_dx, base, fx, w);
+      p2g_terms<D>(fx, P.dx, mv, A);
+      const int64_t f0 = flat_index<D>(base, N);
+#pragma unroll
+      for (int o = 0; o < S; ++o) {
+        const int64_t f = stencil_flat<D>(f0, o, N);
+        if (f < 0 || f >= P.nodes) {
+          atomicOr(err, kErrOutOfRange);
+          continue;
+        }
+        float c[4];
+        p2g_contrib<D>(o, w, mv, m, A, c);
+        red_add_v4(G + f, c[0], c[1], c[2], c[3]);
+      }
+      mark_stencil<D>(flags, base, P);
+    }
+    if (!grid_barrier(bar, err, ctas)) return;
+    // ---- grid_op (src/nclr.h:263-310) on the flagged blocks: V = op(G), G = 0 ----
+    for (int b = warp; b < P.nblocks; b += warps) {
+      const uint8_t fl = __ldcg(flags + b);
+      if (!fl) continue;
+      int bc[D];
+      {
+        int r = b;
+#pragma unroll
+        for (int d = D - 1; d >= 0; --d) {
+          bc[d] = (r % P.nb) * BS;
+          r /= P.nb;
+        }
+      }
+      for (int t = lane; t < BN; t += 32) {
+        int idx[D];
+        bool in = true;
+        int r = t;
+#pragma unroll
+        for (int d = D - 1; d >= 0; --d) {
+          idx[d] = bc[d] + r % BS;
+          r /= BS;
+          in &= idx[d] < N;
+        }
+        if (!in) continue;
+        const int64_t f = flat_index<D>(idx, N);
+        float v[D], m;
+        grid_update<D>(__ldcg(G + f), idx, P, v, m);
+        V[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
+        G[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+      if (lane == 0) flags[b] = (fl & kPending) ? kVNonzero : 0;
+    }
+    if (!grid_barrier(bar, err, ctas)) return;
+    // ---- g2p (src/nclr.h:167-261) ----
+    for (int q = tid; q < P.n; q += stride) {
+      const int p = p0 + q;
       float x[D], v[D], fx[D], w[3][D];
       int base[D];
 #pragma unroll
@@ -1061,6 +1205,25 @@ cudaError_t launch_small_steps(const PState &s, const Params &P, float4 *G, floa
 }
 
 template <int D>
+cudaError_t launch_small_batch(const PState &s, const Scene *scenes, const uint16_t *cta_scene,
+                               const int *group_first, float4 *G, float4 *V, uint8_t *flags,
+                               int steps, int *err, unsigned *bars, bool ref, int ctas,
+                               cudaStream_t st) {
+  PState sv = s;
+  void *args[] = {&sv, &scenes, &cta_scene, &group_first, &G, &V, &flags, &steps, &err, &bars};
+  const void *fn = ref ? (const void *)small_batch_kernel<D, true> : (const void *)small_batch_kernel<D, false>;
+  return cudaLaunchCooperativeKernel(fn, dim3((unsigned)ctas), dim3(kSmallThreads), args, 0, st);
+}
+
+template <int D>
+int small_batch_ctas_per_sm(bool ref) {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &n, ref ? small_batch_kernel<D, true> : small_batch_kernel<D, false>, kSmallThreads, 0);
+  return n;
+}
+
+template <int D>
 int small_ctas_per_sm(bool ref) {
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -1149,6 +1312,10 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
   template cudaError_t launch_small_steps<D>(const PState &, const Params &, float4 *, float4 *,   \
                                              int, int *, unsigned *, bool, int, cudaStream_t);  \
   template int small_ctas_per_sm<D>(bool);                                                       \
+  template cudaError_t launch_small_batch<D>(const PState &, const Scene *, const uint16_t *,      \
+                                             const int *, float4 *, float4 *, uint8_t *, int,     \
+                                             int *, unsigned *, bool, int, cudaStream_t);         \
+  template int small_batch_ctas_per_sm<D>(bool);                                                 \
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \
                                       cudaStream_t);                                             \

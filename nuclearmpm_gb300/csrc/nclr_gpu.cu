@@ -61,7 +61,10 @@ struct nclr_sim {
   int *moved_h = nullptr;     // pinned copy
   bool sorted_once = false;   // slot_block is valid
   cudaStream_t copy_stream = nullptr;  // host transfers, pipelined field by field
-  unsigned *bar = nullptr;    // the small-scene kernel's grid barrier (2 counters)
+  unsigned *bar = nullptr;    // the small-scene kernels' barriers (2 counters per scene)
+  uint16_t *cta_scene = nullptr;  // batches: scene of each CTA of the small-scene kernel
+  int *group_first = nullptr;     // batches: first CTA of each scene's group (nscenes + 1)
+  int batch_ctas = 0;             // batches: CTAs of that launch (0: not possible)
   int small_max = 0;          // particles up to which advance() uses the small-scene kernel
   int small_ctas = 0;         // its CTAs that fit on the device at once (0: no cooperative launch)
   cudaEvent_t field_ev[5] = {};        // x, v, F, C, Jp ready (staged / imported)
@@ -408,6 +411,8 @@ void release(nclr_sim *s) {
   cudaFree(s->nblocks_active);
   cudaFree(s->sparse);
   cudaFree(s->bar);
+  cudaFree(s->cta_scene);
+  cudaFree(s->group_first);
   cudaFree(s->inv);
   cudaFree(s->slot_block);
   cudaFree(s->moved_d);
@@ -551,9 +556,53 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
     s->small_ctas = coop ? s->sms * (dim == 3 ? mpm::small_ctas_per_sm<3>(ref)
                                              : mpm::small_ctas_per_sm<2>(ref))
                          : 0;
-    s->small_max = nscenes > 1 ? 0
-                   : s->opt.small_scene_max < 0 ? (dim == 3 ? kSmallMax3 : kSmallMax2)
-                                                : s->opt.small_scene_max;
+    // batches keep the tile path unless asked: their small-scene kernel measured 2.9x slower
+    // on 256 scenes of 1k-64k particles (its P2G scatters through L2 atomics)
+    s->small_max = s->opt.small_scene_max >= 0 ? s->opt.small_scene_max
+                   : nscenes > 1               ? 0
+                   : dim == 3                  ? kSmallMax3
+                                               : kSmallMax2;
+    if (nscenes > 1 && coop) {
+      // A batch on the small-scene kernel: each scene a group of CTAs in proportion to its
+      // particles (at least one), all groups resident at once.
+      const int cap = s->sms * (dim == 3 ? mpm::small_batch_ctas_per_sm<3>(ref)
+                                         : mpm::small_batch_ctas_per_sm<2>(ref));
+      const int64_t per = (int64_t)mpm::kSmallThreadsPerCta * std::max(1, s->opt.p2g_particles_per_thread);
+      std::vector<int64_t> want((size_t)nscenes, 0);
+      int64_t total = 0, busy = 0;
+      for (int i = 0; i < nscenes; ++i) {
+        const int64_t n = descs[i].n;
+        want[(size_t)i] = n > 0 ? (n + per - 1) / per : 0;
+        total += want[(size_t)i];
+        busy += n > 0;
+      }
+      if (busy > 0 && busy <= cap) {
+        std::vector<int> ctas((size_t)nscenes, 0);
+        int64_t sum = 0;
+        for (int i = 0; i < nscenes; ++i) {
+          if (!want[(size_t)i]) continue;
+          ctas[(size_t)i] = (int)std::max<int64_t>(1, total <= cap ? want[(size_t)i]
+                                                                 : want[(size_t)i] * cap / total);
+          sum += ctas[(size_t)i];
+        }
+        while (sum > cap) {  // rounding up the smallest to 1 can overshoot: trim the largest
+          auto it = std::max_element(ctas.begin(), ctas.end());
+          --*it;
+          --sum;
+        }
+        std::vector<int> first((size_t)nscenes + 1, 0);
+        std::vector<uint16_t> owner((size_t)sum);
+        for (int i = 0; i < nscenes; ++i) {
+          first[(size_t)i + 1] = first[(size_t)i] + ctas[(size_t)i];
+          for (int c = first[(size_t)i]; c < first[(size_t)i + 1]; ++c) owner[(size_t)c] = (uint16_t)i;
+        }
+        CREATE_TRY(cudaMalloc((void **)&s->cta_scene, sizeof(uint16_t) * (size_t)sum));
+        CREATE_TRY(cudaMalloc((void **)&s->group_first, sizeof(int) * first.size()));
+        CREATE_TRY(cudaMemcpy(s->cta_scene, owner.data(), sizeof(uint16_t) * (size_t)sum, cudaMemcpyHostToDevice));
+        CREATE_TRY(cudaMemcpy(s->group_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
+        s->batch_ctas = (int)sum;
+      }
+    }
   }
   CREATE_TRY(cudaMalloc((void **)&s->scenes_d, sizeof(Scene) * (size_t)nscenes));
   CREATE_TRY(cudaMemcpyAsync(s->scenes_d, s->scenes.data(), sizeof(Scene) * (size_t)nscenes,
@@ -579,7 +628,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMalloc((void **)&s->blocks, sizeof(int) * nblk));
   CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, 2 * sizeof(int)));
   CREATE_TRY(cudaMalloc((void **)&s->sparse, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
-  CREATE_TRY(cudaMalloc((void **)&s->bar, 2 * sizeof(unsigned)));
+  CREATE_TRY(cudaMalloc((void **)&s->bar, 2 * sizeof(unsigned) * (size_t)nscenes));
   CREATE_TRY(cudaMalloc((void **)&s->inv, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->slot_block, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->moved_d, sizeof(int)));
@@ -817,20 +866,34 @@ nclr_status advance_regular(nclr_sim *s, int64_t nsteps) {
 
 // The steps of nclr_advance for a small scene: one cooperative launch per 2^30 steps.
 nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
+  const bool batch = s->nscenes > 1;
   const int64_t per_cta = (int64_t)mpm::kSmallThreadsPerCta * std::max(1, s->opt.p2g_particles_per_thread);
-  const int ctas = (int)std::min<int64_t>((s->n + per_cta - 1) / per_cta, s->small_ctas);
+  const int ctas = batch ? s->batch_ctas
+                         : (int)std::min<int64_t>((s->n + per_cta - 1) / per_cta, s->small_ctas);
   std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // a pending P2G is redone
-  if (s->acc_valid)  // drop the regular path's pending P2G: the kernel starts with its own
-    CUDA_TRY(s, cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)s->total_nodes, s->stream));
+  if (s->acc_valid) {  // drop the regular path's pending P2G: the kernel starts with its own
+    if (batch) {
+      dispatch_dim(s->dim, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
+                                       s->total_blocks, s->sms, s->stream);
+      });
+    } else {
+      CUDA_TRY(s, cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)s->total_nodes, s->stream));
+    }
+  }
   for (int64_t left = nsteps; left > 0;) {
     const int k = (int)std::min<int64_t>(left, (int64_t)1 << 30);
-    CUDA_TRY(s, cudaMemsetAsync(s->bar, 0, 2 * sizeof(unsigned), s->stream));
+    CUDA_TRY(s, cudaMemsetAsync(s->bar, 0, 2 * sizeof(unsigned) * (size_t)s->nscenes, s->stream));
     cudaError_t e = cudaSuccess;
     dispatch_dim(s->dim, [&](auto dc) {
       constexpr int D = decltype(dc)::value;
       phase(s, NCLR_PHASE_G2P2G, 1, [&] {
-        e = mpm::launch_small_steps<D>(s->ps[s->cur], s->P0(), s->G, s->V, k, s->err_d, s->bar,
-                                       s->ref, ctas, s->stream);
+        e = batch ? mpm::launch_small_batch<D>(s->ps[s->cur], s->scenes_d, s->cta_scene,
+                                               s->group_first, s->G, s->V, s->flags, k, s->err_d,
+                                               s->bar, s->ref, ctas, s->stream)
+                  : mpm::launch_small_steps<D>(s->ps[s->cur], s->P0(), s->G, s->V, k, s->err_d,
+                                               s->bar, s->ref, ctas, s->stream);
       });
     });
     if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("small-scene launch: ") + cudaGetErrorString(e));
@@ -838,13 +901,20 @@ nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
     left -= k;
   }
   s->acc_valid = false;  // G is clear: the regular path recomputes its P2G if it takes over
-  // V was rewritten everywhere: the next regular sweep visits every block
-  CUDA_TRY(s, cudaMemsetAsync(s->flags, mpm::kFlagVNonzeroBit, (size_t)s->total_blocks, s->stream));
+  // one scene: V was rewritten everywhere, so the next regular sweep visits every block (a
+  // batch's kernel kept the flags itself)
+  if (!batch)
+    CUDA_TRY(s, cudaMemsetAsync(s->flags, mpm::kFlagVNonzeroBit, (size_t)s->total_blocks, s->stream));
   return NCLR_OK;
 }
 
 bool small_scene(const nclr_sim *s) {
-  return s->n > 0 && s->n <= s->small_max && s->small_ctas > 0 && s->nscenes == 1;
+  if (s->n <= 0 || s->small_ctas <= 0) return false;
+  if (s->nscenes == 1) return s->n <= s->small_max;
+  if (s->batch_ctas <= 0) return false;
+  for (const auto &sc : s->scenes)
+    if (sc.P.n > s->small_max) return false;
+  return true;
 }
 
 }  // namespace
@@ -940,8 +1010,9 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
     s->scene_err[(size_t)i] = (e & mpm::kErrOutOfRange) ? NCLR_ERR_OUT_OF_RANGE : NCLR_OK;
     if ((e & mpm::kErrOutOfRange) && first < 0) first = i;
   }
-  if (s->err_h[0] & mpm::kErrBarrier)
-    return fail(s, NCLR_ERR_CUDA, "the small-scene kernel's grid barrier ran out of time");
+  for (int i = 0; i < s->nscenes; ++i)
+    if (s->err_h[2 * i] & mpm::kErrBarrier)
+      return fail(s, NCLR_ERR_CUDA, "the small-scene kernel's grid barrier ran out of time");
   if (first >= 0)
     return fail(s, NCLR_ERR_OUT_OF_RANGE,
                 "a particle's stencil left the grid (the reference's vector::at throws "

@@ -312,7 +312,8 @@ class BatchSimulation:
 
     def __init__(self, scenes: list, *, dim: int | None = None,
                  physics: int = capi.PHYSICS_REFERENCE, sort_interval: int = 8, device: int = 0,
-                 use_graphs: bool = True, graph_steps: int = 0, profile: bool = False):
+                 use_graphs: bool = True, graph_steps: int = 0, profile: bool = False,
+                 small_scene_max: int = -1, particles_per_thread: int = 1):
         L = capi.lib()
         if not scenes:
             raise ValueError("a batch needs at least one scene")
@@ -345,7 +346,8 @@ class BatchSimulation:
         self.dim = self.dims[0]
         opt = capi.default_options(physics=physics, sort_interval=sort_interval, device=device,
                                    use_graphs=int(use_graphs), profile=int(profile),
-                                   graph_steps=graph_steps)
+                                   graph_steps=graph_steps, small_scene_max=small_scene_max,
+                                   p2g_particles_per_thread=particles_per_thread)
         h = ctypes.c_void_p()
         capi.check(L.nclr_batch_create(ctypes.byref(h), self.dim, len(scenes), descs,
                                        ctypes.byref(opt)), None)

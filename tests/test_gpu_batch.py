@@ -45,10 +45,17 @@ def alone(sc, steps, physics=scenes.REFERENCE):
     return {f: getattr(p, f) for f in FIELDS}, g
 
 
+# The batch's two step paths: "tile" the block-sorted fused kernel with CUDA graphs (the
+# default), "small" all of a call's steps in one cooperative launch with a group of CTAs per
+# scene (an option).
+PATHS = {"small": {"small_scene_max": 1 << 30}, "tile": {}}
+
+
+@pytest.mark.parametrize("path", sorted(PATHS))
 @pytest.mark.parametrize("dim,physics,steps", [(2, scenes.REFERENCE, 10),
                                                (3, scenes.REFERENCE, 1),
                                                (3, scenes.CORRECTED, 10)])
-def test_batch_matches_scenes_stepped_alone(dim, physics, steps):
+def test_batch_matches_scenes_stepped_alone(dim, physics, steps, path):
     """Ten steps where the physics is well conditioned; under the reference's 3D physics the
     snow scenes clamp a zero singular value every step and their velocities grow towards the
     clip, so two runs that differ only in summation order part after a few steps: one step."""
@@ -56,7 +63,7 @@ def test_batch_matches_scenes_stepped_alone(dim, physics, steps):
     if dim == 3 and physics == scenes.CORRECTED:
         for sc in scs:
             sc["F"] = np.broadcast_to(np.eye(3, dtype=np.float32), sc["F"].shape).copy()
-    batch = BatchSimulation(scs, sort_interval=4, graph_steps=8, physics=physics)
+    batch = BatchSimulation(scs, sort_interval=4, graph_steps=8, physics=physics, **PATHS[path])
     batch.advance(steps)
     tol = TEN_STEPS if steps > 1 else {f: ONE_STEP for f in FIELDS}
     for i, sc in enumerate(scs):
@@ -70,9 +77,10 @@ def test_batch_matches_scenes_stepped_alone(dim, physics, steps):
     batch.close()
 
 
-def test_batch_one_step_matches_oracle(oracle):
+@pytest.mark.parametrize("path", sorted(PATHS))
+def test_batch_one_step_matches_oracle(oracle, path):
     scs = small_batch(seed=7, count=5)
-    batch = BatchSimulation(scs)
+    batch = BatchSimulation(scs, **PATHS[path])
     batch.advance(1)
     for i, sc in enumerate(scs):
         o, og, st, _ = oracle.advance(sc, dim=2, model=sc["model"], res=sc["res"], dt=sc["dt"],
@@ -89,26 +97,34 @@ def test_batch_one_step_matches_oracle(oracle):
 
 def test_batch_graph_of_many_steps_equals_direct_launches():
     scs = small_batch(seed=3, count=4)
-    a = BatchSimulation(scs, graph_steps=20)
+    a = BatchSimulation(scs, graph_steps=20, small_scene_max=0)
     a.advance(20)  # exactly one graph, whose last step is the call's final step
     a.advance(25)
-    b = BatchSimulation(scs, use_graphs=False)
+    b = BatchSimulation(scs, use_graphs=False, small_scene_max=0)
     b.advance(20)
     b.advance(25)
+    c = BatchSimulation(scs, small_scene_max=1 << 30)  # the small-scene kernel
+    c.advance(20)
+    c2 = BatchSimulation(scs, small_scene_max=0)
+    c2.advance(20)
     for i in range(len(scs)):
         pa, pb = a.particles(i), b.particles(i)
         for f in FIELDS:
             assert field_err(pa[f], pb[f], f) <= TEN_STEPS[f], (i, f)
-    a.close()
-    b.close()
+        pc, pc2 = c.particles(i), c2.particles(i)
+        for f in FIELDS:
+            assert field_err(pc[f], pc2[f], f) <= TEN_STEPS[f], (i, f)
+    for sim in (a, b, c, c2):
+        sim.close()
 
 
-def test_batch_scene_set_get_and_error_isolated():
+@pytest.mark.parametrize("path", sorted(PATHS))
+def test_batch_scene_set_get_and_error_isolated(path):
     scs = small_batch(seed=5, count=3)
     bad = dict(scs[1])
     bad["x"] = bad["x"].copy()
     bad["x"][0] = (-0.3, 0.5)  # leaves the grid on the first step
-    batch = BatchSimulation([scs[0], bad, scs[2]])
+    batch = BatchSimulation([scs[0], bad, scs[2]], **PATHS[path])
     with pytest.raises(IndexError):
         batch.advance(1)
     assert batch.status(0) == 0 and batch.status(1) == 2 and batch.status(2) == 0
