@@ -55,6 +55,14 @@ enum { NCLR_SNOW = 0, NCLR_JELLY = 1, NCLR_LIQUID = 2 };
  * NCLR_PHYSICS_CORRECTED uses the true identity and applies the 2D sign fix to column 1. */
 enum { NCLR_PHYSICS_REFERENCE = 0, NCLR_PHYSICS_CORRECTED = 1 };
 
+/* Stress model.  NCLR_STRESS_COROTATED is the reference's fixed-corotated stress
+ * (first_piola_kirchoff_stress, src/nclr.h:313-337): Kirchhoff stress
+ * 2 mu (F - R) F^T + constmat(lambda (J - 1) J).  NCLR_STRESS_NEOHOOKEAN is the model the
+ * reference lists as a TODO (src/nclr.h:339): mu (F F^T - I) + lambda ln(J) I, with the same
+ * hardening of mu and lambda and the same plasticity; it needs det F > 0, so 3D takes it only
+ * with NCLR_PHYSICS_CORRECTED (the reference's diag<3>(1) = diag(1,1,0) keeps det F at 0). */
+enum { NCLR_STRESS_COROTATED = 0, NCLR_STRESS_NEOHOOKEAN = 1 };
+
 typedef struct nclr_options {
   int physics;             /* NCLR_PHYSICS_* (default REFERENCE) */
   int sort_interval;       /* re-sort particles by grid block every this many steps (0 = only
@@ -80,6 +88,7 @@ typedef struct nclr_options {
                               launches per step; 0 = never, -1 = the default (default -1:
                               65,536 particles in 2D and 32,768 in 3D for one scene, never for
                               a batch, where the tile path is faster) */
+  int stress_model;        /* NCLR_STRESS_* (default COROTATED); a batch's scenes share it */
 } nclr_options;
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid
@@ -164,6 +173,17 @@ nclr_status nclr_get_particles(nclr_sim *sim, float *x, float *v, float *F, floa
 nclr_status nclr_set_particles(nclr_sim *sim, const float *x, const float *v, const float *F,
                                const float *C, const float *Jp);
 
+/* Per-particle Young's modulus and Poisson ratio (an extension: the reference has one pair per
+ * simulation, src/nclr.h:74-78).  E and nu hold one value per particle in the caller's order
+ * (all scenes concatenated for a batch); every particle's mu_0 and lambda_0 then follow from
+ * its own pair by the constructor's formula (src/nclr.h:77-78), and the material's hardening
+ * scales them as before.  Both NULL returns to the simulation's (each scene's) E and nu.  Takes
+ * effect from the next advance(); the values stay with their particles.  nclr_set_moduli takes
+ * HOST arrays and synchronises; nclr_set_moduli_device takes DEVICE arrays, ordered on the
+ * handle's stream. */
+nclr_status nclr_set_moduli(nclr_sim *sim, const float *E, const float *nu);
+nclr_status nclr_set_moduli_device(nclr_sim *sim, const float *E, const float *nu);
+
 /* grid() (src/nclr.h:87): the post-update grid of the last step, (res+1)^dim nodes, in the
  * reference's node order.  Before the first advance the reference's grid is empty: returns
  * NCLR_ERR_INVALID then. */
@@ -222,8 +242,9 @@ void nclr_destroy(nclr_sim *sim);
  * Differentiable rollouts (no counterpart in the reference).  A rollout is `nsteps` jelly
  * steps (src/nclr.h:80-337, MaterialModel::kJelly) from a given state; the reverse pass is a
  * hand-written adjoint of the whole step (G2P, grid update with its clamp and boundary masks,
- * P2G, the fixed-corotated stress and its polar rotation) run backwards through the rollout,
- * recomputing each segment of `checkpoint_every` steps from a checkpoint.
+ * P2G, the stress of opt->stress_model -- fixed corotated with its polar rotation, or
+ * neo-Hookean) run backwards through the rollout, recomputing each segment of
+ * `checkpoint_every` steps from a checkpoint.
  *
  * All state arrays are DEVICE pointers in the host layout above (caller order, rows).
  * nclr_rollout_create takes the particle count, initial positions (HOST, used only to size and

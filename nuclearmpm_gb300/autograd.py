@@ -30,13 +30,15 @@ class Rollout:
 
     def __init__(self, x0, *, res: int = 64, steps: int = 100, checkpoint_every: int = 50,
                  dt: float = 1e-4, gravity: float = -100.0, mass=None, volume=None,
-                 physics: int = capi.PHYSICS_REFERENCE, device: int = 0, sort_interval: int = 8):
+                 physics: int = capi.PHYSICS_REFERENCE, device: int = 0, sort_interval: int = 8,
+                 stress_model: int = capi.STRESS_COROTATED):
         x = np.ascontiguousarray(torch.as_tensor(x0).detach().cpu().numpy(), dtype=np.float32)
         self.n, self.dim = x.shape
         self.steps = int(steps)
         m = None if mass is None else np.ascontiguousarray(mass, dtype=np.float32)
         vo = None if volume is None else np.ascontiguousarray(volume, dtype=np.float32)
-        opt = capi.default_options(physics=physics, device=device, sort_interval=sort_interval)
+        opt = capi.default_options(physics=physics, device=device, sort_interval=sort_interval,
+                                   stress_model=stress_model)
         h = ctypes.c_void_p()
         L = capi.lib()
         st = L.nclr_rollout_create(ctypes.byref(h), self.dim, self.n, x.ctypes.data,

@@ -15,6 +15,7 @@ NCLR_OK, NCLR_ERR_INVALID, NCLR_ERR_OUT_OF_RANGE, NCLR_ERR_CUDA, NCLR_ERR_NO_DEV
 STATUS_NAMES = {0: "NCLR_OK", 1: "NCLR_ERR_INVALID", 2: "NCLR_ERR_OUT_OF_RANGE",
                 3: "NCLR_ERR_CUDA", 4: "NCLR_ERR_NO_DEVICE"}
 PHYSICS_REFERENCE, PHYSICS_CORRECTED = 0, 1
+STRESS_COROTATED, STRESS_NEOHOOKEAN = 0, 1
 PHASE_SORT, PHASE_GRID, PHASE_P2G, PHASE_G2P2G = range(4)
 PHASE_NAMES = ("sort", "grid", "p2g", "g2p2g")
 NOALLOC_MAX_NODES = 1 << 20
@@ -25,7 +26,7 @@ class Options(ctypes.Structure):
                 ("p2g_particles_per_thread", ctypes.c_int), ("device", ctypes.c_int),
                 ("use_graphs", ctypes.c_int), ("profile", ctypes.c_int),
                 ("graph_steps", ctypes.c_int), ("sparse_block_max", ctypes.c_int),
-                ("small_scene_max", ctypes.c_int)]
+                ("small_scene_max", ctypes.c_int), ("stress_model", ctypes.c_int)]
 
 
 class Scene(ctypes.Structure):
@@ -75,6 +76,8 @@ SIGNATURES = {
     "nclr_get_particles_device": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp]),
     "nclr_set_particles_device": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp]),
     "nclr_get_lame": (ctypes.c_int, [_h, _fp, _fp]),
+    "nclr_set_moduli": (ctypes.c_int, [_h, _vp, _vp]),
+    "nclr_set_moduli_device": (ctypes.c_int, [_h, _vp, _vp]),
     "nclr_num_particles": (_i64, [_h]),
     "nclr_dim": (ctypes.c_int, [_h]),
     "nclr_res": (ctypes.c_int, [_h]),

@@ -12,6 +12,8 @@
 // updated grid V_t of the step is the float4 {v, m} grid the forward step produced.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "mpm_device.cuh"
 #include "mpm_launch.h"
 
@@ -183,6 +185,12 @@ struct Polar<3> {
     return polar_backward_svd(U, sg, V, Rb);
   }
 };
+// What the neo-Hookean stress has in place of the polar rotation: nothing (R is unused).
+template <int D>
+struct NoPolar {
+  Mat<D> R;
+  __device__ __forceinline__ explicit NoPolar(const Mat<D> &F) : R(F) {}
+};
 
 }  // namespace
 
@@ -311,11 +319,12 @@ __global__ void __launch_bounds__(256) adj_grid_kernel(const float4 *__restrict_
 
 // ---------------------------------------------------------------------------------------
 // adj_p2g: reverse of mv_i += W (m v + A dpos), m_i += W m, with the fused APIC + stress
-// A = -(dt vol Dinv)(2 mu (F - R) F^T + lambda (J - 1) J 1) + m C (jelly: mu = 0.3 mu_0,
-// lambda = 0.3 lambda_0).  Adds to the adjoints of x and F, writes those of v and C, and
-// accumulates the adjoints of mu_0 and lambda_0 into gml[0..1].
+// A = -(dt vol Dinv) PF + m C (jelly: mu = 0.3 mu_0, lambda = 0.3 lambda_0) and PF the
+// fixed-corotated 2 mu (F - R) F^T + lambda (J - 1) J 1 or (kStress == kNeoHookean)
+// mu (F F^T - I) + lambda ln(J) I.  Adds to the adjoints of x and F, writes those of v and C,
+// and accumulates the adjoints of mu_0 and lambda_0 into gml[0..1].
 // ---------------------------------------------------------------------------------------
-template <int D>
+template <int D, int kStress>
 __global__ void __launch_bounds__(128) adj_p2g_kernel(
     int n, const float *__restrict__ x, const float *__restrict__ v, const float *__restrict__ F,
     const float *__restrict__ C, const float *__restrict__ mass, const float *__restrict__ vol,
@@ -335,9 +344,10 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     const Mat<D> Fm = load_row_mat<D>(F, p);
     const Mat<D> Cm = load_row_mat<D>(C, p);
     const float m = mass[p], vo = vol[p];
-    const Polar<D> pol(Fm);
-    const Mat<D> &R = pol.R;
-    const Mat<D> A = fused_affine<D>(Fm, R, Cm, 1.0f, m, vo, kJelly, P);
+    // the corotated stress's polar rotation, whose factorisation its adjoint reuses
+    const std::conditional_t<kStress == kNeoHookean, NoPolar<D>, Polar<D>> pol(Fm);
+    const Mat<D> A = fused_affine<D>(Fm, pol.R, Cm, 1.0f, m, vo, kJelly,
+                                     make_float2(P.mu0, P.lambda0), P);
     Mat<D> gA;
 #pragma unroll
     for (int i = 0; i < D; ++i)
@@ -404,6 +414,38 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     const float kappa = P.dt * vo * P.Dinv;
     const float mu = P.mu0 * 0.3f, lam = P.lambda0 * 0.3f;
     const float J = det(Fm);
+    Mat<D> gF = load_row_mat<D>(oF, p);
+    const Mat<D> cof = cofactor(Fm);  // d det(F) / dF = J F^-T
+    if constexpr (kStress == kNeoHookean) {
+      // PF = mu (F F^T - I) + lambda ln(J) I; G = dL/dPF:
+      //   F_bar = mu (G + G^T) F + lambda tr(G) F^-T, mu_bar = <G, F F^T - I>,
+      //   lambda_bar = tr(G) ln(J)
+      Mat<D> G;
+      float trG = 0.0f;
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) G.a[i][j] = -kappa * gA.a[i][j];
+        trG += G.a[i][i];
+      }
+      const Mat<D> FFt = mat_mul_t<D>(Fm, Fm);
+      Mat<D> Sg;
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          gmu += G.a[i][j] * (FFt.a[i][j] - (i == j ? 1.0f : 0.0f));
+          Sg.a[i][j] = mu * (G.a[i][j] + G.a[j][i]);
+        }
+      glam = trG * logf(J);
+      const Mat<D> SF = mat_mul<D>(Sg, Fm);
+      const float c = lam * trG / J;
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) gF.a[i][j] += SF.a[i][j] + c * cof.a[i][j];
+    } else {
+    const Mat<D> &R = pol.R;
     Mat<D> X, G;
     float sbar = 0.0f;
 #pragma unroll
@@ -438,13 +480,12 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
         FQ.a[i][j] = s;
       }
     const Mat<D> Fp = pol.backward(Fm, Rb);
-    const Mat<D> cof = cofactor(Fm);
     const float dJ = sbar * lam * (2.0f * J - 1.0f);
-    Mat<D> gF = load_row_mat<D>(oF, p);
 #pragma unroll
     for (int i = 0; i < D; ++i)
 #pragma unroll
       for (int j = 0; j < D; ++j) gF.a[i][j] += FQ.a[i][j] + Xb.a[i][j] + Fp.a[i][j] + dJ * cof.a[i][j];
+    }
     store_row_mat<D>(oF, p, gF);
     gmu *= 0.3f;  // jelly hardening (src/nclr.h:362-364)
     glam *= 0.3f;
@@ -479,7 +520,12 @@ void launch_adjoint_step(int n, const float *x, const float *v, const float *F, 
   }
   adj_grid_kernel<D><<<(unsigned)((P.nodes + 255) / 256), 256, 0, st>>>(V, VB, GB, P);
   if (n > 0)
-    adj_p2g_kernel<D><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF, oC, gml, err);
+    if (P.stress == kNeoHookean)
+      adj_p2g_kernel<D, kNeoHookean><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF,
+                                                         oC, gml, err);
+    else
+      adj_p2g_kernel<D, kCorotated><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF,
+                                                        oC, gml, err);
 }
 
 template void launch_adjoint_step<2>(int, const float *, const float *, const float *, const float *,

@@ -6,7 +6,8 @@
 //              field[c * stride + p] (x: dim comps; F, C: dim*dim comps, row-major; v: dim;
 //              Jp, mass, volume: 1).  `id[p]` is the caller's index of slot p: slots are
 //              re-sorted by grid block every few steps and the caller's order is restored on
-//              download.  `mat[p]` (optional) is a per-particle material.  v and C are written
+//              download.  `mat[p]` (optional) is a per-particle material and `lame[p]`
+//              (optional) per-particle base Lame parameters (mu_0, lambda_0).  v and C are written
 //              only by the last step of an advance() call (nothing else reads them: each
 //              G2P rebuilds them from the grid).
 //   G          dense (res+1)^dim float4 nodes {sum w (m v + A dpos), sum w m} (the reference's
@@ -27,6 +28,9 @@ namespace mpm {
 
 enum : int { kSnow = 0, kJelly = 1, kLiquid = 2 };
 enum : int { kErrOutOfRange = 1, kErrBarrier = 2 };  // error flag bits
+// Stress models: the reference's fixed-corotated stress (src/nclr.h:313-337) and the
+// neo-Hookean one it lists as a TODO (src/nclr.h:339).
+enum : int { kCorotated = 0, kNeoHookean = 1 };
 
 // Block tiling of the grid (see the layout note above).  Particles are sorted by block and,
 // inside a block, stored cell by cell in rounds (the first particle of every cell in x-major
@@ -56,6 +60,7 @@ struct Params {
   float Dinv;           // 4 inv_dx^2 (src/nclr.h:325)
   float cscale;         // 4 inv_dx  (src/nclr.h:206,223)
   float dt_gravity;     // dt * gravity (src/nclr.h:292)
+  int stress;           // kCorotated or kNeoHookean
   int64_t nodes;        // N^dim
   int nb;               // grid blocks per axis: ceil(N / Tiling<dim>::BS)
   int nblocks;          // nb^dim
@@ -65,6 +70,7 @@ struct PState {
   float *x, *v, *F, *C, *Jp, *mass, *vol;  // v and C: see the layout note
   int *id;
   uint8_t *mat;     // may be null
+  float2 *lame;     // per-particle (mu_0, lambda_0); null: the scene's P.mu0, P.lambda0
   uint16_t *scene;  // scene of each slot (batched simulations), null for a single scene
   int stride;       // component stride (capacity)
 };
@@ -149,30 +155,63 @@ __device__ __forceinline__ float hardening(int material, float Jp) {
   return material == kJelly ? 0.3f : 1.0f;
 }
 
-// first_piola_kirchoff_stress (src/nclr.h:313-337):
-//   A = -(dt vol) Dinv (2 mu (F - R) F^T + constmat(lambda (J - 1) J)) + m C
+// Base Lame parameters of slot p: its own (per-particle moduli) or the scene's.
+__device__ __forceinline__ float2 lame0(const PState &s, int p, const Params &P) {
+  return s.lame ? s.lame[p] : make_float2(P.mu0, P.lambda0);
+}
+
+// Affine momentum of the fused P2G (src/nclr.h:313-337):
+//   A = -(dt vol) Dinv PF + m C, with the Kirchhoff stress PF of the scene's stress model:
+//   fixed corotated  2 mu (F - R) F^T + constmat(lambda (J - 1) J)   (the reference; constmat
+//                    adds the term to every entry, src/nclr_math.h:40-43)
+//   neo-Hookean      mu (F F^T - I) + lambda ln(J) I                 (src/nclr.h:339's TODO;
+//                    R is not used)
+// mu, lambda = (mu_0, lambda_0) of `l0` times the material's hardening (src/nclr.h:351-372).
 template <int D>
 __device__ __forceinline__ Mat<D> fused_affine(const Mat<D> &F, const Mat<D> &R, const Mat<D> &C,
                                                float Jp, float m, float vol, int material,
-                                               const Params &P) {
+                                               float2 l0, const Params &P) {
   const float e = hardening(material, Jp);
-  const float mu = P.mu0 * e, lambda = P.lambda0 * e;
+  const float mu = l0.x * e, lambda = l0.y * e;
   const float J = det(F);
-  Mat<D> FmR;
-  const float two_mu = 2.0f * mu;
+  Mat<D> PF;
+  float lam;
+  bool every_entry;
+  if (P.stress == kNeoHookean) {
+    PF = mat_mul_t<D>(F, F);
 #pragma unroll
-  for (int i = 0; i < D; ++i)
+    for (int i = 0; i < D; ++i)
 #pragma unroll
-    for (int j = 0; j < D; ++j) FmR.a[i][j] = two_mu * (F.a[i][j] - R.a[i][j]);
-  const Mat<D> PF = mat_mul_t<D>(FmR, F);
-  const float lam = lambda * (J - 1.0f) * J;
+      for (int j = 0; j < D; ++j) PF.a[i][j] = mu * (PF.a[i][j] - (i == j ? 1.0f : 0.0f));
+    lam = lambda * logf(J);
+    every_entry = false;
+  } else {
+    Mat<D> FmR;
+    const float two_mu = 2.0f * mu;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) FmR.a[i][j] = two_mu * (F.a[i][j] - R.a[i][j]);
+    PF = mat_mul_t<D>(FmR, F);
+    lam = lambda * (J - 1.0f) * J;
+    every_entry = true;
+  }
   const float s = -(P.dt * vol);
   Mat<D> A;
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
-    for (int j = 0; j < D; ++j) A.a[i][j] = s * (P.Dinv * (PF.a[i][j] + lam)) + m * C.a[i][j];
+    for (int j = 0; j < D; ++j)
+      A.a[i][j] = s * (P.Dinv * (PF.a[i][j] + ((every_entry || i == j) ? lam : 0.0f))) +
+                  m * C.a[i][j];
   return A;
+}
+
+// The rotation the stress needs: the polar factor of F for the corotated model, nothing for
+// the neo-Hookean one.
+template <int D>
+__device__ __forceinline__ Mat<D> stress_R(const Mat<D> &F, const Params &P) {
+  return P.stress == kNeoHookean ? F : polar_R(F);
 }
 
 template <int D>

@@ -73,6 +73,9 @@ void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_ma
 // Counts material[] entries above NCLR_LIQUID into *out (host); synchronises `st`
 // (scene_build.cu).
 cudaError_t count_bad_materials(const uint8_t *mat, int64_t n, int *scratch, int *out, cudaStream_t st);
+// lame[p] = (mu_0, lambda_0) of caller row id[p]'s E and nu, for the n slots.
+cudaError_t launch_set_lame(const int *id, int n, const float *E, const float *nu, float2 *lame,
+                            cudaStream_t st);
 
 // Reverse of one jelly step (adjoint.cu): adjoint of s_{t+1} (gx, gv, gF, gC; NULL = 0) ->
 // adjoint of s_t (ox, ov, oF, oC), mu_0 / lambda_0 adjoints added to gml[0..1].  States are

@@ -160,19 +160,20 @@ __device__ __forceinline__ void scale_mat(Mat<D> &C, float c) {
 }
 
 // The F update and plasticity of G2P (src/nclr.h:228-259) from the gathered C; returns the
-// rotation R of the updated F (the polar factor the next step's stress needs).
+// rotation R of the updated F (the polar factor the next step's corotated stress needs; with
+// need_R false -- the neo-Hookean stress -- whatever is at hand).
 template <int D, bool kRef>
 __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp, int material,
-                                           float dt) {
+                                           float dt, bool need_R = true) {
   Mat<D> M;
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
     for (int j = 0; j < D; ++j) M.a[i][j] = diag_one<D, kRef>(i, j) + dt * C.a[i][j];
   Mat<D> Fh = mat_mul<D>(M, F);
-  Mat<D> R;
+  Mat<D> R = Fh;
   if (material == kJelly) {
-    R = polar_R(Fh);
+    if (need_R) R = polar_R(Fh);
   } else {
     Mat<D> U, Vm;
     float sig[D];
@@ -190,7 +191,7 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
       if constexpr (D == 3) {
         R = uvt<3>(U, Vm);  // the clamped sigma are positive: F = (U V^T)(V S V^T)
       } else {
-        R = polar_rotation(Fh);
+        if (need_R) R = polar_rotation(Fh);
       }
     } else {  // liquid: J = prod sigma accumulated in double (src/nclr.h:253-257)
       double J = 1.0;
@@ -201,7 +202,7 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
 #pragma unroll
         for (int j = 0; j < D; ++j) Fh.a[i][j] = diag_one<D, kRef>(i, j);
       Fh.a[0][0] = (float)J;
-      R = polar_R(Fh);
+      R = need_R ? polar_R(Fh) : Fh;
     }
   }
   F = Fh;
@@ -495,7 +496,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
           F = load_mat<D>(s.F, st, p);
           C = load_mat<D>(s.C, st, p);
           Jp = s.Jp[p];
-          R = polar_R(F);
+          R = stress_R<D>(F, P);
         } else {
         // ---- G2P of this step ----
         float fx[D], w[3][D];
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
         for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];  // advection, src/nclr.h:229
         F = load_mat<D>(s.F, st, p);
         Jp = s.Jp[p];
-        R = update_F<D, kRef>(C, F, Jp, material, P.dt);
+        R = update_F<D, kRef>(C, F, Jp, material, P.dt, P.stress == kCorotated);
 #pragma unroll
         for (int d = 0; d < D; ++d) s.x[(size_t)d * st + p] = x[d];
         store_mat<D>(s.F, st, p, F);
@@ -560,7 +561,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
 
         // ---- P2G of the next step: stress, stencil ----
         m = s.mass[p];
-        A = fused_affine<D>(F, R, C, Jp, m, s.vol[p], material, P);
+        A = fused_affine<D>(F, R, C, Jp, m, s.vol[p], material, lame0(s, p, P), P);
         int *err_p2g = (kMode == kP2GOnly) ? err_now : err_next;
 #pragma unroll
         for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
@@ -793,7 +794,7 @@ __global__ void import_rows_kernel(PState s, int id_off, int n, const float *__r
 // nb^dim * cells-per-block keys): keys + ranks, exclusive scan of the counts, the list of
 // non-empty blocks, then the
 // fields the step reads (x, F, Jp, mass, volume, id, material) move to start[key] + rank in
-// the other buffer.  v and C do not move: they are rewritten by the last step of every
+// the other buffer (and the per-particle moduli, when set).  v and C do not move: they are rewritten by the last step of every
 // advance() call before anyone reads them.
 // ---------------------------------------------------------------------------------------
 template <int D>
@@ -847,6 +848,7 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
   inv[id] = q;                     // caller row -> slot
   slot_block[q] = k / CPB;         // the block this slot now belongs to
   if (src.mat) dst.mat[q] = src.mat[p];
+  if (src.lame) dst.lame[q] = src.lame[p];
   if (src.scene) dst.scene[q] = src.scene[p];
   if (move_vc) {  // the next P2G reads v and C (right after an upload)
 #pragma unroll
@@ -921,7 +923,8 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
       const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
       const float m = s.mass[p];
       const int material = s.mat ? (int)s.mat[p] : P.model;
-      Mat<D> A = fused_affine<D>(F, polar_R(F), C, s.Jp[p], m, s.vol[p], material, P);
+      Mat<D> A = fused_affine<D>(F, stress_R<D>(F, P), C, s.Jp[p], m, s.vol[p], material,
+                                 lame0(s, p, P), P);
 #pragma unroll
       for (int d = 0; d < D; ++d) mv[d] = s.v[(size_t)d * st + p] * m;
       stencil<D>(x, P.inv_dx, base, fx, w);
@@ -979,7 +982,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
       for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];
       Mat<D> F = load_mat<D>(s.F, st, p);
       float Jp = s.Jp[p];
-      update_F<D, kRef>(C, F, Jp, s.mat ? (int)s.mat[p] : P.model, P.dt);
+      update_F<D, kRef>(C, F, Jp, s.mat ? (int)s.mat[p] : P.model, P.dt, false);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         s.x[(size_t)d * st + p] = x[d];
@@ -1040,7 +1043,8 @@ __global__ void __launch_bounds__(kSmallThreads) small_batch_kernel(
       const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
       const float m = s.mass[p];
       const int material = s.mat ? (int)s.mat[p] : P.model;
-      Mat<D> A = fused_affine<D>(F, polar_R(F), C, s.Jp[p], m, s.vol[p], material, P);
+      Mat<D> A = fused_affine<D>(F, stress_R<D>(F, P), C, s.Jp[p], m, s.vol[p], material,
+                                 lame0(s, p, P), P);
 #pragma unroll
       for (int d = 0; d < D; ++d) mv[d] = s.v[(size_t)d * st + p] * m;
       stencil<D>(x, P.inv_dx, base, fx, w);
@@ -1123,7 +1127,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_batch_kernel(
       for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];
       Mat<D> F = load_mat<D>(s.F, st, p);
       float Jp = s.Jp[p];
-      update_F<D, kRef>(C, F, Jp, s.mat ? (int)s.mat[p] : P.model, P.dt);
+      update_F<D, kRef>(C, F, Jp, s.mat ? (int)s.mat[p] : P.model, P.dt, false);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         s.x[(size_t)d * st + p] = x[d];

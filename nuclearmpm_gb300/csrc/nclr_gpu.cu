@@ -42,6 +42,7 @@ struct nclr_sim {
 
   void *slab[2] = {nullptr, nullptr};  // particle SoA buffers
   PState ps[2]{};
+  float2 *lame_buf = nullptr;  // per-particle (mu_0, lambda_0) of ps[0] and ps[1] (2 n), if set
   int cur = 0;
   int sms = 1;         // streaming multiprocessors of the device
   int g2p2g_ctas = 1;  // persistent CTAs of the fused kernel
@@ -394,14 +395,24 @@ Rows staging_rows(nclr_sim *s, int64_t n) {
   return r;
 }
 
+// Drops the captured step graphs: they hold the kernels' parameters (scene constants,
+// particle buffers) by value, so the next advance() recaptures them.
+void drop_graphs(nclr_sim *s) {
+  for (auto &row : s->graph)
+    for (auto &g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+}
+
 void release(nclr_sim *s) {
   if (!s) return;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  for (auto &row : s->graph)
-    for (auto &g : row)
-      if (g) cudaGraphExecDestroy(g);
+  drop_graphs(s);
   for (auto p : s->slab) cudaFree(p);
+  cudaFree(s->lame_buf);
   cudaFree(s->scenes_d);
   cudaFree(s->block_scene);
   cudaFree(s->G);
@@ -480,6 +491,17 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   nclr_default_options(&s->opt);
   if (opt) s->opt = *opt;
   if (s->opt.sort_interval < 0) s->opt.sort_interval = 0;
+  if (s->opt.stress_model != NCLR_STRESS_COROTATED && s->opt.stress_model != NCLR_STRESS_NEOHOOKEAN) {
+    delete s;
+    return fail(nullptr, NCLR_ERR_INVALID, "unknown stress model");
+  }
+  if (s->opt.stress_model == NCLR_STRESS_NEOHOOKEAN && dim == 3 &&
+      s->opt.physics != NCLR_PHYSICS_CORRECTED) {
+    // diag<3>(1) = diag(1,1,0) (src/nclr_math.h:13-19) keeps det F at 0, where ln(J) diverges
+    delete s;
+    return fail(nullptr, NCLR_ERR_INVALID,
+                "the neo-Hookean stress needs det F > 0: use NCLR_PHYSICS_CORRECTED in 3D");
+  }
   s->dim = dim;
   s->n = total_n;
   s->nscenes = nscenes;
@@ -499,6 +521,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
     const nclr_scene &d = descs[i];
     Scene sc{};
     sc.P = scene_params(dim, d.n, d.model, d.res, d.dt, d.E, d.nu, d.gravity);
+    sc.P.stress = s->opt.stress_model;
     sc.slot_off = (int)slot;
     sc.node_off = node;
     sc.block_off = (int)std::min<int64_t>(block, 0x7fffffff);
@@ -932,6 +955,7 @@ void nclr_default_options(nclr_options *opt) {
   opt->graph_steps = 0;
   opt->sparse_block_max = -1;
   opt->small_scene_max = -1;
+  opt->stress_model = NCLR_STRESS_COROTATED;
 }
 
 nclr_status nclr_create(nclr_sim **out, int dim, int64_t n, const float *x, const float *v,
@@ -1036,6 +1060,56 @@ nclr_status nclr_set_particles_device(nclr_sim *s, const float *x, const float *
   CUDA_TRY(s, cudaSetDevice(s->device));
   if (s->n == 0) return NCLR_OK;
   return import_rows(s, -1, x, v, F, C, Jp);
+}
+
+// Per-particle moduli: E, nu in the caller's row order (host arrays staged first, or device
+// arrays), turned into (mu_0, lambda_0) per slot; both NULL returns to the scenes' pairs.
+static nclr_status set_moduli(nclr_sim *s, const float *E, const float *nu, bool device) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->error.clear();
+  if ((!E) != (!nu)) return fail(s, NCLR_ERR_INVALID, "E and nu go together");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  if (!E) {
+    if (s->lame_buf) {
+      CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+      cudaFree(s->lame_buf);
+      s->lame_buf = nullptr;
+      s->ps[0].lame = s->ps[1].lame = nullptr;
+      drop_graphs(s);
+      s->acc_valid = false;
+    }
+    return NCLR_OK;
+  }
+  if (s->n == 0) return NCLR_OK;
+  if (!s->lame_buf) {
+    CUDA_TRY(s, cudaMalloc((void **)&s->lame_buf, sizeof(float2) * 2 * (size_t)s->n));
+    s->ps[0].lame = s->lame_buf;
+    s->ps[1].lame = s->lame_buf + s->n;
+    drop_graphs(s);  // the captured kernels hold the particle buffers without it
+  }
+  const float *Ed = E, *nud = nu;
+  if (!device) {
+    const nclr_status st = ensure_staging(s);
+    if (st != NCLR_OK) return st;
+    const size_t bytes = sizeof(float) * (size_t)s->n;
+    CUDA_TRY(s, cudaMemcpyAsync(s->staging, E, bytes, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(s->staging + s->n, nu, bytes, cudaMemcpyHostToDevice, s->stream));
+    Ed = s->staging;
+    nud = s->staging + s->n;
+  }
+  CUDA_TRY(s, mpm::launch_set_lame(s->ps[s->cur].id, (int)s->n, Ed, nud, s->ps[s->cur].lame,
+                                   s->stream));
+  s->acc_valid = false;  // the pending P2G used the old moduli
+  if (!device) CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return NCLR_OK;
+}
+
+nclr_status nclr_set_moduli(nclr_sim *s, const float *E, const float *nu) {
+  return set_moduli(s, E, nu, false);
+}
+
+nclr_status nclr_set_moduli_device(nclr_sim *s, const float *E, const float *nu) {
+  return set_moduli(s, E, nu, true);
 }
 
 nclr_status nclr_get_particles(nclr_sim *s, float *x, float *v, float *F, float *C, float *Jp) {
@@ -1264,12 +1338,7 @@ void set_material(nclr_sim *s, float E, float nu) {
   P.mu0 = E / (2.0f * (1.0f + nu));
   P.lambda0 = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
   cudaMemcpyAsync(s->scenes_d, s->scenes.data(), sizeof(Scene), cudaMemcpyHostToDevice, s->stream);
-  for (auto &row : s->graph)
-    for (auto &g : row)
-      if (g) {
-        cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
+  drop_graphs(s);
 }
 
 // Loads a state (rows) into the simulation; the next advance() starts from it.

@@ -82,7 +82,8 @@ __global__ void __launch_bounds__(128) p2g_rows_kernel(int n, const float *__res
       C.a[i][j] = Cs[((size_t)p * D + i) * D + j];
     }
   const float Jp = Jps[p], m = ms[p], vol = vols[p];
-  const Mat<D> A = fused_affine<D>(F, polar_R(F), C, Jp, m, vol, P.model, P);
+  const Mat<D> A = fused_affine<D>(F, polar_R(F), C, Jp, m, vol, P.model,
+                                   make_float2(P.mu0, P.lambda0), P);
   int base[D];
   float fx[D], w[3][D];
   stencil<D>(x, P.inv_dx, base, fx, w);

@@ -1,7 +1,7 @@
 // Scene builders on the device: the reference's cube<dim>() lattice (src/nclr_math.h:100-129)
 // and the headless solver's generate_cubes (src/solver.cpp:133-149) written straight into
-// device memory, so that large scenes are not assembled on the host; and the check of a
-// device-resident material[] array for nclr_create_device.
+// device memory, so that large scenes are not assembled on the host; the check of a
+// device-resident material[] array for nclr_create_device; and the per-particle moduli.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -46,7 +46,28 @@ __global__ void bad_materials_kernel(const uint8_t *__restrict__ mat, int64_t n,
   if (i < n && mat[i] > 2) atomicAdd(bad, 1);
 }
 
+// Slot p takes the moduli of caller row id[p]: mu_0 = E / (2 (1 + nu)),
+// lambda_0 = E nu / ((1 + nu)(1 - 2 nu)) (src/nclr.h:77-78), each operation rounded on its
+// own as the host evaluates the simulation's pair (no fused multiply-add).
+__global__ void set_lame_kernel(const int *__restrict__ id, int n, const float *__restrict__ E,
+                                const float *__restrict__ nu, float2 *__restrict__ lame) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int q = id[p];
+  const float e = E[q], v = nu[q];
+  const float one_v = __fadd_rn(1.0f, v);
+  lame[p] = make_float2(__fdiv_rn(e, __fmul_rn(2.0f, one_v)),
+                        __fdiv_rn(__fmul_rn(e, v),
+                                  __fmul_rn(one_v, __fsub_rn(1.0f, __fmul_rn(2.0f, v)))));
+}
+
 }  // namespace
+
+cudaError_t launch_set_lame(const int *id, int n, const float *E, const float *nu, float2 *lame,
+                            cudaStream_t st) {
+  if (n > 0) set_lame_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(id, n, E, nu, lame);
+  return cudaGetLastError();
+}
 
 cudaError_t count_bad_materials(const uint8_t *mat, int64_t n, int *scratch, int *out,
                                 cudaStream_t st) {

@@ -11,6 +11,11 @@
                                               reference)
         .mu_0, .lambda_0, kBoundary, kSnowHardening, kJellyHardening, kLiquidHardening
 
+Extensions of the model: `material=` (one MaterialModel per particle), `set_moduli(E, nu)`
+(one Young's modulus and Poisson ratio per particle) and `stress_model=` (the reference's
+fixed-corotated stress, src/nclr.h:313-337, or the neo-Hookean one its TODO names,
+src/nclr.h:339).
+
 `particles` may be a list of Particle objects (as the reference takes a
 std::vector<Particle<dim>>) or, for large scenes, a dict of arrays in the C ABI host layout
 (x (n,dim), v, F (n,dim,dim), C, Jp, mass, volume).  Errors: a stencil that leaves the grid
@@ -127,6 +132,31 @@ def _soa_from(particles, dim_hint: int | None):
         c=np.array([p.c for p in plist], np.int32))
 
 
+def _set_moduli(h, n: int, E, nu) -> None:
+    L = capi.lib()
+    if (E is None) != (nu is None):
+        raise ValueError("E and nu go together")
+    if E is None:
+        capi.check(L.nclr_set_moduli(h, None, None), h)
+        return
+    try:
+        import torch
+        on_device = isinstance(E, torch.Tensor) and E.is_cuda
+    except ImportError:
+        on_device = False
+    if on_device:
+        for t in (E, nu):
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32
+                    and t.is_contiguous() and t.numel() == n):
+                raise TypeError("device moduli must be contiguous float32 CUDA tensors of n values")
+        capi.check(L.nclr_set_moduli_device(h, ctypes.c_void_p(E.data_ptr()),
+                                            ctypes.c_void_p(nu.data_ptr())), h)
+        return
+    Ea = np.ascontiguousarray(np.broadcast_to(np.asarray(E, np.float32), (n,)))
+    nua = np.ascontiguousarray(np.broadcast_to(np.asarray(nu, np.float32), (n,)))
+    capi.check(L.nclr_set_moduli(h, _ptr(Ea), _ptr(nua)), h)
+
+
 class MPMSimulation:
     """MPMSimulation<dim> (src/nclr.h:63-384) running on the GPU."""
     kBoundary = 3
@@ -139,7 +169,8 @@ class MPMSimulation:
                  material: np.ndarray | None = None, physics: int = capi.PHYSICS_REFERENCE,
                  sort_interval: int = 8, particles_per_thread: int = 1, device: int = 0,
                  use_graphs: bool = True, profile: bool = False, graph_steps: int = 0,
-                 sparse_block_max: int = -1, small_scene_max: int = -1):
+                 sparse_block_max: int = -1, small_scene_max: int = -1,
+                 stress_model: int = capi.STRESS_COROTATED):
         L = capi.lib()
         self.dim, soa = _soa_from(particles, dim)
         self._c = soa.pop("c")
@@ -153,7 +184,7 @@ class MPMSimulation:
                                    p2g_particles_per_thread=particles_per_thread, device=device,
                                    use_graphs=int(use_graphs), profile=int(profile),
                                    graph_steps=graph_steps, sparse_block_max=sparse_block_max,
-                                   small_scene_max=small_scene_max)
+                                   small_scene_max=small_scene_max, stress_model=stress_model)
         h = ctypes.c_void_p()
         st = L.nclr_create(ctypes.byref(h), self.dim, self.n, _ptr(soa["x"]), _ptr(soa["v"]),
                            _ptr(soa["F"]), _ptr(soa["C"]), _ptr(soa["Jp"]), _ptr(soa["mass"]),
@@ -173,7 +204,8 @@ class MPMSimulation:
                     physics: int = capi.PHYSICS_REFERENCE, sort_interval: int = 8,
                     device: int | None = None, use_graphs: bool = True, profile: bool = False,
                     graph_steps: int = 0, sparse_block_max: int = -1,
-                    small_scene_max: int = -1) -> "MPMSimulation":
+                    small_scene_max: int = -1,
+                    stress_model: int = capi.STRESS_COROTATED) -> "MPMSimulation":
         """A simulation created from CUDA tensors (nclr_create_device): x (n, dim) and the
         optional fields in the layouts of the constructor, already on the GPU (e.g. from
         scenes.cubes_device), never staged through the host."""
@@ -201,7 +233,7 @@ class MPMSimulation:
         opt = capi.default_options(physics=physics, sort_interval=sort_interval, device=dev,
                                    use_graphs=int(use_graphs), profile=int(profile),
                                    graph_steps=graph_steps, sparse_block_max=sparse_block_max,
-                                   small_scene_max=small_scene_max)
+                                   small_scene_max=small_scene_max, stress_model=stress_model)
         h = ctypes.c_void_p()
         st = L.nclr_create_device(ctypes.byref(h), self.dim, self.n, ptr(x.contiguous()), ptr(v),
                                   ptr(F), ptr(C), ptr(Jp), ptr(mass), ptr(volume),
@@ -248,6 +280,12 @@ class MPMSimulation:
         x, v, F, C, Jp = arr(x, (n, d)), arr(v, (n, d)), arr(F, (n, d, d)), arr(C, (n, d, d)), arr(Jp, (n,))
         capi.check(capi.lib().nclr_set_particles(self._h, _ptr(x), _ptr(v), _ptr(F), _ptr(C),
                                                  _ptr(Jp)), self._h)
+
+    def set_moduli(self, E=None, nu=None) -> None:
+        """Per-particle Young's modulus and Poisson ratio (nclr_set_moduli): `E`, `nu` hold one
+        value per particle in caller order (numpy arrays or sequences, or contiguous float32
+        CUDA tensors); both None return to the simulation's pair."""
+        _set_moduli(self._h, self.n, E, nu)
 
     def get_particles_device(self, x=0, v=0, F=0, C=0, Jp=0) -> None:
         """Device-pointer export (integers = device addresses, 0 skips); stream-ordered."""
@@ -313,7 +351,8 @@ class BatchSimulation:
     def __init__(self, scenes: list, *, dim: int | None = None,
                  physics: int = capi.PHYSICS_REFERENCE, sort_interval: int = 8, device: int = 0,
                  use_graphs: bool = True, graph_steps: int = 0, profile: bool = False,
-                 small_scene_max: int = -1, particles_per_thread: int = 1):
+                 small_scene_max: int = -1, particles_per_thread: int = 1,
+                 stress_model: int = capi.STRESS_COROTATED):
         L = capi.lib()
         if not scenes:
             raise ValueError("a batch needs at least one scene")
@@ -347,7 +386,8 @@ class BatchSimulation:
         opt = capi.default_options(physics=physics, sort_interval=sort_interval, device=device,
                                    use_graphs=int(use_graphs), profile=int(profile),
                                    graph_steps=graph_steps, small_scene_max=small_scene_max,
-                                   p2g_particles_per_thread=particles_per_thread)
+                                   p2g_particles_per_thread=particles_per_thread,
+                                   stress_model=stress_model)
         h = ctypes.c_void_p()
         capi.check(L.nclr_batch_create(ctypes.byref(h), self.dim, len(scenes), descs,
                                        ctypes.byref(opt)), None)
@@ -357,6 +397,11 @@ class BatchSimulation:
 
     def __len__(self):
         return len(self.sizes)
+
+    def set_moduli(self, E=None, nu=None) -> None:
+        """Per-particle Young's modulus and Poisson ratio of every scene's particles, the
+        scenes concatenated in order (see MPMSimulation.set_moduli)."""
+        _set_moduli(self._h, sum(self.sizes), E, nu)
 
     def advance(self, steps: int = 1) -> None:
         capi.check(capi.lib().nclr_advance(self._h, int(steps)), self._h)

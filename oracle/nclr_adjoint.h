@@ -14,6 +14,9 @@
 //   P2G    mv_i = sum_p W_o (m v + A dpos_o), m_i = sum_p W_o m, dpos_o = (o - fx) dx,
 //          A = -(dt vol 4 inv_dx^2) (2 mu (F - R) F^T + lambda (J - 1) J 1) + m C
 //                                                                        (src/nclr.h:104-337)
+//          or, with the neo-Hookean stress extension (src/nclr.h:339's TODO),
+//          A = -(dt vol 4 inv_dx^2) (mu (F F^T - I) + lambda ln(J) I) + m C, whose F adjoint
+//          is mu (G + G^T) F + lambda tr(G) F^-T for the stress adjoint G
 // with W_o the product of the quadratic B-spline weights of fx = x inv_dx - base.  Clamped
 // velocity components and stuck or empty nodes pass no gradient.  The polar rotation's
 // derivative: with F = U S V^T and R = U V^T, a perturbation dF moves R by
@@ -99,9 +102,10 @@ class Adjoint {
 
   // Runs `nsteps` forward steps from `initial`, keeping every state and updated grid.
   Adjoint(std::vector<Particle<T, D>> initial, Model model, int res, T dt, T E, T nu,
-          T gravity, Physics mode, int nsteps)
+          T gravity, Physics mode, int nsteps, Stress stress = Stress::kCorotated)
       : sim_(initial, model, res, dt, E, nu, gravity, mode), mode_(mode) {
     if (model != Model::kJelly) throw std::invalid_argument("the adjoint covers jelly");
+    sim_.stress_ = stress;
     states_.push_back(sim_.particles());
     for (int t = 0; t < nsteps; ++t) {
       sim_.p2g();
@@ -299,6 +303,26 @@ class Adjoint {
         for (int j = 0; j < D; ++j) G(i, j) = -kappa * gA(i, j);
       const Mat<T, D> &F = q.F;
       const T J = det(F);
+      const T e = T(0.3);  // jelly hardening (src/nclr.h:362-364)
+      if (sim_.stress_ == Stress::kNeoHookean) {
+        const Mat<T, D> FFt = mul(F, transpose(F));
+        T trG = 0, gmu = 0;
+        for (int i = 0; i < D; ++i) {
+          trG += G(i, i);
+          for (int j = 0; j < D; ++j) gmu += G(i, j) * (FFt(i, j) - (i == j ? T(1) : T(0)));
+        }
+        Mat<T, D> S;
+        for (int i = 0; i < D; ++i)
+          for (int j = 0; j < D; ++j) S(i, j) = mu * (G(i, j) + G(j, i));
+        const Mat<T, D> SF = mul(S, F);
+        const Mat<T, D> cof = cofactor(F);  // J F^-T
+        const T c = lambda * trG / J;
+        for (int i = 0; i < D; ++i)
+          for (int j = 0; j < D; ++j) out.F[p](i, j) += SF(i, j) + c * cof(i, j);
+        gmu0 += e * gmu;
+        glambda0 += e * (trG * std::log(J));
+        continue;
+      }
       const Mat<T, D> R = nclr_polar_R<T, D>(F, mode_);
       Mat<T, D> X;
       for (int i = 0; i < D; ++i)
@@ -325,7 +349,6 @@ class Adjoint {
       for (int i = 0; i < D; ++i)
         for (int j = 0; j < D; ++j)
           out.F[p](i, j) += FfromQ(i, j) + Xbar(i, j) + Fpolar(i, j) + dJ * cof(i, j);
-      const T e = T(0.3);  // jelly hardening (src/nclr.h:362-364)
       gmu0 += e * gmu;
       glambda0 += e * glambda;
     }

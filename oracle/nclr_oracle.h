@@ -23,6 +23,14 @@
 //                   writes are out of bounds (undefined behaviour under NDEBUG) and are
 //                   treated as no-ops.
 //   kCorrected  diag is the true identity and the 2D sign fix acts on column dim-1.
+//
+// Two extensions of the reference's model, both off by default:
+//   * per-particle Young's modulus and Poisson ratio (Particle::mu0 / lambda0, from
+//     lame_of(E, nu), the constructor's formula src/nclr.h:77-78) in place of the
+//     simulation's one pair (src/nclr.h:74-78);
+//   * the neo-Hookean stress (Stress::kNeoHookean), the model src/nclr.h:339 leaves as a TODO:
+//     Kirchhoff stress mu (F F^T - I) + lambda ln(J) I in place of the fixed-corotated
+//     2 mu (F - R) F^T + constmat(lambda (J - 1) J).
 #pragma once
 
 #include <algorithm>
@@ -38,6 +46,13 @@ namespace oracle {
 
 enum class Model : int { kSnow = 0, kJelly = 1, kLiquid = 2 };  // src/nclr.h:57-61
 enum class Physics : int { kReference = 0, kCorrected = 1 };
+enum class Stress : int { kCorotated = 0, kNeoHookean = 1 };
+
+// mu_0, lambda_0 of (E, nu) in the scalar type (src/nclr.h:77-78).
+template <typename T>
+std::pair<T, T> lame_of(T E, T nu) {
+  return {E / (T(2) * (T(1) + nu)), E * nu / ((T(1) + nu) * (T(1) - T(2) * nu))};
+}
 
 template <typename T, int D>
 struct Vec {
@@ -300,6 +315,8 @@ struct Particle {
   Mat<T, D> F, C;
   T Jp, mass, volume;
   int material = -1;  // per-particle material (an extension); -1: the simulation's model
+  T mu0 = T(-1), lambda0 = T(0);  // per-particle base moduli (an extension); mu0 < 0: the
+                                  // simulation's mu_0, lambda_0
 };
 
 // Cell<dim>, src/nclr.h:50-55.
@@ -342,6 +359,7 @@ class Simulation {
   // Internals are public: the adjoint restatement (nclr_adjoint.h) steps the phases itself.
   const Model model_;
   const Physics mode_;
+  Stress stress_ = Stress::kCorotated;  // the reference's model unless set
   const int res_;
   const T dt_, dx_, inv_dx_, gravity_;
   std::vector<Cell<T, D>> cells_;
@@ -390,7 +408,8 @@ class Simulation {
   }
 
   // hardening, src/nclr.h:351-372.  Snow: e = exp(10*(1.0 - Jp)) in double, narrowed to
-  // the scalar (constant_hardening takes `real`); jelly 0.3; liquid 1.0.
+  // the scalar (constant_hardening takes `real`); jelly 0.3; liquid 1.0.  The base moduli
+  // are the particle's own when it carries them.
   std::pair<T, T> hardening(const Particle<T, D> &p) const {
     T e;
     switch (model_of(p)) {
@@ -399,24 +418,34 @@ class Simulation {
       case Model::kLiquid: e = T(1.0); break;
       default: e = T(0); break;
     }
-    return {mu_0 * e, lambda_0 * e};
+    return p.mu0 < T(0) ? std::pair<T, T>{mu_0 * e, lambda_0 * e}
+                        : std::pair<T, T>{p.mu0 * e, p.lambda0 * e};
   }
 
-  // first_piola_kirchoff_stress, src/nclr.h:313-337.
+  // first_piola_kirchoff_stress, src/nclr.h:313-337 (and the neo-Hookean extension).
   Mat<T, D> affine(const Particle<T, D> &p) const {
     const auto [mu, lambda] = hardening(p);
     const T J = det(p.F);
-    const Mat<T, D> r = nclr_polar_R<T, D>(p.F, mode_);
     const T Dinv = T(4) * inv_dx_ * inv_dx_;
     const Mat<T, D> FT = transpose(p.F);
-    Mat<T, D> FmR;
-    const T two_mu = T(2) * mu;
-    for (int i = 0; i < D; ++i)
-      for (int j = 0; j < D; ++j) FmR(i, j) = two_mu * (p.F(i, j) - r(i, j));
-    Mat<T, D> PF = mul(FmR, FT);
-    const T lam_term = lambda * (J - T(1)) * J;  // constmat: every entry, src/nclr.h:328
-    for (int i = 0; i < D; ++i)
-      for (int j = 0; j < D; ++j) PF(i, j) = PF(i, j) + lam_term;
+    Mat<T, D> PF;
+    if (stress_ == Stress::kNeoHookean) {  // mu (F F^T - I) + lambda ln(J) I
+      PF = mul(p.F, FT);
+      const T lam_term = lambda * std::log(J);
+      for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) PF(i, j) = mu * (PF(i, j) - (i == j ? T(1) : T(0)));
+      for (int i = 0; i < D; ++i) PF(i, i) = PF(i, i) + lam_term;
+    } else {
+      const Mat<T, D> r = nclr_polar_R<T, D>(p.F, mode_);
+      Mat<T, D> FmR;
+      const T two_mu = T(2) * mu;
+      for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) FmR(i, j) = two_mu * (p.F(i, j) - r(i, j));
+      PF = mul(FmR, FT);
+      const T lam_term = lambda * (J - T(1)) * J;  // constmat: every entry, src/nclr.h:328
+      for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) PF(i, j) = PF(i, j) + lam_term;
+    }
     const T s = -(dt_ * p.volume);
     Mat<T, D> out;
     for (int i = 0; i < D; ++i)

@@ -7,6 +7,7 @@
 //   mass[p], volume[p]; grid_vel[node*dim+d], grid_mass[node] in the reference's x-major
 //   node order (src/nclr.h:141-142,152).
 #include <cstring>
+#include <tuple>
 #include <vector>
 
 #include "nclr_adjoint.h"
@@ -21,7 +22,8 @@ template <typename T, int D>
 int run(int physics, int64_t n, double *x, double *v, double *F, double *C, double *Jp,
         const double *mass, const double *volume, int model, int res, double dt, double E,
         double nu, double gravity, int nsteps, double *grid_vel, double *grid_mass,
-        int64_t *counters, const uint8_t *material, int threads = 1) {
+        int64_t *counters, const uint8_t *material, int threads = 1,
+        const double *E_p = nullptr, const double *nu_p = nullptr, int stress = 0) {
   std::vector<Particle<T, D>> ps((size_t)n);
   for (int64_t p = 0; p < n; ++p) {
     auto &q = ps[(size_t)p];
@@ -38,9 +40,11 @@ int run(int physics, int64_t n, double *x, double *v, double *F, double *C, doub
     q.mass = (T)mass[p];
     q.volume = (T)volume[p];
     q.material = material ? (int)material[p] : -1;
+    if (E_p && nu_p) std::tie(q.mu0, q.lambda0) = lame_of<T>((T)E_p[p], (T)nu_p[p]);
   }
   Simulation<T, D> sim(std::move(ps), (Model)model, res, (T)dt, (T)E, (T)nu, (T)gravity,
                        (Physics)physics);
+  sim.stress_ = (Stress)stress;
   int status = 0;
   try {
     for (int s = 0; s < nsteps; ++s) {
@@ -110,7 +114,8 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
             const double *C0, const double *mass, const double *volume, int res, double dt,
             double E, double nu, double gravity, int nsteps, double *xT, double *vT, double *FT,
             double *CT, const double *gx, const double *gv, const double *gF, const double *gC,
-            double *gx0, double *gv0, double *gF0, double *gC0, double *gmu_glambda) {
+            double *gx0, double *gv0, double *gF0, double *gC0, double *gmu_glambda,
+            int stress) {
   using T = double;
   std::vector<Particle<T, D>> ps((size_t)n);
   for (int64_t p = 0; p < n; ++p) {
@@ -130,7 +135,7 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
   }
   try {
     Adjoint<T, D> adj(std::move(ps), Model::kJelly, res, dt, E, nu, gravity, (Physics)physics,
-                      nsteps);
+                      nsteps, (Stress)stress);
     const auto &fin = adj.final_state();
     StepAdjoint<T, D> seed;
     seed.x.resize((size_t)n);
@@ -181,20 +186,21 @@ extern "C" {
 // FP64 reverse pass of an `nsteps` jelly rollout (nclr_adjoint.h): the forward final state
 // into xT/vT/FT/CT, the adjoint of the initial state (given the final state's adjoint
 // gx/gv/gF/gC, any may be NULL = 0) into gx0/gv0/gF0/gC0, and the adjoints of mu_0 and
-// lambda_0 into gmu_glambda[0..1].  Returns 0, 2 (a stencil left the grid) or 1.
+// lambda_0 into gmu_glambda[0..1].  stress: 0 fixed corotated, 1 neo-Hookean.  Returns 0, 2
+// (a stencil left the grid) or 1.
 int oracle_adjoint(int dim, int physics, int64_t n, const double *x0, const double *v0,
                    const double *F0, const double *C0, const double *mass, const double *volume,
                    int res, double dt, double E, double nu, double gravity, int nsteps,
                    double *xT, double *vT, double *FT, double *CT, const double *gx,
                    const double *gv, const double *gF, const double *gC, double *gx0,
-                   double *gv0, double *gF0, double *gC0, double *gmu_glambda) {
-  if (n < 0 || res < 1 || nsteps < 0) return 1;
+                   double *gv0, double *gF0, double *gC0, double *gmu_glambda, int stress) {
+  if (n < 0 || res < 1 || nsteps < 0 || stress < 0 || stress > 1) return 1;
   if (dim == 2)
     return adjoint<2>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
-                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda);
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress);
   if (dim == 3)
     return adjoint<3>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
-                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda);
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress);
   return 1;
 }
 
@@ -232,6 +238,30 @@ int oracle_advance_threads(int dim, int fp64, int physics, int64_t n, double *x,
 #define ORACLE_RUN(T, D)                                                                   \
   return run<T, D>(physics, n, x, v, F, C, Jp, mass, volume, model, res, dt, E, nu, gravity, \
                    nsteps, grid_vel, grid_mass, counters, material, threads)
+  if (dim == 2) {
+    if (fp64) ORACLE_RUN(double, 2);
+    ORACLE_RUN(float, 2);
+  }
+  if (fp64) ORACLE_RUN(double, 3);
+  ORACLE_RUN(float, 3);
+#undef ORACLE_RUN
+}
+
+// oracle_advance with the model extensions: E_p / nu_p (both or neither, may be NULL) give
+// every particle its own Young's modulus and Poisson ratio; stress 0 is the reference's
+// fixed-corotated stress, 1 the neo-Hookean one; threads > 1 runs the multi-threaded step.
+int oracle_advance_ex(int dim, int fp64, int physics, int64_t n, double *x, double *v, double *F,
+                      double *C, double *Jp, const double *mass, const double *volume, int model,
+                      int res, double dt, double E, double nu, double gravity, int nsteps,
+                      double *grid_vel, double *grid_mass, int64_t *counters,
+                      const uint8_t *material, const double *E_p, const double *nu_p,
+                      int stress, int threads) {
+  if (n < 0 || res < 1 || (dim != 2 && dim != 3) || model < 0 || model > 2 || threads < 1 ||
+      stress < 0 || stress > 1 || (!E_p) != (!nu_p))
+    return 1;
+#define ORACLE_RUN(T, D)                                                                   \
+  return run<T, D>(physics, n, x, v, F, C, Jp, mass, volume, model, res, dt, E, nu, gravity, \
+                   nsteps, grid_vel, grid_mass, counters, material, threads, E_p, nu_p, stress)
   if (dim == 2) {
     if (fp64) ORACLE_RUN(double, 2);
     ORACLE_RUN(float, 2);

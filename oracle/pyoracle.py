@@ -18,6 +18,7 @@ _LIBS: dict[str, ctypes.CDLL] = {}
 
 SNOW, JELLY, LIQUID = 0, 1, 2
 REFERENCE, CORRECTED = 0, 1
+COROTATED, NEOHOOKEAN = 0, 1  # stress models
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int64)
@@ -39,6 +40,9 @@ def _load(name: str, sub: str) -> ctypes.CDLL:
                                            _dp, _ip, ctypes.c_void_p]
             lib.oracle_advance_threads.restype = ctypes.c_int
             lib.oracle_advance_threads.argtypes = lib.oracle_advance.argtypes + [ctypes.c_int]
+            lib.oracle_advance_ex.restype = ctypes.c_int
+            lib.oracle_advance_ex.argtypes = lib.oracle_advance.argtypes + [
+                _dp, _dp, ctypes.c_int, ctypes.c_int]
             lib.oracle_svd.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp]
             lib.oracle_polar.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]
             lib.oracle_linspaced.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float,
@@ -46,7 +50,7 @@ def _load(name: str, sub: str) -> ctypes.CDLL:
             lib.oracle_adjoint.restype = ctypes.c_int
             lib.oracle_adjoint.argtypes = ([ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [_dp] * 6 +
                                            [ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int] +
-                                           [_dp] * 13)
+                                           [_dp] * 13 + [ctypes.c_int])
         else:
             lib.ref_advance.restype = ctypes.c_int
             lib.ref_advance.argtypes = [ctypes.c_int, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -87,13 +91,15 @@ def _prep(state: dict, dim: int):
 def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-4,
             E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, steps: int = 1,
             fp64: bool = False, physics: int = REFERENCE, fast: bool = False,
-            want_grid: bool = True, material=None, threads: int = 1):
+            want_grid: bool = True, material=None, threads: int = 1, E_particles=None,
+            nu_particles=None, stress: int = COROTATED):
     """Runs `steps` reference steps on a copy of `state`; returns (state, grid, status, counters).
 
     grid = (velocity (nodes, dim), mass (nodes,)) of the last step, post grid update.
     status 0 = ok, 2 = a grid index left the grid (the reference throws std::out_of_range).
     threads > 1 runs the multi-threaded baseline (nclr_oracle_mt.h): the same step up to the
-    FP32 summation order of the grid.
+    FP32 summation order of the grid.  E_particles / nu_particles (both or neither) give each
+    particle its own moduli; stress picks the fixed-corotated or the neo-Hookean stress.
     """
     n, s = _prep(state, dim)
     mat = None if material is None else np.ascontiguousarray(material, dtype=np.uint8)
@@ -106,7 +112,17 @@ def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-
             _p(gv) if want_grid else None, _p(gm) if want_grid else None,
             counters.ctypes.data_as(_ip), mat.ctypes.data if mat is not None else None)
     lib = oracle_lib(fast)
-    st = lib.oracle_advance_threads(*args, threads) if threads > 1 else lib.oracle_advance(*args)
+    if (E_particles is None) != (nu_particles is None):
+        raise ValueError("E_particles and nu_particles go together")
+    if E_particles is None and stress == COROTATED:
+        st = lib.oracle_advance_threads(*args, threads) if threads > 1 else lib.oracle_advance(*args)
+    else:
+        Ep = nup = None
+        if E_particles is not None:
+            Ep = np.ascontiguousarray(np.broadcast_to(np.asarray(E_particles, np.float64), (n,)))
+            nup = np.ascontiguousarray(np.broadcast_to(np.asarray(nu_particles, np.float64), (n,)))
+        st = lib.oracle_advance_ex(*args, None if Ep is None else _p(Ep),
+                                   None if nup is None else _p(nup), int(stress), max(1, threads))
     return s, ((gv, gm) if want_grid else None), st, counters
 
 
@@ -161,7 +177,8 @@ def lame(E: float, nu: float):
 
 
 def adjoint(state: dict, *, dim: int, res: int, steps: int, dt: float = 1e-4, E: float = 1e4,
-            nu: float = 0.2, gravity: float = -100.0, physics: int = REFERENCE, seed: dict):
+            nu: float = 0.2, gravity: float = -100.0, physics: int = REFERENCE, seed: dict,
+            stress: int = COROTATED):
     """FP64 jelly rollout and its reverse pass.  `seed` holds the final state's adjoint (keys
     among x, v, F, C).  Returns (final state, adjoint of the initial state incl. 'E' and 'nu')."""
     n, s = _prep(state, dim)
@@ -174,7 +191,7 @@ def adjoint(state: dict, *, dim: int, res: int, steps: int, dt: float = 1e-4, E:
         dim, physics, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]), _p(s["mass"]),
         _p(s["volume"]), res, dt, E, nu, gravity, steps, _p(out["x"]), _p(out["v"]),
         _p(out["F"]), _p(out["C"]), *(None if sd[k] is None else _p(sd[k]) for k in ("x", "v", "F", "C")),
-        _p(g["x"]), _p(g["v"]), _p(g["F"]), _p(g["C"]), _p(ml))
+        _p(g["x"]), _p(g["v"]), _p(g["F"]), _p(g["C"]), _p(ml), int(stress))
     if st != 0:
         raise RuntimeError(f"oracle adjoint failed ({st})")
     _, _, dmu, dlam = lame(E, nu)

@@ -50,6 +50,20 @@ def state_at(z, k):
     return s
 
 
+def random_state(rng, dim, n, res, physics):
+    """Seeded random particles in the middle of the box: velocities of order 0.3, F a 1%
+    perturbation of the physics' identity, C of order 0.5, Jp, mass and volume varied."""
+    from nuclearmpm_gb300 import scenes
+    x = rng.uniform(0.3, 0.7, size=(n, dim)).astype(np.float32)
+    s = scenes.particles(x, rng.normal(0, 0.3, size=(n, dim)).astype(np.float32), physics=physics)
+    s["F"] = (s["F"] + rng.normal(0, 0.01, size=s["F"].shape)).astype(np.float32)
+    s["C"] = rng.normal(0, 0.5, size=s["C"].shape).astype(np.float32)
+    s["Jp"] = rng.uniform(0.9, 1.1, size=n).astype(np.float32)
+    s["mass"] = rng.uniform(0.5, 2.0, size=n).astype(np.float32)
+    s["volume"] = rng.uniform(0.5, 2.0, size=n).astype(np.float32)
+    return s
+
+
 @pytest.fixture(scope="session")
 def oracle():
     from oracle import pyoracle

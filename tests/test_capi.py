@@ -30,6 +30,7 @@ def test_default_options():
     o = capi.default_options()
     assert (o.physics, o.sort_interval, o.p2g_particles_per_thread, o.device, o.use_graphs) == (0, 8, 1, 0, 1)
     assert (o.sparse_block_max, o.small_scene_max) == (-1, -1)
+    assert o.stress_model == capi.STRESS_COROTATED
 
 
 def test_invalid_arguments_are_rejected_before_touching_a_device():
@@ -41,6 +42,21 @@ def test_invalid_arguments_are_rejected_before_touching_a_device():
     assert L.nclr_create(ctypes.byref(h), 2, 5, None, None, None, None, None, None, None, None,
                          0, 64, 1e-4, 1e4, 0.2, -100.0, None) == capi.NCLR_ERR_INVALID
     assert L.nclr_advance(None, 1) == capi.NCLR_ERR_INVALID
+    assert L.nclr_set_moduli(None, None, None) == capi.NCLR_ERR_INVALID
+
+
+@pytest.mark.parametrize("dim,physics,stress", [
+    (3, capi.PHYSICS_REFERENCE, capi.STRESS_NEOHOOKEAN),  # det F = 0 under diag(1,1,0)
+    (2, capi.PHYSICS_REFERENCE, 7),
+    (3, capi.PHYSICS_CORRECTED, -1),
+])
+def test_stress_model_is_validated_before_touching_a_device(dim, physics, stress):
+    L = capi.lib()
+    h = ctypes.c_void_p()
+    opt = capi.default_options(physics=physics, stress_model=stress)
+    assert L.nclr_create(ctypes.byref(h), dim, 0, None, None, None, None, None, None, None, None,
+                         1, 16, 1e-4, 1e4, 0.2, -100.0, ctypes.byref(opt)) == capi.NCLR_ERR_INVALID
+    assert b"stress" in L.nclr_last_error(None)
 
 
 @pytest.mark.skipif(os.environ.get("CUDA_VISIBLE_DEVICES") is None and

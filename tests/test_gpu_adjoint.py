@@ -24,9 +24,10 @@ def setup(dim, res, n, physics, seed=0):
     return s
 
 
-def gpu_grads(s, dim, res, steps, physics, every, seed_fn, E=1e4, nu=0.2):
+def gpu_grads(s, dim, res, steps, physics, every, seed_fn, E=1e4, nu=0.2, stress=0):
     from nuclearmpm_gb300.autograd import Rollout
-    roll = Rollout(s["x"], res=res, steps=steps, checkpoint_every=every, physics=physics)
+    roll = Rollout(s["x"], res=res, steps=steps, checkpoint_every=every, physics=physics,
+                   stress_model=stress)
     dev = torch.device("cuda", 0)
     x0 = torch.tensor(s["x"], device=dev, requires_grad=True)
     v0 = torch.tensor(s["v"], device=dev, requires_grad=True)
@@ -62,15 +63,20 @@ def rel(a, b):
 
 @pytest.mark.parametrize("dim,res,steps,n", [(2, 32, 50, 1024), (3, 16, 10, 512)])
 @pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
-def test_gpu_adjoint_matches_fp64_adjoint(oracle, dim, res, steps, n, physics):
+@pytest.mark.parametrize("stress", [0, 1])  # fixed corotated, neo-Hookean
+def test_gpu_adjoint_matches_fp64_adjoint(oracle, dim, res, steps, n, physics, stress):
+    if stress == 1 and dim == 3 and physics == scenes.REFERENCE:
+        pytest.skip("the neo-Hookean stress needs det F > 0")
     s = setup(dim, res, n, physics)
     rng = np.random.default_rng(3)
+    kw = dict(dim=dim, res=res, steps=steps, physics=physics, stress=stress)
     # pointwise loss: depends on the deformation (E / nu gradients non-zero)
-    fwd, _ = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={})
+    fwd, _ = oracle.adjoint(s, seed={}, **kw)
     targets = (fwd["x"] + rng.normal(0, 1e-3, size=fwd["x"].shape)).astype(np.float32)
-    g = gpu_grads(s, dim, res, steps, physics, every=7, seed_fn=point_loss(targets))
+    g = gpu_grads(s, dim, res, steps, physics, every=7, seed_fn=point_loss(targets),
+                  stress=stress)
     seed = 2 * (g["xT"].astype(np.float64) - targets)  # the GPU's own final state
-    _, o = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={"x": seed})
+    _, o = oracle.adjoint(s, seed={"x": seed}, **kw)
     for f in ("x", "v", "F", "C"):
         assert rel(g[f], o[f]) <= GRAD_TOL, (f, rel(g[f], o[f]))
     for p in ("E", "nu"):

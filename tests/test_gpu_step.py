@@ -14,7 +14,7 @@ Tolerances (FP32; error = max|gpu - ref| / max(max|ref|, floor), floors in conft
 import numpy as np
 import pytest
 
-from conftest import DRIFT, FIELDS, field_err, golden_names, load_golden, state_at
+from conftest import DRIFT, FIELDS, field_err, golden_names, load_golden, random_state, state_at
 from nuclearmpm_gb300 import MPMSimulation, OutOfRange, scenes
 
 pytestmark = pytest.mark.gpu
@@ -70,17 +70,6 @@ def test_one_step_from_reference_midrun_state(name):
         assert field_err(out[f], z[f"{f}@{b}"], f) <= MIDRUN[f], f
 
 
-def _random_state(rng, dim, n, res, physics):
-    x = rng.uniform(0.3, 0.7, size=(n, dim)).astype(np.float32)
-    s = scenes.particles(x, rng.normal(0, 0.3, size=(n, dim)).astype(np.float32), physics=physics)
-    s["F"] = (s["F"] + rng.normal(0, 0.01, size=s["F"].shape)).astype(np.float32)
-    s["C"] = rng.normal(0, 0.5, size=s["C"].shape).astype(np.float32)
-    s["Jp"] = rng.uniform(0.9, 1.1, size=n).astype(np.float32)
-    s["mass"] = rng.uniform(0.5, 2.0, size=n).astype(np.float32)
-    s["volume"] = rng.uniform(0.5, 2.0, size=n).astype(np.float32)
-    return s
-
-
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("model", [scenes.SNOW, scenes.JELLY, scenes.LIQUID])
 @pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
@@ -96,7 +85,7 @@ def test_one_step_vs_oracle_random(oracle, dim, model, physics, thin):
                     "rotation is not unique, so parity there is implementation-defined")
     rng = np.random.default_rng(100 * dim + 10 * model + physics)
     res = 32
-    s = _random_state(rng, dim, 2000 if dim == 2 else 4000, res, physics)
+    s = random_state(rng, dim, 2000 if dim == 2 else 4000, res, physics)
     path = dict(small_scene_max=-1) if thin == -2 else dict(small_scene_max=0, sparse_block_max=thin)
     out, grid = run_gpu(s, dict(model=model, res=res, dt=1e-4, E=1e4, nu=0.2, gravity=-100.0), 1,
                         physics=physics, **path)
@@ -147,7 +136,7 @@ def test_particle_order_is_callers_after_sorting():
 
 def test_set_and_get_round_trip():
     rng = np.random.default_rng(4)
-    s = _random_state(rng, 3, 500, 32, scenes.REFERENCE)
+    s = random_state(rng, 3, 500, 32, scenes.REFERENCE)
     sim = MPMSimulation(dict(s), scenes.JELLY, res=32)
     p = sim.particles()
     for f in ("x", "v", "F", "C", "Jp"):

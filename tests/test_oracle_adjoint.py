@@ -3,13 +3,16 @@ differences.  Loss 1 = |centre of mass of the final positions - target|^2 (gradi
 respect to initial velocities, positions and deformation gradients); internal forces conserve
 momentum, so away from the boundary this loss does not depend on the material and its E / nu
 gradients vanish -- loss 2 = sum_p m_p |x_p - target_p|^2 over the final positions depends on
-the deformation and checks the Young's modulus and Poisson ratio gradients."""
+the deformation and checks the Young's modulus and Poisson ratio gradients.  Both stress
+models: the reference's fixed-corotated one and the neo-Hookean extension (3D under the
+corrected physics only: the reference's diag<3>(1) = diag(1,1,0) leaves det F near 0)."""
 import numpy as np
 import pytest
 
 from nuclearmpm_gb300 import scenes
 
 CASES = [(2, 32, 50, 1024), (3, 16, 10, 216)]  # dim, res, steps, particles
+COROTATED, NEOHOOKEAN = 0, 1
 
 
 def setup(dim, res, n, physics, seed=0):
@@ -34,20 +37,25 @@ def pointwise(xT, mass, targets):
     return float((mass[:, None] * d * d).sum()), 2 * mass[:, None] * d
 
 
-def forward_loss(oracle, s, target, dim, res, steps, physics, E=1e4, nu=0.2, loss=loss_and_seed):
+def forward_loss(oracle, s, target, dim, res, steps, physics, E=1e4, nu=0.2, loss=loss_and_seed,
+                 stress=COROTATED):
     out, _, st, _ = oracle.advance(s, dim=dim, model=scenes.JELLY, res=res, steps=steps, fp64=True,
-                                   physics=physics, E=E, nu=nu, want_grid=False)
+                                   physics=physics, E=E, nu=nu, want_grid=False, stress=stress)
     assert st == 0
     return loss(out["x"], s["mass"], target)[0]
 
 
 @pytest.mark.parametrize("dim,res,steps,n", CASES)
 @pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
-def test_oracle_adjoint_matches_finite_differences(oracle, dim, res, steps, n, physics):
+@pytest.mark.parametrize("stress", [COROTATED, NEOHOOKEAN])
+def test_oracle_adjoint_matches_finite_differences(oracle, dim, res, steps, n, physics, stress):
+    if stress == NEOHOOKEAN and dim == 3 and physics == scenes.REFERENCE:
+        pytest.skip("the neo-Hookean stress needs det F > 0")
     s, target = setup(dim, res, n, physics)
-    out, _ = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={})
+    kw = dict(dim=dim, res=res, steps=steps, physics=physics, stress=stress)
+    out, _ = oracle.adjoint(s, seed={}, **kw)
     _, seed = loss_and_seed(out["x"], s["mass"], target)
-    _, g = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={"x": seed})
+    _, g = oracle.adjoint(s, seed={"x": seed}, **kw)
     rng = np.random.default_rng(1)
     checks = []
     for _ in range(4):
@@ -60,20 +68,22 @@ def test_oracle_adjoint_matches_finite_differences(oracle, dim, res, steps, n, p
         sm = {k: v.copy() for k, v in s.items()}
         sp[field][idx] += h
         sm[field][idx] -= h
-        fd = (forward_loss(oracle, sp, target, dim, res, steps, physics) -
-              forward_loss(oracle, sm, target, dim, res, steps, physics)) / (2 * h)
+        fd = (forward_loss(oracle, sp, target, dim, res, steps, physics, stress=stress) -
+              forward_loss(oracle, sm, target, dim, res, steps, physics, stress=stress)) / (2 * h)
         ad = g[field][idx]
         assert abs(ad - fd) <= 1e-6 * max(1.0, abs(fd)) + 1e-4 * abs(fd), (field, idx, ad, fd)
     assert abs(g["E"]) < 1e-15 and abs(g["nu"]) < 1e-12  # momentum conservation
     targets = out["x"] + np.random.default_rng(2).normal(0, 1e-3, size=out["x"].shape)
     _, seed2 = pointwise(out["x"], s["mass"], targets)
-    _, g2 = oracle.adjoint(s, dim=dim, res=res, steps=steps, physics=physics, seed={"x": seed2})
+    _, g2 = oracle.adjoint(s, seed={"x": seed2}, **kw)
     for name, h in (("E", 1.0), ("nu", 1e-5)):
         kp = {"E": 1e4, "nu": 0.2}
         km = dict(kp)
         kp[name] += h
         km[name] -= h
-        fd = (forward_loss(oracle, s, targets, dim, res, steps, physics, loss=pointwise, **kp) -
-              forward_loss(oracle, s, targets, dim, res, steps, physics, loss=pointwise, **km)) / (2 * h)
+        fd = (forward_loss(oracle, s, targets, dim, res, steps, physics, loss=pointwise,
+                           stress=stress, **kp) -
+              forward_loss(oracle, s, targets, dim, res, steps, physics, loss=pointwise,
+                           stress=stress, **km)) / (2 * h)
         assert abs(fd) > 0
         assert abs(g2[name] - fd) <= 1e-4 * abs(fd), (name, g2[name], fd)
