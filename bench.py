@@ -391,8 +391,48 @@ def run_readme(device: int, steps: int = 4000, cpu_steps: int = 400) -> dict:
                       "physics, CUDA graphs of 200 steps"}
 
 
+def run_models(device: int, steps: int = 100) -> dict:
+    """The model extensions on the headline geometry: the four jittered 64^3 jelly lattices,
+    128^3 grid, under the corrected physics (det F > 0, which the neo-Hookean stress needs).
+    Three runs: the reference's fixed-corotated stress; the neo-Hookean stress; and the
+    corotated stress with every particle's own E (log-uniform in [1e3, 1e4]) and nu (uniform
+    in [0.1, 0.4]). Each is `steps` steps, timed with CUDA events on the simulation's stream
+    after warm-up."""
+    import torch
+
+    from nuclearmpm_gb300 import MPMSimulation, capi, scenes
+    sc = scenes.jelly_cubes_3d(seed=0, res=128, physics=scenes.CORRECTED)
+    n = len(sc["x"])
+    rng = np.random.default_rng(0)
+    E = np.exp(rng.uniform(np.log(1e3), np.log(1e4), size=n)).astype(np.float32)
+    nu = rng.uniform(0.1, 0.4, size=n).astype(np.float32)
+    out = {"unit": UNIT, "particles": n, "steps": steps}
+    for name, stress, own in (("corotated", capi.STRESS_COROTATED, False),
+                              ("neohookean", capi.STRESS_NEOHOOKEAN, False),
+                              ("per_particle_moduli", capi.STRESS_COROTATED, True)):
+        sim = MPMSimulation(dict(sc), scenes.JELLY, res=128, physics=scenes.CORRECTED,
+                            stress_model=stress, device=device)
+        if own:
+            sim.set_moduli(E, nu)
+        sim.advance(10)
+        st = torch.cuda.ExternalStream(sim.stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        sim.advance(steps)
+        b.record(st)
+        b.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        out[name] = {"value": n * steps / t, "ms_per_step": t / steps * 1e3,
+                     "gpu_launches": sim.stats()[0]}
+        sim.close()
+    out["config"] = ("3D jelly, the 1M-particle scene of the headline built under the corrected "
+                     "physics, 128^3 grid, dt 1e-4; corotated / neo-Hookean stress / corotated "
+                     "with per-particle E in [1e3, 1e4] and nu in [0.1, 0.4]")
+    return out
+
+
 FORMS = {"batched": run_batched, "adjoint": run_adjoint, "mixed": run_mixed, "snow": run_snow,
-         "readme": run_readme}
+         "readme": run_readme, "models": run_models}
 
 
 def run_form(args):
@@ -543,6 +583,9 @@ def run_ours(args):
     readme = None
     if not args.no_readme and rank == 0:
         readme = run_readme(local)
+    models = None
+    if not args.no_models:
+        models = run_models(local)
 
     cpu = cpu_mt = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -567,7 +610,7 @@ def run_ours(args):
                 "roofline": roofline, "cpu_baseline": cpu, "cpu_baseline_mt": cpu_mt,
                 "e2e": e2e, "batched": batched,
                 "adjoint": adjoint, "mixed": mixed, "snow": snow, "readme": readme,
-                "gpu_launches": launches_total, "clocks": clk}
+                "models": models, "gpu_launches": launches_total, "clocks": clk}
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
@@ -588,6 +631,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-snow", action="store_true")
     ap.add_argument("--no-readme", action="store_true")
+    ap.add_argument("--no-models", action="store_true")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the end-to-end (host buffers) measurement, e.g. for a launch list "
                          "of the device-resident steps alone")

@@ -340,6 +340,12 @@ class MPMSimulation {
 
   MPMSimulation(std::vector<Particle<dim>> particles, const MaterialModel model, int res = 64,
                 real dt = 1e-4, real E = 1e4, real nu = 0.2, real gravity = -100)
+      : MPMSimulation(std::move(particles), model, res, dt, E, nu, gravity, nullptr) {}
+
+  // An extension: the same with the options of include/nclr_gpu.h (physics mode, stress
+  // model, sort interval, ...); opt == nullptr gives the defaults.
+  MPMSimulation(std::vector<Particle<dim>> particles, const MaterialModel model, int res,
+                real dt, real E, real nu, real gravity, const nclr_options *opt)
       : mu_0(E / (2 * (1 + nu))), lambda_0(E * nu / ((1 + nu) * (1 - 2 * nu))),
         particles_(std::move(particles)), res_(res) {
     const size_t n = particles_.size();
@@ -363,7 +369,7 @@ class MPMSimulation {
     nclr_sim *h = nullptr;
     const nclr_status st =
         nclr_create(&h, dim, (int64_t)n, x.data(), v.data(), F.data(), C.data(), Jp.data(),
-                    m.data(), vol.data(), nullptr, (int)model, res, dt, E, nu, gravity, nullptr);
+                    m.data(), vol.data(), nullptr, (int)model, res, dt, E, nu, gravity, opt);
     if (st != NCLR_OK) throw std::runtime_error(std::string("nclr_create: ") + nclr_last_error(nullptr));
     sim_.reset(h);
   }
@@ -392,6 +398,17 @@ class MPMSimulation {
   auto grid() const -> const std::vector<Cell<dim>> & {
     if (!grid_fresh_) download_grid();
     return cells_;
+  }
+
+  // An extension: every particle's own Young's modulus and Poisson ratio (one value each per
+  // particle, in the order of the constructor's particles), from the next advance() on; empty
+  // vectors return to the simulation's E and nu.
+  auto set_moduli(const std::vector<real> &E, const std::vector<real> &nu) -> void {
+    if (E.size() != nu.size() || (!E.empty() && E.size() != particles_.size()))
+      throw std::invalid_argument("set_moduli takes one E and one nu per particle");
+    const nclr_status st = E.empty() ? nclr_set_moduli(sim_.get(), nullptr, nullptr)
+                                     : nclr_set_moduli(sim_.get(), E.data(), nu.data());
+    if (st != NCLR_OK) throw std::runtime_error(nclr_last_error(sim_.get()));
   }
 
   // The underlying C handle, for the extensions of include/nclr_gpu.h.

@@ -17,7 +17,7 @@
 //   * --render writes every --render-every'th step as a PPM frame drawn on the device
 //     (nclr_render_device: the canvas of src/solver.cpp:184-201, headless);
 //   * --out DIR (default tmp), --res (default 64, the reference's kGridResolution),
-//     --physics reference|corrected, --device N.
+//     --physics reference|corrected, --stress corotated|neohookean, --device N.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -66,6 +66,7 @@ void help_msg() {
       "\t--out\tDIR\t[default:tmp]\tOutput directory\n"
       "\t--res\tINTEGER\t[default:64]\tGrid resolution\n"
       "\t--physics\t[reference, corrected]\t[default:reference]\n"
+      "\t--stress\t[corotated, neohookean]\t[default:corotated]\tThe stress model\n"
       "\t--device\tINTEGER\t[default:0]\tCUDA device\n"
       "\t--help\tShow this message and exit\n");
 }
@@ -294,6 +295,11 @@ int main(int argc, char **argv) {
   const fs::path out = args.str("out", "tmp");
   const int device = (int)args.num("device", 0);
   const std::string physics = args.str("physics", "reference");
+  const std::string stress = args.str("stress", "corotated");
+  if (stress != "corotated" && stress != "neohookean") {
+    std::fprintf(stderr, "Invalid Option: %s\n", stress.c_str());
+    return EXIT_FAILURE;
+  }
   if (dim != 2 && dim != 3) {
     std::fprintf(stderr, "--dim must be 2 or 3\n");
     return EXIT_FAILURE;
@@ -324,6 +330,7 @@ int main(int argc, char **argv) {
   nclr_default_options(&opt);
   opt.device = device;
   opt.physics = physics == "corrected" ? NCLR_PHYSICS_CORRECTED : NCLR_PHYSICS_REFERENCE;
+  opt.stress_model = stress == "neohookean" ? NCLR_STRESS_NEOHOOKEAN : NCLR_STRESS_COROTATED;
   nclr_sim *sim = nullptr;
   check(nclr_create_device(&sim, dim, n, x, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
                            nullptr, model, res, kDt, E, nu, gravity, &opt),

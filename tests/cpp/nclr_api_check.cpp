@@ -1,8 +1,10 @@
 // Drives the drop-in C++ API (include/nclr.h) the way an embedder of the reference's header
 // does: builds the two-cube 2D snow scene with cube<2>(), constructs MPMSimulation<2>, steps
 // it with advance() and reads particles() and grid(); then checks the out-of-range error and a
-// small 3D jelly run.  Writes the initial and final particle states to a binary file so the
-// Python test can compare them with the CPU oracle.
+// small 3D jelly run; then the extensions: the same scene with the neo-Hookean stress (an
+// nclr_options constructor) and per-particle moduli (set_moduli).  Writes the initial and
+// final particle states to <out.bin>, and the extension run's initial state, final state and
+// moduli to <out.bin>.ext, so the Python test can compare them with the CPU oracle.
 //
 //   nclr_api_check <out.bin> <steps>
 // Exit codes: 0 ok, 10+ a failed check.
@@ -10,6 +12,8 @@
 #include <cstdlib>
 #include <fstream>
 #include <memory>
+#include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "nclr.h"
@@ -82,6 +86,32 @@ int main(int argc, char **argv) {
   const float dz = sim3.particles()[0].x(2) - p3[0].x(2);
   if (!(dz < 1e-3f && dz > -1e-3f)) return 16;
   if (sim3.mu_0 <= 0.0f || sim3.lambda_0 <= 0.0f) return 17;
+
+  // Extensions: neo-Hookean stress and one E / nu per particle.
+  nclr_options opt;
+  nclr_default_options(&opt);
+  opt.stress_model = NCLR_STRESS_NEOHOOKEAN;
+  MPMSimulation<2> ext(particles, MaterialModel::kSnow, 64, 1e-4f, 1e4f, 0.2f, -100.0f, &opt);
+  std::vector<real> E(particles.size()), nu(particles.size());
+  for (size_t p = 0; p < particles.size(); ++p) {
+    E[p] = 2000.0f + 37.0f * (float)(p % 1000);
+    nu[p] = 0.1f + 0.0003f * (float)(p % 1000);
+  }
+  bool rejected = false;
+  try {
+    ext.set_moduli(std::vector<real>(3, 1.0f), std::vector<real>(3, 0.2f));
+  } catch (const std::invalid_argument &) {
+    rejected = true;
+  }
+  if (!rejected) return 18;
+  ext.set_moduli(E, nu);
+  for (int s = 0; s < steps; ++s) ext.advance();
+  std::ofstream g(std::string(out) + ".ext", std::ios::binary);
+  write_state<2>(g, particles);
+  write_state<2>(g, ext.particles());
+  g.write(reinterpret_cast<const char *>(E.data()), sizeof(real) * E.size());
+  g.write(reinterpret_cast<const char *>(nu.data()), sizeof(real) * nu.size());
+  g.close();
   std::printf("ok\n");
   return 0;
 }

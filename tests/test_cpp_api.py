@@ -50,3 +50,15 @@ def test_header_example_matches_oracle(tmp_path, oracle):
     assert st == 0
     for f in ("x", "v", "F", "C", "Jp"):
         assert field_err(final[f], ref[f], f) <= 1e-5, f
+    # the extensions: neo-Hookean stress, one E / nu per particle
+    raw = np.fromfile(out + ".ext", dtype=np.float32)
+    states = raw[:2 * 5000 * rec].reshape(2, 5000, rec)
+    E, nu = raw[2 * 5000 * rec:].reshape(2, 5000)
+    init, final = unpack(states[0]), unpack(states[1])
+    init["mass"] = np.ones(5000, np.float32)
+    init["volume"] = np.ones(5000, np.float32)
+    ref, _, st, _ = oracle.advance(init, dim=2, model=0, res=64, steps=1, stress=1,
+                                   E_particles=E, nu_particles=nu)
+    assert st == 0
+    for f in ("x", "v", "F", "C", "Jp"):
+        assert field_err(final[f], ref[f], f) <= 1e-5, f

@@ -30,10 +30,11 @@ def solver(*args, cwd=None):
                           timeout=300)
 
 
-def api_states(dim, model, cubes, cube_res, steps, E=1000.0, nu=0.3, gravity=-100.0):
+def api_states(dim, model, cubes, cube_res, steps, E=1000.0, nu=0.3, gravity=-100.0, **kw):
     """The same run through the Python API: particles before each advance, grid after."""
     x = np.concatenate([scenes.cube(dim, cube_res, lo, hi) for lo, hi in cubes])
-    sim = MPMSimulation(scenes.particles(x), model, res=64, dt=1e-4, E=E, nu=nu, gravity=gravity)
+    sim = MPMSimulation(scenes.particles(x, physics=kw.get("physics", scenes.REFERENCE)), model,
+                        res=64, dt=1e-4, E=E, nu=nu, gravity=gravity, **kw)
     out = []
     for _ in range(steps):
         p = sim.particles()
@@ -78,6 +79,24 @@ def test_dump_equals_the_api_run(tmp_path, dim, material, model):
         assert math.isclose(mu, sim_mu * e, rel_tol=1e-6) and math.isclose(lam, sim_lam * e, rel_tol=1e-6)
         expected_ts = np.float32(1e-4) * np.float32(s) if s > 0 else np.float32(1e-4)
         assert got.timestep[0] == expected_ts
+
+
+def test_neohookean_dump_equals_the_api_run(tmp_path):
+    """--stress neohookean (3D, --physics corrected) steps as the API with the same options."""
+    steps, cube_res = 10, 6
+    r = solver("--dim", 3, "--steps", steps, "--cube-res", cube_res, "--cube0-x", 0.4,
+               "--cube0-y", 0.55, "--material-model", "jelly", "--physics", "corrected",
+               "--stress", "neohookean", "--dump", "--out", tmp_path)
+    assert r.returncode == 0, r.stderr
+    res = dumpio.load(str(tmp_path / "dump.nclr"))
+    ref = api_states(3, scenes.JELLY, [(0.4, 0.55)], cube_res, steps,
+                     physics=scenes.CORRECTED, stress_model=capi.STRESS_NEOHOOKEAN)
+    for s, (p, _) in enumerate(ref):
+        for f in FIELDS:
+            assert field_err(getattr(res[f"{s}_"], f).astype(np.float32), p[f], f) <= DRIFT[f], (s, f)
+    bad = solver("--stress", "hookean", "--cube0-x", 0.4, "--cube0-y", 0.6, "--steps", 1,
+                 "--out", tmp_path)
+    assert bad.returncode != 0 and "Invalid Option" in bad.stderr
 
 
 def test_missing_cube_coordinates_is_an_error(tmp_path):
