@@ -407,6 +407,10 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
   const int nitems = nact + (nsp + kG2P2GThreads - 1) / kG2P2GThreads;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float4 *mytile = gt + warp * GS;
+  // The G tiles start clear and every item's flush clears what it read, so they are clear
+  // again at the start of the next item (padding entries are never written).
+  for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
+    gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
   for (;;) {
     __syncthreads();
@@ -462,9 +466,6 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
             in ? __ldg(V + flat_index<D>(g, N)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
     }
-    if (!chunk)
-      for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
-        gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     __syncthreads();
 
     // The block's particles, stored cell by cell in rounds (see sort_move_kernel), one per
@@ -636,6 +637,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
       }
       const int ti = tile_index<D>(l[0], l[1], l[2]);
       float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      bool touched = false;
 #pragma unroll
       for (int wi = 0; wi < kWarps; ++wi) {
         const float4 g4 = gt[wi * GS + ti];
@@ -643,7 +645,11 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
         a[1] += g4.y;
         a[2] += g4.z;
         a[3] += g4.w;
+        touched |= g4.x != 0.0f || g4.y != 0.0f || g4.z != 0.0f || g4.w != 0.0f;
       }
+      if (!touched) continue;
+#pragma unroll
+      for (int wi = 0; wi < kWarps; ++wi) gt[wi * GS + ti] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (a[0] == 0.0f && a[1] == 0.0f && a[2] == 0.0f && a[3] == 0.0f) continue;
       if (in) red_add_v4(G + flat_index<D>(g, N), a[0], a[1], a[2], a[3]);
     }
