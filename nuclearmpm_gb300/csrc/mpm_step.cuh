@@ -472,8 +472,8 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
     // thread in slot order.  Every lane of a warp runs the same number of iterations (the
     // warp-wide steps below need them all).
     const int c0 = (item - nact) * kG2P2GThreads;
-    const int p0 = chunk ? 0 : bstart[gb * CPB];
-    const int np = chunk ? min(kG2P2GThreads, nsp - c0) : bstart[(gb + 1) * CPB] - p0;
+    const int p0 = chunk ? 0 : bstart[gb];
+    const int np = chunk ? min(kG2P2GThreads, nsp - c0) : bstart[gb + 1] - p0;
     for (int j0 = 0; j0 < np; j0 += kG2P2GThreads) {
       const int j = j0 + threadIdx.x;
       const bool valid = j < np;
@@ -825,21 +825,31 @@ __global__ void block_keys_kernel(const float *__restrict__ xs, const uint16_t *
 // in rounds -- the first particle of every non-empty cell (cells in x-major order), then the
 // second of every cell that has two, and so on -- so consecutive slots lie in different,
 // neighbouring cells.  Particle `rank` of cell c goes to
-//   start[block] + sum_c' min(count[c'], rank) + #{c' < c : count[c'] > rank}.
+//   bstart[block] + sum_c' min(count[c'], rank) + #{c' < c : count[c'] > rank},
+// which the block's round table holds for ranks below kRoundTable (block_tables_kernel);
+// later ranks count cell by cell.
 template <int D>
 __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__restrict__ key,
-                                 const int *__restrict__ rank, const int *__restrict__ start,
-                                 const int *__restrict__ count, int move_vc, int *__restrict__ inv,
-                                 int *__restrict__ slot_block) {
+                                 const int *__restrict__ rank, const int *__restrict__ bstart,
+                                 const int4 *__restrict__ rounds, const int *__restrict__ count,
+                                 int move_vc, int *__restrict__ inv, int *__restrict__ slot_block) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   constexpr int CPB = Tiling<D>::CPB;
+  static_assert(CPB == kCellsPerBlock, "the round tables assume 64 cells per block");
   const int k = key[p], r = rank[p];
-  const int b0 = k - k % CPB, c = k % CPB;
-  int q = start[b0];
-  for (int cc = 0; cc < CPB; ++cc) {
-    const int m = __ldg(count + b0 + cc);
-    q += min(m, r) + ((cc < c && m > r) ? 1 : 0);
+  const int blk = k / CPB, c = k % CPB;
+  int q = __ldg(bstart + blk);
+  if (r < kRoundTable) {
+    const int4 t = __ldg(rounds + (int64_t)blk * kRoundTable + r);
+    const unsigned long long m = ((unsigned long long)(unsigned)t.z << 32) | (unsigned)t.y;
+    q += t.x + __popcll(m & ((1ull << c) - 1ull));
+  } else {
+    const int b0 = blk * CPB;
+    for (int cc = 0; cc < CPB; ++cc) {
+      const int m = __ldg(count + b0 + cc);
+      q += min(m, r) + ((cc < c && m > r) ? 1 : 0);
+    }
   }
   const int ss = src.stride, ds = dst.stride;
 #pragma unroll
@@ -852,7 +862,7 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
   const int id = src.id[p];
   dst.id[q] = id;
   inv[id] = q;                     // caller row -> slot
-  slot_block[q] = k / CPB;         // the block this slot now belongs to
+  slot_block[q] = blk;             // the block this slot now belongs to
   if (src.mat) dst.mat[q] = src.mat[p];
   if (src.lame) dst.lame[q] = src.lame[p];
   if (src.scene) dst.scene[q] = src.scene[p];
@@ -1302,11 +1312,11 @@ void launch_block_keys(const PState &s, int n, const Scene *scenes, int *key, in
 
 template <int D>
 void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank,
-                      const int *start, const int *count, bool move_vc, int *inv, int *slot_block,
-                      cudaStream_t st) {
+                      const int *bstart, const int4 *rounds, const int *count, bool move_vc,
+                      int *inv, int *slot_block, cudaStream_t st) {
   if (n == 0) return;
-  sort_move_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, key, rank, start, count,
-                                                          move_vc ? 1 : 0, inv, slot_block);
+  sort_move_kernel<D><<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, key, rank, bstart, rounds,
+                                                          count, move_vc ? 1 : 0, inv, slot_block);
 }
 
 #define MPM_INSTANTIATE(D)                                                                       \
@@ -1338,6 +1348,7 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
   template void launch_block_keys<D>(const PState &, int, const Scene *, int *, int *, int *,    \
                                      cudaStream_t);                                              \
   template void launch_sort_move<D>(const PState &, const PState &, int, const int *, const int *, \
-                                    const int *, const int *, bool, int *, int *, cudaStream_t);
+                                    const int *, const int4 *, const int *, bool, int *, int *,    \
+                                    cudaStream_t);
 
 }  // namespace mpm

@@ -50,7 +50,10 @@ struct nclr_sim {
   float4 *G = nullptr;        // P2G accumulator of the coming step
   float4 *V = nullptr;        // updated grid of the last step (grid())
   uint8_t *flags = nullptr;   // per grid block: pending contributions in G / non-zero V
-  int *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *tile_sums = nullptr;
+  int *key = nullptr, *rank = nullptr, *count = nullptr, *tile_sums = nullptr;
+  int *btotal = nullptr;      // particles per grid block (the last sort)
+  int *start = nullptr;       // first slot of every grid block (exclusive scan of btotal)
+  int4 *rounds = nullptr;     // per-block round tables of the slot order (see sort_move_kernel)
   int *blocks = nullptr;      // non-empty blocks of the last sort (the dense ones)
   int *nblocks_active = nullptr;  // [0] dense blocks in `blocks`, [1] slots in `sparse`
   int *sparse = nullptr;      // particle slots of the thin blocks (stepped without a tile)
@@ -227,21 +230,24 @@ void enqueue_sort(nclr_sim *s, bool move_vc) {
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     constexpr int cpb = mpm::Tiling<D>::CPB;
-    phase(s, NCLR_PHASE_SORT, 6, [&] {
+    static_assert(cpb == mpm::kCellsPerBlock, "the round tables assume 64 cells per block");
+    phase(s, NCLR_PHASE_SORT, 7, [&] {
       cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)s->nkeys, s->stream);
       cudaMemsetAsync(s->nblocks_active, 0, 2 * sizeof(int), s->stream);
       mpm::launch_block_keys<D>(s->ps[s->cur], (int)s->n, s->scenes_d, s->key, s->rank, s->count,
                                 s->stream);
-      mpm::launch_exclusive_scan(s->count, s->nkeys, s->start, s->tile_sums, s->stream);
-      mpm::launch_compact_blocks(s->start, nb, cpb, s->sparse_max, s->blocks, s->nblocks_active,
+      mpm::launch_block_tables(s->count, nb, s->btotal, s->rounds, s->stream);
+      mpm::launch_exclusive_scan(s->btotal, nb, s->start, s->tile_sums, s->stream);
+      mpm::launch_compact_blocks(s->start, nb, 1, s->sparse_max, s->blocks, s->nblocks_active,
                                  s->sparse, s->stream);
       mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->key, s->rank,
-                               s->start, s->count, move_vc, s->inv, s->slot_block, s->stream);
+                               s->start, s->rounds, s->count, move_vc, s->inv, s->slot_block,
+                               s->stream);
     });
   });
   s->cur ^= 1;
   s->sorted_once = true;
-  s->launches += 6;  // keys, 3 scan kernels, compaction, move
+  s->launches += 7;  // keys, round tables, 3 scan kernels, compaction, move
 }
 
 // Enqueues one step of every scene (optionally preceded by the block sort) on the handle's
@@ -433,6 +439,8 @@ void release(nclr_sim *s) {
   cudaFree(s->rank);
   cudaFree(s->count);
   cudaFree(s->start);
+  cudaFree(s->btotal);
+  cudaFree(s->rounds);
   cudaFree(s->tile_sums);
   cudaFree(s->err_d);
   cudaFree(s->staging);
@@ -646,7 +654,9 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMalloc((void **)&s->key, sizeof(int) * np));
   CREATE_TRY(cudaMalloc((void **)&s->rank, sizeof(int) * np));
   CREATE_TRY(cudaMalloc((void **)&s->count, sizeof(int) * (size_t)s->nkeys));
-  CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (size_t)(s->nkeys + 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->start, sizeof(int) * (nblk + 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->btotal, sizeof(int) * std::max<size_t>(nblk, 1)));
+  CREATE_TRY(cudaMalloc((void **)&s->rounds, sizeof(int4) * mpm::kRoundTable * std::max<size_t>(nblk, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles(s->nkeys), 1)));
   CREATE_TRY(cudaMalloc((void **)&s->blocks, sizeof(int) * nblk));
   CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, 2 * sizeof(int)));

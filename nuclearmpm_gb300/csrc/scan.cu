@@ -1,6 +1,6 @@
-// Dimension-free helpers of the block sort: the exclusive prefix sum over the per-block
-// particle counts of the counting sort, the compaction of the non-empty blocks and a count of
-// grid nodes holding mass.  The scan:
+// Dimension-free helpers of the block sort: the per-block round tables, the exclusive prefix
+// sum over the per-block particle counts of the counting sort, the compaction of the
+// non-empty blocks and a count of grid nodes holding mass.  The scan:
 // (1) per-tile totals, (2) one block scans the tile totals, (3) each tile scans its counts
 // and adds its tile offset.  Tiles are 2048 counts (256 threads x 8), read as int4 pairs
 // where aligned.
@@ -91,6 +91,36 @@ __global__ void __launch_bounds__(kThreads) tile_apply(const int *__restrict__ c
   }
 }
 
+// One warp per grid block of kCellsPerBlock cells: the block's particle total, and for every
+// round r < min(largest cell count, kRoundTable) the entry {particles in rounds < r, the
+// 64-bit mask of cells holding more than r particles}.  Particle r of cell c then sits at
+// block start + entry.x + popc(mask & ((1 << c) - 1)) in the cell-by-cell-in-rounds order.
+__global__ void __launch_bounds__(kThreads) block_tables_kernel(const int *__restrict__ count,
+                                                                int nblocks,
+                                                                int *__restrict__ btotal,
+                                                                int4 *__restrict__ rounds) {
+  static_assert(kCellsPerBlock == 64, "two cells per lane");
+  const int b = (int)(((int64_t)blockIdx.x * kThreads + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= nblocks) return;  // the whole warp
+  const int *c = count + (int64_t)b * kCellsPerBlock;
+  const int lo = c[lane], hi = c[32 + lane];
+  int total = lo + hi, mx = max(lo, hi);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    total += __shfl_xor_sync(0xffffffffu, total, o);
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if (lane == 0) btotal[b] = total;
+  const int R = min(mx, kRoundTable);
+  int before = 0;
+  for (int r = 0; r < R; ++r) {
+    const unsigned mlo = __ballot_sync(0xffffffffu, lo > r), mhi = __ballot_sync(0xffffffffu, hi > r);
+    if (lane == 0) rounds[(int64_t)b * kRoundTable + r] = make_int4(before, (int)mlo, (int)mhi, 0);
+    before += __popc(mlo) + __popc(mhi);
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) count_active_kernel(const float4 *__restrict__ grid,
                                                                int64_t nodes,
                                                                unsigned long long *out) {
@@ -138,6 +168,13 @@ __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks
 }
 
 }  // namespace
+
+void launch_block_tables(const int *count, int nblocks, int *btotal, int4 *rounds, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  const int64_t threads = (int64_t)nblocks * 32;
+  block_tables_kernel<<<(unsigned)((threads + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+      count, nblocks, btotal, rounds);
+}
 
 void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int *list,
                            int *nlist, int *sparse, cudaStream_t st) {
