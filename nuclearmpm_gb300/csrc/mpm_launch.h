@@ -32,6 +32,7 @@ template <int D> void launch_g2p2g(const PState &s, const Params &P0, const Scen
                                    int *err, int next_slot, bool ref, int mode, int ctas, cudaStream_t st,
                                    const Record &rec = Record{});
 template <int D> int g2p2g_ctas_per_sm();
+template <int D> int g2p_final_ctas_per_sm();
 // Small scenes: all `steps` steps of one scene in one cooperative launch (kSmallThreads-thread
 // CTAs, `ctas` of them, all resident); bar = 2 zeroed unsigned.
 template <int D> cudaError_t launch_small_steps(const PState &s, const Params &P, float4 *G, float4 *V,
@@ -47,7 +48,8 @@ template <int D> cudaError_t launch_small_batch(const PState &s, const Scene *sc
 template <int D> int small_batch_ctas_per_sm(bool ref);
 constexpr int kSmallThreadsPerCta = 256;
 constexpr uint8_t kFlagVNonzeroBit = 2;  // mpm_step.cuh's kVNonzero: V may be non-zero there
-enum : int { kModeStep = 0, kModeFinalStep = 1, kModeP2GOnly = 2 };  // g2p2g modes
+// g2p2g modes; kModeG2PFinal exists for single simulations only
+enum : int { kModeStep = 0, kModeFinalStep = 1, kModeP2GOnly = 2, kModeG2PFinal = 3 };
 template <int D> void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st);
 template <int D> void launch_export_grid(const float4 *grid, const Params &P, float *vel, float *mass, cudaStream_t st);
 // Caller rows [0, n) of the scene whose global ids (and slots) start at id_off <-> their

@@ -374,15 +374,20 @@ __global__ void __launch_bounds__(256) discard_pending_kernel(float4 *__restrict
 // touched node.
 // ---------------------------------------------------------------------------------------
 // kMode: kStep (G2P + next P2G), kFinalStep (also writes v and C), kP2GOnly (the P2G of the
-// coming step from the stored state, after an upload; the particles are sorted already).
-enum : int { kStep = kModeStep, kFinalStep = kModeFinalStep, kP2GOnly = kModeP2GOnly };
+// coming step from the stored state, after an upload; the particles are sorted already),
+// kG2PFinal (the final step without the next P2G: for callers that replace the state before
+// the next step, whose pending P2G would be thrown away; no G tiles, no polar rotation).
+enum : int { kStep = kModeStep, kFinalStep = kModeFinalStep, kP2GOnly = kModeP2GOnly,
+             kG2PFinal = kModeG2PFinal };
 
 // kBatch: several scenes (per-block parameters from the scene table, staged in shared memory)
 // or one (its parameters are a kernel argument: constant-bank operands, no registers).
 template <int D, bool kRef, int kMode, bool kBatch>
-// 3D: two CTAs per SM (the tiles take 106 KB of shared memory each); 2D: four, which keeps
-// the 2D kernel within 64 registers without spills.
-__global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
+// 3D: two CTAs per SM (the tiles take 106 KB of shared memory each), three for the G2P-only
+// step (one 12 KB tile); 2D: four, which keeps the 2D kernel within 64 registers without
+// spills.
+__global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? (kMode == kG2PFinal ? 3 : 2) : 4)
+g2p2g_kernel(
     PState s, Params P0, const Scene *__restrict__ scenes, const uint16_t *__restrict__ block_scene,
     const float4 *__restrict__ Vall, float4 *__restrict__ Gall, uint8_t *__restrict__ flags_all,
     const int *__restrict__ blocks, const int *__restrict__ nactive,
@@ -409,8 +414,9 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
   float4 *mytile = gt + warp * GS;
   // The G tiles start clear and every item's flush clears what it read, so they are clear
   // again at the start of the next item (padding entries are never written).
-  for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
-    gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if constexpr (kMode != kG2PFinal)
+    for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
+      gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
   for (;;) {
     __syncthreads();
@@ -533,12 +539,13 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
         for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];  // advection, src/nclr.h:229
         F = load_mat<D>(s.F, st, p);
         Jp = s.Jp[p];
-        R = update_F<D, kRef>(C, F, Jp, material, P.dt, P.stress == kCorotated);
+        R = update_F<D, kRef>(C, F, Jp, material, P.dt,
+                              kMode != kG2PFinal && P.stress == kCorotated);
 #pragma unroll
         for (int d = 0; d < D; ++d) s.x[(size_t)d * st + p] = x[d];
         store_mat<D>(s.F, st, p, F);
         s.Jp[p] = Jp;
-        if (kMode == kFinalStep) {
+        if (kMode == kFinalStep || kMode == kG2PFinal) {
 #pragma unroll
           for (int d = 0; d < D; ++d) s.v[(size_t)d * st + p] = v[d];
           store_mat<D>(s.C, st, p, C);
@@ -560,35 +567,37 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
         }
         }
 
-        // ---- P2G of the next step: stress, stencil ----
-        m = s.mass[p];
-        A = fused_affine<D>(F, R, C, Jp, m, s.vol[p], material, lame0(s, p, P), P);
-        int *err_p2g = (kMode == kP2GOnly) ? err_now : err_next;
+        if constexpr (kMode != kG2PFinal) {
+          // ---- P2G of the next step: stress, stencil ----
+          m = s.mass[p];
+          A = fused_affine<D>(F, R, C, Jp, m, s.vol[p], material, lame0(s, p, P), P);
+          int *err_p2g = (kMode == kP2GOnly) ? err_now : err_next;
 #pragma unroll
-        for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
-        stencil<D>(x, P.inv_dx, base, fx_s, w_s);
-        p2g_terms<D>(fx_s, P.dx, mv, A);  // mv, A now hold q0 and A dx
-        fast_s = !chunk;
+          for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
+          stencil<D>(x, P.inv_dx, base, fx_s, w_s);
+          p2g_terms<D>(fx_s, P.dx, mv, A);  // mv, A now hold q0 and A dx
+          fast_s = !chunk;
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-          lb[d] = base[d] - org[d];
-          fast_s &= lb[d] >= 0 && lb[d] + 2 < T && base[d] >= 0 && base[d] + 2 < N;
-        }
-        tb_s = tile_index<D>(lb[0], lb[1], lb[2]);
-        if (!fast_s) {  // outside the tile: straight to G
-          const int64_t f0 = flat_index<D>(base, N);
-#pragma unroll
-          for (int o = 0; o < S; ++o) {
-            const int64_t f = stencil_flat<D>(f0, o, N);
-            if (f < 0 || f >= P.nodes) {
-              atomicOr(err_p2g, kErrOutOfRange);
-              continue;
-            }
-            float c[4];
-            p2g_contrib<D>(o, w_s, mv, m, A, c);
-            red_add_v4(G + f, c[0], c[1], c[2], c[3]);
+          for (int d = 0; d < D; ++d) {
+            lb[d] = base[d] - org[d];
+            fast_s &= lb[d] >= 0 && lb[d] + 2 < T && base[d] >= 0 && base[d] + 2 < N;
           }
-          mark_stencil<D>(flags, base, P);
+          tb_s = tile_index<D>(lb[0], lb[1], lb[2]);
+          if (!fast_s) {  // outside the tile: straight to G
+            const int64_t f0 = flat_index<D>(base, N);
+#pragma unroll
+            for (int o = 0; o < S; ++o) {
+              const int64_t f = stencil_flat<D>(f0, o, N);
+              if (f < 0 || f >= P.nodes) {
+                atomicOr(err_p2g, kErrOutOfRange);
+                continue;
+              }
+              float c[4];
+              p2g_contrib<D>(o, w_s, mv, m, A, c);
+              red_add_v4(G + f, c[0], c[1], c[2], c[3]);
+            }
+            mark_stencil<D>(flags, base, P);
+          }
         }
       }
       // ---- P2G into this warp's tile.  Shared-memory FP32 atomics are compare-and-swap
@@ -596,7 +605,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
       // same stencil base go in separate rounds (rare: consecutive slots are in different
       // cells), so within a round every lane writes a different node for each
       // stencil offset; __syncwarp orders the offsets.
-      if (chunk) continue;  // nothing for the tile
+      if (chunk || kMode == kG2PFinal) continue;  // nothing for the tile
       const bool tile_lane = valid && fast_s;
       const int key = tile_lane ? tb_s : -1 - lane;
       const unsigned same = __match_any_sync(0xffffffffu, key);
@@ -621,7 +630,7 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
         }
       }
     }
-    if (chunk) continue;  // its P2G went straight to G (and the flags)
+    if (chunk || kMode == kG2PFinal) continue;  // its P2G went straight to G (and the flags)
     __syncthreads();
 
     for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
@@ -671,10 +680,15 @@ __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? 2 : 4) g2p2g_kernel(
   }
 }
 
-// Dynamic shared memory of g2p2g: the V tile plus one G tile per warp.
+// Dynamic shared memory of g2p2g: the V tile plus one G tile per warp (the V tile alone for
+// kG2PFinal, which has no P2G).
 template <int D>
 constexpr size_t g2p2g_smem_bytes() {
   return sizeof(float4) * Tiling<D>::SIZE * (1 + kG2P2GThreads / 32);
+}
+template <int D>
+constexpr size_t g2p_final_smem_bytes() {
+  return sizeof(float4) * Tiling<D>::SIZE;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1190,21 +1204,29 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                   int *work, int *err, int next_slot, bool ref, int mode, int ctas,
                   cudaStream_t st, const Record &rec) {
 #define MPM_G2P2G(R, MODE, B)                                                            \
-  g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D>(), st>>>(         \
-      s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart, sparse, work, err,  \
-      next_slot, rec)
+  g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads,                                      \
+                                (MODE) == kG2PFinal ? g2p_final_smem_bytes<D>()           \
+                                                    : g2p2g_smem_bytes<D>(),              \
+                                st>>>(s, P0, scenes, block_scene, V, G, flags, blocks,   \
+                                      nactive, bstart, sparse, work, err, next_slot, rec)
 #define MPM_G2P2G_B(R, MODE)          \
   if (block_scene) {                  \
     MPM_G2P2G(R, MODE, true);         \
   } else {                            \
     MPM_G2P2G(R, MODE, false);        \
   }
-  if (ref) {
-    if (mode == kFinalStep) { MPM_G2P2G_B(true, kFinalStep) }
+  if (mode == kG2PFinal && !block_scene) {  // single simulations only
+    if (ref) {
+      MPM_G2P2G(true, kG2PFinal, false);
+    } else {
+      MPM_G2P2G(false, kG2PFinal, false);
+    }
+  } else if (ref) {
+    if (mode == kFinalStep || mode == kG2PFinal) { MPM_G2P2G_B(true, kFinalStep) }
     else if (mode == kP2GOnly) { MPM_G2P2G_B(true, kP2GOnly) }
     else { MPM_G2P2G_B(true, kStep) }
   } else {
-    if (mode == kFinalStep) { MPM_G2P2G_B(false, kFinalStep) }
+    if (mode == kFinalStep || mode == kG2PFinal) { MPM_G2P2G_B(false, kFinalStep) }
     else if (mode == kP2GOnly) { MPM_G2P2G_B(false, kP2GOnly) }
     else { MPM_G2P2G_B(false, kStep) }
   }
@@ -1276,6 +1298,18 @@ int g2p2g_ctas_per_sm() {
   return n > 0 ? n : 1;
 }
 
+// Resident CTAs per SM of the G2P-only final step (registers and its one tile).
+template <int D>
+int g2p_final_ctas_per_sm() {
+  int a = 0, b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, g2p2g_kernel<D, true, kG2PFinal, false>,
+                                                kG2P2GThreads, g2p_final_smem_bytes<D>());
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, g2p2g_kernel<D, false, kG2PFinal, false>,
+                                                kG2P2GThreads, g2p_final_smem_bytes<D>());
+  const int n = a < b ? a : b;
+  return n > 0 ? n : 1;
+}
+
 template <int D>
 void launch_copy_vgrid(const float4 *V, int64_t nodes, float *vel, float *mass, cudaStream_t st) {
   copy_vgrid_kernel<D><<<blocks_for(nodes, 256), 256, 0, st>>>(V, nodes, vel, mass);
@@ -1329,6 +1363,7 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
                                 const int *, const int *, int *, int *, int, bool, int, int,     \
                                 cudaStream_t, const Record &);                                   \
   template int g2p2g_ctas_per_sm<D>();                                                           \
+  template int g2p_final_ctas_per_sm<D>();                                                       \
   template cudaError_t launch_small_steps<D>(const PState &, const Params &, float4 *, float4 *,   \
                                              int, int *, unsigned *, bool, int, cudaStream_t);  \
   template int small_ctas_per_sm<D>(bool);                                                       \

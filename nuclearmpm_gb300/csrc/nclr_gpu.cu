@@ -46,6 +46,7 @@ struct nclr_sim {
   int cur = 0;
   int sms = 1;         // streaming multiprocessors of the device
   int g2p2g_ctas = 1;  // persistent CTAs of the fused kernel
+  int g2p_ctas = 1;    // persistent CTAs of its G2P-only final step
 
   float4 *G = nullptr;        // P2G accumulator of the coming step
   float4 *V = nullptr;        // updated grid of the last step (grid())
@@ -78,6 +79,11 @@ struct nclr_sim {
   std::vector<int> deferred_err;  // [2s+1] of the previous call, reported by the next one
   std::vector<int> scene_err;     // the last call's errors per scene
   bool acc_valid = false;     // G holds the P2G of the coming step
+  // The last call's pending P2G was thrown away by an upload before the next step (the caller
+  // replaces the state between calls): the next call ends with a G2P-only step, and the call
+  // after it recomputes its first P2G.  A call that finds no upload in between switches back.
+  bool p2g_discarded = false;
+  bool replaced = false;      // an upload (or new moduli) since the last advance() call
   bool need_sort = true;      // the block lists do not describe the particles yet
 
   float *staging = nullptr;       // particle-major transfer buffer (n * row floats)
@@ -85,7 +91,9 @@ struct nclr_sim {
 
   bool stepped = false;  // grid() is empty until the first advance (src/nclr.h:101)
   int64_t steps_since_sort = 0;
-  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [parity][final]
+  // [parity][0: a chunk that does not end the call, 1: the call's last chunk, 2: the same
+  // ending with the G2P-only step]
+  cudaGraphExec_t graph[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   int64_t graph_launches = 0;
   int64_t launches = 0;
   int64_t active_nodes = 0;
@@ -250,10 +258,13 @@ void enqueue_sort(nclr_sim *s, bool move_vc) {
   s->launches += 7;  // keys, round tables, 3 scan kernels, compaction, move
 }
 
+// How a call's last step ends: with the next step's P2G (kept pending in G) or without it.
+enum : int { kNotFinal = 0, kFinalWithP2G = 1, kFinalG2POnly = 2 };
+
 // Enqueues one step of every scene (optionally preceded by the block sort) on the handle's
-// stream.  The last step of a call writes v and C and reports the next step's P2G errors
-// separately.
-void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
+// stream.  The last step of a call (final != kNotFinal) writes v and C and, with its P2G,
+// reports the next step's P2G errors separately.
+void enqueue_step(nclr_sim *s, bool sort, int final) {
   if (sort && s->n > 0) enqueue_sort(s, false);
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
@@ -266,9 +277,12 @@ void enqueue_step(nclr_sim *s, bool sort, bool final_step) {
       phase(s, NCLR_PHASE_G2P2G, 1, [&] {
         mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
                              s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d,
-                             final_step ? 1 : 0, s->ref,
-                             final_step ? mpm::kModeFinalStep : mpm::kModeStep, s->g2p2g_ctas,
-                             s->stream, s->record);
+                             final != kNotFinal ? 1 : 0, s->ref,
+                             final == kFinalG2POnly  ? mpm::kModeG2PFinal
+                             : final == kNotFinal    ? mpm::kModeStep
+                                                     : mpm::kModeFinalStep,
+                             final == kFinalG2POnly ? s->g2p_ctas : s->g2p2g_ctas, s->stream,
+                             s->record);
       });
       s->launches += 1;
     }
@@ -293,8 +307,8 @@ int64_t chunk_sorts(const nclr_sim *s) {
 }
 
 // Captures chunk_steps() steps starting at a sort boundary from buffer parity `parity`; with
-// `final_chunk` its last step is the call's final step (writes v and C).
-nclr_status capture_graph(nclr_sim *s, int parity, bool final_chunk) {
+// `final` != kNotFinal its last step is the call's final step of that kind (writes v and C).
+nclr_status capture_graph(nclr_sim *s, int parity, int final) {
   const int saved_cur = s->cur;
   const int64_t saved_launches = s->launches;
   s->cur = parity;
@@ -302,13 +316,13 @@ nclr_status capture_graph(nclr_sim *s, int parity, bool final_chunk) {
   CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const int64_t k = chunk_steps(s);
   const int64_t si = s->opt.sort_interval;
-  for (int64_t i = 0; i < k; ++i) enqueue_step(s, si > 0 && i % si == 0, final_chunk && i == k - 1);
+  for (int64_t i = 0; i < k; ++i) enqueue_step(s, si > 0 && i % si == 0, i == k - 1 ? final : kNotFinal);
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   s->graph_launches = s->launches - saved_launches;
   s->launches = saved_launches;
   s->cur = saved_cur;
   if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&s->graph[parity][final_chunk ? 1 : 0], g, 0);
+  e = cudaGraphInstantiate(&s->graph[parity][final], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   return NCLR_OK;
@@ -365,7 +379,9 @@ nclr_status import_rows(nclr_sim *s, int sc, const float *x, const float *v, con
     CUDA_TRY(s, cudaMemcpyAsync(s->moved_h, moved, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   else if (count_moved)
     *s->moved_h = -1;  // not counted
+  if (s->acc_valid && s->stepped) s->p2g_discarded = true;
   s->acc_valid = false;  // the coming step's P2G must be recomputed from the new state
+  s->replaced = true;
   if (x) s->need_sort = true;
   return check_launch(s, "import particles");
 }
@@ -580,6 +596,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   const size_t nodes = (size_t)node;
   CREATE_TRY(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
   s->g2p2g_ctas = s->sms * (dim == 3 ? mpm::g2p2g_ctas_per_sm<3>() : mpm::g2p2g_ctas_per_sm<2>());
+  s->g2p_ctas = s->sms * (dim == 3 ? mpm::g2p_final_ctas_per_sm<3>() : mpm::g2p_final_ctas_per_sm<2>());
   {
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
@@ -848,6 +865,10 @@ nclr_status get_grid_host(nclr_sim *s, int sc, float *velocity, float *mass) {
 
 // The steps of nclr_advance on the regular path: block sort, fused G2P2G, graphs.
 nclr_status advance_regular(nclr_sim *s, int64_t nsteps) {
+  // the last call ended without its P2G but nothing replaced the state since: stop guessing
+  if (!s->acc_valid && !s->replaced && s->stepped) s->p2g_discarded = false;
+  s->replaced = false;
+  const int last = (s->p2g_discarded && s->nscenes == 1) ? kFinalG2POnly : kFinalWithP2G;
   if (s->need_sort && s->n > 0) {  // the uploaded particles: sort them (with v and C) first
     enqueue_sort(s, !s->acc_valid);
     s->need_sort = false;
@@ -877,9 +898,9 @@ nclr_status advance_regular(nclr_sim *s, int64_t nsteps) {
     const bool sort = sort_due(s);
     const bool at_boundary = s->opt.sort_interval == 0 || sort;
     if (s->opt.use_graphs && !s->opt.profile && s->n > 0 && at_boundary && left >= chunk) {
-      const int fin = (left == chunk) ? 1 : 0;
+      const int fin = (left == chunk) ? last : kNotFinal;
       if (!s->graph[s->cur][fin]) {
-        nclr_status st = capture_graph(s, s->cur, fin != 0);
+        nclr_status st = capture_graph(s, s->cur, fin);
         if (st != NCLR_OK) return st;
       }
       CUDA_TRY(s, cudaGraphLaunch(s->graph[s->cur][fin], s->stream));
@@ -889,11 +910,12 @@ nclr_status advance_regular(nclr_sim *s, int64_t nsteps) {
       left -= chunk;
       continue;
     }
-    enqueue_step(s, sort, left == 1);
+    enqueue_step(s, sort, left == 1 ? last : kNotFinal);
     if (sort) s->steps_since_sort = 0;
     ++s->steps_since_sort;
     --left;
   }
+  if (last == kFinalG2POnly && s->n > 0) s->acc_valid = false;  // G holds no pending P2G
   return NCLR_OK;
 }
 
@@ -1109,7 +1131,9 @@ static nclr_status set_moduli(nclr_sim *s, const float *E, const float *nu, bool
   }
   CUDA_TRY(s, mpm::launch_set_lame(s->ps[s->cur].id, (int)s->n, Ed, nud, s->ps[s->cur].lame,
                                    s->stream));
+  if (s->acc_valid && s->stepped) s->p2g_discarded = true;
   s->acc_valid = false;  // the pending P2G used the old moduli
+  s->replaced = true;
   if (!device) CUDA_TRY(s, cudaStreamSynchronize(s->stream));
   return NCLR_OK;
 }
@@ -1390,7 +1414,7 @@ nclr_status record_segment(nclr_rollout *r, int L, int buf) {
     const bool sort = sort_due(s);
     float *st = r->state(r->seg[buf], i + 1);
     s->record = mpm::Record{r->x(st), r->v(st), r->F(st), r->C(st)};  // written by the step
-    enqueue_step(s, sort, true);
+    enqueue_step(s, sort, kFinalWithP2G);
     s->record = mpm::Record{};
     if (sort) s->steps_since_sort = 0;
     ++s->steps_since_sort;

@@ -236,6 +236,40 @@ def test_upload_keeping_positions_matches_fresh_simulation():
         assert field_err(getattr(pa, f), getattr(pb, f), f) <= 1e-5, f
 
 
+@pytest.mark.parametrize("steps_per_call", [1, 16])
+def test_replacing_the_state_before_every_call(oracle, steps_per_call):
+    """A caller that replaces the state before every call throws the pending P2G away, so the
+    handle ends such calls with a G2P-only step and recomputes the P2G at the start of the
+    next. It switches back once a call finds the state unchanged. Each call (direct launches
+    for 1 step, CUDA graphs of 4-step chunks for 16, with their v and C) equals the oracle
+    stepped from the same state, and grid() is the last step's."""
+    dim, res, physics = 3, 32, scenes.REFERENCE
+    rng = np.random.default_rng(12)
+    s = random_state(rng, dim, 4000, res, physics)
+    sim = MPMSimulation(dict(s), scenes.JELLY, res=res, small_scene_max=0, sort_interval=4)
+    sim.advance(steps_per_call)  # the first call: no upload yet, ends with the fused step
+    p = sim.particles()
+    cur = {"x": p.x, "v": p.v, "F": p.F, "C": p.C, "Jp": p.Jp}
+    for call in range(6):
+        replace = call < 4
+        if replace:
+            cur = dict(cur, v=(cur["v"] * np.float32(0.9)).astype(np.float32))
+            sim.set_particles(**cur)
+        sim.advance(steps_per_call)
+        p = sim.particles()
+        got = {"x": p.x, "v": p.v, "F": p.F, "C": p.C, "Jp": p.Jp}
+        ref, grid, st, _ = oracle.advance(dict(s, **cur), dim=dim, model=scenes.JELLY, res=res,
+                                          steps=steps_per_call, physics=physics)
+        assert st == 0
+        for f in FIELDS:
+            assert field_err(got[f], ref[f], f) <= DRIFT[f], (call, f, field_err(got[f], ref[f], f))
+        g = sim.grid()
+        assert field_err(g.velocity, grid[0], "grid_v") <= DRIFT["v"], call
+        assert field_err(g.mass, grid[1], "grid_m") <= 1e-4, call
+        cur = got
+    sim.close()
+
+
 def test_empty_scene_and_empty_grid_before_advance():
     sim = MPMSimulation([], scenes.SNOW, res=16, dim=2)
     assert len(sim.grid()) == 0  # the reference's grid() is empty before the first step
