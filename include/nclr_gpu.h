@@ -85,9 +85,10 @@ typedef struct nclr_options {
                               the steps of an advance() call in one cooperative kernel launch
                               (reference order p2g / grid_op / g2p, grid-wide barriers; a
                               batch gives each scene its own group of CTAs) instead of two
-                              launches per step; 0 = never, -1 = the default (default -1:
-                              65,536 particles in 2D and 32,768 in 3D for one scene, never for
-                              a batch, where the tile path is faster) */
+                              launches per step; 0 = never, -1 = automatic (default -1: one
+                              scene of at most 65,536 particles in 2D or 32,768 in 3D whose grid
+                              has at most 8 nodes per particle -- that kernel updates every
+                              node each step; never a batch, where the tile path is faster) */
   int stress_model;        /* NCLR_STRESS_* (default COROTATED); a batch's scenes share it */
 } nclr_options;
 

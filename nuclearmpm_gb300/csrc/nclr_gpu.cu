@@ -71,6 +71,7 @@ struct nclr_sim {
   int *group_first = nullptr;     // batches: first CTA of each scene's group (nscenes + 1)
   int batch_ctas = 0;             // batches: CTAs of that launch (0: not possible)
   int small_max = 0;          // particles up to which advance() uses the small-scene kernel
+  bool small_auto = false;    // the default limits: also at most kSmallNodesPerParticle nodes
   int small_ctas = 0;         // its CTAs that fit on the device at once (0: no cooperative launch)
   cudaEvent_t field_ev[5] = {};        // x, v, F, C, Jp ready (staged / imported)
   int *work = nullptr;        // fused kernel's block counter
@@ -122,10 +123,14 @@ thread_local std::string g_create_error;
 // than the block's particles gathering and scattering through L2 directly.
 constexpr int kSparseMax3 = 64;
 constexpr int kSparseMax2 = 32;
-// Default small-scene limits (particles): up to them one persistent launch per advance() call
-// beats two launches per step (measured on GB300: 2D up to 64k particles, 3D up to 32k).
+// Default small-scene limits: up to them one persistent launch per advance() call beats two
+// launches per step.  Measured on GB300: up to 64k particles in 2D and 32k in 3D, and only
+// while the grid has at most about 8 nodes per particle -- the small kernel updates every
+// node each step, so a sparse scene on a large grid (1,000 particles on a 65^3 grid: 210 us
+// per step against 17 us) belongs on the tile path, which visits only touched blocks.
 constexpr int kSmallMax2 = 65536;
 constexpr int kSmallMax3 = 32768;
+constexpr int64_t kSmallNodesPerParticle = 8;
 
 int row_floats(int dim) { return 2 * dim + 2 * dim * dim + 1; }  // x, v, F, C, Jp
 
@@ -610,6 +615,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
                    : nscenes > 1               ? 0
                    : dim == 3                  ? kSmallMax3
                                                : kSmallMax2;
+    s->small_auto = s->opt.small_scene_max < 0;
     if (nscenes > 1 && coop) {
       // A batch on the small-scene kernel: each scene a group of CTAs in proportion to its
       // particles (at least one), all groups resident at once.
@@ -965,7 +971,9 @@ nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
 
 bool small_scene(const nclr_sim *s) {
   if (s->n <= 0 || s->small_ctas <= 0) return false;
-  if (s->nscenes == 1) return s->n <= s->small_max;
+  if (s->nscenes == 1)
+    return s->n <= s->small_max &&
+           (!s->small_auto || s->P0().nodes <= kSmallNodesPerParticle * s->n);
   if (s->batch_ctas <= 0) return false;
   for (const auto &sc : s->scenes)
     if (sc.P.n > s->small_max) return false;

@@ -21,7 +21,8 @@ RANDOM_FP64_FACTOR = 2.5
 COROTATED, NEOHOOKEAN = capi.STRESS_COROTATED, capi.STRESS_NEOHOOKEAN
 # the single-simulation step paths: the small-scene kernel, the tile kernel, and the tile
 # kernel with every block stepped particle by particle
-PATHS = {"small": {}, "tile": {"small_scene_max": 0, "sparse_block_max": 0},
+PATHS = {"small": {"small_scene_max": 1 << 30},
+         "tile": {"small_scene_max": 0, "sparse_block_max": 0},
          "thin": {"small_scene_max": 0, "sparse_block_max": 1 << 30}}
 # (dim, physics) pairs the neo-Hookean stress is defined for (det F > 0)
 NEO_CASES = [(2, scenes.REFERENCE), (2, scenes.CORRECTED), (3, scenes.CORRECTED)]

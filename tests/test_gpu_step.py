@@ -41,8 +41,8 @@ def run_gpu(state, params, steps, **kw):
 
 
 # The two step paths of a single simulation: "small" runs every step of a call in one
-# cooperative launch (the default for scenes this size), "tile" the block-sorted fused kernel.
-PATHS = {"small": {}, "tile": {"small_scene_max": 0}}
+# cooperative launch, "tile" the block-sorted fused kernel.
+PATHS = {"small": {"small_scene_max": 1 << 30}, "tile": {"small_scene_max": 0}}
 
 
 @pytest.mark.parametrize("path", sorted(PATHS))
@@ -86,7 +86,7 @@ def test_one_step_vs_oracle_random(oracle, dim, model, physics, thin):
     rng = np.random.default_rng(100 * dim + 10 * model + physics)
     res = 32
     s = random_state(rng, dim, 2000 if dim == 2 else 4000, res, physics)
-    path = dict(small_scene_max=-1) if thin == -2 else dict(small_scene_max=0, sparse_block_max=thin)
+    path = dict(small_scene_max=1 << 30) if thin == -2 else dict(small_scene_max=0, sparse_block_max=thin)
     out, grid = run_gpu(s, dict(model=model, res=res, dt=1e-4, E=1e4, nu=0.2, gravity=-100.0), 1,
                         physics=physics, **path)
     o32, og, st, _ = oracle.advance(s, dim=dim, model=model, res=res, steps=1, physics=physics)
@@ -268,6 +268,56 @@ def test_replacing_the_state_before_every_call(oracle, steps_per_call):
         assert field_err(g.mass, grid[1], "grid_m") <= 1e-4, call
         cur = got
     sim.close()
+
+
+@pytest.mark.parametrize("dim,n,res,small", [(2, 5000, 64, True), (2, 65536, 512, True),
+                                             (2, 4096, 1024, False), (3, 15625, 32, True),
+                                             (3, 1000, 64, False), (3, 32768, 128, False)])
+def test_automatic_path_choice(dim, n, res, small):
+    """The default picks the one-launch small-scene kernel only for scenes of at most 64k (2D)
+    or 32k (3D) particles whose grid has at most 8 nodes per particle: that kernel updates
+    every node each step, so sparse scenes on large grids take the tile path."""
+    side = round(n ** (1 / dim))
+    sp = min(0.5 / res, 0.3 / side)
+    x = scenes.jittered_block(np.random.default_rng(1), (side,) * dim, sp, (0.35,) * dim, 0.2 * sp)
+    sim = MPMSimulation(scenes.particles(x.astype(np.float32)), scenes.JELLY, res=res)
+    sim.advance(3)
+    launches, _ = sim.stats()
+    sim.close()
+    assert (launches == 1) == small, launches
+
+
+@pytest.mark.parametrize("path", sorted(PATHS))
+def test_largest_2d_grid_matches_oracle(oracle, path):
+    """res 1024, the largest grid the C ABI accepts (1025^2 nodes), against the oracle."""
+    rng = np.random.default_rng(3)
+    s = random_state(rng, 2, 3000, 1024, scenes.REFERENCE)
+    s["v"] = (s["v"] * np.float32(0.1)).astype(np.float32)
+    out, grid = run_gpu(s, dict(model=scenes.SNOW, res=1024, dt=1e-5, E=1e4, nu=0.2,
+                                gravity=-100.0), 2, **PATHS[path])
+    ref, og, st, _ = oracle.advance(s, dim=2, model=scenes.SNOW, res=1024, dt=1e-5, steps=2)
+    assert st == 0
+    for f in FIELDS:
+        assert field_err(out[f], ref[f], f) <= DRIFT[f], f
+    assert field_err(grid.mass, og[1], "grid_m") <= 1e-4
+
+
+def test_largest_3d_grid_free_fall():
+    """res 1024 in 3D: 1025^3 nodes (about 34 GB of grid in HBM).  An undeformed, soft jelly
+    cube (F = I, C = 0, at rest, corrected physics, E = 1) is stress-free up to rounding, so
+    after k steps every particle moves with v = k dt g, and only the nodes under the cube
+    hold mass."""
+    res, k, dt, g = 1024, 3, 1e-4, -100.0
+    x = scenes.cube(3, 16, 0.5, 0.5 + 15 * 0.5 / res)
+    sim = MPMSimulation(scenes.particles(x, physics=scenes.CORRECTED), scenes.JELLY, res=res,
+                        dt=dt, E=1.0, gravity=g, physics=scenes.CORRECTED, small_scene_max=0)
+    sim.advance(k)
+    p = sim.particles()
+    active = sim.active_nodes()
+    sim.close()
+    np.testing.assert_allclose(p.v[:, 1], k * dt * g, rtol=1e-5)
+    assert np.abs(p.v[:, [0, 2]]).max() < 1e-8
+    assert 0 < active <= 12 ** 3, active
 
 
 def test_empty_scene_and_empty_grid_before_advance():
