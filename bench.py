@@ -48,7 +48,7 @@ WORKLOAD = {"workload": "3D jelly (MaterialModel::kJelly), 4 cubes of 64^3 latti
 
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel
 # from one ncu capture of this workload (profiles/g2p2g_jelly3d_1M.md).
-NCU_TRAFFIC = {"g2p2g": 68.730624e6 + 4.993024e6}
+NCU_TRAFFIC = {"g2p2g": 68.470784e6 + 5.270016e6}
 
 
 def peaks():
