@@ -294,6 +294,28 @@ void enqueue_step(nclr_sim *s, bool sort, int final) {
   });
 }
 
+// The P2G of the coming step from the stored state (after an upload, new moduli, or a call
+// that ended without it): clears what G holds, then one P2G-only launch.
+void enqueue_pending_p2g(nclr_sim *s) {
+  std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // discarded with the P2G
+  dispatch_dim(s->dim, [&](auto dc) {
+    constexpr int D = decltype(dc)::value;
+    phase(s, NCLR_PHASE_P2G, 2, [&] {
+      mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
+                                     s->total_blocks, s->sms, s->stream);
+      // the fused kernel's block counter (before a regular step the sweep resets it)
+      cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
+      if (s->n > 0)
+        mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
+                             s->flags, s->blocks, s->nblocks_active, s->start, s->sparse,
+                             s->work, s->err_d, 0, s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas,
+                             s->stream);
+    });
+  });
+  s->launches += (s->n > 0) ? 2 : 1;
+  s->acc_valid = true;
+}
+
 bool sort_due(const nclr_sim *s) {
   return s->need_sort ||
          (s->opt.sort_interval > 0 && s->steps_since_sort >= s->opt.sort_interval);
@@ -880,24 +902,7 @@ nclr_status advance_regular(nclr_sim *s, int64_t nsteps) {
     s->need_sort = false;
     s->steps_since_sort = 0;
   }
-  if (!s->acc_valid) {  // the first step's P2G, from the uploaded state
-    std::fill(s->deferred_err.begin(), s->deferred_err.end(), 0);  // discarded with the P2G
-    dispatch_dim(s->dim, [&](auto dc) {
-      constexpr int D = decltype(dc)::value;
-      phase(s, NCLR_PHASE_P2G, 2, [&] {
-        mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
-                                       s->total_blocks, s->sms, s->stream);
-        // the fused kernel's block counter (before a regular step the sweep resets it)
-        cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
-        if (s->n > 0)
-          mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
-                               s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d, 0,
-                               s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
-      });
-    });
-    s->launches += (s->n > 0) ? 2 : 1;
-    s->acc_valid = true;
-  }
+  if (!s->acc_valid) enqueue_pending_p2g(s);  // the first step's P2G, from the uploaded state
   int64_t left = nsteps;
   const int64_t chunk = chunk_steps(s);
   while (left > 0) {
@@ -1406,18 +1411,7 @@ nclr_status record_segment(nclr_rollout *r, int L, int buf) {
     s->need_sort = false;
     s->steps_since_sort = 0;
   }
-  if (!s->acc_valid) {
-    dispatch_dim(s->dim, [&](auto dc) {
-      constexpr int D = decltype(dc)::value;
-      mpm::launch_discard_pending<D>(s->G, s->flags, s->scenes_d, s->block_scene,
-                                     s->total_blocks, s->sms, s->stream);
-      cudaMemsetAsync(s->work, 0, sizeof(int), s->stream);
-      mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
-                           s->flags, s->blocks, s->nblocks_active, s->start, s->sparse, s->work, s->err_d, 0,
-                           s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas, s->stream);
-    });
-    s->acc_valid = true;
-  }
+  if (!s->acc_valid) enqueue_pending_p2g(s);
   for (int i = 0; i < L; ++i) {
     const bool sort = sort_due(s);
     float *st = r->state(r->seg[buf], i + 1);
