@@ -161,8 +161,10 @@ def tune_plain(state: dict, model: int, res: int, device: int) -> dict:
     """The project's autotuner (nuclearmpm_gb300.autotune) on this workload: re-sort interval
     and thin-block threshold, from short timed runs of the simulation itself."""
     from nuclearmpm_gb300 import MPMSimulation, autotune
+    # 64-step runs (about 12 ms each at 1M particles): the candidates differ by a few percent,
+    # which shorter runs timed on the host do not resolve
     return autotune.tune(lambda **o: MPMSimulation(dict(state), model, res=res, device=device, **o),
-                         key=None, candidates=autotune.PLAIN_CANDIDATES, steps=16, repeats=2,
+                         key=None, candidates=autotune.PLAIN_CANDIDATES, steps=64, repeats=2,
                          cache_path=None)
 
 
