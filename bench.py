@@ -474,30 +474,58 @@ def run_reference(args):
     return 0
 
 
+class Replicas:
+    """The ranks of a run: one independent replica of the workload per rank (one simulation
+    does not shard; there is no data-path collective), with a barrier around the timed region
+    and the max over ranks of its duration.  NCCL between GPUs; gloo on the host (tests)."""
+
+    def __init__(self, backend: str = "nccl"):
+        import torch
+        import torch.distributed as dist
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.cuda = backend == "nccl"
+        self._dist = dist
+        if self.cuda:
+            torch.cuda.set_device(self.local)
+        if self.world > 1:
+            kw = {"device_id": torch.device("cuda", self.local)} if self.cuda else {}
+            dist.init_process_group(backend, **kw)
+
+    def barrier(self) -> None:
+        import torch
+        if self.world > 1:
+            self._dist.barrier()
+        if self.cuda:
+            torch.cuda.synchronize()
+
+    def max(self, x: float) -> float:
+        import torch
+        if self.world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if self.cuda else "cpu")
+        self._dist.all_reduce(t, op=self._dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.world > 1:
+            self._dist.destroy_process_group()
+
+
+def replica_value(world: int, particles: int, steps: int, ms_max: float) -> float:
+    """Whole-job particle-steps/s: every rank steps its own replica, timed by the slowest."""
+    return world * particles * steps / (ms_max / 1e3)
+
+
 def run_ours(args):
     import torch
-    import torch.distributed as dist
 
     from nuclearmpm_gb300 import MPMSimulation, scenes
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    def barrier():
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    ranks = Replicas("nccl")
+    world, rank, local = ranks.world, ranks.rank, ranks.local
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     scene = make_scene()
     n = len(scene["x"])
@@ -523,7 +551,7 @@ def run_ours(args):
     prof = sim.profile()
     active = sim.active_nodes()
     clk = clocks.summary()
-    value = world * n * args.steps / (ms_max / 1e3)
+    value = replica_value(world, n, args.steps, ms_max)
 
     # ---- roofline of the dominant kernel ------------------------------------------------
     hbm_peak, peak_kind = peaks()
@@ -569,7 +597,7 @@ def run_ours(args):
         e2e_s = max_over_ranks(time.perf_counter() - t0)
         barrier()
         row = 4 * (2 * 3 + 2 * 9 + 1)
-        e2e = {"value": world * n * args.steps / e2e_s, "unit": UNIT,
+        e2e = {"value": replica_value(world, n, args.steps, e2e_s * 1e3), "unit": UNIT,
                "h2d_bytes_per_step": n * row, "d2h_bytes_per_step": n * row,
                "path": "nclr_set_particles (pinned host) + nclr_advance(1) + nclr_get_particles"}
 
@@ -618,8 +646,7 @@ def run_ours(args):
                 "models": models, "gpu_launches": launches_total, "clocks": clk}
         print(json.dumps(line), flush=True)
     sim.close()
-    if world > 1:
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 
