@@ -16,6 +16,10 @@ namespace mpm {
 
 constexpr int kG2P2GThreads = 256;
 
+// 0 <= v <= hi, as one unsigned compare that no large v (a saturated float-to-int conversion
+// of a huge position) can overflow into passing.
+__device__ __forceinline__ bool in_range(int v, int hi) { return (unsigned)v <= (unsigned)hi; }
+
 template <int D>
 __device__ __forceinline__ void stencil_offset(int o, int &oi, int &oj, int &ok) {
   oi = (D == 3) ? o / 9 : o / 3;
@@ -512,7 +516,7 @@ g2p2g_kernel(
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           lb[d] = base[d] - org[d];
-          fast &= lb[d] >= 0 && lb[d] + 2 < T && base[d] >= 0 && base[d] + 2 < N;
+          fast &= in_range(lb[d], T - 3) && in_range(base[d], N - 3);
         }
         const int tb = tile_index<D>(lb[0], lb[1], lb[2]);
 #pragma unroll
@@ -580,7 +584,7 @@ g2p2g_kernel(
 #pragma unroll
           for (int d = 0; d < D; ++d) {
             lb[d] = base[d] - org[d];
-            fast_s &= lb[d] >= 0 && lb[d] + 2 < T && base[d] >= 0 && base[d] + 2 < N;
+            fast_s &= in_range(lb[d], T - 3) && in_range(base[d], N - 3);
           }
           tb_s = tile_index<D>(lb[0], lb[1], lb[2]);
           if (!fast_s) {  // outside the tile: straight to G
