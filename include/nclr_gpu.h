@@ -266,6 +266,20 @@ nclr_status nclr_rollout_forward(nclr_rollout *r, const float *x0, const float *
 nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float *gvT,
                                   const float *gFT, const float *gCT, float *gx0, float *gv0,
                                   float *gF0, float *gC0, double *gE, double *gnu);
+/* The same with one Young's modulus and Poisson ratio per particle (the extension of
+ * nclr_set_moduli): E and nu are DEVICE arrays of n values in row order.  The matching
+ * backward writes the adjoint of every particle's E and nu into the DEVICE arrays gE, gnu
+ * (n values each, may be NULL).  A backward must match its forward: after
+ * nclr_rollout_forward_moduli only nclr_rollout_backward_moduli, after nclr_rollout_forward
+ * only nclr_rollout_backward (NCLR_ERR_INVALID otherwise). */
+nclr_status nclr_rollout_forward_moduli(nclr_rollout *r, const float *x0, const float *v0,
+                                        const float *F0, const float *C0, const float *E,
+                                        const float *nu, float *xT, float *vT, float *FT,
+                                        float *CT);
+nclr_status nclr_rollout_backward_moduli(nclr_rollout *r, const float *gxT, const float *gvT,
+                                         const float *gFT, const float *gCT, float *gx0,
+                                         float *gv0, float *gF0, float *gC0, float *gE,
+                                         float *gnu);
 /* Device time (ms, CUDA events on the rollout's stream) of the last forward and backward. */
 nclr_status nclr_rollout_timing(const nclr_rollout *r, double *forward_ms, double *backward_ms);
 void *nclr_rollout_stream(nclr_rollout *r);

@@ -80,7 +80,9 @@ class Rollout:
 
 
 class RolloutFunction(torch.autograd.Function):
-    """(x0, v0, E, nu[, F0, C0]) -> (x_T, v_T); backward via the adjoint rollout."""
+    """(x0, v0, E, nu[, F0, C0]) -> (x_T, v_T); backward via the adjoint rollout.  E and nu are
+    the scene's pair (numbers or 0-d tensors) or one value per particle (tensors of n values,
+    nclr_rollout_forward_moduli), with gradients of the same shape."""
 
     @staticmethod
     def forward(ctx, roll: Rollout, x0, v0, E, nu, F0=None, C0=None):
@@ -98,10 +100,23 @@ class RolloutFunction(torch.autograd.Function):
         C0c = torch.zeros(n, d, d, **f32) if C0 is None else C0.detach().to(**f32).contiguous()
         xT = torch.empty(n, d, **f32)
         vT = torch.empty(n, d, **f32)
-        Ef, nuf = float(E), float(nu)
-        torch.cuda.synchronize(dev)
-        roll._check(capi.lib().nclr_rollout_forward(roll._h, _dp(x0c), _dp(v0c), _dp(F0c), _dp(C0c),
-                                                     Ef, nuf, _dp(xT), _dp(vT), None, None))
+        per_particle = torch.is_tensor(E) and E.numel() > 1
+        if per_particle:
+            Ec = E.detach().to(**f32).reshape(n).contiguous()
+            nuc = torch.as_tensor(nu).detach().to(**f32).reshape(n).contiguous()
+            ctx.moduli = (Ec, nuc)  # kept alive until the call below has read them
+            ctx.shapes = (E.shape, torch.as_tensor(nu).shape)
+            torch.cuda.synchronize(dev)
+            roll._check(capi.lib().nclr_rollout_forward_moduli(
+                roll._h, _dp(x0c), _dp(v0c), _dp(F0c), _dp(C0c), _dp(Ec), _dp(nuc), _dp(xT),
+                _dp(vT), None, None))
+        else:
+            Ef, nuf = float(E), float(nu)
+            torch.cuda.synchronize(dev)
+            roll._check(capi.lib().nclr_rollout_forward(roll._h, _dp(x0c), _dp(v0c), _dp(F0c),
+                                                         _dp(C0c), Ef, nuf, _dp(xT), _dp(vT),
+                                                         None, None))
+        ctx.per_particle = per_particle
         ctx.roll = roll
         ctx.params = [(t.dtype, t.device) if torch.is_tensor(t) else None for t in (E, nu)]
         ctx.given = (F0 is not None, C0 is not None)
@@ -119,13 +134,24 @@ class RolloutFunction(torch.autograd.Function):
         gv0 = torch.empty(n, d, **f32)
         gF0 = torch.empty(n, d, d, **f32)
         gC0 = torch.empty(n, d, d, **f32)
-        gE, gnu = ctypes.c_double(), ctypes.c_double()
         torch.cuda.synchronize(dev)
-        roll._check(capi.lib().nclr_rollout_backward(roll._h, _dp(gx), _dp(gv), None, None,
-                                                      _dp(gx0), _dp(gv0), _dp(gF0), _dp(gC0),
-                                                      ctypes.byref(gE), ctypes.byref(gnu)))
         out = []
-        for val, spec in ((gE.value, ctx.params[0]), (gnu.value, ctx.params[1])):
-            out.append(None if spec is None else torch.tensor(val, dtype=spec[0], device=spec[1]))
+        if ctx.per_particle:
+            gEp = torch.empty(n, **f32)
+            gnup = torch.empty(n, **f32)
+            roll._check(capi.lib().nclr_rollout_backward_moduli(
+                roll._h, _dp(gx), _dp(gv), None, None, _dp(gx0), _dp(gv0), _dp(gF0), _dp(gC0),
+                _dp(gEp), _dp(gnup)))
+            for val, spec, shape in ((gEp, ctx.params[0], ctx.shapes[0]),
+                                     (gnup, ctx.params[1], ctx.shapes[1])):
+                out.append(None if spec is None
+                           else val.to(dtype=spec[0], device=spec[1]).reshape(shape))
+        else:
+            gE, gnu = ctypes.c_double(), ctypes.c_double()
+            roll._check(capi.lib().nclr_rollout_backward(roll._h, _dp(gx), _dp(gv), None, None,
+                                                          _dp(gx0), _dp(gv0), _dp(gF0), _dp(gC0),
+                                                          ctypes.byref(gE), ctypes.byref(gnu)))
+            for val, spec in ((gE.value, ctx.params[0]), (gnu.value, ctx.params[1])):
+                out.append(None if spec is None else torch.tensor(val, dtype=spec[0], device=spec[1]))
         return (None, gx0, gv0, out[0], out[1], gF0 if ctx.given[0] else None,
                 gC0 if ctx.given[1] else None)

@@ -98,6 +98,10 @@ SIGNATURES = {
     "nclr_rollout_backward": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                              ctypes.POINTER(ctypes.c_double),
                                              ctypes.POINTER(ctypes.c_double)]),
+    "nclr_rollout_forward_moduli": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                   _vp, _vp]),
+    "nclr_rollout_backward_moduli": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                    _vp, _vp]),
     "nclr_rollout_timing": (ctypes.c_int, [_h, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]),
     "nclr_rollout_stream": (_vp, [_h]),

@@ -322,14 +322,16 @@ __global__ void __launch_bounds__(256) adj_grid_kernel(const float4 *__restrict_
 // A = -(dt vol Dinv) PF + m C (jelly: mu = 0.3 mu_0, lambda = 0.3 lambda_0) and PF the
 // fixed-corotated 2 mu (F - R) F^T + lambda (J - 1) J 1 or (kStress == kNeoHookean)
 // mu (F F^T - I) + lambda ln(J) I.  Adds to the adjoints of x and F, writes those of v and C,
-// and accumulates the adjoints of mu_0 and lambda_0 into gml[0..1].
+// and accumulates the adjoints of mu_0 and lambda_0 into gml[0..1].  With per-particle moduli
+// (rm.lame: each row's mu_0, lambda_0) it also accumulates each row's own adjoints into
+// rm.grad[2 row], rm.grad[2 row + 1]: one thread per row, so no atomics.
 // ---------------------------------------------------------------------------------------
 template <int D, int kStress>
 __global__ void __launch_bounds__(128) adj_p2g_kernel(
     int n, const float *__restrict__ x, const float *__restrict__ v, const float *__restrict__ F,
     const float *__restrict__ C, const float *__restrict__ mass, const float *__restrict__ vol,
     const float4 *__restrict__ GB, Params P, float *__restrict__ ox, float *__restrict__ ov,
-    float *__restrict__ oF, float *__restrict__ oC, double *gml, int *err) {
+    float *__restrict__ oF, float *__restrict__ oC, double *gml, RowModuli rm, int *err) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int S = (D == 3) ? 27 : 9;
   float gmu = 0.0f, glam = 0.0f;
@@ -344,10 +346,10 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     const Mat<D> Fm = load_row_mat<D>(F, p);
     const Mat<D> Cm = load_row_mat<D>(C, p);
     const float m = mass[p], vo = vol[p];
+    const float2 l0 = rm.lame ? rm.lame[p] : make_float2(P.mu0, P.lambda0);
     // the corotated stress's polar rotation, whose factorisation its adjoint reuses
     const std::conditional_t<kStress == kNeoHookean, NoPolar<D>, Polar<D>> pol(Fm);
-    const Mat<D> A = fused_affine<D>(Fm, pol.R, Cm, 1.0f, m, vo, kJelly,
-                                     make_float2(P.mu0, P.lambda0), P);
+    const Mat<D> A = fused_affine<D>(Fm, pol.R, Cm, 1.0f, m, vo, kJelly, l0, P);
     Mat<D> gA;
 #pragma unroll
     for (int i = 0; i < D; ++i)
@@ -412,7 +414,7 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     store_row_mat<D>(oC, p, gC);
     // stress
     const float kappa = P.dt * vo * P.Dinv;
-    const float mu = P.mu0 * 0.3f, lam = P.lambda0 * 0.3f;
+    const float mu = l0.x * 0.3f, lam = l0.y * 0.3f;
     const float J = det(Fm);
     Mat<D> gF = load_row_mat<D>(oF, p);
     const Mat<D> cof = cofactor(Fm);  // d det(F) / dF = J F^-T
@@ -489,6 +491,10 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     store_row_mat<D>(oF, p, gF);
     gmu *= 0.3f;  // jelly hardening (src/nclr.h:362-364)
     glam *= 0.3f;
+    if (rm.grad) {
+      rm.grad[2 * (size_t)p] += gmu;
+      rm.grad[2 * (size_t)p + 1] += glam;
+    }
   }
   // block reduction of the parameter adjoints, one double atomic per warp
   double a = gmu, b = glam;
@@ -509,8 +515,8 @@ void launch_adjoint_step(int n, const float *x, const float *v, const float *F, 
                          const float *Cn, const float *mass, const float *vol, const float4 *V,
                          const Params &P, bool ref, const float *gx, const float *gv,
                          const float *gF, const float *gC, float *ox, float *ov, float *oF,
-                         float *oC, float *VB, float4 *GB, double *gml, int *err,
-                         cudaStream_t st) {
+                         float *oC, float *VB, float4 *GB, double *gml, RowModuli rm,
+                         int *err, cudaStream_t st) {
   const unsigned pb = (unsigned)((n + 127) / 128);
   if (n > 0) {
     if (ref)
@@ -522,21 +528,47 @@ void launch_adjoint_step(int n, const float *x, const float *v, const float *F, 
   if (n > 0)
     if (P.stress == kNeoHookean)
       adj_p2g_kernel<D, kNeoHookean><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF,
-                                                         oC, gml, err);
+                                                         oC, gml, rm, err);
     else
       adj_p2g_kernel<D, kCorotated><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF,
-                                                        oC, gml, err);
+                                                        oC, gml, rm, err);
+}
+
+namespace {
+
+// Row q's E and nu adjoints from its mu_0 / lambda_0 adjoints (src/nclr.h:77-78):
+//   dmu/dE = 1 / (2 (1 + nu)),  dmu/dnu = -E / (2 (1 + nu)^2),
+//   dlambda/dE = nu / q,  dlambda/dnu = E (1 + 2 nu^2) / q^2,  q = (1 + nu)(1 - 2 nu).
+__global__ void moduli_grads_kernel(int n, const float *__restrict__ E, const float *__restrict__ nu,
+                                    const double *__restrict__ grad, float *__restrict__ gE,
+                                    float *__restrict__ gnu) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double e = E[i], v = nu[i], gm = grad[2 * (size_t)i], gl = grad[2 * (size_t)i + 1];
+  const double q = (1.0 + v) * (1.0 - 2.0 * v);
+  if (gE) gE[i] = (float)(gm / (2.0 * (1.0 + v)) + gl * v / q);
+  if (gnu) gnu[i] = (float)(-gm * e / (2.0 * (1.0 + v) * (1.0 + v)) + gl * e * (1.0 + 2.0 * v * v) / (q * q));
+}
+
+}  // namespace
+
+cudaError_t launch_moduli_grads(int n, const float *E, const float *nu, const double *grad,
+                                float *gE, float *gnu, cudaStream_t st) {
+  if (n > 0) moduli_grads_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, E, nu, grad, gE, gnu);
+  return cudaGetLastError();
 }
 
 template void launch_adjoint_step<2>(int, const float *, const float *, const float *, const float *,
                                      const float *, const float *, const float *, const float4 *,
                                      const Params &, bool, const float *, const float *,
                                      const float *, const float *, float *, float *, float *,
-                                     float *, float *, float4 *, double *, int *, cudaStream_t);
+                                     float *, float *, float4 *, double *, RowModuli, int *,
+                                     cudaStream_t);
 template void launch_adjoint_step<3>(int, const float *, const float *, const float *, const float *,
                                      const float *, const float *, const float *, const float4 *,
                                      const Params &, bool, const float *, const float *,
                                      const float *, const float *, float *, float *, float *,
-                                     float *, float *, float4 *, double *, int *, cudaStream_t);
+                                     float *, float *, float4 *, double *, RowModuli, int *,
+                                     cudaStream_t);
 
 }  // namespace mpm

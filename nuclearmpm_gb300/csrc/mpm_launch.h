@@ -80,7 +80,8 @@ void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_ma
 // Counts material[] entries above NCLR_LIQUID into *out (host); synchronises `st`
 // (scene_build.cu).
 cudaError_t count_bad_materials(const uint8_t *mat, int64_t n, int *scratch, int *out, cudaStream_t st);
-// lame[p] = (mu_0, lambda_0) of caller row id[p]'s E and nu, for the n slots.
+// lame[p] = (mu_0, lambda_0) of caller row id[p]'s E and nu (row p when id is null), for the
+// n slots.
 cudaError_t launch_set_lame(const int *id, int n, const float *E, const float *nu, float2 *lame,
                             cudaStream_t st);
 
@@ -88,13 +89,24 @@ cudaError_t launch_set_lame(const int *id, int n, const float *E, const float *n
 // adjoint of s_t (ox, ov, oF, oC), mu_0 / lambda_0 adjoints added to gml[0..1].  States are
 // caller-order rows; V is the step's updated grid; VB (4 floats per node) must be zero on
 // entry and is zero again on exit; GB holds nodes float4.
+// Per-particle moduli of a rollout, per row in the caller's order (both null: the scene's
+// pair): lame[q] = (mu_0, lambda_0) of row q; grad[2q], grad[2q + 1] accumulate the adjoints of
+// row q's mu_0 and lambda_0 over the reverse steps.
+struct RowModuli {
+  const float2 *lame = nullptr;
+  double *grad = nullptr;
+};
 template <int D>
 void launch_adjoint_step(int n, const float *x, const float *v, const float *F, const float *C,
                          const float *Cn, const float *mass, const float *vol, const float4 *V,
                          const Params &P, bool ref, const float *gx, const float *gv,
                          const float *gF, const float *gC, float *ox, float *ov, float *oF,
-                         float *oC, float *VB, float4 *GB, double *gml, int *err,
+                         float *oC, float *VB, float4 *GB, double *gml, RowModuli rm, int *err,
                          cudaStream_t st);
+// gE[q], gnu[q] from row q's accumulated mu_0 / lambda_0 adjoints (grad) and its E[q], nu[q],
+// through mu_0 = E / (2 (1 + nu)), lambda_0 = E nu / ((1 + nu)(1 - 2 nu)).
+cudaError_t launch_moduli_grads(int n, const float *E, const float *nu, const double *grad,
+                                float *gE, float *gnu, cudaStream_t st);
 
 // Exclusive prefix sum of count[0..n) into start[0..n]; tile_sums must hold
 // scan_tiles(n) ints.  Three launches.

@@ -1314,6 +1314,12 @@ struct nclr_rollout {
   float *VB = nullptr;
   float4 *GB = nullptr;
   double *gml = nullptr;      // adjoints of mu_0, lambda_0
+  // per-particle moduli of the last forward (nclr_rollout_forward_moduli): E and nu per row,
+  // each row's (mu_0, lambda_0), and each row's accumulated mu_0 / lambda_0 adjoints
+  bool per_particle = false;
+  float *mod_E = nullptr, *mod_nu = nullptr;
+  float2 *lame_rows = nullptr;
+  double *grad_rows = nullptr;
   int *err = nullptr;
   float *mass = nullptr, *vol = nullptr, *ones = nullptr;
   bool have_forward = false;
@@ -1368,6 +1374,10 @@ void rollout_release(nclr_rollout *r) {
   cudaFree(r->VB);
   cudaFree(r->GB);
   cudaFree(r->gml);
+  cudaFree(r->mod_E);
+  cudaFree(r->mod_nu);
+  cudaFree(r->lame_rows);
+  cudaFree(r->grad_rows);
   cudaFree(r->err);
   cudaFree(r->mass);
   cudaFree(r->vol);
@@ -1496,15 +1506,36 @@ nclr_status nclr_rollout_create(nclr_rollout **out, int dim, int64_t n, const fl
   return NCLR_OK;
 }
 
-nclr_status nclr_rollout_forward(nclr_rollout *r, const float *x0, const float *v0, const float *F0,
-                                 const float *C0, float E, float nu, float *xT, float *vT,
-                                 float *FT, float *CT) {
+// The forward of both entry points: the scene's E and nu, or (Ep, nup: device arrays, one per
+// row) every particle's own.
+static nclr_status rollout_forward(nclr_rollout *r, const float *x0, const float *v0,
+                                   const float *F0, const float *C0, float E, float nu,
+                                   const float *Ep, const float *nup, float *xT, float *vT,
+                                   float *FT, float *CT) {
   if (!r || !x0 || !v0 || !F0 || !C0) return rfail(r, NCLR_ERR_INVALID, "NULL argument");
   nclr_sim *s = r->sim;
   R_TRY(r, cudaSetDevice(s->device));
-  r->E = E;
-  r->nu = nu;
-  set_material(s, E, nu);
+  r->have_forward = false;
+  if (Ep) {
+    const size_t row = sizeof(float) * (size_t)r->n;
+    if (!r->mod_E) {
+      R_TRY(r, cudaMalloc((void **)&r->mod_E, row));
+      R_TRY(r, cudaMalloc((void **)&r->mod_nu, row));
+      R_TRY(r, cudaMalloc((void **)&r->lame_rows, sizeof(float2) * (size_t)r->n));
+      R_TRY(r, cudaMalloc((void **)&r->grad_rows, 2 * sizeof(double) * (size_t)r->n));
+    }
+    R_TRY(r, cudaMemcpyAsync(r->mod_E, Ep, row, cudaMemcpyDeviceToDevice, s->stream));
+    R_TRY(r, cudaMemcpyAsync(r->mod_nu, nup, row, cudaMemcpyDeviceToDevice, s->stream));
+    R_TRY(r, mpm::launch_set_lame(nullptr, (int)r->n, r->mod_E, r->mod_nu, r->lame_rows, s->stream));
+    R_SIM(r, nclr_set_moduli_device(s, r->mod_E, r->mod_nu));
+    r->per_particle = true;
+  } else {
+    if (r->per_particle) R_SIM(r, nclr_set_moduli(s, nullptr, nullptr));
+    r->per_particle = false;
+    r->E = E;
+    r->nu = nu;
+    set_material(s, E, nu);
+  }
   float *c0 = r->state(r->ckpt, 0);
   const size_t vec = sizeof(float) * (size_t)r->n * r->dim, mat = vec * r->dim;
   R_TRY(r, cudaMemcpyAsync(r->x(c0), x0, vec, cudaMemcpyDeviceToDevice, s->stream));
@@ -1527,11 +1558,33 @@ nclr_status nclr_rollout_forward(nclr_rollout *r, const float *x0, const float *
   return NCLR_OK;
 }
 
-nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float *gvT,
-                                  const float *gFT, const float *gCT, float *gx0, float *gv0,
-                                  float *gF0, float *gC0, double *gE, double *gnu) {
+nclr_status nclr_rollout_forward(nclr_rollout *r, const float *x0, const float *v0, const float *F0,
+                                 const float *C0, float E, float nu, float *xT, float *vT,
+                                 float *FT, float *CT) {
+  return rollout_forward(r, x0, v0, F0, C0, E, nu, nullptr, nullptr, xT, vT, FT, CT);
+}
+
+nclr_status nclr_rollout_forward_moduli(nclr_rollout *r, const float *x0, const float *v0,
+                                        const float *F0, const float *C0, const float *E,
+                                        const float *nu, float *xT, float *vT, float *FT,
+                                        float *CT) {
+  if (!E || !nu) return rfail(r, NCLR_ERR_INVALID, "E and nu are required");
+  return rollout_forward(r, x0, v0, F0, C0, 0.0f, 0.0f, E, nu, xT, vT, FT, CT);
+}
+
+// The reverse pass of both entry points: scalar E / nu adjoints after a forward with the
+// scene's pair, per-row ones (gEp, gnup) after a forward with per-particle moduli.
+static nclr_status rollout_backward(nclr_rollout *r, const float *gxT, const float *gvT,
+                                    const float *gFT, const float *gCT, float *gx0, float *gv0,
+                                    float *gF0, float *gC0, double *gE, double *gnu,
+                                    bool per_particle, float *gEp, float *gnup) {
   if (!r) return NCLR_ERR_INVALID;
   if (!r->have_forward) return rfail(r, NCLR_ERR_INVALID, "backward before forward");
+  if (per_particle != r->per_particle)
+    return rfail(r, NCLR_ERR_INVALID,
+                 per_particle ? "the forward used the scene's E and nu: use nclr_rollout_backward"
+                              : "the forward used per-particle moduli: use "
+                                "nclr_rollout_backward_moduli");
   nclr_sim *s = r->sim;
   R_TRY(r, cudaSetDevice(s->device));
   const int D = r->dim;
@@ -1548,6 +1601,12 @@ nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float
   R_TRY(r, seed(r->F(a), gFT, mat));
   R_TRY(r, seed(r->C(a), gCT, mat));
   R_TRY(r, cudaMemsetAsync(r->gml, 0, 2 * sizeof(double), s->stream));
+  mpm::RowModuli rm;
+  if (r->per_particle) {
+    R_TRY(r, cudaMemsetAsync(r->grad_rows, 0, 2 * sizeof(double) * (size_t)n, s->stream));
+    rm.lame = r->lame_rows;
+    rm.grad = r->grad_rows;
+  }
   R_TRY(r, cudaMemsetAsync(r->err, 0, sizeof(int), s->stream));
   R_TRY(r, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)s->nscenes, s->stream));
   const Params &P = s->P0();
@@ -1575,7 +1634,7 @@ nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float
         mpm::launch_adjoint_step<DD>(n, r->x(st_t), r->v(st_t), r->F(st_t), r->C(st_t), r->C(st_n),
                                      r->mass, r->vol, r->grids[buf] + (size_t)i * r->nodes, P,
                                      s->ref, r->x(a), r->v(a), r->F(a), r->C(a), r->x(b), r->v(b),
-                                     r->F(b), r->C(b), r->VB, r->GB, r->gml, r->err, r->rev);
+                                     r->F(b), r->C(b), r->VB, r->GB, r->gml, rm, r->err, r->rev);
       });
       std::swap(a, b);
     }
@@ -1593,6 +1652,8 @@ nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float
   if (gv0) R_TRY(r, cudaMemcpyAsync(gv0, r->v(a), vec, cudaMemcpyDeviceToDevice, s->stream));
   if (gF0) R_TRY(r, cudaMemcpyAsync(gF0, r->F(a), mat, cudaMemcpyDeviceToDevice, s->stream));
   if (gC0) R_TRY(r, cudaMemcpyAsync(gC0, r->C(a), mat, cudaMemcpyDeviceToDevice, s->stream));
+  if (r->per_particle)
+    R_TRY(r, mpm::launch_moduli_grads(n, r->mod_E, r->mod_nu, r->grad_rows, gEp, gnup, s->stream));
   double gml[2] = {0.0, 0.0};
   int err = 0;
   R_TRY(r, cudaMemcpyAsync(gml, r->gml, sizeof(gml), cudaMemcpyDeviceToHost, s->stream));
@@ -1611,6 +1672,21 @@ nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float
     return rfail(r, NCLR_ERR_OUT_OF_RANGE, "a stencil left the grid during the recomputation");
   if (err & mpm::kErrOutOfRange) return rfail(r, NCLR_ERR_OUT_OF_RANGE, "a stencil left the grid");
   return NCLR_OK;
+}
+
+nclr_status nclr_rollout_backward(nclr_rollout *r, const float *gxT, const float *gvT,
+                                  const float *gFT, const float *gCT, float *gx0, float *gv0,
+                                  float *gF0, float *gC0, double *gE, double *gnu) {
+  return rollout_backward(r, gxT, gvT, gFT, gCT, gx0, gv0, gF0, gC0, gE, gnu, false, nullptr,
+                          nullptr);
+}
+
+nclr_status nclr_rollout_backward_moduli(nclr_rollout *r, const float *gxT, const float *gvT,
+                                         const float *gFT, const float *gCT, float *gx0,
+                                         float *gv0, float *gF0, float *gC0, float *gE,
+                                         float *gnu) {
+  return rollout_backward(r, gxT, gvT, gFT, gCT, gx0, gv0, gF0, gC0, nullptr, nullptr, true, gE,
+                          gnu);
 }
 
 nclr_status nclr_rollout_timing(const nclr_rollout *r, double *forward_ms, double *backward_ms) {

@@ -46,14 +46,14 @@ __global__ void bad_materials_kernel(const uint8_t *__restrict__ mat, int64_t n,
   if (i < n && mat[i] > 2) atomicAdd(bad, 1);
 }
 
-// Slot p takes the moduli of caller row id[p]: mu_0 = E / (2 (1 + nu)),
+// Slot p takes the moduli of caller row id[p] (row p when id is null): mu_0 = E / (2 (1 + nu)),
 // lambda_0 = E nu / ((1 + nu)(1 - 2 nu)) (src/nclr.h:77-78), each operation rounded on its
 // own as the host evaluates the simulation's pair (no fused multiply-add).
 __global__ void set_lame_kernel(const int *__restrict__ id, int n, const float *__restrict__ E,
                                 const float *__restrict__ nu, float2 *__restrict__ lame) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  const int q = id[p];
+  const int q = id ? id[p] : p;
   const float e = E[q], v = nu[q];
   const float one_v = __fadd_rn(1.0f, v);
   lame[p] = make_float2(__fdiv_rn(e, __fmul_rn(2.0f, one_v)),

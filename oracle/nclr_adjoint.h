@@ -120,9 +120,17 @@ class Adjoint {
 
   // Reverse pass from the adjoint of the final state; returns the adjoint of the initial
   // state, accumulates mu_0 / lambda_0 adjoints.
-  StepAdjoint<T, D> backward(StepAdjoint<T, D> adj, T &gmu0, T &glambda0) {
+  // With per-particle moduli (Particle::mu0 / lambda0), gmu_rows / glambda_rows (may be null)
+  // receive each particle's own mu_0 / lambda_0 adjoints; gmu0 / glambda0 are their sums.
+  StepAdjoint<T, D> backward(StepAdjoint<T, D> adj, T &gmu0, T &glambda0,
+                             std::vector<T> *gmu_rows = nullptr,
+                             std::vector<T> *glambda_rows = nullptr) {
     gmu0 = T(0);
     glambda0 = T(0);
+    rows_mu_ = gmu_rows;
+    rows_lambda_ = glambda_rows;
+    if (rows_mu_) rows_mu_->assign(states_.front().size(), T(0));
+    if (rows_lambda_) rows_lambda_->assign(states_.front().size(), T(0));
     for (int t = (int)grids_.size() - 1; t >= 0; --t) adj = step_backward(t, adj, gmu0, glambda0);
     return adj;
   }
@@ -130,6 +138,7 @@ class Adjoint {
  private:
   Sim sim_;
   Physics mode_;
+  std::vector<T> *rows_mu_ = nullptr, *rows_lambda_ = nullptr;  // per-particle adjoints
   std::vector<std::vector<Particle<T, D>>> states_;
   std::vector<std::vector<Cell<T, D>>> grids_;
 
@@ -321,6 +330,8 @@ class Adjoint {
           for (int j = 0; j < D; ++j) out.F[p](i, j) += SF(i, j) + c * cof(i, j);
         gmu0 += e * gmu;
         glambda0 += e * (trG * std::log(J));
+        if (rows_mu_) (*rows_mu_)[p] += e * gmu;
+        if (rows_lambda_) (*rows_lambda_)[p] += e * (trG * std::log(J));
         continue;
       }
       const Mat<T, D> R = nclr_polar_R<T, D>(F, mode_);
@@ -351,6 +362,8 @@ class Adjoint {
           out.F[p](i, j) += FfromQ(i, j) + Xbar(i, j) + Fpolar(i, j) + dJ * cof(i, j);
       gmu0 += e * gmu;
       glambda0 += e * glambda;
+      if (rows_mu_) (*rows_mu_)[p] += e * gmu;
+      if (rows_lambda_) (*rows_lambda_)[p] += e * glambda;
     }
     return out;
   }

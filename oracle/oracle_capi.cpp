@@ -115,7 +115,8 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
             double E, double nu, double gravity, int nsteps, double *xT, double *vT, double *FT,
             double *CT, const double *gx, const double *gv, const double *gF, const double *gC,
             double *gx0, double *gv0, double *gF0, double *gC0, double *gmu_glambda,
-            int stress) {
+            int stress, const double *E_p, const double *nu_p, double *gmu_rows,
+            double *glambda_rows) {
   using T = double;
   std::vector<Particle<T, D>> ps((size_t)n);
   for (int64_t p = 0; p < n; ++p) {
@@ -132,6 +133,7 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
     q.Jp = 1;
     q.mass = mass[p];
     q.volume = volume[p];
+    if (E_p && nu_p) std::tie(q.mu0, q.lambda0) = lame_of<T>(E_p[p], nu_p[p]);
   }
   try {
     Adjoint<T, D> adj(std::move(ps), Model::kJelly, res, dt, E, nu, gravity, (Physics)physics,
@@ -159,7 +161,14 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
         }
     }
     T gmu = 0, glam = 0;
-    const StepAdjoint<T, D> out = adj.backward(seed, gmu, glam);
+    std::vector<T> rows_mu, rows_lambda;
+    const bool rows = gmu_rows || glambda_rows;
+    const StepAdjoint<T, D> out = adj.backward(seed, gmu, glam, rows ? &rows_mu : nullptr,
+                                               rows ? &rows_lambda : nullptr);
+    for (int64_t p = 0; rows && p < n; ++p) {
+      if (gmu_rows) gmu_rows[p] = rows_mu[(size_t)p];
+      if (glambda_rows) glambda_rows[p] = rows_lambda[(size_t)p];
+    }
     for (int64_t p = 0; p < n; ++p) {
       for (int d = 0; d < D; ++d) {
         gx0[p * D + d] = out.x[(size_t)p][d];
@@ -186,21 +195,27 @@ extern "C" {
 // FP64 reverse pass of an `nsteps` jelly rollout (nclr_adjoint.h): the forward final state
 // into xT/vT/FT/CT, the adjoint of the initial state (given the final state's adjoint
 // gx/gv/gF/gC, any may be NULL = 0) into gx0/gv0/gF0/gC0, and the adjoints of mu_0 and
-// lambda_0 into gmu_glambda[0..1].  stress: 0 fixed corotated, 1 neo-Hookean.  Returns 0, 2
-// (a stencil left the grid) or 1.
+// lambda_0 into gmu_glambda[0..1].  stress: 0 fixed corotated, 1 neo-Hookean.  E_p / nu_p (may
+// be NULL) give every particle its own moduli; gmu_rows / glambda_rows (may be NULL) then
+// receive each particle's own mu_0 / lambda_0 adjoints.  Returns 0, 2 (a stencil left the
+// grid) or 1.
 int oracle_adjoint(int dim, int physics, int64_t n, const double *x0, const double *v0,
                    const double *F0, const double *C0, const double *mass, const double *volume,
                    int res, double dt, double E, double nu, double gravity, int nsteps,
                    double *xT, double *vT, double *FT, double *CT, const double *gx,
                    const double *gv, const double *gF, const double *gC, double *gx0,
-                   double *gv0, double *gF0, double *gC0, double *gmu_glambda, int stress) {
-  if (n < 0 || res < 1 || nsteps < 0 || stress < 0 || stress > 1) return 1;
+                   double *gv0, double *gF0, double *gC0, double *gmu_glambda, int stress,
+                   const double *E_p, const double *nu_p, double *gmu_rows,
+                   double *glambda_rows) {
+  if (n < 0 || res < 1 || nsteps < 0 || stress < 0 || stress > 1 || (!E_p) != (!nu_p)) return 1;
   if (dim == 2)
     return adjoint<2>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
-                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress);
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress,
+                      E_p, nu_p, gmu_rows, glambda_rows);
   if (dim == 3)
     return adjoint<3>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
-                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress);
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress,
+                      E_p, nu_p, gmu_rows, glambda_rows);
   return 1;
 }
 

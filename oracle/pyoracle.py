@@ -50,7 +50,7 @@ def _load(name: str, sub: str) -> ctypes.CDLL:
             lib.oracle_adjoint.restype = ctypes.c_int
             lib.oracle_adjoint.argtypes = ([ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [_dp] * 6 +
                                            [ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int] +
-                                           [_dp] * 13 + [ctypes.c_int])
+                                           [_dp] * 13 + [ctypes.c_int] + [_dp] * 4)
         else:
             lib.ref_advance.restype = ctypes.c_int
             lib.ref_advance.argtypes = [ctypes.c_int, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -178,22 +178,39 @@ def lame(E: float, nu: float):
 
 def adjoint(state: dict, *, dim: int, res: int, steps: int, dt: float = 1e-4, E: float = 1e4,
             nu: float = 0.2, gravity: float = -100.0, physics: int = REFERENCE, seed: dict,
-            stress: int = COROTATED):
+            stress: int = COROTATED, E_particles=None, nu_particles=None):
     """FP64 jelly rollout and its reverse pass.  `seed` holds the final state's adjoint (keys
-    among x, v, F, C).  Returns (final state, adjoint of the initial state incl. 'E' and 'nu')."""
+    among x, v, F, C).  Returns (final state, adjoint of the initial state incl. 'E' and 'nu').
+    With E_particles / nu_particles (one value per particle), 'E' and 'nu' (and 'mu0',
+    'lambda0') are arrays: every particle's own adjoints."""
     n, s = _prep(state, dim)
     out = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C")}
     g = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C")}
     sd = {k: (np.ascontiguousarray(seed[k], dtype=np.float64) if k in seed else None)
           for k in ("x", "v", "F", "C")}
     ml = np.zeros(2)
+    rows = E_particles is not None
+    if rows != (nu_particles is not None):
+        raise ValueError("E_particles and nu_particles go together")
+    Ep = nup = gmr = glr = None
+    if rows:
+        Ep = np.ascontiguousarray(np.broadcast_to(np.asarray(E_particles, np.float64), (n,)))
+        nup = np.ascontiguousarray(np.broadcast_to(np.asarray(nu_particles, np.float64), (n,)))
+        gmr, glr = np.zeros(n), np.zeros(n)
     st = oracle_lib().oracle_adjoint(
         dim, physics, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]), _p(s["mass"]),
         _p(s["volume"]), res, dt, E, nu, gravity, steps, _p(out["x"]), _p(out["v"]),
         _p(out["F"]), _p(out["C"]), *(None if sd[k] is None else _p(sd[k]) for k in ("x", "v", "F", "C")),
-        _p(g["x"]), _p(g["v"]), _p(g["F"]), _p(g["C"]), _p(ml), int(stress))
+        _p(g["x"]), _p(g["v"]), _p(g["F"]), _p(g["C"]), _p(ml), int(stress),
+        *((_p(Ep), _p(nup), _p(gmr), _p(glr)) if rows else (None,) * 4))
     if st != 0:
         raise RuntimeError(f"oracle adjoint failed ({st})")
+    if rows:
+        _, _, dmu, dlam = lame(Ep, nup)
+        g["mu0"], g["lambda0"] = gmr, glr
+        g["E"] = gmr * dmu[0] + glr * dlam[0]
+        g["nu"] = gmr * dmu[1] + glr * dlam[1]
+        return out, g
     _, _, dmu, dlam = lame(E, nu)
     g["mu0"], g["lambda0"] = float(ml[0]), float(ml[1])
     g["E"] = ml[0] * dmu[0] + ml[1] * dlam[0]

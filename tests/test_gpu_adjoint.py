@@ -39,7 +39,8 @@ def gpu_grads(s, dim, res, steps, physics, every, seed_fn, E=1e4, nu=0.2, stress
     loss = seed_fn(xT)
     loss.backward()
     out = {"x": x0.grad.cpu().numpy(), "v": v0.grad.cpu().numpy(), "F": F0.grad.cpu().numpy(),
-           "C": C0.grad.cpu().numpy(), "E": float(Et.grad), "nu": float(nut.grad),
+           "C": C0.grad.cpu().numpy(), "E": Et.grad.detach().cpu().numpy(),
+           "nu": nut.grad.detach().cpu().numpy(),
            "xT": xT.detach().cpu().numpy(), "loss": float(loss.detach())}
     out["timing"] = roll.timing()
     roll.close()
@@ -121,3 +122,29 @@ def test_checkpoint_interval_does_not_change_gradients():
     b = gpu_grads(s, dim, res, steps, scenes.REFERENCE, every=3, seed_fn=loss)
     for f in ("x", "v", "F", "C"):
         assert rel(a[f], b[f]) <= GRAD_TOL, f
+
+
+@pytest.mark.parametrize("dim,res,steps,n,physics,stress", [
+    (2, 32, 50, 1024, scenes.REFERENCE, 0),
+    (3, 16, 10, 512, scenes.CORRECTED, 1),
+])
+def test_gpu_per_particle_moduli_gradients_match_fp64_adjoint(oracle, dim, res, steps, n,
+                                                              physics, stress):
+    """One E and nu per particle (nclr_rollout_forward_moduli / backward_moduli through the
+    autograd function with E and nu tensors of n values): every particle's E and nu gradient,
+    and those of the initial state, against the FP64 CPU adjoint."""
+    s = setup(dim, res, n, physics)
+    rng = np.random.default_rng(6)
+    Ep = np.exp(rng.uniform(np.log(1e3), np.log(1e4), size=n)).astype(np.float32)
+    nup = rng.uniform(0.15, 0.35, size=n).astype(np.float32)
+    kw = dict(dim=dim, res=res, steps=steps, physics=physics, stress=stress,
+              E_particles=Ep.astype(np.float64), nu_particles=nup.astype(np.float64))
+    fwd, _ = oracle.adjoint(s, seed={}, **kw)
+    targets = (fwd["x"] + rng.normal(0, 1e-3, size=fwd["x"].shape)).astype(np.float32)
+    g = gpu_grads(s, dim, res, steps, physics, every=7, seed_fn=point_loss(targets), E=Ep, nu=nup,
+                  stress=stress)
+    assert g["E"].shape == (n,) and g["nu"].shape == (n,)
+    seed = 2 * (g["xT"].astype(np.float64) - targets)  # the GPU's own final state
+    _, o = oracle.adjoint(s, seed={"x": seed}, **kw)
+    for f in ("x", "v", "F", "C", "E", "nu"):
+        assert rel(g[f], o[f]) <= GRAD_TOL, (f, rel(g[f], o[f]))
