@@ -79,8 +79,8 @@ typedef struct nclr_options {
   int sparse_block_max;    /* grid blocks holding fewer particles than this (at the last sort)
                               are stepped particle by particle, gathering from and scattering
                               into the grid directly instead of through a shared-memory tile;
-                              0 = never, -1 = the default for the dimension (default -1);
-                              single simulations only, batches ignore it */
+                              0 = never, -1 = the default (default -1: 64 in 3D and 32 in 2D
+                              for one simulation, 32 for a batch) */
   int small_scene_max;     /* simulations of at most this many particles (per scene) run all
                               the steps of an advance() call in one cooperative kernel launch
                               (reference order p2g / grid_op / g2p, grid-wide barriers; a

@@ -61,6 +61,7 @@ struct Params {
   float cscale;         // 4 inv_dx  (src/nclr.h:206,223)
   float dt_gravity;     // dt * gravity (src/nclr.h:292)
   int stress;           // kCorotated or kNeoHookean
+  int thin_max;         // batches: blocks with fewer particles skip the shared-memory tiles
   int64_t nodes;        // N^dim
   int nb;               // grid blocks per axis: ceil(N / Tiling<dim>::BS)
   int nblocks;          // nb^dim

@@ -460,7 +460,14 @@ g2p2g_kernel(
     uint8_t *__restrict__ flags = flags_all + block_off;
     const int b = gb - block_off;
     int *err_now = err + 2 * sid, *err_next = err + 2 * sid + next_slot;
-    if (kMode != kP2GOnly && !chunk) {
+    // The block's particles, stored cell by cell in rounds (see sort_move_kernel), or a chunk's.
+    const int c0 = (item - nact) * kG2P2GThreads;
+    const int p0 = chunk ? 0 : bstart[gb];
+    const int np = chunk ? min(kG2P2GThreads, nsp - c0) : bstart[gb + 1] - p0;
+    // A batch's thin block (fewer than P.thin_max particles) skips the tiles like a chunk:
+    // gathered from V and scattered into G directly (CTA-uniform).
+    const bool direct = chunk || (kBatch && np < P.thin_max);
+    if (kMode != kP2GOnly && !direct) {
       for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
         int g[D], l[3] = {0, 0, 0};
         bool in = true;
@@ -478,12 +485,8 @@ g2p2g_kernel(
     }
     __syncthreads();
 
-    // The block's particles, stored cell by cell in rounds (see sort_move_kernel), one per
-    // thread in slot order.  Every lane of a warp runs the same number of iterations (the
-    // warp-wide steps below need them all).
-    const int c0 = (item - nact) * kG2P2GThreads;
-    const int p0 = chunk ? 0 : bstart[gb];
-    const int np = chunk ? min(kG2P2GThreads, nsp - c0) : bstart[gb + 1] - p0;
+    // One particle per thread in slot order.  Every lane of a warp runs the same number of
+    // iterations (the warp-wide steps below need them all).
     for (int j0 = 0; j0 < np; j0 += kG2P2GThreads) {
       const int j = j0 + threadIdx.x;
       const bool valid = j < np;
@@ -512,7 +515,7 @@ g2p2g_kernel(
         // ---- G2P of this step ----
         float fx[D], w[3][D];
         stencil<D>(x, P.inv_dx, base, fx, w);
-        bool fast = !chunk;
+        bool fast = !direct;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           lb[d] = base[d] - org[d];
@@ -580,7 +583,7 @@ g2p2g_kernel(
           for (int d = 0; d < D; ++d) mv[d] = v[d] * m;
           stencil<D>(x, P.inv_dx, base, fx_s, w_s);
           p2g_terms<D>(fx_s, P.dx, mv, A);  // mv, A now hold q0 and A dx
-          fast_s = !chunk;
+          fast_s = !direct;
 #pragma unroll
           for (int d = 0; d < D; ++d) {
             lb[d] = base[d] - org[d];
@@ -609,7 +612,7 @@ g2p2g_kernel(
       // same stencil base go in separate rounds (rare: consecutive slots are in different
       // cells), so within a round every lane writes a different node for each
       // stencil offset; __syncwarp orders the offsets.
-      if (chunk || kMode == kG2PFinal) continue;  // nothing for the tile
+      if (direct || kMode == kG2PFinal) continue;  // nothing for the tile
       const bool tile_lane = valid && fast_s;
       const int key = tile_lane ? tb_s : -1 - lane;
       const unsigned same = __match_any_sync(0xffffffffu, key);
@@ -634,7 +637,7 @@ g2p2g_kernel(
         }
       }
     }
-    if (chunk || kMode == kG2PFinal) continue;  // its P2G went straight to G (and the flags)
+    if (direct || kMode == kG2PFinal) continue;  // its P2G went straight to G (and the flags)
     __syncthreads();
 
     for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {

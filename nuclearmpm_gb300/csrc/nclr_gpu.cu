@@ -123,6 +123,7 @@ thread_local std::string g_create_error;
 // than the block's particles gathering and scattering through L2 directly.
 constexpr int kSparseMax3 = 64;
 constexpr int kSparseMax2 = 32;
+constexpr int kBatchThin = 32;  // batches: blocks below this many particles skip the tiles
 // Default small-scene limits: up to them one persistent launch per advance() call beats two
 // launches per step.  Measured on GB300: up to 64k particles in 2D and 32k in 3D, and only
 // while the grid has at most about 8 nodes per particle -- the small kernel updates every
@@ -559,10 +560,13 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   s->device = s->opt.device;
   s->ref = s->opt.physics != NCLR_PHYSICS_CORRECTED;
   s->has_mat = any_mat;
-  // thin blocks are a single-simulation path (a batch's fused kernel reads its scene per block)
-  s->sparse_max = nscenes > 1 ? 0
-                  : s->opt.sparse_block_max < 0 ? (dim == 3 ? kSparseMax3 : kSparseMax2)
-                                                : s->opt.sparse_block_max;
+  // thin blocks: a single simulation steps their particles in chunks of the sparse list; a
+  // batch, whose fused kernel reads its scene per block, steps each as a tile-free item
+  const int thin = s->opt.sparse_block_max >= 0 ? s->opt.sparse_block_max
+                   : nscenes > 1                ? kBatchThin
+                   : dim == 3                   ? kSparseMax3
+                                                : kSparseMax2;
+  s->sparse_max = nscenes > 1 ? 0 : thin;
   s->deferred_err.assign((size_t)nscenes, 0);
   s->scene_err.assign((size_t)nscenes, 0);
 
@@ -573,6 +577,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
     Scene sc{};
     sc.P = scene_params(dim, d.n, d.model, d.res, d.dt, d.E, d.nu, d.gravity);
     sc.P.stress = s->opt.stress_model;
+    sc.P.thin_max = nscenes > 1 ? thin : 0;
     sc.slot_off = (int)slot;
     sc.node_off = node;
     sc.block_off = (int)std::min<int64_t>(block, 0x7fffffff);
