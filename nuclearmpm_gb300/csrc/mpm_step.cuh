@@ -9,12 +9,25 @@
 // The P2G of the first step after an upload is g2p2g in its P2G-only mode.
 #pragma once
 
+#include <algorithm>
+
 #include "mpm_device.cuh"
 #include "mpm_launch.h"
 
 namespace mpm {
 
 constexpr int kG2P2GThreads = 256;
+
+// Threads that work on one item of the fused kernel (a grid block, or a chunk of thin-block
+// particles): the whole CTA, except in 2D batches.  There the tiles are small (2.3 KB), and a
+// block of a few hundred particles runs in passes of 128, with each half of the CTA on its
+// own item, tiles and barrier.  That replaces a 256-thread pass and a mostly idle second one
+// (measured on 256 mixed scenes: 1.50-1.58e10 particle-steps/s against 1.37e10; one warp per
+// item measured 3x slower, and the half-CTA items slow a single 2D simulation's tile path).
+template <int D, bool kBatch>
+__host__ __device__ constexpr int g2p2g_group() {
+  return (D == 2 && kBatch) ? kG2P2GThreads / 2 : kG2P2GThreads;
+}
 
 // 0 <= v <= hi, as one unsigned compare that no large v (a saturated float-to-int conversion
 // of a huge position) can overflow into passing.
@@ -400,31 +413,45 @@ g2p2g_kernel(
   using Tl = Tiling<D>;
   constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, CPB = Tl::CPB, GS = Tl::SIZE;
   constexpr int S = (D == 3) ? 27 : 9;
-  constexpr int kWarps = kG2P2GThreads / 32;
+  constexpr int kGroup = g2p2g_group<D, kBatch>();  // threads per item
+  constexpr int kGroups = kG2P2GThreads / kGroup;  // items in flight per CTA
+  constexpr int kWarps = kGroup / 32;              // warps per item, each with its G tile
+  constexpr int kTiles = (kMode == kG2PFinal) ? 1 : 1 + kWarps;  // tiles per group
   extern __shared__ float4 smem[];
-  float4 *vt = smem;            // V tile
-  float4 *gt = smem + Tl::SIZE;  // kWarps private G tiles: [warp][SIZE]
-  __shared__ int s_item;
-  __shared__ Params sP;  // the current block's scene (shared: keeps registers for the math)
-  __shared__ int64_t s_node_off;
-  __shared__ int s_block_off;
+  const int grp = threadIdx.x / kGroup, gtid = threadIdx.x % kGroup;
+  float4 *vt = smem + grp * kTiles * GS;  // the group's V tile
+  float4 *gt = vt + GS;                   // its kWarps private G tiles: [warp][SIZE]
+  __shared__ int s_items[kGroups];
+  __shared__ Params sPs[kGroups];  // each item's scene (shared: keeps registers for the math)
+  __shared__ int64_t s_node_offs[kGroups];
+  __shared__ int s_block_offs[kGroups];
+  int &s_item = s_items[grp];
+  Params &sP = sPs[grp];
+  int64_t &s_node_off = s_node_offs[grp];
+  int &s_block_off = s_block_offs[grp];
+  // the barrier of one item's threads (a named barrier per group when the CTA has several)
+  auto group_sync = [grp] {
+    if constexpr (kGroups == 1)
+      __syncthreads();
+    else
+      asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "n"(kGroup) : "memory");
+  };
   const int st = s.stride;
   // work items: the dense blocks of the list, then chunks of kG2P2GThreads particles of the
   // sparse blocks (single simulations only; see compact_blocks_kernel)
   const int nact = nactive[0];
   const int nsp = kBatch ? 0 : nactive[1];
-  const int nitems = nact + (nsp + kG2P2GThreads - 1) / kG2P2GThreads;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float4 *mytile = gt + warp * GS;
+  const int nitems = nact + (nsp + kGroup - 1) / kGroup;
+  const int lane = threadIdx.x & 31;
+  float4 *mytile = gt + (gtid >> 5) * GS;
   // The G tiles start clear and every item's flush clears what it read, so they are clear
   // again at the start of the next item (padding entries are never written).
   if constexpr (kMode != kG2PFinal)
-    for (int t = threadIdx.x; t < kWarps * GS; t += kG2P2GThreads)
-      gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int t = gtid; t < kWarps * GS; t += kGroup) gt[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
   for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) {  // the next block of the list, and its scene
+    group_sync();
+    if (gtid == 0) {  // the next block of the list, and its scene
       const int it = atomicAdd(work, 1);
       s_item = it;
       if (kBatch && it < nact) {
@@ -434,7 +461,7 @@ g2p2g_kernel(
         s_block_off = scenes[sid0].block_off;
       }
     }
-    __syncthreads();
+    group_sync();
     const int item = s_item;
     if (item >= nitems) return;
     // a sparse chunk: particles of blocks too thin for the tile to pay, one per thread,
@@ -461,14 +488,14 @@ g2p2g_kernel(
     const int b = gb - block_off;
     int *err_now = err + 2 * sid, *err_next = err + 2 * sid + next_slot;
     // The block's particles, stored cell by cell in rounds (see sort_move_kernel), or a chunk's.
-    const int c0 = (item - nact) * kG2P2GThreads;
+    const int c0 = (item - nact) * kGroup;
     const int p0 = chunk ? 0 : bstart[gb];
-    const int np = chunk ? min(kG2P2GThreads, nsp - c0) : bstart[gb + 1] - p0;
+    const int np = chunk ? min(kGroup, nsp - c0) : bstart[gb + 1] - p0;
     // A batch's thin block (fewer than P.thin_max particles) skips the tiles like a chunk:
     // gathered from V and scattered into G directly (CTA-uniform).
     const bool direct = chunk || (kBatch && np < P.thin_max);
     if (kMode != kP2GOnly && !direct) {
-      for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
+      for (int t = gtid; t < NODES; t += kGroup) {
         int g[D], l[3] = {0, 0, 0};
         bool in = true;
         int r = t;
@@ -483,12 +510,12 @@ g2p2g_kernel(
             in ? __ldg(V + flat_index<D>(g, N)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
     }
-    __syncthreads();
+    group_sync();
 
     // One particle per thread in slot order.  Every lane of a warp runs the same number of
     // iterations (the warp-wide steps below need them all).
-    for (int j0 = 0; j0 < np; j0 += kG2P2GThreads) {
-      const int j = j0 + threadIdx.x;
+    for (int j0 = 0; j0 < np; j0 += kGroup) {
+      const int j = j0 + gtid;
       const bool valid = j < np;
       const int p = chunk ? (valid ? sparse[c0 + j] : 0) : p0 + j;
       // what the particle contributes to the next P2G
@@ -638,9 +665,9 @@ g2p2g_kernel(
       }
     }
     if (direct || kMode == kG2PFinal) continue;  // its P2G went straight to G (and the flags)
-    __syncthreads();
+    group_sync();
 
-    for (int t = threadIdx.x; t < NODES; t += kG2P2GThreads) {
+    for (int t = gtid; t < NODES; t += kGroup) {
       int g[D], l[3] = {0, 0, 0};
       bool in = true;
       int r = t;
@@ -670,14 +697,14 @@ g2p2g_kernel(
       if (in) red_add_v4(G + flat_index<D>(g, N), a[0], a[1], a[2], a[3]);
     }
     // the tile spans node blocks b-1 .. b+1 on every axis
-    if (threadIdx.x < ((D == 3) ? 27 : 9)) {
+    if (gtid < ((D == 3) ? 27 : 9)) {
       int nbc[3] = {0, 0, 0}, r = b;
 #pragma unroll
       for (int d = D - 1; d >= 0; --d) {
         nbc[d] = r % P.nb;
         r /= P.nb;
       }
-      const int t = threadIdx.x;
+      const int t = gtid;
       const int di = (D == 3) ? t / 9 - 1 : t / 3 - 1, dj = (D == 3) ? (t / 3) % 3 - 1 : t % 3 - 1;
       const int dk = (D == 3) ? t % 3 - 1 : 0;
       const int bi = nbc[0] + di, bj = nbc[1] + dj, bk = nbc[D - 1] + dk;
@@ -687,11 +714,12 @@ g2p2g_kernel(
   }
 }
 
-// Dynamic shared memory of g2p2g: the V tile plus one G tile per warp (the V tile alone for
-// kG2PFinal, which has no P2G).
-template <int D>
+// Dynamic shared memory of g2p2g: per item group, the V tile plus one G tile per warp (the V
+// tile alone for kG2PFinal, which has no P2G and runs single simulations only).
+template <int D, bool kBatch>
 constexpr size_t g2p2g_smem_bytes() {
-  return sizeof(float4) * Tiling<D>::SIZE * (1 + kG2P2GThreads / 32);
+  return sizeof(float4) * Tiling<D>::SIZE * (kG2P2GThreads / g2p2g_group<D, kBatch>()) *
+         (1 + g2p2g_group<D, kBatch>() / 32);
 }
 template <int D>
 constexpr size_t g2p_final_smem_bytes() {
@@ -1213,7 +1241,7 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
 #define MPM_G2P2G(R, MODE, B)                                                            \
   g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads,                                      \
                                 (MODE) == kG2PFinal ? g2p_final_smem_bytes<D>()           \
-                                                    : g2p2g_smem_bytes<D>(),              \
+                                                    : g2p2g_smem_bytes<D, B>(),           \
                                 st>>>(s, P0, scenes, block_scene, V, G, flags, blocks,   \
                                       nactive, bstart, sparse, work, err, next_slot, rec)
 #define MPM_G2P2G_B(R, MODE)          \
@@ -1283,7 +1311,7 @@ int small_ctas_per_sm(bool ref) {
 template <int D>
 int g2p2g_ctas_per_sm() {
   // the tiles exceed the default 48 KB of dynamic shared memory in 3D
-  const int bytes = (int)g2p2g_smem_bytes<D>();
+  const int bytes = (int)std::max(g2p2g_smem_bytes<D, false>(), g2p2g_smem_bytes<D, true>());
   {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaFuncSetAttribute(g2p2g_kernel<D, true, kStep, false>, a, bytes);
@@ -1301,7 +1329,7 @@ int g2p2g_ctas_per_sm() {
   }
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, g2p2g_kernel<D, true, kStep, true>, kG2P2GThreads,
-                                                g2p2g_smem_bytes<D>());
+                                                g2p2g_smem_bytes<D, true>());
   return n > 0 ? n : 1;
 }
 
