@@ -260,11 +260,11 @@ __device__ void mark_stencil(uint8_t *flags, const int base[D], const Params &P)
   const int k0 = base[D - 1] / BS, k1 = (base[D - 1] + 2) / BS;
   for (int i = i0; i <= i1; ++i)
     for (int j = j0; j <= j1; ++j) {
-      if (D == 2) {
+      if constexpr (D == 2) {
         flags[i * P.nb + j] |= kPending;
-        continue;
+      } else {
+        for (int k = k0; k <= k1; ++k) flags[(i * P.nb + j) * P.nb + k] |= kPending;
       }
-      for (int k = k0; k <= k1; ++k) flags[(i * P.nb + j) * P.nb + k] |= kPending;
     }
 }
 
@@ -411,7 +411,7 @@ g2p2g_kernel(
     const int *__restrict__ bstart, const int *__restrict__ sparse, int *__restrict__ work,
     int *__restrict__ err, int next_slot, Record rec) {
   using Tl = Tiling<D>;
-  constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, CPB = Tl::CPB, GS = Tl::SIZE;
+  constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, GS = Tl::SIZE;
   constexpr int S = (D == 3) ? 27 : 9;
   constexpr int kGroup = g2p2g_group<D, kBatch>();  // threads per item
   constexpr int kGroups = kG2P2GThreads / kGroup;  // items in flight per CTA
