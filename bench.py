@@ -49,6 +49,10 @@ WORKLOAD = {"workload": "3D jelly (MaterialModel::kJelly), 4 cubes of 64^3 latti
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel
 # from one ncu capture of this workload (profiles/g2p2g_jelly3d_1M.md).
 NCU_TRAFFIC = {"g2p2g": 68.470784e6 + 5.270016e6}
+# Warp-instructions of one launch of that kernel (smsp__inst_executed.sum, same capture): the
+# kernel is bound by issue and latency rather than HBM, so the line also reports how close one
+# launch comes to its issue floor (4 schedulers per SM, one warp-instruction per cycle each).
+NCU_INSTRUCTIONS = {"g2p2g": 69.943003e6}
 
 
 def peaks():
@@ -567,6 +571,14 @@ def run_ours(args):
                                 "avg_ms": prof[k][0] / max(prof[k][1], 1),
                                 "share": prof[k][0] / max(ms, 1e-9)} for k in prof},
                 "active_nodes": active}
+    inst = NCU_INSTRUCTIONS.get(dom)
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    if inst and mhz:
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        floor_ms = inst / (sms * 4 * mhz * 1e6) * 1e3
+        roofline["issue"] = {"warp_instructions": inst, "sms": sms, "sm_mhz": mhz,
+                             "floor_ms": floor_ms, "frac": floor_ms / per_launch[dom],
+                             "source": "ncu smsp__inst_executed.sum of one launch"}
 
     # ---- end to end through the C ABI with host buffers ----------------------------------
     pin = lambda shape: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
