@@ -1,6 +1,6 @@
 """The measured workloads at their full sizes, on the GPU.
-- The 1M-particle 3D jelly scene and the 4.19M-particle liquid + snow scene: one step against
-  the FP32 oracle, run on all host cores.
+- The 1M-particle 3D jelly scene, the same in snow, and the 4.19M-particle liquid + snow
+  scene: one step against the FP32 oracle, run on all host cores.
 - The same two scenes conserve their total mass, and with gravity off their total momentum,
   through a step.
 - The 256-scene batch: one step of the batch equals every scene stepped alone.
@@ -33,10 +33,12 @@ def gpu_step(state, model, res, steps=1, material=None, **kw):
     return out, grid
 
 
-@pytest.mark.parametrize("scene", ["jelly_1M", "mixed_4M"])
+@pytest.mark.parametrize("scene", ["jelly_1M", "snow_1M", "mixed_4M"])
 def test_full_size_step_matches_oracle(oracle, scene):
     if scene == "jelly_1M":
         s, mat, model, res = scenes.jelly_cubes_3d(seed=0, res=128), None, scenes.JELLY, 128
+    elif scene == "snow_1M":  # the same geometry in snow
+        s, mat, model, res = scenes.jelly_cubes_3d(seed=0, res=128), None, scenes.SNOW, 128
     else:
         s, mat = scenes.liquid_snow_boxes_3d(seed=0, res=256)
         model, res = scenes.SNOW, 256
