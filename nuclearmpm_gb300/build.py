@@ -21,8 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libnclr_gpu.so")
 SOLVER = os.path.join(OUT_DIR, "nclr_solver")  # the headless solver (cli/nclr_solver.cpp)
-SOURCES = ["nclr_gpu.cu", "step2d.cu", "step3d.cu", "scan.cu", "noalloc.cu", "adjoint.cu",
-           "scene_build.cu", "render.cu"]
+SOURCES = ["nclr_gpu.cu", "step2d.cu", "step3d.cu", "step3d_mat.cu", "scan.cu", "noalloc.cu",
+           "adjoint.cu", "scene_build.cu", "render.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -10,6 +10,7 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "mpm_device.cuh"
 #include "mpm_launch.h"
@@ -399,10 +400,11 @@ enum : int { kStep = kModeStep, kFinalStep = kModeFinalStep, kP2GOnly = kModeP2G
 
 // kBatch: several scenes (per-block parameters from the scene table, staged in shared memory)
 // or one (its parameters are a kernel argument: constant-bank operands, no registers).
-template <int D, bool kRef, int kMode, bool kBatch>
+template <int D, bool kRef, int kMode, bool kBatch, int kMat = -1>
 // 3D: two CTAs per SM (the tiles take 106 KB of shared memory each), three for the G2P-only
 // step (one 12 KB tile); 2D: four, which keeps the 2D kernel within 64 registers without
-// spills.
+// spills.  kMat >= 0 fixes every particle's material at compile time (a single simulation
+// without per-particle materials): the other materials' branches drop out of the code.
 __global__ void __launch_bounds__(kG2P2GThreads, D == 3 ? (kMode == kG2PFinal ? 3 : 2) : 4)
 g2p2g_kernel(
     PState s, Params P0, const Scene *__restrict__ scenes, const uint16_t *__restrict__ block_scene,
@@ -527,7 +529,7 @@ g2p2g_kernel(
         float x[D];
         Mat<D> F, C, R;
         float v[D], Jp;
-        const int material = s.mat ? (int)s.mat[p] : P.model;
+        const int material = kMat >= 0 ? kMat : (s.mat ? (int)s.mat[p] : P.model);
         int base[D], lb[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < D; ++d) x[d] = s.x[(size_t)d * st + p];
@@ -1232,12 +1234,33 @@ void launch_discard_pending(float4 *G, uint8_t *flags, const Scene *scenes,
                                                                total_blocks);
 }
 
+// The fused step (kStep or kFinalStep) of a single simulation whose particles all have
+// `material`, fixed at compile time.  Defined and instantiated for 3D in step3d_mat.cu, a
+// translation unit of its own that compiles beside step3d.cu.
+template <int D>
+void launch_g2p2g_fixed(const PState &s, const Params &P0, const float4 *V, float4 *G,
+                        uint8_t *flags, const int *blocks, const int *nactive,
+                        const int *bstart, const int *sparse, int *work, int *err, int next_slot,
+                        bool ref, int mode, int material, int ctas, cudaStream_t st,
+                        const Record &rec);
+// Raises the dynamic shared-memory limit of every launch_g2p2g_fixed<D> kernel to `bytes`.
+template <int D>
+void g2p2g_fixed_set_smem(int bytes);
+
 template <int D>
 void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                   const uint16_t *block_scene, const float4 *V, float4 *G, uint8_t *flags,
                   const int *blocks, const int *nactive, const int *bstart, const int *sparse,
                   int *work, int *err, int next_slot, bool ref, int mode, int ctas,
                   cudaStream_t st, const Record &rec) {
+  if constexpr (D == 3) {  // one material for every particle: the specialised kernel
+    if (!block_scene && !s.mat && (mode == kStep || mode == kFinalStep) &&
+        (P0.model == kSnow || P0.model == kJelly || P0.model == kLiquid)) {
+      launch_g2p2g_fixed<D>(s, P0, V, G, flags, blocks, nactive, bstart, sparse, work, err,
+                            next_slot, ref, mode, P0.model, ctas, st, rec);
+      return;
+    }
+  }
 #define MPM_G2P2G(R, MODE, B)                                                            \
   g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads,                                      \
                                 (MODE) == kG2PFinal ? g2p_final_smem_bytes<D>()           \
@@ -1326,6 +1349,7 @@ int g2p2g_ctas_per_sm() {
     cudaFuncSetAttribute(g2p2g_kernel<D, false, kStep, true>, a, bytes);
     cudaFuncSetAttribute(g2p2g_kernel<D, false, kFinalStep, true>, a, bytes);
     cudaFuncSetAttribute(g2p2g_kernel<D, false, kP2GOnly, true>, a, bytes);
+    if constexpr (D == 3) g2p2g_fixed_set_smem<D>(bytes);
   }
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, g2p2g_kernel<D, true, kStep, true>, kG2P2GThreads,
