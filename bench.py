@@ -14,7 +14,13 @@ A step is one advance() over all particles.  Lines printed (rank 0, one JSON lin
   roofline  the dominant kernel's algorithmic bytes per launch / its average launch time,
             measured with CUDA events on the simulation's stream inside the timed region;
   cpu_baseline  the CPU oracle (a restatement of the reference's step, built -Ofast like the
-            reference) on one host core, on a bounded sample of the same workload.
+            reference) on one host core, on a bounded sample of the same workload;
+  error_vs_fp64  one GPU step at the timed size from the state the timed region ended in,
+            against the FP64 oracle on all host cores (normwise per field and for the grid).
+Further forms (objects on the same line; `--only FORM` runs one alone): batched (256 2D
+scenes), adjoint (fwd + backward rollout), mixed (4.19M liquid + snow), snow, corrected (the
+headline geometry in jelly and snow under the corrected physics), readme, models.  Each carries
+its own roofline and error_vs_fp64.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -74,6 +80,78 @@ def algorithmic_bytes(dim: int, n: int, active: int) -> dict:
     d2 = dim * dim
     g2p2g = n * ((dim + d2 + 3) + (dim + d2 + 1)) * 4 + active * 32
     return {"g2p2g": g2p2g}
+
+
+FIELDS = ("x", "v", "F", "C", "Jp")
+# Floors of the normwise error, in each field's units (the measure of the parity tests).
+FLOORS = {"x": 1.0, "v": 1e-2, "F": 1.0, "C": 1.0, "Jp": 1.0, "grid_v": 1e-2, "grid_m": 1e-3}
+
+
+def field_err(a, b, name: str) -> float:
+    """max|a - b| / max(max|b|, floor): the normwise relative error of one field."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if a.size == 0:
+        return 0.0
+    return float(np.abs(a - b).max() / max(float(np.abs(b).max()), FLOORS.get(name, 0.0), 1e-30))
+
+
+def roofline_of(kernel: str, alg_bytes: float, avg_ms: float, traffic=None, **extra) -> dict:
+    """HBM roofline of one kernel: algorithmic bytes per launch / its CUDA-event launch time."""
+    hbm, kind = peaks()
+    achieved = alg_bytes / (avg_ms / 1e3) / 1e9
+    out = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+           "frac": achieved / hbm, "peak_source": kind, "traffic": traffic,
+           "algorithmic_bytes": alg_bytes, "avg_launch_ms": avg_ms}
+    out.update(extra)
+    return out
+
+
+def state_of(sim, scene: dict) -> dict:
+    """The particles of a simulation as an oracle state (caller order)."""
+    p = sim.particles()
+    return {"x": p.x, "v": p.v, "F": p.F, "C": p.C, "Jp": p.Jp, "mass": scene["mass"],
+            "volume": scene["volume"]}
+
+
+def error_vs_fp64(state: dict, *, dim: int, model: int, res: int, device: int, what: str,
+                  material=None, physics: int = 0, dt: float = 1e-4, E: float = 1e4,
+                  nu: float = 0.2, gravity: float = -100.0, stress: int = 0, E_p=None,
+                  nu_p=None) -> dict:
+    """The error of one GPU step at the timed size against the FP64 oracle (the reference's step
+    restated in double precision, on all host cores) from the same state: a fresh simulation
+    created from `state` advances one step; every field and the grid are compared normwise."""
+    from oracle import pyoracle as po
+    from nuclearmpm_gb300 import MPMSimulation
+    sim = MPMSimulation(dict(state), model, res=res, dt=dt, E=E, nu=nu, gravity=gravity,
+                        material=material, physics=physics, stress_model=stress, device=device)
+    if E_p is not None:
+        sim.set_moduli(E_p, nu_p)
+    sim.advance(1)
+    p = sim.particles()
+    g = sim.grid()
+    sim.close()
+    threads = os.cpu_count() or 1
+    kw = dict(dim=dim, model=model, res=res, dt=dt, E=E, nu=nu, gravity=gravity, steps=1,
+              physics=physics, material=material, threads=threads, stress=stress,
+              E_particles=E_p, nu_particles=nu_p)
+    o, og, st, _ = po.advance(state, fp64=True, **kw)
+    o32, og32, _, _ = po.advance(state, **kw)  # the FP32 restatement: its own distance
+    gpu = {f: getattr(p, f) for f in FIELDS}
+    gpu.update(grid_v=g.velocity, grid_m=g.mass)
+    o.update(grid_v=og[0], grid_m=og[1])
+    o32.update(grid_v=og32[0], grid_m=og32[1])
+    fields = {f: field_err(gpu[f], o[f], f) for f in gpu}
+    own = {f: field_err(o32[f], o[f], f) for f in gpu}
+    # particles whose F row is further than 1e-5 from FP64 (each F entry is of order 1)
+    rows = lambda a: np.abs(np.asarray(a, np.float64) - o["F"]).reshape(len(o["F"]), -1).max(1)  # noqa: E731
+    return {"max": max(fields.values()), "fields": fields, "state": what,
+            "fp32_oracle_vs_fp64": own,
+            "F_rows_over_1e-5": {"gpu": int((rows(p.F) > 1e-5).sum()),
+                                 "fp32_oracle": int((rows(o32["F"]) > 1e-5).sum()),
+                                 "particles": int(len(o["F"]))},
+            "measure": "max|gpu - fp64| / max(max|fp64|, floor) per field",
+            "oracle": f"FP64 oracle, one step, {threads} host threads", "oracle_status": st}
 
 
 class ClockSampler:
@@ -162,13 +240,15 @@ def host_cpu() -> dict:
             "arch": platform.machine()}
 
 
-def tune_plain(state: dict, model: int, res: int, device: int) -> dict:
+def tune_plain(state: dict, model: int, res: int, device: int, physics: int = 0,
+               material=None) -> dict:
     """The project's autotuner (nuclearmpm_gb300.autotune) on this workload: re-sort interval
     and thin-block threshold, from short timed runs of the simulation itself."""
     from nuclearmpm_gb300 import MPMSimulation, autotune
     # 64-step runs (about 12 ms each at 1M particles): the candidates differ by a few percent,
     # which shorter runs timed on the host do not resolve
-    return autotune.tune(lambda **o: MPMSimulation(dict(state), model, res=res, device=device, **o),
+    return autotune.tune(lambda **o: MPMSimulation(dict(state), model, res=res, device=device,
+                                                   physics=physics, material=material, **o),
                          key=None, candidates=autotune.PLAIN_CANDIDATES, steps=64, repeats=2,
                          cache_path=None)
 
@@ -178,35 +258,33 @@ def make_scene():
     return scenes.jelly_cubes_3d(seed=0, res=128)
 
 
-def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float, threads: int = 1):
+def cpu_reference_run(scene: dict, steps: int, warmup: int, budget_s: float, threads: int = 1,
+                      model: int = 1, res: int = 128, material=None):
     """The CPU oracle (-Ofast build; one thread, or `threads` for the multi-threaded port of
     oracle/nclr_oracle_mt.h) on the workload: `warmup` untimed steps, then `steps` timed
     steps, on the full scene if that fits `budget_s`, else on the first particles of the scene
     (same per-particle work) so that it does."""
     from oracle import pyoracle as po
-    from nuclearmpm_gb300 import scenes
     n = len(scene["x"])
+    kw = dict(dim=3, model=model, res=res, fast=True, want_grid=False, threads=threads)
     t0 = time.perf_counter()
-    state, _, st, _ = po.advance(scene, dim=3, model=scenes.JELLY, res=128, steps=1, fast=True,
-                                 want_grid=False, threads=threads)
+    state, _, st, _ = po.advance(scene, steps=1, material=material, **kw)
     one = time.perf_counter() - t0
     total = max(1, steps + max(warmup - 1, 0))
     frac = min(1.0, budget_s / max(one * total, 1e-9))
     m = n if frac >= 1.0 else max(4096, int(n * frac) // 4096 * 4096)
     sample = {k: (np.asarray(v)[:m] if k in ("x", "v", "F", "C", "Jp", "mass", "volume") else v)
               for k, v in state.items()}
+    mat = None if material is None else np.asarray(material)[:m]
     if warmup > 1:
-        sample, _, st, _ = po.advance(sample, dim=3, model=scenes.JELLY, res=128,
-                                      steps=warmup - 1, fast=True, want_grid=False,
-                                      threads=threads)
+        sample, _, st, _ = po.advance(sample, steps=warmup - 1, material=mat, **kw)
     t0 = time.perf_counter()
-    _, _, st, _ = po.advance(sample, dim=3, model=scenes.JELLY, res=128, steps=steps, fast=True,
-                             want_grid=False, threads=threads)
+    _, _, st, _ = po.advance(sample, steps=steps, material=mat, **kw)
     dt = time.perf_counter() - t0
     if st != 0:
         raise RuntimeError("CPU oracle reported an out-of-range stencil")
-    desc = (f"{m:,} of {n:,} particles (first cube) x {steps} steps, 128^3 grid"
-            if m < n else f"all {n:,} particles x {steps} steps, 128^3 grid")
+    desc = (f"{m:,} of {n:,} particles (the scene's first) x {steps} steps, {res}^3 grid"
+            if m < n else f"all {n:,} particles x {steps} steps, {res}^3 grid")
     return m * steps / dt, desc
 
 
@@ -243,6 +321,21 @@ def run_batched(device: int, steps: int = 100, sequential: bool = True, repeats:
     t_batch = best_of(batch)
     launches = batch.stats()[0]
     batch.close()
+    # the fused kernel's roofline: the same batch with per-kernel CUDA events (direct launches)
+    pb = BatchSimulation(scs, device=device, profile=True, **tuned)
+    pb.advance(steps)
+    pb.profile_reset()
+    pb.advance(steps)
+    prof = pb.profile()
+    active = pb.active_nodes()
+    pb.close()
+    g_ms = prof["g2p2g"][0] / max(prof["g2p2g"][1], 1)
+    alg = algorithmic_bytes(2, total, active)["g2p2g"]
+    roof = roofline_of("g2p2g", alg, g_ms, active_nodes=active,
+                       kernels={k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1)}
+                                for k, v in prof.items() if v[1] > 0},
+                       timing="a separate run of the same batch with per-kernel CUDA events")
+    err = batched_error_vs_fp64(scs, device)
     t_seq = 0.0
     for sc in (scs if sequential else []):
         sim = MPMSimulation({k: sc[k] for k in ("x", "v", "F", "C", "Jp", "mass", "volume")},
@@ -252,13 +345,77 @@ def run_batched(device: int, steps: int = 100, sequential: bool = True, repeats:
         sim.close()
     return {"value": total * steps / t_batch, "unit": UNIT, "scenes": len(scs),
             "particles": total, "steps": steps, "ms_per_step": t_batch / steps * 1e3,
-            "gpu_launches": launches, "tuned": tuned,
+            "gpu_launches": launches, "tuned": tuned, "roofline": roof, "error_vs_fp64": err,
             "sequential_value": total * steps / t_seq if sequential else None,
             "speedup_vs_sequential": t_seq / t_batch if sequential else None,
             "config": "256 2D scenes, n log-uniform [1e3, 65536], res {64,128,256}, "
                       "materials uniform, E log-uniform [1e3,1e5], nu uniform [0.1,0.4], "
                       "dt 1e-4, one CUDA graph per 100 steps; sequential = the same scenes as "
                       "plain simulations one after another; best of 3 calls on both sides"}
+
+
+def batched_error_vs_fp64(scs: list, device: int) -> dict:
+    """One step of all 256 scenes as one batch against the FP64 oracle of each scene: the
+    largest normwise error over the scenes, per field and for the grid."""
+    from oracle import pyoracle as po
+    from nuclearmpm_gb300 import BatchSimulation
+    b = BatchSimulation(scs, device=device)
+    b.advance(1)
+    threads = os.cpu_count() or 1
+    worst = {}
+    for i, sc in enumerate(scs):
+        got = b.particles(i)
+        g = b.grid(i)
+        state = {k: sc[k] for k in ("x", "v", "F", "C", "Jp", "mass", "volume")}
+        o, og, st, _ = po.advance(state, dim=2, model=sc["model"], res=sc["res"], dt=sc["dt"],
+                                  E=sc["E"], nu=sc["nu"], gravity=sc["gravity"], steps=1,
+                                  fp64=True, threads=threads)
+        errs = {f: field_err(got[f], o[f], f) for f in FIELDS}
+        errs["grid_v"] = field_err(g.velocity, og[0], "grid_v")
+        errs["grid_m"] = field_err(g.mass, og[1], "grid_m")
+        for f, e in errs.items():
+            worst[f] = max(worst.get(f, 0.0), e)
+    b.close()
+    return {"max": max(worst.values()), "fields": worst,
+            "state": f"the {len(scs)} scenes as built, one batched step",
+            "measure": "max over scenes of max|gpu - fp64| / max(max|fp64|, floor) per field",
+            "oracle": f"FP64 oracle per scene, one step, {threads} host threads"}
+
+
+def adjoint_error_vs_fp64(device: int, sc: dict, v0: np.ndarray, target: np.ndarray,
+                          steps: int = 1) -> dict:
+    """The gradients of the timed rollout's loss through `steps` steps at the timed size
+    (131,072 particles) against the FP64 adjoint of the reference step on the host: the
+    initial-velocity gradients normwise, E and nu relative."""
+    import torch
+
+    from oracle import pyoracle as po
+    from nuclearmpm_gb300.autograd import Rollout
+    n = len(sc["x"])
+    dev = torch.device("cuda", device)
+    roll = Rollout(sc["x"], res=64, steps=steps, checkpoint_every=1, device=device)
+    x0 = torch.tensor(sc["x"], device=dev)
+    v = torch.tensor(v0, device=dev, requires_grad=True)
+    E = torch.tensor(1e4, dtype=torch.float64, requires_grad=True)
+    nu = torch.tensor(0.2, dtype=torch.float64, requires_grad=True)
+    tgt = torch.tensor(target, device=dev)
+    xT, _ = roll(x0, v, E, nu)
+    loss = ((xT.mean(0) - tgt) ** 2).sum()
+    loss.backward()
+    roll.close()
+    # the loss's adjoint of the final positions, evaluated at the GPU's final state
+    seed_x = np.broadcast_to((2.0 * (xT.mean(0) - tgt) / n).detach().cpu().numpy().astype(np.float64),
+                             (n, 3)).copy()
+    state = dict(sc, v=v0)
+    _, g = po.adjoint(state, dim=3, res=64, steps=steps, seed={"x": seed_x})
+    gv = v.grad.detach().cpu().numpy().astype(np.float64)
+    e_v = float(np.abs(gv - g["v"]).max() / max(np.abs(g["v"]).max(), 1e-300))
+    e_E = abs(float(E.grad) - g["E"]) / max(abs(g["E"]), 1e-300)
+    e_nu = abs(float(nu.grad) - g["nu"]) / max(abs(g["nu"]), 1e-300)
+    return {"max": max(e_v, e_E, e_nu), "fields": {"grad_v0": e_v, "grad_E": e_E, "grad_nu": e_nu},
+            "state": f"the timed rollout's scene, initial velocities and loss, {steps} step",
+            "measure": "grad_v0: max|gpu - fp64| / max|fp64|; grad_E, grad_nu: relative",
+            "oracle": "FP64 adjoint of the reference step (oracle/nclr_adjoint.h), one thread"}
 
 
 def run_adjoint(device: int, steps: int = 2000, every: int = 50) -> dict:
@@ -292,7 +449,40 @@ def run_adjoint(device: int, steps: int = 2000, every: int = 50) -> dict:
         loss.backward()
     fwd_ms, bwd_ms = roll.timing()
     roll.close()
+    # per-kernel CUDA events: a second rollout of the same scene with profiling (direct launches)
+    proll = Rollout(sc["x"], res=64, steps=steps, checkpoint_every=every, device=device,
+                    profile=True)
+    v0.grad = None
+    xT, _ = proll(x0, v0, E, nu)
+    ((xT.mean(0) - target) ** 2).sum().backward()
+    prof = proll.profile()
+    proll.close()
+    nodes = 65 ** 3
+    per_particle = {"adj_g2p": 228, "adj_p2g": 248}  # bytes per particle: see bytes_note below
+    roofs = {}
+    for k in ("adj_g2p", "adj_grid", "adj_p2g", "g2p2g"):
+        if prof[k][1] == 0:
+            continue
+        avg = prof[k][0] / prof[k][1]
+        if k == "adj_grid":
+            alg = 64 * nodes
+        elif k == "g2p2g":
+            alg = algorithmic_bytes(3, n, 0)["g2p2g"]
+        else:
+            alg = per_particle[k] * n
+        roofs[k] = roofline_of(k, alg, avg, launches=prof[k][1])
+    dom = max(("adj_g2p", "adj_grid", "adj_p2g"), key=lambda k: prof[k][0])
+    err = adjoint_error_vs_fp64(device, sc, v0.detach().cpu().numpy(), target.cpu().numpy())
     return {"value": n * steps / ((fwd_ms + bwd_ms) / 1e3), "unit": UNIT,
+            "roofline": dict(roofs[dom], kernels=roofs,
+                             bytes_note="algorithmic bytes per launch: adj_g2p reads x, F, C', "
+                             "gF', gC', gx', gv' and writes gx, gF (228 B per particle); adj_p2g "
+                             "reads x, v, F, C, m, vol, gx, gF and writes gx, gv, gF, gC (248 B); "
+                             "adj_grid reads V, VB and writes GB and the cleared VB over all 65^3 "
+                             "nodes (64 B per node); the particle kernels' node gathers and "
+                             "reductions (about 23k touched nodes) are not counted; g2p2g counts "
+                             "the plain step's 112 B per particle (the recorded rows are extra)"),
+            "error_vs_fp64": err,
             "metric": "fwd+adjoint particle-steps/s", "particles": n, "steps": steps,
             "checkpoint_every": every, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
             "backward_over_forward": bwd_ms / fwd_ms,
@@ -302,45 +492,19 @@ def run_adjoint(device: int, steps: int = 2000, every: int = 50) -> dict:
                       "target|^2, gradients w.r.t. v0, E, nu"}
 
 
-def run_mixed(device: int, steps: int = 100) -> dict:
-    """The mixed-material workload: 3D, 256^3 grid, 4,194,304 particles in 16 seeded boxes in
-    the upper half of the domain, half liquid and half snow (one material per particle, an
-    extension of the reference), falling under gravity; `steps` steps timed with CUDA events
-    on the simulation's stream after warm-up."""
+def run_plain_form(scene: dict, model: int, res: int, device: int, steps: int, *, physics: int,
+                   material=None, label: str, tune: bool = True) -> dict:
+    """One single-simulation form: the autotuned simulation advances `steps` steps after a
+    10-step warm-up, timed with CUDA events on its stream; per-kernel CUDA events in the same
+    region (direct launches) give the fused kernel's roofline; then the error of one step from
+    the state the timed region ended in, against the FP64 oracle."""
     import torch
 
-    from nuclearmpm_gb300 import MPMSimulation, scenes
-    sc, mat = scenes.liquid_snow_boxes_3d(seed=0, res=256)
-    n = len(sc["x"])
-    sim = MPMSimulation(dict(sc), scenes.SNOW, res=256, material=mat, device=device)
-    sim.advance(10)
-    st = torch.cuda.ExternalStream(sim.stream)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(st)
-    sim.advance(steps)
-    b.record(st)
-    b.synchronize()
-    t = a.elapsed_time(b) / 1e3
-    launches = sim.stats()[0]
-    sim.close()
-    return {"value": n * steps / t, "unit": UNIT, "particles": n, "steps": steps,
-            "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
-            "config": "3D liquid + snow, 256^3 grid, 16 boxes (sides U[0.05,0.2]), per-particle "
-                      "material, dt 1e-4, reference physics"}
-
-
-def run_snow(device: int, steps: int = 100) -> dict:
-    """3D snow on the headline geometry: the four jittered 64^3 lattices of the 1M-particle
-    jelly scene (128^3 grid, same seed) with MaterialModel::kSnow, reference physics; `steps`
-    steps timed with CUDA events on the simulation's stream after warm-up, with the fused
-    kernel's per-launch device time and its fraction of the HBM roofline."""
-    import torch
-
-    from nuclearmpm_gb300 import MPMSimulation, scenes
-    sc = make_scene()
-    n = len(sc["x"])
-    tuned = tune_plain(sc, scenes.SNOW, 128, device)
-    sim = MPMSimulation(dict(sc), scenes.SNOW, res=128, profile=True, device=device, **tuned)
+    from nuclearmpm_gb300 import MPMSimulation
+    n = len(scene["x"])
+    tuned = tune_plain(scene, model, res, device, physics, material) if tune else {}
+    sim = MPMSimulation(dict(scene), model, res=res, material=material, physics=physics,
+                        profile=True, device=device, **tuned)
     sim.advance(10)
     sim.profile_reset()
     st = torch.cuda.ExternalStream(sim.stream)
@@ -353,16 +517,72 @@ def run_snow(device: int, steps: int = 100) -> dict:
     prof = sim.profile()
     active = sim.active_nodes()
     launches = sim.stats()[0]
+    end_state = state_of(sim, scene)
     sim.close()
     g_ms = prof["g2p2g"][0] / max(prof["g2p2g"][1], 1)
-    alg = algorithmic_bytes(3, n, active)["g2p2g"]
-    peak, kind = peaks()
+    alg = algorithmic_bytes(3, n, active)["g2p2g"] + (n if material is not None else 0)
+    kernels = {k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1),
+                   "share": v[0] / max(t * 1e3, 1e-9)} for k, v in prof.items() if v[1] > 0}
+    err = error_vs_fp64(end_state, dim=3, model=model, res=res, device=device, material=material,
+                        physics=physics, what=f"the state after the {10 + steps} steps run")
     return {"value": n * steps / t, "unit": UNIT, "particles": n, "steps": steps,
             "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
-            "g2p2g_avg_ms": g_ms, "g2p2g_gbs": alg / (g_ms / 1e3) / 1e9,
-            "g2p2g_frac": alg / (g_ms / 1e3) / 1e9 / peak, "peak_source": kind, "tuned": tuned,
-            "config": "3D snow (MaterialModel::kSnow), the 1M-particle scene above, 128^3 grid, "
-                      "dt 1e-4, reference physics"}
+            "physics": "reference" if physics == 0 else "corrected", "tuned": tuned,
+            "roofline": roofline_of("g2p2g", alg, g_ms, kernels=kernels, active_nodes=active),
+            "error_vs_fp64": err, "config": label}
+
+
+def run_mixed(device: int, steps: int = 100) -> dict:
+    """The mixed-material workload: 3D, 256^3 grid, 4,194,304 particles in 16 seeded boxes in
+    the upper half of the domain, half liquid and half snow (one material per particle, an
+    extension of the reference), falling under gravity; `steps` steps timed with CUDA events
+    on the simulation's stream after warm-up; the CPU oracle (one thread, -Ofast) on a sample
+    of the same scene beside it."""
+    from nuclearmpm_gb300 import scenes
+    sc, mat = scenes.liquid_snow_boxes_3d(seed=0, res=256)
+    out = run_plain_form(sc, scenes.SNOW, 256, device, steps, physics=scenes.REFERENCE,
+                         material=mat, tune=False,
+                         label="3D liquid + snow, 256^3 grid, 16 boxes (sides U[0.05,0.2]), "
+                               "per-particle material, dt 1e-4, reference physics")
+    if int(os.environ.get("RANK", "0")) == 0:
+        v, desc = cpu_reference_run(sc, steps=2, warmup=1, budget_s=12.0, model=scenes.SNOW,
+                                    res=256, material=mat)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": desc + "; the reference's step restated in C++ "
+                               "(oracle/, -Ofast like the reference build), one thread"}
+    return out
+
+
+def run_snow(device: int, steps: int = 100) -> dict:
+    """3D snow on the headline geometry: the four jittered 64^3 lattices of the 1M-particle
+    jelly scene (128^3 grid, same seed) with MaterialModel::kSnow, reference physics; `steps`
+    steps timed with CUDA events on the simulation's stream after warm-up, with the fused
+    kernel's per-launch device time and its fraction of the HBM roofline.  Under the
+    reference's diag(1,1,0) this scene flies apart (see run_corrected for the same scene under
+    the corrected physics)."""
+    from nuclearmpm_gb300 import scenes
+    out = run_plain_form(make_scene(), scenes.SNOW, 128, device, steps, physics=scenes.REFERENCE,
+                         label="3D snow (MaterialModel::kSnow), the 1M-particle scene above, "
+                               "128^3 grid, dt 1e-4, reference physics")
+    # the keys of earlier lines
+    out["g2p2g_avg_ms"] = out["roofline"]["avg_launch_ms"]
+    out["g2p2g_frac"] = out["roofline"]["frac"]
+    return out
+
+
+def run_corrected(device: int, steps: int = 100) -> dict:
+    """The headline geometry (four jittered 64^3 lattices, 1,048,576 particles, 128^3 grid)
+    under the corrected physics (the true identity, where the reference has diag(1,1,0)), where
+    the step's physics is meaningful: jelly and snow, each timed, with its roofline and its
+    one-step error against the FP64 oracle."""
+    from nuclearmpm_gb300 import scenes
+    sc = scenes.jelly_cubes_3d(seed=0, res=128, physics=scenes.CORRECTED)
+    out = {}
+    for name, model in (("jelly", scenes.JELLY), ("snow", scenes.SNOW)):
+        out[name] = run_plain_form(sc, model, 128, device, steps, physics=scenes.CORRECTED,
+                                   label=f"3D {name}, the 1M-particle scene of the headline, "
+                                         "128^3 grid, dt 1e-4, corrected physics")
+    return out
 
 
 def run_readme(device: int, steps: int = 4000, cpu_steps: int = 400) -> dict:
@@ -388,15 +608,18 @@ def run_readme(device: int, steps: int = 4000, cpu_steps: int = 400) -> dict:
     b.synchronize()
     t = a.elapsed_time(b) / 1e3
     launches = sim.stats()[0]
+    end_state = state_of(sim, sc)
     sim.close()
     t0 = time.perf_counter()
     po.advance(sc, dim=2, model=scenes.SNOW, res=64, steps=cpu_steps, fast=True, want_grid=False)
     tc = time.perf_counter() - t0
+    err = error_vs_fp64(end_state, dim=2, model=scenes.SNOW, res=64, device=device,
+                        what=f"the state after the {200 + steps} steps run")
     return {"value": n * steps / t, "unit": UNIT, "particles": n, "steps": steps,
             "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
             "cpu_value": n * cpu_steps / tc, "cpu_sample": f"{cpu_steps} steps of the same scene, "
             "oracle -Ofast, one thread", "speedup_vs_cpu": (n * steps / t) / (n * cpu_steps / tc),
-            "tuned": tuned,
+            "tuned": tuned, "error_vs_fp64": err,
             "config": "README scene: 2D snow, 5,000 particles, res 64, dt 1e-4, reference "
                       "physics, CUDA graphs of 200 steps"}
 
@@ -421,10 +644,11 @@ def run_models(device: int, steps: int = 100) -> dict:
                               ("neohookean", capi.STRESS_NEOHOOKEAN, False),
                               ("per_particle_moduli", capi.STRESS_COROTATED, True)):
         sim = MPMSimulation(dict(sc), scenes.JELLY, res=128, physics=scenes.CORRECTED,
-                            stress_model=stress, device=device)
+                            stress_model=stress, device=device, profile=True)
         if own:
             sim.set_moduli(E, nu)
         sim.advance(10)
+        sim.profile_reset()
         st = torch.cuda.ExternalStream(sim.stream)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(st)
@@ -432,9 +656,19 @@ def run_models(device: int, steps: int = 100) -> dict:
         b.record(st)
         b.synchronize()
         t = a.elapsed_time(b) / 1e3
+        prof = sim.profile()
+        active = sim.active_nodes()
+        g_ms = prof["g2p2g"][0] / max(prof["g2p2g"][1], 1)
+        alg = algorithmic_bytes(3, n, active)["g2p2g"] + (8 * n if own else 0)
+        end_state = state_of(sim, sc)
         out[name] = {"value": n * steps / t, "ms_per_step": t / steps * 1e3,
-                     "gpu_launches": sim.stats()[0]}
+                     "gpu_launches": sim.stats()[0],
+                     "roofline": roofline_of("g2p2g", alg, g_ms, active_nodes=active)}
         sim.close()
+        out[name]["error_vs_fp64"] = error_vs_fp64(
+            end_state, dim=3, model=scenes.JELLY, res=128, device=device,
+            physics=scenes.CORRECTED, stress=stress, E_p=E if own else None,
+            nu_p=nu if own else None, what=f"the state after the {10 + steps} steps run")
     out["config"] = ("3D jelly, the 1M-particle scene of the headline built under the corrected "
                      "physics, 128^3 grid, dt 1e-4; corotated / neo-Hookean stress / corotated "
                      "with per-particle E in [1e3, 1e4] and nu in [0.1, 0.4]")
@@ -442,7 +676,7 @@ def run_models(device: int, steps: int = 100) -> dict:
 
 
 FORMS = {"batched": run_batched, "adjoint": run_adjoint, "mixed": run_mixed, "snow": run_snow,
-         "readme": run_readme, "models": run_models}
+         "readme": run_readme, "models": run_models, "corrected": run_corrected}
 
 
 def run_form(args):
@@ -551,6 +785,7 @@ def run_ours(args):
         stop.synchronize()
         barrier()
     launches_total += sim.stats()[0]
+    headline_end_state = state_of(sim, scene)
     ms = start.elapsed_time(stop)
     ms_max = max_over_ranks(ms)
     prof = sim.profile()
@@ -632,6 +867,13 @@ def run_ours(args):
     models = None
     if not args.no_models:
         models = run_models(local)
+    corrected = None
+    if not args.no_corrected:
+        corrected = run_corrected(local)
+    # one step at the headline's size from the state its timed region ended in, against the
+    # FP64 oracle (the handle's state after the end-to-end leg is the uploaded scene stepped)
+    err = error_vs_fp64(headline_end_state, dim=3, model=scenes.JELLY, res=128, device=local,
+                        what=f"the state after the {args.warmup + args.steps} device-resident steps")
 
     cpu = cpu_mt = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -652,11 +894,12 @@ def run_ours(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded scene with the workload's shapes and distributions)",
-                "config": dict(WORKLOAD, parallelism=f"replicas x{world}", tuned=tuned),
-                "roofline": roofline, "cpu_baseline": cpu, "cpu_baseline_mt": cpu_mt,
-                "e2e": e2e, "batched": batched,
-                "adjoint": adjoint, "mixed": mixed, "snow": snow, "readme": readme,
-                "models": models, "gpu_launches": launches_total, "clocks": clk}
+                "config": dict(WORKLOAD), "parallelism": f"replicas x{world}", "tuned": tuned,
+                "roofline": roofline, "error_vs_fp64": err, "cpu_baseline": cpu,
+                "cpu_baseline_mt": cpu_mt, "e2e": e2e, "batched": batched,
+                "adjoint": adjoint, "mixed": mixed, "snow": snow, "corrected": corrected,
+                "readme": readme, "models": models, "gpu_launches": launches_total,
+                "clocks": clk}
         print(json.dumps(line), flush=True)
     sim.close()
     ranks.close()
@@ -677,6 +920,7 @@ def main():
     ap.add_argument("--no-snow", action="store_true")
     ap.add_argument("--no-readme", action="store_true")
     ap.add_argument("--no-models", action="store_true")
+    ap.add_argument("--no-corrected", action="store_true")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the end-to-end (host buffers) measurement, e.g. for a launch list "
                          "of the device-resident steps alone")

@@ -94,9 +94,13 @@ typedef struct nclr_options {
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid
  * update sweep (grid_op + clearing the accumulator), the stand-alone P2G that follows an
- * upload, and the fused G2P + next-step P2G kernel that makes up the rest of a step. */
+ * upload, and the fused G2P + next-step P2G kernel that makes up the rest of a step.  The
+ * last three are the reverse kernels of a rollout's backward pass (nclr_rollout_profile_get):
+ * the adjoint of G2P, of the grid update, and of P2G.  The last is the FP64 recomputation of
+ * the snow clamps that the fused kernel flags as ill-conditioned in FP32. */
 enum { NCLR_PHASE_SORT = 0, NCLR_PHASE_GRID = 1, NCLR_PHASE_P2G = 2, NCLR_PHASE_G2P2G = 3,
-       NCLR_NUM_PHASES = 4 };
+       NCLR_PHASE_ADJ_G2P = 4, NCLR_PHASE_ADJ_GRID = 5, NCLR_PHASE_ADJ_P2G = 6,
+       NCLR_PHASE_SNOW_FIX = 7, NCLR_NUM_PHASES = 8 };
 
 typedef struct nclr_sim nclr_sim;
 
@@ -233,6 +237,15 @@ nclr_status nclr_count_active_nodes(nclr_sim *sim, int64_t *active_nodes);
 nclr_status nclr_profile_get(const nclr_sim *sim, int phase, double *total_ms, int64_t *launches);
 nclr_status nclr_profile_reset(nclr_sim *sim);
 
+/* Test hook for the small-scene kernels' grid barrier (the one-launch-per-call path, single
+ * scenes and batches), which gives up a wait after a bounded number of polls (about a second)
+ * and reports it.  With extra_arrivals > 0 every barrier waits for that many CTAs beyond the
+ * launch's, which never come, so each wait runs out after spin_limit polls (~64 ns each;
+ * 0 = the default limit): the call returns NCLR_ERR_CUDA ("grid barrier ran out of time"),
+ * leaves the particle state half stepped and the handle usable.  (0, 0) restores the normal
+ * barrier.  No counterpart in the reference. */
+nclr_status nclr_debug_set_barrier(nclr_sim *sim, unsigned extra_arrivals, unsigned spin_limit);
+
 /* Message of the last failed call on this handle ("" if none); valid until the next call.
  * With sim == NULL: the last failure of nclr_create on this thread. */
 const char *nclr_last_error(const nclr_sim *sim);
@@ -240,12 +253,15 @@ const char *nclr_last_error(const nclr_sim *sim);
 void nclr_destroy(nclr_sim *sim);
 
 /* ---------------------------------------------------------------------------------------
- * Differentiable rollouts (no counterpart in the reference).  A rollout is `nsteps` jelly
- * steps (src/nclr.h:80-337, MaterialModel::kJelly) from a given state; the reverse pass is a
- * hand-written adjoint of the whole step (G2P, grid update with its clamp and boundary masks,
- * P2G, the stress of opt->stress_model -- fixed corotated with its polar rotation, or
- * neo-Hookean) run backwards through the rollout, recomputing each segment of
- * `checkpoint_every` steps from a checkpoint.
+ * Differentiable rollouts (no counterpart in the reference).  A rollout is `nsteps` steps
+ * (src/nclr.h:80-372) of one material from a given state; the reverse pass is a hand-written
+ * adjoint of the whole step (G2P with the material's plasticity -- the snow clamp through the
+ * derivative of its singular values and the Jp update, the liquid reset through det F --, grid
+ * update with its clamp and boundary masks, P2G, the hardening, the stress of
+ * opt->stress_model -- fixed corotated with its polar rotation, or neo-Hookean) run backwards
+ * through the rollout, recomputing each segment of `checkpoint_every` steps from a checkpoint.
+ * Jp is part of the state (1 at the start, as Particle<dim> sets it); nothing is read of the
+ * final Jp, so its adjoint starts at zero.
  *
  * All state arrays are DEVICE pointers in the host layout above (caller order, rows).
  * nclr_rollout_create takes the particle count, initial positions (HOST, used only to size and
@@ -260,6 +276,12 @@ nclr_status nclr_rollout_create(nclr_rollout **out, int dim, int64_t n, const fl
                                 const float *mass, const float *volume, int res, float dt,
                                 float gravity, int64_t nsteps, int checkpoint_every,
                                 const nclr_options *opt);
+/* The same for any material model (NCLR_SNOW, NCLR_JELLY, NCLR_LIQUID); nclr_rollout_create is
+ * this with NCLR_JELLY. */
+nclr_status nclr_rollout_create_model(nclr_rollout **out, int dim, int64_t n, const float *x0,
+                                      const float *mass, const float *volume, int model, int res,
+                                      float dt, float gravity, int64_t nsteps,
+                                      int checkpoint_every, const nclr_options *opt);
 nclr_status nclr_rollout_forward(nclr_rollout *r, const float *x0, const float *v0, const float *F0,
                                  const float *C0, float E, float nu, float *xT, float *vT,
                                  float *FT, float *CT);
@@ -282,6 +304,13 @@ nclr_status nclr_rollout_backward_moduli(nclr_rollout *r, const float *gxT, cons
                                          float *gnu);
 /* Device time (ms, CUDA events on the rollout's stream) of the last forward and backward. */
 nclr_status nclr_rollout_timing(const nclr_rollout *r, double *forward_ms, double *backward_ms);
+/* With nclr_options.profile set at creation: per kernel phase (NCLR_PHASE_*), the device time
+ * and launch count since the last reset -- the forward kernels of the forward pass and of the
+ * backward's recomputation, and the three reverse kernels of every backward step, each timed
+ * with CUDA events on the stream it runs on.  Profiling launches the forward without graphs. */
+nclr_status nclr_rollout_profile_get(const nclr_rollout *r, int phase, double *total_ms,
+                                     int64_t *launches);
+nclr_status nclr_rollout_profile_reset(nclr_rollout *r);
 void *nclr_rollout_stream(nclr_rollout *r);
 /* Message of the rollout's last failed call; with r == NULL the last nclr_rollout_create
  * failure of this thread. */
@@ -300,8 +329,14 @@ void nclr_rollout_destroy(nclr_rollout *r);
  * DEVICE memory (the host layout above: x[p*dim+d], F[(p*dim+r)*dim+c], ...; all seven
  * arrays required) into the caller's DEVICE arrays grid_velocity[(res+1)^dim * dim] and
  * grid_mass[(res+1)^dim], in the reference's node order.  Runs on `stream` (a cudaStream_t,
- * NULL = legacy default stream) of the calling thread's current device and synchronises it
- * before returning.
+ * NULL = legacy default stream) of the calling thread's current device; every call copies its
+ * error flag back and synchronises that stream before returning.
+ *
+ * What it computes: the fixed-corotated stress of src/nclr.h:313-337 with one material
+ * (`model`), one E and one nu for every particle -- no per-particle materials or moduli and no
+ * neo-Hookean option.  The physics mode of nclr_options does not change this transfer (the
+ * diag(1,1,0) identity and the 2D SVD sign fix enter only G2P), so the grid equals grid()
+ * after one nclr_advance under either mode.
  *
  * The only memory it uses beyond the caller's arrays is a static device array of
  * NCLR_NOALLOC_MAX_NODES float4 nodes (16 MiB) in the library, held by every GPU that loads
@@ -309,9 +344,11 @@ void nclr_rollout_destroy(nclr_rollout *r);
  * NCLR_NOALLOC_MAX_NODES (3D: res <= 100; 2D: res <= 1023): larger grids return
  * NCLR_ERR_INVALID.  The array is shared by all calls and keeps the last call's contents;
  * each call clears it before use.  Calls whose GPU work overlaps (other threads or streams at
- * the same time) race on it: serialise them.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  Errors: NCLR_ERR_INVALID (bad argument, grid too large), NCLR_ERR_OUT_OF_RANGE (a
+ * the same time) race on it: serialise them (the library does not).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and keeps it for the
+ * context it was made in; make that first call before any stream capture.  A call in another
+ * context of the device (after cudaDeviceReset, or in a caller's own context) looks the address
+ * up again, so that call too belongs before any stream capture.  Errors: NCLR_ERR_INVALID (bad argument, grid too large), NCLR_ERR_OUT_OF_RANGE (a
  * stencil left the grid, the reference's std::out_of_range), NCLR_ERR_CUDA; when `message`
  * is non-NULL, up to message_len - 1 bytes of explanation are written there.
  * --------------------------------------------------------------------------------------- */

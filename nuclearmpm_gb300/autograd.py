@@ -25,27 +25,29 @@ def _dp(t):
 
 
 class Rollout:
-    """A differentiable `steps`-step jelly rollout of `n` particles (positions x0 only size and
-    place the simulation; mass / volume default to 1, as Particle<dim> does)."""
+    """A differentiable `steps`-step rollout of `n` particles of one material (`model`: jelly
+    by default, or snow or liquid with their plasticity; positions x0 only size and place the
+    simulation; mass / volume default to 1, as Particle<dim> does)."""
 
     def __init__(self, x0, *, res: int = 64, steps: int = 100, checkpoint_every: int = 50,
                  dt: float = 1e-4, gravity: float = -100.0, mass=None, volume=None,
                  physics: int = capi.PHYSICS_REFERENCE, device: int = 0, sort_interval: int = 8,
-                 stress_model: int = capi.STRESS_COROTATED):
+                 stress_model: int = capi.STRESS_COROTATED, profile: bool = False,
+                 model: int = 1):
         x = np.ascontiguousarray(torch.as_tensor(x0).detach().cpu().numpy(), dtype=np.float32)
         self.n, self.dim = x.shape
         self.steps = int(steps)
         m = None if mass is None else np.ascontiguousarray(mass, dtype=np.float32)
         vo = None if volume is None else np.ascontiguousarray(volume, dtype=np.float32)
         opt = capi.default_options(physics=physics, device=device, sort_interval=sort_interval,
-                                   stress_model=stress_model)
+                                   stress_model=stress_model, profile=int(profile))
         h = ctypes.c_void_p()
         L = capi.lib()
-        st = L.nclr_rollout_create(ctypes.byref(h), self.dim, self.n, x.ctypes.data,
-                                   None if m is None else m.ctypes.data,
-                                   None if vo is None else vo.ctypes.data, int(res), float(dt),
-                                   float(gravity), self.steps, int(checkpoint_every),
-                                   ctypes.byref(opt))
+        st = L.nclr_rollout_create_model(ctypes.byref(h), self.dim, self.n, x.ctypes.data,
+                                         None if m is None else m.ctypes.data,
+                                         None if vo is None else vo.ctypes.data, int(model),
+                                         int(res), float(dt), float(gravity), self.steps,
+                                         int(checkpoint_every), ctypes.byref(opt))
         if st != 0:
             raise capi.NclrError(st, (L.nclr_rollout_error(None) or b"").decode())
         self._h = h
@@ -61,6 +63,21 @@ class Rollout:
 
     def __call__(self, x0, v0, E, nu, F0=None, C0=None):
         return RolloutFunction.apply(self, x0, v0, E, nu, F0, C0)
+
+    def profile(self) -> dict:
+        """Per kernel phase (capi.PHASE_NAMES): (total device ms, launches) since the last
+        reset, with profile=True: the forward kernels of the forward pass and of the
+        backward's recomputation, and the reverse kernels of every backward step."""
+        out = {}
+        for i, name in enumerate(capi.PHASE_NAMES):
+            ms, k = ctypes.c_double(), ctypes.c_int64()
+            self._check(capi.lib().nclr_rollout_profile_get(self._h, i, ctypes.byref(ms),
+                                                            ctypes.byref(k)))
+            out[name] = (float(ms.value), int(k.value))
+        return out
+
+    def profile_reset(self) -> None:
+        self._check(capi.lib().nclr_rollout_profile_reset(self._h))
 
     def timing(self) -> tuple[float, float]:
         f, b = ctypes.c_double(), ctypes.c_double()

@@ -16,8 +16,9 @@ STATUS_NAMES = {0: "NCLR_OK", 1: "NCLR_ERR_INVALID", 2: "NCLR_ERR_OUT_OF_RANGE",
                 3: "NCLR_ERR_CUDA", 4: "NCLR_ERR_NO_DEVICE"}
 PHYSICS_REFERENCE, PHYSICS_CORRECTED = 0, 1
 STRESS_COROTATED, STRESS_NEOHOOKEAN = 0, 1
-PHASE_SORT, PHASE_GRID, PHASE_P2G, PHASE_G2P2G = range(4)
-PHASE_NAMES = ("sort", "grid", "p2g", "g2p2g")
+(PHASE_SORT, PHASE_GRID, PHASE_P2G, PHASE_G2P2G, PHASE_ADJ_G2P, PHASE_ADJ_GRID, PHASE_ADJ_P2G,
+ PHASE_SNOW_FIX) = range(8)
+PHASE_NAMES = ("sort", "grid", "p2g", "g2p2g", "adj_g2p", "adj_grid", "adj_p2g", "snow_fix")
 NOALLOC_MAX_NODES = 1 << 20
 
 
@@ -88,11 +89,16 @@ SIGNATURES = {
     "nclr_profile_get": (ctypes.c_int, [_h, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(_i64)]),
     "nclr_profile_reset": (ctypes.c_int, [_h]),
+    "nclr_debug_set_barrier": (ctypes.c_int, [_h, ctypes.c_uint, ctypes.c_uint]),
     "nclr_last_error": (ctypes.c_char_p, [_h]),
     "nclr_destroy": (None, [_h]),
     "nclr_rollout_create": (ctypes.c_int, [ctypes.POINTER(_h), ctypes.c_int, _i64, _vp, _vp, _vp,
                                            ctypes.c_int, ctypes.c_float, ctypes.c_float, _i64,
                                            ctypes.c_int, ctypes.POINTER(Options)]),
+    "nclr_rollout_create_model": (ctypes.c_int, [ctypes.POINTER(_h), ctypes.c_int, _i64, _vp, _vp,
+                                                 _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                 ctypes.c_float, _i64, ctypes.c_int,
+                                                 ctypes.POINTER(Options)]),
     "nclr_rollout_forward": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
                                             _vp, _vp, _vp, _vp]),
     "nclr_rollout_backward": (ctypes.c_int, [_h, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
@@ -104,6 +110,9 @@ SIGNATURES = {
                                                     _vp, _vp]),
     "nclr_rollout_timing": (ctypes.c_int, [_h, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]),
+    "nclr_rollout_profile_get": (ctypes.c_int, [_h, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(_i64)]),
+    "nclr_rollout_profile_reset": (ctypes.c_int, [_h]),
     "nclr_rollout_stream": (_vp, [_h]),
     "nclr_rollout_error": (ctypes.c_char_p, [_h]),
     "nclr_rollout_destroy": (None, [_h]),

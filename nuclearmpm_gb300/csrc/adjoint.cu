@@ -1,13 +1,14 @@
-// Reverse-mode kernels of one jelly step (the adjoint of MPMSimulation<dim>::advance(),
-// src/nclr.h:80-337 without plasticity).  A step maps s_t = (x, v, F, C) to s_{t+1}; given the
-// adjoint of s_{t+1} these kernels produce the adjoint of s_t and accumulate the adjoints of
-// mu_0 and lambda_0:
-//   adj_g2p   per particle: reverse of the G2P gather, F update and advection; scatters the
-//             adjoint of the updated grid velocity to the nodes;
+// Reverse-mode kernels of one step (the adjoint of MPMSimulation<dim>::advance(),
+// src/nclr.h:80-372, for jelly and for the plasticity of snow and liquid).  A step maps
+// s_t = (x, v, F, C, Jp) to s_{t+1}; given the adjoint of s_{t+1} these kernels produce the
+// adjoint of s_t and accumulate the adjoints of mu_0 and lambda_0:
+//   adj_g2p   per particle: reverse of the G2P gather, F update (with the snow clamp or the
+//             liquid reset) and advection; scatters the adjoint of the updated grid velocity
+//             to the nodes;
 //   adj_grid  per node: reverse of the grid update (v = clamp(mv / m + dt g)); clamped
 //             components and stuck or empty nodes pass nothing;
 //   adj_p2g   per particle: gathers the node adjoints, reverses the P2G scatter, the APIC +
-//             fixed-corotated stress term and the polar rotation.
+//             stress term, the polar rotation and (snow) the Jp-dependent hardening.
 // All arrays are particle-major rows in the caller's order (the layout of the C ABI) and the
 // updated grid V_t of the step is the float4 {v, m} grid the forward step produced.
 #include <cuda_runtime.h>
@@ -194,17 +195,91 @@ struct NoPolar {
 
 }  // namespace
 
+// Reverse of the snow plasticity of src/nclr.h:237-250 (F_hat -> F' = U f(S) V^T, f the clamp
+// to [1 - 2.5e-2, 1 + 4.5e-3], and Jp' = clamp(Jp det F_hat / det F', 0.6, 20)) given the
+// adjoints Fb of F' and Jpb of Jp': the adjoint of F_hat, and that of Jp into *Jp_bar.  With
+// P_bar = U^T Fb V, the adjoint in the singular frame is K_ii = f'(s_i) P_bar_ii and
+// K_ij = (a_ij + b_ij)/2 P_bar_ij + (a_ij - b_ij)/2 P_bar_ji, a_ij = (f_i - f_j) / (s_i - s_j),
+// b_ij = (f_i + f_j) / (s_i + s_j) (the derivative of a function of the singular values;
+// f' = 0 on a clamped value), plus the Jp terms on the diagonal; the result is U K V^T.  The
+// SVD is the one the forward step takes (signed in 3D and in the corrected 2D physics).
+template <int D, bool kRef>
+__device__ __forceinline__ Mat<D> snow_backward(const Mat<D> &Fh, float Jp, const Mat<D> &Fb,
+                                                float Jpb, float *Jp_bar) {
+  Mat<D> U, V;
+  float s[D], f[D], fp[D];
+  if constexpr (D == 3) {
+    svd3<true>(Fh, U, s, V);
+  } else {
+    svd2<kRef>(Fh, U, s, V);
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    f[i] = clampf_(s[i], kSnowLo, kSnowHi);
+    fp[i] = (s[i] > kSnowLo && s[i] < kSnowHi) ? 1.0f : 0.0f;
+  }
+  Mat<D> UtF;  // U^T Fb
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc += U.a[k][i] * Fb.a[k][j];
+      UtF.a[i][j] = acc;
+    }
+  const Mat<D> Pb = mat_mul<D>(UtF, V);
+  Mat<D> K;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      if (i == j) {
+        K.a[i][i] = fp[i] * Pb.a[i][i];
+        continue;
+      }
+      const float dm = s[i] - s[j], dp = s[i] + s[j];
+      const float a = fabsf(dm) > 1e-6f * (fabsf(s[i]) + fabsf(s[j])) ? (f[i] - f[j]) / dm
+                                                                        : 0.5f * (fp[i] + fp[j]);
+      const float b = fabsf(dp) > 1e-30f ? (f[i] + f[j]) / dp : 0.0f;
+      K.a[i][j] = 0.5f * (a + b) * Pb.a[i][j] + 0.5f * (a - b) * Pb.a[j][i];
+    }
+  // Jp' = clamp(r, 0.6, 20), r = Jp prod s / prod f (the det U det V factors cancel)
+  float ps = 1.0f, pf = 1.0f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    ps *= s[i];
+    pf *= f[i];
+  }
+  const float r = Jp * ps / pf;
+  if (r > 0.6f && r < 20.0f && Jpb != 0.0f) {
+    *Jp_bar += Jpb * ps / pf;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      float others = 1.0f;
+#pragma unroll
+      for (int k = 0; k < D; ++k)
+        if (k != i) others *= s[k];
+      K.a[i][i] += Jpb * (Jp * others / pf - r * fp[i] / f[i]);
+    }
+  }
+  return mat_mul_t<D>(mat_mul<D>(U, K), V);
+}
+
 // ---------------------------------------------------------------------------------------
 // adj_g2p: reverse of x' = x + dt v', v' = sum W vg, C' = 4 inv_dx sum W vg (o - fx)^T,
-// F' = (I + dt C') F.  Writes the adjoint of x and F (partial; adj_p2g adds the P2G part)
-// and scatters the adjoint of the updated grid velocity into VB.
+// F_hat = (I + dt C') F and the material's F' (jelly F_hat; snow the clamp, which also moves
+// Jp; liquid the reset to diag with F'_00 = J, the product of the signed singular values).
+// Writes the adjoint of x, F and Jp (partial; adj_p2g adds the P2G part) and scatters the
+// adjoint of the updated grid velocity into VB.
 // ---------------------------------------------------------------------------------------
 template <int D, bool kRef>
 __global__ void __launch_bounds__(128) adj_g2p_kernel(
     int n, const float *__restrict__ x, const float *__restrict__ F,
-    const float *__restrict__ Cn, const float4 *__restrict__ V, Params P,
-    const float *__restrict__ gx, const float *__restrict__ gv, const float *__restrict__ gF,
-    const float *__restrict__ gC, float *__restrict__ ox, float *__restrict__ oF,
+    const float *__restrict__ Jp, const float *__restrict__ Cn, const float4 *__restrict__ V,
+    Params P, int model, const float *__restrict__ gx, const float *__restrict__ gv,
+    const float *__restrict__ gF, const float *__restrict__ gC, const float *__restrict__ gJp,
+    float *__restrict__ ox, float *__restrict__ oF, float *__restrict__ oJp,
     float *__restrict__ VB, int *err) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -215,13 +290,32 @@ __global__ void __launch_bounds__(128) adj_g2p_kernel(
   const Stencil<D> st = make_stencil<D>(xp, P.inv_dx);
   const Mat<D> Fm = load_row_mat<D>(F, p);
   const Mat<D> Cm = load_row_mat<D>(Cn, p);
-  const Mat<D> gFn = row_mat_or_zero<D>(gF, p);
+  Mat<D> gFn = row_mat_or_zero<D>(gF, p);
   Mat<D> gCt = row_mat_or_zero<D>(gC, p);
   Mat<D> M;
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
     for (int j = 0; j < D; ++j) M.a[i][j] = diag_one<D, kRef>(i, j) + P.dt * Cm.a[i][j];
+  // the adjoint of F_hat = M F from that of F' (and Jp'), per material; gFn becomes it
+  const float gJpn = gJp ? gJp[p] : 0.0f;
+  float gJp0 = gJpn;  // jelly and liquid keep Jp
+  if (model != kJelly) {
+    const Mat<D> Fh = mat_mul<D>(M, Fm);
+    if (model == kSnow) {
+      gJp0 = 0.0f;
+      gFn = snow_backward<D, kRef>(Fh, Jp[p], gFn, gJpn, &gJp0);
+    } else {  // liquid: F'_00 = J = prod s = det F_hat (|det F_hat| where sigma >= 0, 2D reference)
+      const float g00 = gFn.a[0][0];
+      const float sgn = (D == 2 && kRef && det(Fh) < 0.0f) ? -1.0f : 1.0f;
+      const Mat<D> cof = cofactor(Fh);
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) gFn.a[i][j] = g00 * sgn * cof.a[i][j];
+    }
+  }
+  if (oJp) oJp[p] = gJp0;
   // F_bar = M^T gF'
   Mat<D> gFp;
 #pragma unroll
@@ -329,9 +423,10 @@ __global__ void __launch_bounds__(256) adj_grid_kernel(const float4 *__restrict_
 template <int D, int kStress>
 __global__ void __launch_bounds__(128) adj_p2g_kernel(
     int n, const float *__restrict__ x, const float *__restrict__ v, const float *__restrict__ F,
-    const float *__restrict__ C, const float *__restrict__ mass, const float *__restrict__ vol,
-    const float4 *__restrict__ GB, Params P, float *__restrict__ ox, float *__restrict__ ov,
-    float *__restrict__ oF, float *__restrict__ oC, double *gml, RowModuli rm, int *err) {
+    const float *__restrict__ C, const float *__restrict__ Jp, const float *__restrict__ mass,
+    const float *__restrict__ vol, const float4 *__restrict__ GB, Params P, int model,
+    float *__restrict__ ox, float *__restrict__ ov, float *__restrict__ oF,
+    float *__restrict__ oC, float *__restrict__ oJp, double *gml, RowModuli rm, int *err) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int S = (D == 3) ? 27 : 9;
   float gmu = 0.0f, glam = 0.0f;
@@ -349,7 +444,8 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     const float2 l0 = rm.lame ? rm.lame[p] : make_float2(P.mu0, P.lambda0);
     // the corotated stress's polar rotation, whose factorisation its adjoint reuses
     const std::conditional_t<kStress == kNeoHookean, NoPolar<D>, Polar<D>> pol(Fm);
-    const Mat<D> A = fused_affine<D>(Fm, pol.R, Cm, 1.0f, m, vo, kJelly, l0, P);
+    const float Jpp = Jp ? Jp[p] : 1.0f;
+    const Mat<D> A = fused_affine<D>(Fm, pol.R, Cm, Jpp, m, vo, model, l0, P);
     Mat<D> gA;
 #pragma unroll
     for (int i = 0; i < D; ++i)
@@ -414,7 +510,8 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     store_row_mat<D>(oC, p, gC);
     // stress
     const float kappa = P.dt * vo * P.Dinv;
-    const float mu = l0.x * 0.3f, lam = l0.y * 0.3f;
+    const float e = hardening(model, Jpp);  // src/nclr.h:351-372
+    const float mu = l0.x * e, lam = l0.y * e;
     const float J = det(Fm);
     Mat<D> gF = load_row_mat<D>(oF, p);
     const Mat<D> cof = cofactor(Fm);  // d det(F) / dF = J F^-T
@@ -489,8 +586,11 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
       for (int j = 0; j < D; ++j) gF.a[i][j] += FQ.a[i][j] + Xb.a[i][j] + Fp.a[i][j] + dJ * cof.a[i][j];
     }
     store_row_mat<D>(oF, p, gF);
-    gmu *= 0.3f;  // jelly hardening (src/nclr.h:362-364)
-    glam *= 0.3f;
+    // snow: e = exp(10 (1 - Jp)), so the adjoint of Jp gains (mu_0 mu_bar + lambda_0
+    // lambda_bar) de/dJp with de/dJp = -10 e (gmu, glam: the adjoints of the hardened pair)
+    if (model == kSnow && oJp) oJp[p] += (gmu * l0.x + glam * l0.y) * (-10.0f * e);
+    gmu *= e;  // the adjoints of mu_0 and lambda_0
+    glam *= e;
     if (rm.grad) {
       rm.grad[2 * (size_t)p] += gmu;
       rm.grad[2 * (size_t)p + 1] += glam;
@@ -512,26 +612,36 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
 // ---------------------------------------------------------------------------------------
 template <int D>
 void launch_adjoint_step(int n, const float *x, const float *v, const float *F, const float *C,
-                         const float *Cn, const float *mass, const float *vol, const float4 *V,
-                         const Params &P, bool ref, const float *gx, const float *gv,
-                         const float *gF, const float *gC, float *ox, float *ov, float *oF,
-                         float *oC, float *VB, float4 *GB, double *gml, RowModuli rm,
-                         int *err, cudaStream_t st) {
+                         const float *Jp, const float *Cn, const float *mass, const float *vol,
+                         const float4 *V, const Params &P, bool ref, const float *gx,
+                         const float *gv, const float *gF, const float *gC, const float *gJp,
+                         float *ox, float *ov, float *oF, float *oC, float *oJp, float *VB,
+                         float4 *GB, double *gml, RowModuli rm, int *err, cudaStream_t st,
+                         cudaEvent_t *ev) {
   const unsigned pb = (unsigned)((n + 127) / 128);
+  const int model = P.model;
+  if (ev) cudaEventRecord(ev[0], st);
   if (n > 0) {
     if (ref)
-      adj_g2p_kernel<D, true><<<pb, 128, 0, st>>>(n, x, F, Cn, V, P, gx, gv, gF, gC, ox, oF, VB, err);
+      adj_g2p_kernel<D, true><<<pb, 128, 0, st>>>(n, x, F, Jp, Cn, V, P, model, gx, gv, gF, gC,
+                                                  gJp, ox, oF, oJp, VB, err);
     else
-      adj_g2p_kernel<D, false><<<pb, 128, 0, st>>>(n, x, F, Cn, V, P, gx, gv, gF, gC, ox, oF, VB, err);
+      adj_g2p_kernel<D, false><<<pb, 128, 0, st>>>(n, x, F, Jp, Cn, V, P, model, gx, gv, gF, gC,
+                                                   gJp, ox, oF, oJp, VB, err);
   }
+  if (ev) cudaEventRecord(ev[1], st);
   adj_grid_kernel<D><<<(unsigned)((P.nodes + 255) / 256), 256, 0, st>>>(V, VB, GB, P);
+  if (ev) cudaEventRecord(ev[2], st);
   if (n > 0)
     if (P.stress == kNeoHookean)
-      adj_p2g_kernel<D, kNeoHookean><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF,
-                                                         oC, gml, rm, err);
+      adj_p2g_kernel<D, kNeoHookean><<<pb, 128, 0, st>>>(n, x, v, F, C, Jp, mass, vol, GB, P,
+                                                         model, ox, ov, oF, oC, oJp, gml, rm,
+                                                         err);
     else
-      adj_p2g_kernel<D, kCorotated><<<pb, 128, 0, st>>>(n, x, v, F, C, mass, vol, GB, P, ox, ov, oF,
-                                                        oC, gml, rm, err);
+      adj_p2g_kernel<D, kCorotated><<<pb, 128, 0, st>>>(n, x, v, F, C, Jp, mass, vol, GB, P,
+                                                        model, ox, ov, oF, oC, oJp, gml, rm,
+                                                        err);
+  if (ev) cudaEventRecord(ev[3], st);
 }
 
 namespace {
@@ -559,16 +669,18 @@ cudaError_t launch_moduli_grads(int n, const float *E, const float *nu, const do
 }
 
 template void launch_adjoint_step<2>(int, const float *, const float *, const float *, const float *,
-                                     const float *, const float *, const float *, const float4 *,
-                                     const Params &, bool, const float *, const float *,
-                                     const float *, const float *, float *, float *, float *,
-                                     float *, float *, float4 *, double *, RowModuli, int *,
-                                     cudaStream_t);
+                                     const float *, const float *, const float *, const float *,
+                                     const float4 *, const Params &, bool, const float *,
+                                     const float *, const float *, const float *, const float *,
+                                     float *, float *, float *, float *, float *, float *,
+                                     float4 *, double *, RowModuli, int *, cudaStream_t,
+                                     cudaEvent_t *);
 template void launch_adjoint_step<3>(int, const float *, const float *, const float *, const float *,
-                                     const float *, const float *, const float *, const float4 *,
-                                     const Params &, bool, const float *, const float *,
-                                     const float *, const float *, float *, float *, float *,
-                                     float *, float *, float4 *, double *, RowModuli, int *,
-                                     cudaStream_t);
+                                     const float *, const float *, const float *, const float *,
+                                     const float4 *, const Params &, bool, const float *,
+                                     const float *, const float *, const float *, const float *,
+                                     float *, float *, float *, float *, float *, float *,
+                                     float4 *, double *, RowModuli, int *, cudaStream_t,
+                                     cudaEvent_t *);
 
 }  // namespace mpm

@@ -150,6 +150,9 @@ __device__ __forceinline__ void unflatten(int64_t f, int N, int idx[D]) {
   }
 }
 
+// The snow clamp's bounds on the singular values (src/nclr.h:237-241): 1 - 2.5e-2, 1 + 4.5e-3.
+constexpr float kSnowLo = 1.0f - 2.5e-2f, kSnowHi = 1.0f + 4.5e-3f;
+
 // hardening (src/nclr.h:351-372): snow e = exp(10 (1 - Jp)); jelly 0.3; liquid 1.0.
 __device__ __forceinline__ float hardening(int material, float Jp) {
   if (material == kSnow) return expf(10.0f * (1.0f - Jp));
@@ -209,10 +212,12 @@ __device__ __forceinline__ Mat<D> fused_affine(const Mat<D> &F, const Mat<D> &R,
 }
 
 // The rotation the stress needs: the polar factor of F for the corotated model, nothing for
-// the neo-Hookean one.
+// the neo-Hookean one.  Snow takes it with correctly rounded rotations, as the fused step
+// takes it from the clamp's SVD (the hardened snow stress amplifies a rotation's rounding).
 template <int D>
-__device__ __forceinline__ Mat<D> stress_R(const Mat<D> &F, const Params &P) {
-  return P.stress == kNeoHookean ? F : polar_R(F);
+__device__ __forceinline__ Mat<D> stress_R(const Mat<D> &F, const Params &P, int material) {
+  if (P.stress == kNeoHookean) return F;
+  return material == kSnow ? polar_R_exact(F) : polar_R(F);
 }
 
 template <int D>

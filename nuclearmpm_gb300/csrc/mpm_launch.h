@@ -16,11 +16,31 @@ struct Scene;
 // when not recording (single simulations only).
 struct Record {
   float *x, *v, *F, *C;
+  float *Jp = nullptr;  // (may be null) Jp rows too
+};
+
+// The snow clamps a fused launch leaves for FP64 (mpm_step.cuh: snow_clamp_needs_fp64): the
+// fused kernel appends the particle's slot, its F_hat and its Jp before the clamp, and keeps its
+// FP32 result meanwhile; launch_snow_fix then recomputes those clamps in FP64, writes F and Jp
+// and corrects the launch's P2G by the difference of the two stresses.  count is reset by the
+// grid sweep that starts every step; cap >= the particles of one launch.  All null: no list
+// (the small-scene kernels recompute in place).
+struct SnowFix {
+  int *count = nullptr;
+  int cap = 0;
+  int *slot = nullptr;
+  float *Fh = nullptr;  // dim*dim per entry
+  float *Jp = nullptr;
 };
 
 template <int D> void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
                                         const uint16_t *block_scene, int total_blocks, int *work, int sms,
-                                        cudaStream_t st);
+                                        cudaStream_t st, int *fix_count = nullptr);
+// The FP64 snow clamps of the last fused launch (see SnowFix); scatter: that launch did the next
+// step's P2G (not the G2P-only final step), whose accumulator G receives the correction.
+template <int D> void launch_snow_fix(const PState &s, const Params &P0, const Scene *scenes,
+                                      const SnowFix &fix, float4 *G, bool scatter, bool ref,
+                                      const Record &rec, int sms, cudaStream_t st);
 template <int D> void launch_discard_pending(float4 *G, uint8_t *flags, const Scene *scenes,
                                              const uint16_t *block_scene, int total_blocks, int sms,
                                              cudaStream_t st);
@@ -30,21 +50,29 @@ template <int D> void launch_g2p2g(const PState &s, const Params &P0, const Scen
                                    const float4 *V, float4 *G, uint8_t *flags, const int *blocks,
                                    const int *nactive, const int *bstart, const int *sparse, int *work,
                                    int *err, int next_slot, bool ref, int mode, int ctas, cudaStream_t st,
-                                   const Record &rec = Record{});
+                                   const Record &rec = Record{}, const SnowFix &fix = SnowFix{});
 template <int D> int g2p2g_ctas_per_sm();
 template <int D> int g2p_final_ctas_per_sm();
+// The small-scene kernels' grid barrier: how many polls a waiting CTA makes before it gives up
+// (about a second at the default), and how many arrivals beyond the launch's CTAs it waits for
+// (0; a test sets 1, so that the wait runs out and the error path runs).
+constexpr unsigned kBarrierSpinsDefault = 1u << 24;
+struct BarrierTest {
+  unsigned extra = 0;
+  unsigned spins = kBarrierSpinsDefault;
+};
 // Small scenes: all `steps` steps of one scene in one cooperative launch (kSmallThreads-thread
 // CTAs, `ctas` of them, all resident); bar = 2 zeroed unsigned.
 template <int D> cudaError_t launch_small_steps(const PState &s, const Params &P, float4 *G, float4 *V,
                                                int steps, int *err, unsigned *bar, bool ref, int ctas,
-                                               cudaStream_t st);
+                                               cudaStream_t st, BarrierTest bt = BarrierTest{});
 template <int D> int small_ctas_per_sm(bool ref);
 // The same for a batch: CTA c works on scene cta_scene[c]; scene s owns CTAs
 // [group_first[s], group_first[s+1]) and the barrier bars[2s..2s+1] (zeroed).
 template <int D> cudaError_t launch_small_batch(const PState &s, const Scene *scenes, const uint16_t *cta_scene,
                                                const int *group_first, float4 *G, float4 *V, uint8_t *flags,
                                                int steps, int *err, unsigned *bars, bool ref, int ctas,
-                                               cudaStream_t st);
+                                               cudaStream_t st, BarrierTest bt = BarrierTest{});
 template <int D> int small_batch_ctas_per_sm(bool ref);
 constexpr int kSmallThreadsPerCta = 256;
 constexpr uint8_t kFlagVNonzeroBit = 2;  // mpm_step.cuh's kVNonzero: V may be non-zero there
@@ -85,10 +113,13 @@ cudaError_t count_bad_materials(const uint8_t *mat, int64_t n, int *scratch, int
 cudaError_t launch_set_lame(const int *id, int n, const float *E, const float *nu, float2 *lame,
                             cudaStream_t st);
 
-// Reverse of one jelly step (adjoint.cu): adjoint of s_{t+1} (gx, gv, gF, gC; NULL = 0) ->
-// adjoint of s_t (ox, ov, oF, oC), mu_0 / lambda_0 adjoints added to gml[0..1].  States are
-// caller-order rows; V is the step's updated grid; VB (4 floats per node) must be zero on
-// entry and is zero again on exit; GB holds nodes float4.
+// Reverse of one step of the scene's material P.model (adjoint.cu): adjoint of s_{t+1}
+// (gx, gv, gF, gC, gJp; NULL = 0) -> adjoint of s_t (ox, ov, oF, oC, oJp; oJp may be NULL for
+// jelly), mu_0 / lambda_0 adjoints added to gml[0..1].  States are caller-order rows (Jp: the
+// state's plastic volume ratio, NULL = 1); V is the step's updated grid; VB (4 floats per
+// node) must be zero on entry and is zero again on exit; GB holds nodes float4.  ev (may be
+// null): four events recorded on `st` before adj_g2p, between the kernels and after adj_p2g
+// (per-kernel timing).
 // Per-particle moduli of a rollout, per row in the caller's order (both null: the scene's
 // pair): lame[q] = (mu_0, lambda_0) of row q; grad[2q], grad[2q + 1] accumulate the adjoints of
 // row q's mu_0 and lambda_0 over the reverse steps.
@@ -98,11 +129,12 @@ struct RowModuli {
 };
 template <int D>
 void launch_adjoint_step(int n, const float *x, const float *v, const float *F, const float *C,
-                         const float *Cn, const float *mass, const float *vol, const float4 *V,
-                         const Params &P, bool ref, const float *gx, const float *gv,
-                         const float *gF, const float *gC, float *ox, float *ov, float *oF,
-                         float *oC, float *VB, float4 *GB, double *gml, RowModuli rm, int *err,
-                         cudaStream_t st);
+                         const float *Jp, const float *Cn, const float *mass, const float *vol,
+                         const float4 *V, const Params &P, bool ref, const float *gx,
+                         const float *gv, const float *gF, const float *gC, const float *gJp,
+                         float *ox, float *ov, float *oF, float *oC, float *oJp, float *VB,
+                         float4 *GB, double *gml, RowModuli rm, int *err, cudaStream_t st,
+                         cudaEvent_t *ev = nullptr);
 // gE[q], gnu[q] from row q's accumulated mu_0 / lambda_0 adjoints (grad) and its E[q], nu[q],
 // through mu_0 = E / (2 (1 + nu)), lambda_0 = E nu / ((1 + nu)(1 - 2 nu)).
 cudaError_t launch_moduli_grads(int n, const float *E, const float *nu, const double *grad,

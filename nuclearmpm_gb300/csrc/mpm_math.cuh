@@ -29,6 +29,7 @@ MPM_HD float fast_div(float a, float b) {
   return a / b;
 #endif
 }
+MPM_HD double fast_div(double a, double b) { return a / b; }
 
 MPM_HD float rsqrt_(float x) {
 #ifdef __CUDA_ARCH__
@@ -37,6 +38,16 @@ MPM_HD float rsqrt_(float x) {
   return 1.0f / sqrtf(x);
 #endif
 }
+MPM_HD double rsqrt_(double x) { return 1.0 / sqrt(x); }
+
+// Scalar helpers in both precisions (the SVD below runs in FP32, and in FP64 where the snow
+// clamp needs it).
+MPM_HD float sqrt_(float x) { return sqrtf(x); }
+MPM_HD double sqrt_(double x) { return sqrt(x); }
+MPM_HD float fabs_(float x) { return fabsf(x); }
+MPM_HD double fabs_(double x) { return fabs(x); }
+MPM_HD float copysign_(float a, float b) { return copysignf(a, b); }
+MPM_HD double copysign_(double a, double b) { return copysign(a, b); }
 
 template <int D>
 struct Mat {
@@ -96,39 +107,56 @@ MPM_HD Mat<2> polar_rotation(const Mat<2> &m) {
   return R;
 }
 
+MPM_HD float atan2_(float y, float x) { return atan2f(y, x); }
+MPM_HD double atan2_(double y, double x) { return atan2(y, x); }
+MPM_HD void sincos_(float a, float *s, float *c) { sincosf(a, s, c); }
+MPM_HD void sincos_(double a, double *s, double *c) {
+#ifdef __CUDA_ARCH__
+  sincos(a, s, c);
+#else
+  *s = sin(a);
+  *c = cos(a);
+#endif
+}
+
 // 2x2 SVD in closed form.  With E=(a00+a11)/2, F=(a00-a11)/2, G=(a10+a01)/2,
 // H=(a10-a01)/2:  A = rot(phi) diag(Q+R, Q-R) rot(theta), Q = |(E,H)|, R = |(F,G)|,
 // phi = (atan2(H,E) + atan2(G,F))/2, theta = (atan2(H,E) - atan2(G,F))/2.
 // So U = rot(phi), V = rot(theta)^T; sigma_2 = Q - R carries sign(det A).
-template <bool kNonNegative>
-MPM_HD void svd2(const Mat<2> &A, Mat<2> &U, float sig[2], Mat<2> &V) {
-  const float E = 0.5f * (A.a[0][0] + A.a[1][1]);
-  const float F = 0.5f * (A.a[0][0] - A.a[1][1]);
-  const float G = 0.5f * (A.a[1][0] + A.a[0][1]);
-  const float H = 0.5f * (A.a[1][0] - A.a[0][1]);
-  const float Q = sqrtf(E * E + H * H);
-  const float R = sqrtf(F * F + G * G);
-  const float a1 = atan2f(G, F), a2 = atan2f(H, E);
-  const float phi = 0.5f * (a2 + a1), theta = 0.5f * (a2 - a1);
-  float sp, cp, st, ct;
-  sincosf(phi, &sp, &cp);
-  sincosf(theta, &st, &ct);
+template <bool kNonNegative, typename T>
+MPM_HD void svd2_t(const T A[2][2], T U[2][2], T sig[2], T V[2][2]) {
+  const T E = T(0.5) * (A[0][0] + A[1][1]);
+  const T F = T(0.5) * (A[0][0] - A[1][1]);
+  const T G = T(0.5) * (A[1][0] + A[0][1]);
+  const T H = T(0.5) * (A[1][0] - A[0][1]);
+  const T Q = sqrt_(E * E + H * H);
+  const T R = sqrt_(F * F + G * G);
+  const T a1 = atan2_(G, F), a2 = atan2_(H, E);
+  const T phi = T(0.5) * (a2 + a1), theta = T(0.5) * (a2 - a1);
+  T sp, cp, st, ct;
+  sincos_(phi, &sp, &cp);
+  sincos_(theta, &st, &ct);
   sig[0] = Q + R;
   sig[1] = Q - R;
-  U.a[0][0] = cp;
-  U.a[0][1] = -sp;
-  U.a[1][0] = sp;
-  U.a[1][1] = cp;
+  U[0][0] = cp;
+  U[0][1] = -sp;
+  U[1][0] = sp;
+  U[1][1] = cp;
   // V = rot(theta)^T
-  V.a[0][0] = ct;
-  V.a[0][1] = st;
-  V.a[1][0] = -st;
-  V.a[1][1] = ct;
-  if (kNonNegative && sig[1] < 0.0f) {
+  V[0][0] = ct;
+  V[0][1] = st;
+  V[1][0] = -st;
+  V[1][1] = ct;
+  if (kNonNegative && sig[1] < T(0)) {
     sig[1] = -sig[1];
-    U.a[0][1] = -U.a[0][1];
-    U.a[1][1] = -U.a[1][1];
+    U[0][1] = -U[0][1];
+    U[1][1] = -U[1][1];
   }
+}
+
+template <bool kNonNegative>
+MPM_HD void svd2(const Mat<2> &A, Mat<2> &U, float sig[2], Mat<2> &V) {
+  svd2_t<kNonNegative, float>(A.a, U.a, sig, V.a);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -152,33 +180,33 @@ namespace detail {
 // come out exactly 1.  Plasticity needs that (the liquid's J = prod sigma enters the
 // pressure lambda (J - 1) J on every entry; snow recomposes F from the clamped sigma); the
 // polar rotation of the stress does not.
-template <int P, int Q, bool kExact>
-MPM_HD void jacobi_rotate(float S[3][3], float V[3][3]) {
-  const float app = S[P][P], aqq = S[Q][Q], apq = S[P][Q];
-  if (apq == 0.0f) return;
+template <int P, int Q, bool kExact, typename T>
+MPM_HD void jacobi_rotate(T S[3][3], T V[3][3]) {
+  const T app = S[P][P], aqq = S[Q][Q], apq = S[P][Q];
+  if (apq == T(0)) return;
   // tau and t only choose the angle; c and s below are formed from t consistently, so the
   // fast reciprocal does here (|tau| -> inf gives t = 0, the identity)
-  const float tau = fast_div(aqq - app, 2.0f * apq);
-  const float t = fast_div(copysignf(1.0f, tau), fabsf(tau) + sqrtf(1.0f + tau * tau));
-  const float c = kExact ? 1.0f / sqrtf(1.0f + t * t) : rsqrt_(1.0f + t * t), s = t * c;
+  const T tau = fast_div(aqq - app, T(2) * apq);
+  const T t = fast_div(copysign_(T(1), tau), fabs_(tau) + sqrt_(T(1) + tau * tau));
+  const T c = kExact ? T(1) / sqrt_(T(1) + t * t) : rsqrt_(T(1) + t * t), s = t * c;
   // S <- Q^T S Q with Q = I except Q_pp = c, Q_pq = s, Q_qp = -s, Q_qq = c
 #pragma unroll
   for (int k = 0; k < 3; ++k) {  // columns: S Q
-    const float skp = S[k][P], skq = S[k][Q];
+    const T skp = S[k][P], skq = S[k][Q];
     S[k][P] = c * skp - s * skq;
     S[k][Q] = s * skp + c * skq;
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {  // rows: Q^T (S Q)
-    const float spk = S[P][k], sqk = S[Q][k];
+    const T spk = S[P][k], sqk = S[Q][k];
     S[P][k] = c * spk - s * sqk;
     S[Q][k] = s * spk + c * sqk;
   }
-  S[P][Q] = 0.0f;
-  S[Q][P] = 0.0f;
+  S[P][Q] = T(0);
+  S[Q][P] = T(0);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float vkp = V[k][P], vkq = V[k][Q];
+    const T vkp = V[k][P], vkq = V[k][Q];
     V[k][P] = c * vkp - s * vkq;
     V[k][Q] = s * vkp + c * vkq;
   }
@@ -186,110 +214,124 @@ MPM_HD void jacobi_rotate(float S[3][3], float V[3][3]) {
 
 // Swap columns i and j of B and V when |b_i| < |b_j|, negating the new column j so V stays
 // a rotation.
-template <int I, int J>
-MPM_HD void cond_swap(float B[3][3], float V[3][3], float rho[3]) {
+template <int I, int J, typename T>
+MPM_HD void cond_swap(T B[3][3], T V[3][3], T rho[3]) {
   if (rho[I] < rho[J]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const float b = B[k][I];
+      const T b = B[k][I];
       B[k][I] = B[k][J];
       B[k][J] = -b;
-      const float v = V[k][I];
+      const T v = V[k][I];
       V[k][I] = V[k][J];
       V[k][J] = -v;
     }
-    const float r = rho[I];
+    const T r = rho[I];
     rho[I] = rho[J];
     rho[J] = r;
   }
 }
 
 // Givens rotation on rows (P,Q) of B zeroing B[Q][COL]; accumulates U <- U G.
-template <int P, int Q, int COL, bool kExact>
-MPM_HD void qr_givens(float B[3][3], float U[3][3]) {
-  const float a1 = B[P][COL], a2 = B[Q][COL];
-  const float n2 = a1 * a1 + a2 * a2;
-  float c = 1.0f, s = 0.0f;
-  if (n2 > 1e-38f) {
+template <int P, int Q, int COL, bool kExact, typename T>
+MPM_HD void qr_givens(T B[3][3], T U[3][3]) {
+  const T a1 = B[P][COL], a2 = B[Q][COL];
+  const T n2 = a1 * a1 + a2 * a2;
+  T c = T(1), s = T(0);
+  if (n2 > T(1e-38)) {
     if constexpr (kExact) {  // c = +-1, s = 0 exactly when a2 is negligible against a1
-      const float r = sqrtf(n2);
+      const T r = sqrt_(n2);
       c = a1 / r;
       s = a2 / r;
     } else {
-      const float inv = rsqrt_(n2);
+      const T inv = rsqrt_(n2);
       c = a1 * inv;
       s = a2 * inv;
     }
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {  // rows: G^T B with G = [[c,-s],[s,c]] in (P,Q)
-    const float bp = B[P][k], bq = B[Q][k];
+    const T bp = B[P][k], bq = B[Q][k];
     B[P][k] = c * bp + s * bq;
     B[Q][k] = -s * bp + c * bq;
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {  // U <- U G
-    const float up = U[k][P], uq = U[k][Q];
+    const T up = U[k][P], uq = U[k][Q];
     U[k][P] = c * up + s * uq;
     U[k][Q] = -s * up + c * uq;
   }
 }
 
-}  // namespace detail
+// Jacobi sweeps and stopping threshold per precision: done once every S_pq^2 is below
+// (2 eps)^2 S_pp S_qq, eps the precision's unit roundoff (2.4e-7 in FP32; 1.1e-16 in FP64).
+template <typename T>
+struct JacobiLimits;
+template <>
+struct JacobiLimits<float> {
+  static constexpr int kSweeps = 4;
+  static constexpr float kDone = 2.3e-13f;  // (4.8e-7)^2
+};
+template <>
+struct JacobiLimits<double> {
+  static constexpr int kSweeps = 6;
+  static constexpr double kDone = 4.9e-32;  // (2.2e-16)^2
+};
 
-constexpr int kJacobiSweeps = 4;
-constexpr float kJacobiDone = 2.3e-13f;  // (4.8e-7)^2
-
-template <bool kExact = true>
-MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
-  using namespace detail;
-  float S[3][3], V[3][3];
+// The SVD of a 3x3 array in precision T (see svd3 below for the conventions).
+template <bool kExact, typename T>
+MPM_HD void svd3_t(const T A[3][3], T U[3][3], T sig[3], T V[3][3]) {
+  T S[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
-      V[i][j] = (i == j) ? 1.0f : 0.0f;
+      S[i][j] = A[0][i] * A[0][j] + A[1][i] * A[1][j] + A[2][i] * A[2][j];
+      V[i][j] = (i == j) ? T(1) : T(0);
     }
 #pragma unroll 1
-  for (int sweep = 0; sweep < kJacobiSweeps; ++sweep) {
-    // Done once every off-diagonal S_pq is below 4.8e-7 sqrt(S_pp S_qq) (the 2 epsilon
-    // relative threshold of a two-sided Jacobi SVD such as Eigen's JacobiSVD, on A^T A);
-    // tested before the first sweep as well, so an input that is diagonal to within rounding
-    // is not rotated at all and keeps its diagonal exactly.
-    if (S[0][1] * S[0][1] <= kJacobiDone * fabsf(S[0][0] * S[1][1]) &&
-        S[0][2] * S[0][2] <= kJacobiDone * fabsf(S[0][0] * S[2][2]) &&
-        S[1][2] * S[1][2] <= kJacobiDone * fabsf(S[1][1] * S[2][2]))
+  for (int sweep = 0; sweep < JacobiLimits<T>::kSweeps; ++sweep) {
+    // Done once every off-diagonal S_pq is below 2 eps sqrt(S_pp S_qq) (the relative
+    // threshold of a two-sided Jacobi SVD such as Eigen's JacobiSVD, on A^T A); tested before
+    // the first sweep as well, so an input that is diagonal to within rounding is not rotated
+    // at all and keeps its diagonal exactly.
+    const T done = JacobiLimits<T>::kDone;
+    if (S[0][1] * S[0][1] <= done * fabs_(S[0][0] * S[1][1]) &&
+        S[0][2] * S[0][2] <= done * fabs_(S[0][0] * S[2][2]) &&
+        S[1][2] * S[1][2] <= done * fabs_(S[1][1] * S[2][2]))
       break;
     jacobi_rotate<0, 1, kExact>(S, V);
     jacobi_rotate<1, 2, kExact>(S, V);
     jacobi_rotate<0, 2, kExact>(S, V);
   }
-  float B[3][3];
+  T B[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) B[i][j] = A.a[i][0] * V[0][j] + A.a[i][1] * V[1][j] + A.a[i][2] * V[2][j];
-  float rho[3];
+    for (int j = 0; j < 3; ++j) B[i][j] = A[i][0] * V[0][j] + A[i][1] * V[1][j] + A[i][2] * V[2][j];
+  T rho[3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) rho[j] = B[0][j] * B[0][j] + B[1][j] * B[1][j] + B[2][j] * B[2][j];
   cond_swap<0, 1>(B, V, rho);
   cond_swap<0, 2>(B, V, rho);
   cond_swap<1, 2>(B, V, rho);
-  float U[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) U[i][j] = (i == j) ? T(1) : T(0);
   qr_givens<0, 1, 0, kExact>(B, U);
   qr_givens<0, 2, 0, kExact>(B, U);
   qr_givens<1, 2, 1, kExact>(B, U);
   sig[0] = B[0][0];
   sig[1] = B[1][1];
   sig[2] = B[2][2];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      Uo.a[i][j] = U[i][j];
-      Vo.a[i][j] = V[i][j];
-    }
+}
+
+}  // namespace detail
+
+template <bool kExact = true>
+MPM_HD void svd3(const Mat<3> &A, Mat<3> &Uo, float sig[3], Mat<3> &Vo) {
+  detail::svd3_t<kExact, float>(A.a, Uo.a, sig, Vo.a);
 }
 
 // U diag(s) V^T
@@ -315,6 +357,16 @@ MPM_HD Mat<3> polar_R(const Mat<3> &F) {
   Mat<3> U, V;
   float s[3];
   svd3<false>(F, U, s, V);
+  return uvt<3>(U, V);
+}
+
+// The same rotation from svd3<true> (correctly rounded rotations): what the fused step takes
+// from the snow clamp's own SVD, so a snow particle's stress sees the same R on every path.
+MPM_HD Mat<2> polar_R_exact(const Mat<2> &F) { return polar_rotation(F); }
+MPM_HD Mat<3> polar_R_exact(const Mat<3> &F) {
+  Mat<3> U, V;
+  float s[3];
+  svd3<true>(F, U, s, V);
   return uvt<3>(U, V);
 }
 

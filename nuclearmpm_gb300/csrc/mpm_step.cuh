@@ -177,12 +177,112 @@ __device__ __forceinline__ void scale_mat(Mat<D> &C, float c) {
     for (int j = 0; j < D; ++j) C.a[i][j] *= c;
 }
 
+// FP64 threshold of the snow clamp (see snow_clamp_needs_fp64): the FP32 clamp's own error
+// measured about 2e-7 per unit of this gain, so below 25 it stays within about 5e-6.
+constexpr float kClampFP64Gain = 25.0f;
+
+// Whether the snow clamp of F_hat (FP32 signed singular values sig, decreasing in magnitude)
+// must be recomputed in FP64.  With det F_hat < 0 the last singular value s_l is negative,
+// and the clamp lifts it to a positive value: the clamped F then depends on F_hat through the
+// divided difference (f(s_p) + f(s_l)) / (s_p + s_l) of the clamp f over the last pair, which
+// grows without bound as |s_l| approaches s_p (the clamped F is discontinuous at |s_l| = s_p,
+// where the SVD's choice of the vector that carries the sign flips).  FP32 rounding of the SVD
+// (about eps s_1) is amplified by that factor; where the gain f s_1 / (s_p + s_l) passes
+// kClampFP64Gain the clamp is recomputed in FP64.  With s_l >= 0 the map is 1-Lipschitz in
+// F_hat and FP32 suffices.
+template <int D, bool kRef>
+__device__ __forceinline__ bool snow_clamp_needs_fp64(const float sig[D]) {
+  if constexpr (D == 2 && kRef) return false;  // that 2D SVD keeps sigma >= 0 (no sign fix)
+  const float sl = sig[D - 1], sp = sig[D - 2];
+  if (!(sl < 0.0f)) return false;
+  const float f = clampf_(sp, kSnowLo, kSnowHi) + clampf_(sl, kSnowLo, kSnowHi);
+  return f * sig[0] > kClampFP64Gain * (sp + sl);
+}
+
+// The snow clamp and Jp update of src/nclr.h:237-250 in FP64 from the FP32 F_hat (exact in
+// double): SVD, clamp, F = U clamp(S) V^T, Jp = clamp(Jp det F_hat / det F, 0.6, 20), and the
+// polar rotation of the clamped F (3D: U V^T).  Not inlined: it runs for a few particles, and
+// its doubles stay out of the fused kernel's register budget.
+template <int D, bool kRef>
+__device__ __noinline__ void snow_clamp_fp64(const Mat<D> *Fh_in, float *Jp, Mat<D> *F_out,
+                                             Mat<D> *R_out) {
+  double A[D][D], U[D][D], V[D][D], sg[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) A[i][j] = (double)Fh_in->a[i][j];
+  if constexpr (D == 3) {
+    detail::svd3_t<true, double>(A, U, sg, V);
+  } else {
+    svd2_t<kRef, double>(A, U, sg, V);
+  }
+  double Fn[D][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) sg[d] = fmin(fmax(sg[d], (double)kSnowLo), (double)kSnowHi);
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      double v = 0.0;
+#pragma unroll
+      for (int k = 0; k < D; ++k) v += U[i][k] * sg[k] * V[j][k];
+      Fn[i][j] = v;
+    }
+  double old_J, new_J;
+  if constexpr (D == 3) {
+    old_J = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+            A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+            A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+    new_J = Fn[0][0] * (Fn[1][1] * Fn[2][2] - Fn[1][2] * Fn[2][1]) -
+            Fn[0][1] * (Fn[1][0] * Fn[2][2] - Fn[1][2] * Fn[2][0]) +
+            Fn[0][2] * (Fn[1][0] * Fn[2][1] - Fn[1][1] * Fn[2][0]);
+  } else {
+    old_J = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+    new_J = Fn[0][0] * Fn[1][1] - Fn[0][1] * Fn[1][0];
+  }
+  *Jp = (float)fmin(fmax((double)*Jp * old_J / new_J, 0.6), 20.0);
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) F_out->a[i][j] = (float)Fn[i][j];
+  if constexpr (D == 3) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        R_out->a[i][j] = (float)(U[i][0] * V[j][0] + U[i][1] * V[j][1] + U[i][2] * V[j][2]);
+  } else {
+    *R_out = polar_rotation(*F_out);
+  }
+}
+
+// The FP32 snow clamp (src/nclr.h:237-250) of F_hat = U S V^T: F_hat becomes U clamp(S) V^T,
+// Jp is updated, and R receives the polar rotation of the result (3D: U V^T; 2D when need_R).
+template <int D>
+__device__ __forceinline__ void snow_clamp_fp32(const Mat<D> &U, float sig[D], const Mat<D> &Vm,
+                                                Mat<D> &Fh, float &Jp, Mat<D> &R, bool need_R) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) sig[d] = clampf_(sig[d], kSnowLo, kSnowHi);
+  const float old_J = det(Fh);
+  Fh = usv<D>(U, sig, Vm);
+  Jp = clampf_(Jp * old_J / det(Fh), 0.6f, 20.0f);
+  if constexpr (D == 3) {
+    R = uvt<3>(U, Vm);  // the clamped sigma are positive: F = (U V^T)(V S V^T)
+  } else {
+    if (need_R) R = polar_rotation(Fh);
+  }
+}
+
 // The F update and plasticity of G2P (src/nclr.h:228-259) from the gathered C; returns the
 // rotation R of the updated F (the polar factor the next step's corotated stress needs; with
-// need_R false -- the neo-Hookean stress -- whatever is at hand).
-template <int D, bool kRef>
+// need_R false -- the neo-Hookean stress -- whatever is at hand).  A snow clamp that needs FP64
+// is, with kDefer (the fused kernel), appended to `fix` -- the FP64 fix-up launch that follows
+// redoes it, and this launch carries on with the FP32 result -- and otherwise recomputed in
+// place (the small-scene kernels).
+template <int D, bool kRef, bool kDefer = false>
 __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp, int material,
-                                           float dt, bool need_R = true) {
+                                           float dt, bool need_R = true,
+                                           const SnowFix *fix = nullptr, int slot = 0) {
   Mat<D> M;
 #pragma unroll
   for (int i = 0; i < D; ++i)
@@ -200,17 +300,23 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
     } else {
       svd2<kRef>(Fh, U, sig, Vm);
     }
-    if (material == kSnow) {
+    const bool fp64 = material == kSnow && snow_clamp_needs_fp64<D, kRef>(sig);
+    if (!kDefer && fp64) {
+      const Mat<D> Fh_in = Fh;
+      snow_clamp_fp64<D, kRef>(&Fh_in, &Jp, &Fh, &R);
+    } else if (material == kSnow) {
+      if (kDefer && fp64 && fix) {  // for the fix-up launch: slot, F_hat and Jp before the clamp
+        const int i = atomicAdd(fix->count, 1);
+        if (i < fix->cap) {
+          fix->slot[i] = slot;
 #pragma unroll
-      for (int d = 0; d < D; ++d) sig[d] = clampf_(sig[d], 1.0f - 2.5e-2f, 1.0f + 4.5e-3f);
-      const float old_J = det(Fh);
-      Fh = usv<D>(U, sig, Vm);
-      Jp = clampf_(Jp * old_J / det(Fh), 0.6f, 20.0f);
-      if constexpr (D == 3) {
-        R = uvt<3>(U, Vm);  // the clamped sigma are positive: F = (U V^T)(V S V^T)
-      } else {
-        if (need_R) R = polar_rotation(Fh);
+          for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b = 0; b < D; ++b) fix->Fh[((size_t)i * D + a) * D + b] = Fh.a[a][b];
+          fix->Jp[i] = Jp;
+        }
       }
+      snow_clamp_fp32<D>(U, sig, Vm, Fh, Jp, R, need_R);
     } else {  // liquid: J = prod sigma accumulated in double (src/nclr.h:253-257)
       double J = 1.0;
 #pragma unroll
@@ -309,10 +415,14 @@ __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
                                                          const Scene *__restrict__ scenes,
                                                          const uint16_t *__restrict__ block_scene,
                                                          int total_blocks,
-                                                         int *__restrict__ work) {
+                                                         int *__restrict__ work,
+                                                         int *__restrict__ fix_count) {
   constexpr int BS = Tiling<D>::BS;
   constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;  // nodes per block
-  if (blockIdx.x == 0 && threadIdx.x == 0) *work = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *work = 0;
+    if (fix_count) *fix_count = 0;  // the FP64 snow list of the step that follows
+  }
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
   for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < total_blocks;
@@ -411,7 +521,7 @@ g2p2g_kernel(
     const float4 *__restrict__ Vall, float4 *__restrict__ Gall, uint8_t *__restrict__ flags_all,
     const int *__restrict__ blocks, const int *__restrict__ nactive,
     const int *__restrict__ bstart, const int *__restrict__ sparse, int *__restrict__ work,
-    int *__restrict__ err, int next_slot, Record rec) {
+    int *__restrict__ err, int next_slot, Record rec, SnowFix fix) {
   using Tl = Tiling<D>;
   constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, GS = Tl::SIZE;
   constexpr int S = (D == 3) ? 27 : 9;
@@ -424,10 +534,16 @@ g2p2g_kernel(
   float4 *vt = smem + grp * kTiles * GS;  // the group's V tile
   float4 *gt = vt + GS;                   // its kWarps private G tiles: [warp][SIZE]
   __shared__ int s_items[kGroups];
+  // Per group, per axis and tile coordinate c: the warps whose stencils reached a node with
+  // coordinate c on that axis in the current item (bit w = warp w of the group).  A node's
+  // AND over its axes names the warp tiles that can hold contributions there: the flush reads
+  // (and clears) only those, instead of every warp's tile at every tile node.
+  __shared__ unsigned s_covs[kGroups][D * T];
   __shared__ Params sPs[kGroups];  // each item's scene (shared: keeps registers for the math)
   __shared__ int64_t s_node_offs[kGroups];
   __shared__ int s_block_offs[kGroups];
   int &s_item = s_items[grp];
+  unsigned *s_cov = s_covs[grp];
   Params &sP = sPs[grp];
   int64_t &s_node_off = s_node_offs[grp];
   int &s_block_off = s_block_offs[grp];
@@ -453,6 +569,7 @@ g2p2g_kernel(
 
   for (;;) {
     group_sync();
+    if (gtid < D * T) s_cov[gtid] = 0u;  // the last item's flush is done reading them
     if (gtid == 0) {  // the next block of the list, and its scene
       const int it = atomicAdd(work, 1);
       s_item = it;
@@ -523,6 +640,8 @@ g2p2g_kernel(
       // what the particle contributes to the next P2G
       bool fast_s = false;
       int tb_s = 0;
+      unsigned cov_s = 0;  // the tile nodes the stencil covers, per axis (bits c..c+2 of axis d
+                           // at d * T)
       float fx_s[D], w_s[3][D], mv[D], m = 0.0f;
       Mat<D> A;
       if (valid) {
@@ -539,7 +658,7 @@ g2p2g_kernel(
           F = load_mat<D>(s.F, st, p);
           C = load_mat<D>(s.C, st, p);
           Jp = s.Jp[p];
-          R = stress_R<D>(F, P);
+          R = stress_R<D>(F, P, material);
         } else {
         // ---- G2P of this step ----
         float fx[D], w[3][D];
@@ -575,8 +694,9 @@ g2p2g_kernel(
         for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];  // advection, src/nclr.h:229
         F = load_mat<D>(s.F, st, p);
         Jp = s.Jp[p];
-        R = update_F<D, kRef>(C, F, Jp, material, P.dt,
-                              kMode != kG2PFinal && P.stress == kCorotated);
+        R = update_F<D, kRef, true>(C, F, Jp, material, P.dt,
+                                    kMode != kG2PFinal && P.stress == kCorotated,
+                                    fix.count ? &fix : nullptr, p);
 #pragma unroll
         for (int d = 0; d < D; ++d) s.x[(size_t)d * st + p] = x[d];
         store_mat<D>(s.F, st, p, F);
@@ -599,6 +719,7 @@ g2p2g_kernel(
                 rec.F[(q * D + i) * D + jj] = F.a[i][jj];
                 rec.C[(q * D + i) * D + jj] = C.a[i][jj];
               }
+            if (rec.Jp) rec.Jp[q] = Jp;
           }
         }
         }
@@ -619,6 +740,8 @@ g2p2g_kernel(
             fast_s &= in_range(lb[d], T - 3) && in_range(base[d], N - 3);
           }
           tb_s = tile_index<D>(lb[0], lb[1], lb[2]);
+#pragma unroll
+          for (int d = 0; d < D; ++d) cov_s |= 7u << (d * T + lb[d]);
           if (!fast_s) {  // outside the tile: straight to G
             const int64_t f0 = flat_index<D>(base, N);
 #pragma unroll
@@ -665,6 +788,10 @@ g2p2g_kernel(
           __syncwarp();
         }
       }
+      {  // the nodes this pass of the warp reached, per axis, into the item's coverage
+        const unsigned cov = __reduce_or_sync(0xffffffffu, tile_lane ? cov_s : 0u);
+        if (lane < D * T && ((cov >> lane) & 1u)) atomicOr(s_cov + lane, 1u << (gtid >> 5));
+      }
     }
     if (direct || kMode == kG2PFinal) continue;  // its P2G went straight to G (and the flags)
     group_sync();
@@ -680,21 +807,23 @@ g2p2g_kernel(
         r /= T;
         in &= g[d] >= 0 && g[d] < N;
       }
+      // the warps whose stencils reached this node's coordinates on every axis
+      unsigned mask = s_cov[l[0]] & s_cov[T + l[1]];
+      if constexpr (D == 3) mask &= s_cov[2 * T + l[2]];
+      if (!mask) continue;  // no warp's tile holds anything here
       const int ti = tile_index<D>(l[0], l[1], l[2]);
       float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      bool touched = false;
 #pragma unroll
       for (int wi = 0; wi < kWarps; ++wi) {
-        const float4 g4 = gt[wi * GS + ti];
+        if (!((mask >> wi) & 1u)) continue;
+        float4 *e = gt + wi * GS + ti;
+        const float4 g4 = *e;
         a[0] += g4.x;
         a[1] += g4.y;
         a[2] += g4.z;
         a[3] += g4.w;
-        touched |= g4.x != 0.0f || g4.y != 0.0f || g4.z != 0.0f || g4.w != 0.0f;
+        *e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
-      if (!touched) continue;
-#pragma unroll
-      for (int wi = 0; wi < kWarps; ++wi) gt[wi * GS + ti] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (a[0] == 0.0f && a[1] == 0.0f && a[2] == 0.0f && a[3] == 0.0f) continue;
       if (in) red_add_v4(G + flat_index<D>(g, N), a[0], a[1], a[2], a[3]);
     }
@@ -935,12 +1064,13 @@ __global__ void sort_move_kernel(PState src, PState dst, int n, const int *__res
 // thousand particles) by one per advance() call.
 // ---------------------------------------------------------------------------------------
 constexpr int kSmallThreads = 256;
-constexpr unsigned kBarrierSpins = 1u << 24;  // x ~64 ns: about a second, then an error
 
 // Barrier of `ctas` CTAs of a cooperative launch (every CTA is resident): bar[0] counts
-// arrivals, bar[1] is the generation.  A wait that runs out sets kErrBarrier and every CTA
-// returns false (and leaves the kernel); nothing waits without a bound.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned ctas) {
+// arrivals, bar[1] is the generation.  A wait that runs out (`spins` polls of ~64 ns; the
+// default kBarrierSpinsDefault is about a second) sets kErrBarrier and every CTA returns false
+// (and leaves the kernel); nothing waits without a bound.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned ctas,
+                                             unsigned spin_limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -955,7 +1085,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned c
     } else {
       unsigned spins = 0;
       while (*gen == g) {
-        if (++spins > kBarrierSpins) {
+        if (++spins > spin_limit) {
           atomicOr(err, kErrBarrier);
           ok = 0;
           break;
@@ -975,7 +1105,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
                                                                     float4 *__restrict__ G,
                                                                     float4 *__restrict__ V,
                                                                     int steps, int *err,
-                                                                    unsigned *bar) {
+                                                                    unsigned *bar, BarrierTest bt) {
   constexpr int S = (D == 3) ? 27 : 9;
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -990,8 +1120,8 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
       const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
       const float m = s.mass[p];
       const int material = s.mat ? (int)s.mat[p] : P.model;
-      Mat<D> A = fused_affine<D>(F, stress_R<D>(F, P), C, s.Jp[p], m, s.vol[p], material,
-                                 lame0(s, p, P), P);
+      Mat<D> A = fused_affine<D>(F, stress_R<D>(F, P, material), C, s.Jp[p], m, s.vol[p],
+                                 material, lame0(s, p, P), P);
 #pragma unroll
       for (int d = 0; d < D; ++d) mv[d] = s.v[(size_t)d * st + p] * m;
       stencil<D>(x, P.inv_dx, base, fx, w);
@@ -1009,7 +1139,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
         red_add_v4(G + f, c[0], c[1], c[2], c[3]);
       }
     }
-    if (!grid_barrier(bar, err, gridDim.x)) return;
+    if (!grid_barrier(bar, err, gridDim.x + bt.extra, bt.spins)) return;
     // ---- grid_op (src/nclr.h:263-310): V = op(G), and G cleared for the next p2g ----
     for (int64_t i = tid; i < P.nodes; i += stride) {
       int idx[D];
@@ -1019,7 +1149,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
       V[i] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
       G[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    if (!grid_barrier(bar, err, gridDim.x)) return;
+    if (!grid_barrier(bar, err, gridDim.x + bt.extra, bt.spins)) return;
     // ---- g2p (src/nclr.h:167-261) ----
     for (int p = tid; p < P.n; p += stride) {
       float x[D], v[D], fx[D], w[3][D];
@@ -1071,7 +1201,7 @@ template <int D, bool kRef>
 __global__ void __launch_bounds__(kSmallThreads) small_batch_kernel(
     PState s, const Scene *__restrict__ scenes, const uint16_t *__restrict__ cta_scene,
     const int *__restrict__ group_first, float4 *__restrict__ Gall, float4 *__restrict__ Vall,
-    uint8_t *__restrict__ flags_all, int steps, int *err_all, unsigned *bars) {
+    uint8_t *__restrict__ flags_all, int steps, int *err_all, unsigned *bars, BarrierTest bt) {
   constexpr int S = (D == 3) ? 27 : 9;
   constexpr int BS = Tiling<D>::BS;
   constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;
@@ -1110,8 +1240,8 @@ __global__ void __launch_bounds__(kSmallThreads) small_batch_kernel(
       const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
       const float m = s.mass[p];
       const int material = s.mat ? (int)s.mat[p] : P.model;
-      Mat<D> A = fused_affine<D>(F, stress_R<D>(F, P), C, s.Jp[p], m, s.vol[p], material,
-                                 lame0(s, p, P), P);
+      Mat<D> A = fused_affine<D>(F, stress_R<D>(F, P, material), C, s.Jp[p], m, s.vol[p],
+                                 material, lame0(s, p, P), P);
 #pragma unroll
       for (int d = 0; d < D; ++d) mv[d] = s.v[(size_t)d * st + p] * m;
       stencil<D>(x, P.inv_dx, base, fx, w);
@@ -1130,7 +1260,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_batch_kernel(
       }
       mark_stencil<D>(flags, base, P);
     }
-    if (!grid_barrier(bar, err, ctas)) return;
+    if (!grid_barrier(bar, err, ctas + bt.extra, bt.spins)) return;
     // ---- grid_op (src/nclr.h:263-310) on the flagged blocks: V = op(G), G = 0 ----
     for (int b = warp; b < P.nblocks; b += warps) {
       const uint8_t fl = __ldcg(flags + b);
@@ -1163,7 +1293,7 @@ __global__ void __launch_bounds__(kSmallThreads) small_batch_kernel(
       }
       if (lane == 0) flags[b] = (fl & kPending) ? kVNonzero : 0;
     }
-    if (!grid_barrier(bar, err, ctas)) return;
+    if (!grid_barrier(bar, err, ctas + bt.extra, bt.spins)) return;
     // ---- g2p (src/nclr.h:167-261) ----
     for (int q = tid; q < P.n; q += stride) {
       const int p = p0 + q;
@@ -1215,12 +1345,112 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 template <int D>
 void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
                        const uint16_t *block_scene, int total_blocks, int *work, int sms,
-                       cudaStream_t st) {
+                       cudaStream_t st, int *fix_count) {
   int64_t blocks = blocks_for((int64_t)total_blocks * 32, 256);
   if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
   if (blocks < 1) blocks = 1;
   grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, flags, scenes, block_scene,
-                                                          total_blocks, work);
+                                                          total_blocks, work, fix_count);
+}
+
+// ---------------------------------------------------------------------------------------
+// snow_fix: the snow clamps the last fused launch left for FP64 (SnowFix), one per thread.
+// Each recomputes its FP32 result as the fused kernel did (the same functions on the same
+// F_hat and Jp), and the clamp in FP64; writes the FP64 F and Jp to the particle (and to the
+// recorded caller-order rows of a rollout segment); and, when that launch did the next step's
+// P2G, adds to G the difference the FP64 stress makes there: weight_o (A_64 - A_32) (o - fx)
+// dx for the stencil of the particle's updated position, with A the stress part of the fused
+// APIC momentum (src/nclr.h:313-337; the m C part is the same in both).
+// ---------------------------------------------------------------------------------------
+template <int D, bool kRef>
+__global__ void __launch_bounds__(128) snow_fix_kernel(PState s, Params P0,
+                                                       const Scene *__restrict__ scenes,
+                                                       SnowFix fix, float4 *__restrict__ Gall,
+                                                       int scatter, Record rec) {
+  const int count = min(*fix.count, fix.cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const int p = fix.slot[i];
+    const int sid = s.scene ? (int)s.scene[p] : 0;
+    const Params P = scenes ? scenes[sid].P : P0;
+    Mat<D> Fh;
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+      for (int b = 0; b < D; ++b) Fh.a[a][b] = fix.Fh[((size_t)i * D + a) * D + b];
+    const float Jp_in = fix.Jp[i];
+    const bool need_R = P.stress == kCorotated;
+    // the FP32 result the fused launch carried on with
+    Mat<D> U, Vm, F32 = Fh, R32 = Fh;
+    float sig[D], Jp32 = Jp_in;
+    if constexpr (D == 3) {
+      svd3(Fh, U, sig, Vm);
+    } else {
+      svd2<kRef>(Fh, U, sig, Vm);
+    }
+    snow_clamp_fp32<D>(U, sig, Vm, F32, Jp32, R32, need_R);
+    // the FP64 one
+    Mat<D> F64, R64;
+    float Jp64 = Jp_in;
+    snow_clamp_fp64<D, kRef>(&Fh, &Jp64, &F64, &R64);
+    const int st = s.stride;
+    store_mat<D>(s.F, st, p, F64);
+    s.Jp[p] = Jp64;
+    if (rec.F) {  // a rollout segment's recorded rows (caller order)
+      const size_t q = (size_t)s.id[p];
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int b = 0; b < D; ++b) rec.F[(q * D + a) * D + b] = F64.a[a][b];
+      if (rec.Jp) rec.Jp[q] = Jp64;
+    }
+    if (!scatter) continue;
+    Mat<D> Z;
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+      for (int b = 0; b < D; ++b) Z.a[a][b] = 0.0f;
+    const float m = s.mass[p], vol = s.vol[p];
+    const float2 l0 = lame0(s, p, P);
+    const Mat<D> A64 = fused_affine<D>(F64, need_R ? R64 : F64, Z, Jp64, m, vol, kSnow, l0, P);
+    const Mat<D> A32 = fused_affine<D>(F32, need_R ? R32 : F32, Z, Jp32, m, vol, kSnow, l0, P);
+    Mat<D> dA;
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+      for (int b = 0; b < D; ++b) dA.a[a][b] = A64.a[a][b] - A32.a[a][b];
+    float x[D], fx[D], w[3][D], q0[D];
+    int base[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      x[d] = s.x[(size_t)d * st + p];
+      q0[d] = 0.0f;
+    }
+    stencil<D>(x, P.inv_dx, base, fx, w);
+    p2g_terms<D>(fx, P.dx, q0, dA);  // q0 = -dA fx dx, dA becomes dA dx
+    float4 *G = Gall + (scenes ? scenes[sid].node_off : 0);
+    const int64_t f0 = flat_index<D>(base, P.N);
+    constexpr int S = (D == 3) ? 27 : 9;
+#pragma unroll
+    for (int o = 0; o < S; ++o) {
+      const int64_t f = stencil_flat<D>(f0, o, P.N);
+      if (f < 0 || f >= P.nodes) continue;  // the fused launch reported it already
+      float c[4];
+      p2g_contrib<D>(o, w, q0, 0.0f, dA, c);
+      red_add_v4(G + f, c[0], c[1], c[2], 0.0f);
+    }
+  }
+}
+
+template <int D>
+void launch_snow_fix(const PState &s, const Params &P0, const Scene *scenes, const SnowFix &fix,
+                     float4 *G, bool scatter, bool ref, const Record &rec, int sms,
+                     cudaStream_t st) {
+  if (!fix.count) return;
+  const unsigned blocks = (unsigned)std::max(1, sms);
+  if (ref)
+    snow_fix_kernel<D, true><<<blocks, 128, 0, st>>>(s, P0, scenes, fix, G, scatter ? 1 : 0, rec);
+  else
+    snow_fix_kernel<D, false><<<blocks, 128, 0, st>>>(s, P0, scenes, fix, G, scatter ? 1 : 0, rec);
 }
 
 template <int D>
@@ -1242,7 +1472,7 @@ void launch_g2p2g_fixed(const PState &s, const Params &P0, const float4 *V, floa
                         uint8_t *flags, const int *blocks, const int *nactive,
                         const int *bstart, const int *sparse, int *work, int *err, int next_slot,
                         bool ref, int mode, int material, int ctas, cudaStream_t st,
-                        const Record &rec);
+                        const Record &rec, const SnowFix &fix);
 // Raises the dynamic shared-memory limit of every launch_g2p2g_fixed<D> kernel to `bytes`.
 template <int D>
 void g2p2g_fixed_set_smem(int bytes);
@@ -1252,12 +1482,12 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                   const uint16_t *block_scene, const float4 *V, float4 *G, uint8_t *flags,
                   const int *blocks, const int *nactive, const int *bstart, const int *sparse,
                   int *work, int *err, int next_slot, bool ref, int mode, int ctas,
-                  cudaStream_t st, const Record &rec) {
+                  cudaStream_t st, const Record &rec, const SnowFix &fix) {
   if constexpr (D == 3) {  // one material for every particle: the specialised kernel
     if (!block_scene && !s.mat && (mode == kStep || mode == kFinalStep) &&
         (P0.model == kSnow || P0.model == kJelly || P0.model == kLiquid)) {
       launch_g2p2g_fixed<D>(s, P0, V, G, flags, blocks, nactive, bstart, sparse, work, err,
-                            next_slot, ref, mode, P0.model, ctas, st, rec);
+                            next_slot, ref, mode, P0.model, ctas, st, rec, fix);
       return;
     }
   }
@@ -1266,7 +1496,7 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                                 (MODE) == kG2PFinal ? g2p_final_smem_bytes<D>()           \
                                                     : g2p2g_smem_bytes<D, B>(),           \
                                 st>>>(s, P0, scenes, block_scene, V, G, flags, blocks,   \
-                                      nactive, bstart, sparse, work, err, next_slot, rec)
+                                      nactive, bstart, sparse, work, err, next_slot, rec, fix)
 #define MPM_G2P2G_B(R, MODE)          \
   if (block_scene) {                  \
     MPM_G2P2G(R, MODE, true);         \
@@ -1296,10 +1526,11 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
 // bar (2 unsigned) must be zero.  Returns the launch error (e.g. too many CTAs).
 template <int D>
 cudaError_t launch_small_steps(const PState &s, const Params &P, float4 *G, float4 *V, int steps,
-                               int *err, unsigned *bar, bool ref, int ctas, cudaStream_t st) {
+                               int *err, unsigned *bar, bool ref, int ctas, cudaStream_t st,
+                               BarrierTest bt) {
   PState sv = s;
   Params Pv = P;
-  void *args[] = {&sv, &Pv, &G, &V, &steps, &err, &bar};
+  void *args[] = {&sv, &Pv, &G, &V, &steps, &err, &bar, &bt};
   const void *fn = ref ? (const void *)small_steps_kernel<D, true> : (const void *)small_steps_kernel<D, false>;
   return cudaLaunchCooperativeKernel(fn, dim3((unsigned)ctas), dim3(kSmallThreads), args, 0, st);
 }
@@ -1308,9 +1539,10 @@ template <int D>
 cudaError_t launch_small_batch(const PState &s, const Scene *scenes, const uint16_t *cta_scene,
                                const int *group_first, float4 *G, float4 *V, uint8_t *flags,
                                int steps, int *err, unsigned *bars, bool ref, int ctas,
-                               cudaStream_t st) {
+                               cudaStream_t st, BarrierTest bt) {
   PState sv = s;
-  void *args[] = {&sv, &scenes, &cta_scene, &group_first, &G, &V, &flags, &steps, &err, &bars};
+  void *args[] = {&sv, &scenes, &cta_scene, &group_first, &G, &V, &flags, &steps, &err, &bars,
+                  &bt};
   const void *fn = ref ? (const void *)small_batch_kernel<D, true> : (const void *)small_batch_kernel<D, false>;
   return cudaLaunchCooperativeKernel(fn, dim3((unsigned)ctas), dim3(kSmallThreads), args, 0, st);
 }
@@ -1414,21 +1646,26 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
 
 #define MPM_INSTANTIATE(D)                                                                       \
   template void launch_grid_sweep<D>(float4 *, float4 *, uint8_t *, const Scene *,              \
-                                     const uint16_t *, int, int *, int, cudaStream_t);           \
+                                     const uint16_t *, int, int *, int, cudaStream_t, int *);    \
+  template void launch_snow_fix<D>(const PState &, const Params &, const Scene *,                \
+                                   const SnowFix &, float4 *, bool, bool, const Record &, int,   \
+                                   cudaStream_t);                                                \
   template void launch_discard_pending<D>(float4 *, uint8_t *, const Scene *, const uint16_t *,  \
                                           int, int, cudaStream_t);                               \
   template void launch_g2p2g<D>(const PState &, const Params &, const Scene *, const uint16_t *, \
                                 const float4 *, float4 *, uint8_t *, const int *, const int *,   \
                                 const int *, const int *, int *, int *, int, bool, int, int,     \
-                                cudaStream_t, const Record &);                                   \
+                                cudaStream_t, const Record &, const SnowFix &);                  \
   template int g2p2g_ctas_per_sm<D>();                                                           \
   template int g2p_final_ctas_per_sm<D>();                                                       \
   template cudaError_t launch_small_steps<D>(const PState &, const Params &, float4 *, float4 *,   \
-                                             int, int *, unsigned *, bool, int, cudaStream_t);  \
+                                             int, int *, unsigned *, bool, int, cudaStream_t,   \
+                                             BarrierTest);                                       \
   template int small_ctas_per_sm<D>(bool);                                                       \
   template cudaError_t launch_small_batch<D>(const PState &, const Scene *, const uint16_t *,      \
                                              const int *, float4 *, float4 *, uint8_t *, int,     \
-                                             int *, unsigned *, bool, int, cudaStream_t);         \
+                                             int *, unsigned *, bool, int, cudaStream_t,          \
+                                             BarrierTest);                                        \
   template int small_batch_ctas_per_sm<D>(bool);                                                 \
   template void launch_copy_vgrid<D>(const float4 *, int64_t, float *, float *, cudaStream_t);   \
   template void launch_export_grid<D>(const float4 *, const Params &, float *, float *,          \

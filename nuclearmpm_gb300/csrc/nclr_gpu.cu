@@ -67,6 +67,8 @@ struct nclr_sim {
   bool sorted_once = false;   // slot_block is valid
   cudaStream_t copy_stream = nullptr;  // host transfers, pipelined field by field
   unsigned *bar = nullptr;    // the small-scene kernels' barriers (2 counters per scene)
+  mpm::BarrierTest bar_test;  // nclr_debug_set_barrier: the barrier's poll limit and extra arrivals
+  mpm::SnowFix fix;           // the FP64 snow clamps of a fused launch (allocated when snow may occur)
   uint16_t *cta_scene = nullptr;  // batches: scene of each CTA of the small-scene kernel
   int *group_first = nullptr;     // batches: first CTA of each scene's group (nscenes + 1)
   int batch_ctas = 0;             // batches: CTAs of that launch (0: not possible)
@@ -276,7 +278,7 @@ void enqueue_step(nclr_sim *s, bool sort, int final) {
     constexpr int D = decltype(dc)::value;
     phase(s, NCLR_PHASE_GRID, 1, [&] {
       mpm::launch_grid_sweep<D>(s->G, s->V, s->flags, s->scenes_d, s->block_scene,
-                                s->total_blocks, s->work, s->sms, s->stream);
+                                s->total_blocks, s->work, s->sms, s->stream, s->fix.count);
     });
     s->launches += 1;
     if (s->n > 0) {
@@ -288,9 +290,17 @@ void enqueue_step(nclr_sim *s, bool sort, int final) {
                              : final == kNotFinal    ? mpm::kModeStep
                                                      : mpm::kModeFinalStep,
                              final == kFinalG2POnly ? s->g2p_ctas : s->g2p2g_ctas, s->stream,
-                             s->record);
+                             s->record, s->fix);
       });
       s->launches += 1;
+      if (s->fix.count) {  // the snow clamps that launch left for FP64
+        phase(s, NCLR_PHASE_SNOW_FIX, 1, [&] {
+          mpm::launch_snow_fix<D>(s->ps[s->cur], s->P0(), s->nscenes > 1 ? s->scenes_d : nullptr,
+                                  s->fix, s->G, final != kFinalG2POnly, s->ref, s->record, s->sms,
+                                  s->stream);
+        });
+        s->launches += 1;
+      }
     }
   });
 }
@@ -479,6 +489,10 @@ void release(nclr_sim *s) {
   cudaFree(s->moved_d);
   if (s->moved_h) cudaFreeHost(s->moved_h);
   cudaFree(s->work);
+  cudaFree(s->fix.count);
+  cudaFree(s->fix.slot);
+  cudaFree(s->fix.Fh);
+  cudaFree(s->fix.Jp);
   cudaFree(s->key);
   cudaFree(s->rank);
   cudaFree(s->count);
@@ -717,6 +731,16 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMalloc((void **)&s->moved_d, sizeof(int)));
   CREATE_TRY(cudaMallocHost((void **)&s->moved_h, sizeof(int)));
   CREATE_TRY(cudaMalloc((void **)&s->work, sizeof(int)));
+  bool snow = any_mat;  // a material[] may hold snow
+  for (int i = 0; i < nscenes; ++i) snow |= descs[i].model == NCLR_SNOW;
+  if (snow && np > 0) {  // the FP64 list of the snow clamp: at most one entry per particle
+    s->fix.cap = (int)np;
+    CREATE_TRY(cudaMalloc((void **)&s->fix.count, sizeof(int)));
+    CREATE_TRY(cudaMalloc((void **)&s->fix.slot, sizeof(int) * np));
+    CREATE_TRY(cudaMalloc((void **)&s->fix.Fh, sizeof(float) * np * dim * dim));
+    CREATE_TRY(cudaMalloc((void **)&s->fix.Jp, sizeof(float) * np));
+    CREATE_TRY(cudaMemsetAsync(s->fix.count, 0, sizeof(int), s->stream));
+  }
   CREATE_TRY(cudaMalloc((void **)&s->err_d, 2 * sizeof(int) * (size_t)nscenes));
   CREATE_TRY(cudaMallocHost((void **)&s->err_h, 2 * sizeof(int) * (size_t)nscenes));
   CREATE_TRY(cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)nscenes, s->stream));
@@ -962,9 +986,9 @@ nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
       phase(s, NCLR_PHASE_G2P2G, 1, [&] {
         e = batch ? mpm::launch_small_batch<D>(s->ps[s->cur], s->scenes_d, s->cta_scene,
                                                s->group_first, s->G, s->V, s->flags, k, s->err_d,
-                                               s->bar, s->ref, ctas, s->stream)
+                                               s->bar, s->ref, ctas, s->stream, s->bar_test)
                   : mpm::launch_small_steps<D>(s->ps[s->cur], s->P0(), s->G, s->V, k, s->err_d,
-                                               s->bar, s->ref, ctas, s->stream);
+                                               s->bar, s->ref, ctas, s->stream, s->bar_test);
       });
     });
     if (e != cudaSuccess) return fail(s, NCLR_ERR_CUDA, std::string("small-scene launch: ") + cudaGetErrorString(e));
@@ -1085,8 +1109,16 @@ nclr_status nclr_advance(nclr_sim *s, int64_t nsteps) {
     if ((e & mpm::kErrOutOfRange) && first < 0) first = i;
   }
   for (int i = 0; i < s->nscenes; ++i)
-    if (s->err_h[2 * i] & mpm::kErrBarrier)
+    if (s->err_h[2 * i] & mpm::kErrBarrier) {
+      // Every CTA left the launch at the barrier that ran out: the accumulator may hold a
+      // partial P2G, so clear it (the next call starts a fresh P2G); the particle state is that
+      // of a step left half done, for the caller to replace.
+      CUDA_TRY(s, cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)s->total_nodes, s->stream));
+      CUDA_TRY(s, cudaMemsetAsync(s->flags, mpm::kFlagVNonzeroBit, (size_t)s->total_blocks, s->stream));
+      CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+      s->acc_valid = false;
       return fail(s, NCLR_ERR_CUDA, "the small-scene kernel's grid barrier ran out of time");
+    }
   if (first >= 0)
     return fail(s, NCLR_ERR_OUT_OF_RANGE,
                 "a particle's stencil left the grid (the reference's vector::at throws "
@@ -1278,6 +1310,14 @@ nclr_status nclr_profile_get(const nclr_sim *s, int which, double *total_ms, int
   return NCLR_OK;
 }
 
+nclr_status nclr_debug_set_barrier(nclr_sim *s, unsigned extra_arrivals, unsigned spin_limit) {
+  if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
+  s->bar_test.extra = extra_arrivals;
+  s->bar_test.spins = spin_limit ? spin_limit : mpm::kBarrierSpinsDefault;
+  drop_graphs(s);  // captured launches hold the old barrier arguments
+  return NCLR_OK;
+}
+
 nclr_status nclr_profile_reset(nclr_sim *s) {
   if (!s) return fail(nullptr, NCLR_ERR_INVALID, "sim is NULL");
   for (int i = 0; i < NCLR_NUM_PHASES; ++i) {
@@ -1306,10 +1346,11 @@ void nclr_destroy(nclr_sim *s) { release(s); }
 struct nclr_rollout {
   nclr_sim *sim = nullptr;
   int dim = 0;
+  int model = NCLR_JELLY;
   int64_t n = 0, nsteps = 0, nodes = 0;
   int every = 0, nseg = 0;
   float E = 0.0f, nu = 0.0f;
-  size_t rowf = 0;            // floats of one state: x, v, F, C rows
+  size_t rowf = 0;            // floats of one state: x, v, F, C rows, then Jp
   float *ckpt = nullptr;      // nseg states
   float *seg[2] = {nullptr, nullptr};     // every + 1 states of a recorded segment
   float4 *grids[2] = {nullptr, nullptr};  // `every` updated grids of that segment
@@ -1330,12 +1371,16 @@ struct nclr_rollout {
   bool have_forward = false;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   float fwd_ms = 0.0f, bwd_ms = 0.0f;
+  // profiling (the simulation's opt.profile): four events per reverse step, folded into the
+  // simulation's phase totals once the backward has drained
+  std::vector<cudaEvent_t> rev_events;
   std::string error;
 
   float *x(float *st) const { return st; }
   float *v(float *st) const { return st + n * dim; }
   float *F(float *st) const { return st + 2 * n * dim; }
   float *C(float *st) const { return st + 2 * n * dim + n * dim * dim; }
+  float *Jp(float *st) const { return st + 2 * n * dim + 2 * n * dim * dim; }
   float *state(float *base, int64_t i) const { return base + (size_t)i * rowf; }
 };
 
@@ -1389,6 +1434,7 @@ void rollout_release(nclr_rollout *r) {
   cudaFree(r->ones);
   for (auto e : r->ev)
     if (e) cudaEventDestroy(e);
+  for (auto e : r->rev_events) cudaEventDestroy(e);
   if (r->sim) nclr_destroy(r->sim);
   delete r;
 }
@@ -1405,12 +1451,12 @@ void set_material(nclr_sim *s, float E, float nu) {
 
 // Loads a state (rows) into the simulation; the next advance() starts from it.
 nclr_status load_state(nclr_rollout *r, float *st) {
-  R_SIM(r, nclr_set_particles_device(r->sim, r->x(st), r->v(st), r->F(st), r->C(st), r->ones));
+  R_SIM(r, nclr_set_particles_device(r->sim, r->x(st), r->v(st), r->F(st), r->C(st), r->Jp(st)));
   return NCLR_OK;
 }
 
 nclr_status save_state(nclr_rollout *r, float *st) {
-  R_SIM(r, nclr_get_particles_device(r->sim, r->x(st), r->v(st), r->F(st), r->C(st), nullptr));
+  R_SIM(r, nclr_get_particles_device(r->sim, r->x(st), r->v(st), r->F(st), r->C(st), r->Jp(st)));
   return NCLR_OK;
 }
 
@@ -1430,7 +1476,7 @@ nclr_status record_segment(nclr_rollout *r, int L, int buf) {
   for (int i = 0; i < L; ++i) {
     const bool sort = sort_due(s);
     float *st = r->state(r->seg[buf], i + 1);
-    s->record = mpm::Record{r->x(st), r->v(st), r->F(st), r->C(st)};  // written by the step
+    s->record = mpm::Record{r->x(st), r->v(st), r->F(st), r->C(st), r->Jp(st)};  // by the step
     enqueue_step(s, sort, kFinalWithP2G);
     s->record = mpm::Record{};
     if (sort) s->steps_since_sort = 0;
@@ -1452,27 +1498,37 @@ nclr_status nclr_rollout_create(nclr_rollout **out, int dim, int64_t n, const fl
                                 const float *mass, const float *volume, int res, float dt,
                                 float gravity, int64_t nsteps, int checkpoint_every,
                                 const nclr_options *opt) {
+  return nclr_rollout_create_model(out, dim, n, x0, mass, volume, NCLR_JELLY, res, dt, gravity,
+                                   nsteps, checkpoint_every, opt);
+}
+
+nclr_status nclr_rollout_create_model(nclr_rollout **out, int dim, int64_t n, const float *x0,
+                                      const float *mass, const float *volume, int model, int res,
+                                      float dt, float gravity, int64_t nsteps,
+                                      int checkpoint_every, const nclr_options *opt) {
   if (!out) return NCLR_ERR_INVALID;
   *out = nullptr;
   g_create_error.clear();
+  if (model < NCLR_SNOW || model > NCLR_LIQUID) return fail(nullptr, NCLR_ERR_INVALID, "unknown material model");
   if (nsteps < 1 || checkpoint_every < 1) return fail(nullptr, NCLR_ERR_INVALID, "nsteps and checkpoint_every must be >= 1");
   if (n < 1 || !x0) return fail(nullptr, NCLR_ERR_INVALID, "a rollout needs particles");
   nclr_rollout *r = new (std::nothrow) nclr_rollout();
   if (!r) return fail(nullptr, NCLR_ERR_INVALID, "out of host memory");
   nclr_status st = nclr_create(&r->sim, dim, n, x0, nullptr, nullptr, nullptr, nullptr, mass, volume,
-                               nullptr, NCLR_JELLY, res, dt, 1e4f, 0.2f, gravity, opt);
+                               nullptr, model, res, dt, 1e4f, 0.2f, gravity, opt);
   if (st != NCLR_OK) {
     delete r;
     return st;
   }
   nclr_sim *s = r->sim;
   r->dim = dim;
+  r->model = model;
   r->n = n;
   r->nsteps = nsteps;
   r->every = (int)std::min<int64_t>(checkpoint_every, nsteps);
   r->nseg = (int)((nsteps + r->every - 1) / r->every);
   r->nodes = s->P0().nodes;
-  r->rowf = (size_t)n * (2 * dim + 2 * dim * dim);
+  r->rowf = (size_t)n * (2 * dim + 2 * dim * dim + 1);
   auto bail = [&](const std::string &m) {
     g_create_error = m;
     rollout_release(r);
@@ -1547,6 +1603,9 @@ static nclr_status rollout_forward(nclr_rollout *r, const float *x0, const float
   R_TRY(r, cudaMemcpyAsync(r->v(c0), v0, vec, cudaMemcpyDeviceToDevice, s->stream));
   R_TRY(r, cudaMemcpyAsync(r->F(c0), F0, mat, cudaMemcpyDeviceToDevice, s->stream));
   R_TRY(r, cudaMemcpyAsync(r->C(c0), C0, mat, cudaMemcpyDeviceToDevice, s->stream));
+  // Jp starts at 1, as Particle<dim> sets it (src/nclr.h:46-47)
+  R_TRY(r, cudaMemcpyAsync(r->Jp(c0), r->ones, sizeof(float) * (size_t)r->n,
+                           cudaMemcpyDeviceToDevice, s->stream));
   R_TRY(r, cudaEventRecord(r->ev[0], s->stream));
   nclr_status st = load_state(r, c0);
   if (st != NCLR_OK) return st;
@@ -1605,6 +1664,7 @@ static nclr_status rollout_backward(nclr_rollout *r, const float *gxT, const flo
   R_TRY(r, seed(r->v(a), gvT, vec));
   R_TRY(r, seed(r->F(a), gFT, mat));
   R_TRY(r, seed(r->C(a), gCT, mat));
+  R_TRY(r, seed(r->Jp(a), nullptr, sizeof(float) * (size_t)n));  // nothing depends on Jp_T
   R_TRY(r, cudaMemsetAsync(r->gml, 0, 2 * sizeof(double), s->stream));
   mpm::RowModuli rm;
   if (r->per_particle) {
@@ -1616,6 +1676,16 @@ static nclr_status rollout_backward(nclr_rollout *r, const float *gxT, const flo
   R_TRY(r, cudaMemsetAsync(s->err_d, 0, 2 * sizeof(int) * (size_t)s->nscenes, s->stream));
   const Params &P = s->P0();
   bool used[2] = {false, false};
+  const bool prof = s->opt.profile != 0;
+  int64_t rstep = 0;  // reverse steps enqueued so far
+  if (prof && r->rev_events.size() < 4 * (size_t)r->nsteps) {
+    const size_t want = 4 * (size_t)r->nsteps;
+    while (r->rev_events.size() < want) {
+      cudaEvent_t e = nullptr;
+      R_TRY(r, cudaEventCreate(&e));
+      r->rev_events.push_back(e);
+    }
+  }
   for (int sg = r->nseg - 1; sg >= 0; --sg) {
     const int64_t t0 = (int64_t)sg * r->every;
     const int L = (int)std::min<int64_t>(r->every, r->nsteps - t0);
@@ -1634,13 +1704,17 @@ static nclr_status rollout_backward(nclr_rollout *r, const float *gxT, const flo
     R_TRY(r, cudaStreamWaitEvent(r->rev, r->recorded[buf], 0));
     for (int i = L - 1; i >= 0; --i) {
       float *st_t = r->state(r->seg[buf], i), *st_n = r->state(r->seg[buf], i + 1);
+      cudaEvent_t *evs = prof ? r->rev_events.data() + 4 * (size_t)rstep : nullptr;
       dispatch_dim(D, [&](auto dc) {
         constexpr int DD = decltype(dc)::value;
-        mpm::launch_adjoint_step<DD>(n, r->x(st_t), r->v(st_t), r->F(st_t), r->C(st_t), r->C(st_n),
-                                     r->mass, r->vol, r->grids[buf] + (size_t)i * r->nodes, P,
-                                     s->ref, r->x(a), r->v(a), r->F(a), r->C(a), r->x(b), r->v(b),
-                                     r->F(b), r->C(b), r->VB, r->GB, r->gml, rm, r->err, r->rev);
+        mpm::launch_adjoint_step<DD>(n, r->x(st_t), r->v(st_t), r->F(st_t), r->C(st_t),
+                                     r->Jp(st_t), r->C(st_n), r->mass, r->vol,
+                                     r->grids[buf] + (size_t)i * r->nodes, P, s->ref, r->x(a),
+                                     r->v(a), r->F(a), r->C(a), r->Jp(a), r->x(b), r->v(b),
+                                     r->F(b), r->C(b), r->Jp(b), r->VB, r->GB, r->gml, rm, r->err,
+                                     r->rev, evs);
       });
+      ++rstep;
       std::swap(a, b);
     }
     R_TRY(r, cudaEventRecord(r->reversed[buf], r->rev));
@@ -1666,6 +1740,19 @@ static nclr_status rollout_backward(nclr_rollout *r, const float *gxT, const flo
   R_TRY(r, cudaEventRecord(r->ev[1], s->stream));
   R_TRY(r, cudaEventSynchronize(r->ev[1]));
   cudaEventElapsedTime(&r->bwd_ms, r->ev[0], r->ev[1]);
+  if (prof) {  // the reverse kernels of every step, and the recomputation's forward kernels
+    for (int64_t k = 0; k < rstep; ++k) {
+      const cudaEvent_t *e4 = r->rev_events.data() + 4 * (size_t)k;
+      const int phases[3] = {NCLR_PHASE_ADJ_G2P, NCLR_PHASE_ADJ_GRID, NCLR_PHASE_ADJ_P2G};
+      for (int j = 0; j < 3; ++j) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, e4[j], e4[j + 1]) == cudaSuccess) s->prof_ms[phases[j]] += ms;
+        // adj_g2p and adj_p2g do not launch without particles; n >= 1 in a rollout
+        s->prof_launches[phases[j]] += 1;
+      }
+    }
+    collect_profile(s);
+  }
   // mu_0 = E / (2 (1 + nu)), lambda_0 = E nu / ((1 + nu)(1 - 2 nu)) (src/nclr.h:77-78)
   const double E = r->E, nu = r->nu;
   const double dmu_dE = 1.0 / (2.0 * (1.0 + nu)), dmu_dnu = -E / (2.0 * (1.0 + nu) * (1.0 + nu));
@@ -1692,6 +1779,17 @@ nclr_status nclr_rollout_backward_moduli(nclr_rollout *r, const float *gxT, cons
                                          float *gnu) {
   return rollout_backward(r, gxT, gvT, gFT, gCT, gx0, gv0, gF0, gC0, nullptr, nullptr, true, gE,
                           gnu);
+}
+
+nclr_status nclr_rollout_profile_get(const nclr_rollout *r, int phase, double *total_ms,
+                                     int64_t *launches) {
+  if (!r) return NCLR_ERR_INVALID;
+  return nclr_profile_get(r->sim, phase, total_ms, launches);
+}
+
+nclr_status nclr_rollout_profile_reset(nclr_rollout *r) {
+  if (!r) return NCLR_ERR_INVALID;
+  return nclr_profile_reset(r->sim);
 }
 
 nclr_status nclr_rollout_timing(const nclr_rollout *r, double *forward_ms, double *backward_ms) {

@@ -13,7 +13,13 @@
 // device code is loaded on a GPU and held by every GPU that loads it until the process exits.
 // Every call on a device shares it and it keeps the last call's contents, so each call clears
 // it first; calls whose work overlaps on the GPU (different streams or threads at once) race
-// on it and must be serialised by the caller.
+// on it and must be serialised by the caller (nothing here serialises them).
+//
+// The transfer uses the reference's fixed-corotated stress and one material, E and nu for all
+// particles; it takes no options.  The physics mode does not matter here: the diag(1,1,0)
+// identity of src/nclr_math.h:13-19 and the 2D SVD sign fix enter only G2P, so the grid equals
+// grid() after one advance() under either mode.
+#include <cuda.h>  // CUcontext / CUresult types only: the two driver calls come through the runtime
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -32,11 +38,47 @@ namespace {
 constexpr int64_t kNoallocMaxNodes = NCLR_NOALLOC_MAX_NODES;
 constexpr int kMaxDevices = 64;
 
-// Host-side device addresses of the two symbols, looked up once per device.  In host code
-// the names g_noalloc_grid / g_noalloc_status are host-side stand-ins, not device addresses.
-std::mutex g_setup_mutex;
-float4 *g_grid_ptr[kMaxDevices] = {};
-int *g_status_ptr[kMaxDevices] = {};
+// Host-side device addresses of the two symbols, looked up once per device and context.  In
+// host code the names g_noalloc_grid / g_noalloc_status are host-side stand-ins, not device
+// addresses.  A context that is destroyed (cudaDeviceReset, or a caller's own context torn
+// down) takes the module and its addresses with it, so each entry remembers the unique id of
+// the context it was looked up in, and a call in another context looks the addresses up again.
+struct DeviceScratch {
+  unsigned long long ctx_id;  // 0: no entry
+  float4 *grid;
+  int *status;
+};
+std::mutex g_setup_mutex;  // guards g_scratch and the driver entry points (not the GPU work)
+DeviceScratch g_scratch[kMaxDevices] = {};
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+bool g_driver_looked_up = false;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Unique id (over the process's life) of the calling thread's current context, 0 when there is
+// none yet or the driver cannot say.  Called with g_setup_mutex held.
+unsigned long long current_context_id() {
+  if (!g_driver_looked_up) {
+    g_driver_looked_up = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      g_ctx_get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      g_ctx_get_id = (CtxGetIdFn)f;
+  }
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // Where the current call reports its message (the caller's buffer, may be null).
 thread_local char *g_msg = nullptr;
@@ -82,7 +124,7 @@ __global__ void __launch_bounds__(128) p2g_rows_kernel(int n, const float *__res
       C.a[i][j] = Cs[((size_t)p * D + i) * D + j];
     }
   const float Jp = Jps[p], m = ms[p], vol = vols[p];
-  const Mat<D> A = fused_affine<D>(F, polar_R(F), C, Jp, m, vol, P.model,
+  const Mat<D> A = fused_affine<D>(F, stress_R<D>(F, P, P.model), C, Jp, m, vol, P.model,
                                    make_float2(P.mu0, P.lambda0), P);
   int base[D];
   float fx[D], w[3][D];
@@ -117,26 +159,34 @@ __global__ void __launch_bounds__(128) p2g_rows_kernel(int n, const float *__res
   }
 }
 
-// The device addresses of the scratch symbols on the current device (looked up on the first
-// call on that device).
+// The device addresses of the scratch symbols on the current device, looked up on the first
+// call in the current context of that device (and again after that context was replaced).
 nclr_status scratch_for_current_device(int *device, float4 **grid, int **status) {
   cudaError_t e = cudaGetDevice(device);
   if (e != cudaSuccess) return noalloc_fail(NCLR_ERR_NO_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (*device < 0 || *device >= kMaxDevices) return noalloc_fail(NCLR_ERR_INVALID, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_grid_ptr[*device]) {
+  DeviceScratch &ds = g_scratch[*device];
+  const unsigned long long id = current_context_id();
+  if (id == 0 || ds.ctx_id != id) {
     void *gp = nullptr, *sp = nullptr;
-    e = cudaGetSymbolAddress(&gp, g_noalloc_grid);
+    e = cudaGetSymbolAddress(&gp, g_noalloc_grid);  // also brings up the runtime's context
     if (e != cudaSuccess)
       return noalloc_fail(NCLR_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch grid): ") + cudaGetErrorString(e));
     e = cudaGetSymbolAddress(&sp, g_noalloc_status);
     if (e != cudaSuccess)
       return noalloc_fail(NCLR_ERR_CUDA, std::string("cudaGetSymbolAddress(status): ") + cudaGetErrorString(e));
-    g_grid_ptr[*device] = (float4 *)gp;
-    g_status_ptr[*device] = (int *)sp;
+    // the context the lookup ran in (the runtime may have just created it); 0 keeps no entry,
+    // so the next call looks the addresses up again
+    ds.ctx_id = current_context_id();
+    ds.grid = (float4 *)gp;
+    ds.status = (int *)sp;
+    *grid = ds.grid;
+    *status = ds.status;
+    return NCLR_OK;
   }
-  *grid = g_grid_ptr[*device];
-  *status = g_status_ptr[*device];
+  *grid = ds.grid;
+  *status = ds.status;
   return NCLR_OK;
 }
 

@@ -9,12 +9,12 @@ void launch_g2p2g_fixed(const PState &s, const Params &P0, const float4 *V, floa
                         uint8_t *flags, const int *blocks, const int *nactive,
                         const int *bstart, const int *sparse, int *work, int *err, int next_slot,
                         bool ref, int mode, int material, int ctas, cudaStream_t st,
-                        const Record &rec) {
+                        const Record &rec, const SnowFix &fix) {
   auto go = [&](auto r, auto m, auto mat) {
     g2p2g_kernel<D, decltype(r)::value, decltype(m)::value, false, decltype(mat)::value>
         <<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D, false>(), st>>>(
             s, P0, nullptr, nullptr, V, G, flags, blocks, nactive, bstart, sparse, work, err,
-            next_slot, rec);
+            next_slot, rec, fix);
   };
   auto by_material = [&](auto r, auto m) {
     if (material == kSnow) go(r, m, std::integral_constant<int, kSnow>{});
@@ -49,5 +49,5 @@ template void g2p2g_fixed_set_smem<3>(int);
 template void launch_g2p2g_fixed<3>(const PState &, const Params &, const float4 *, float4 *,
                                     uint8_t *, const int *, const int *, const int *,
                                     const int *, int *, int *, int, bool, int, int, int,
-                                    cudaStream_t, const Record &);
+                                    cudaStream_t, const Record &, const SnowFix &);
 }  // namespace mpm

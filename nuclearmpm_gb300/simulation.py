@@ -445,6 +445,12 @@ class BatchSimulation:
         capi.check(capi.lib().nclr_stats(self._h, ctypes.byref(a), ctypes.byref(b)), self._h)
         return int(a.value), int(b.value)
 
+    def active_nodes(self) -> int:
+        """Grid nodes of all scenes with mass > 0 after the last step."""
+        a = ctypes.c_int64()
+        capi.check(capi.lib().nclr_count_active_nodes(self._h, ctypes.byref(a)), self._h)
+        return int(a.value)
+
     def profile(self) -> dict:
         out = {}
         for i, name in enumerate(capi.PHASE_NAMES):

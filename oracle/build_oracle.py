@@ -8,6 +8,10 @@ Outputs (all git-ignored, rebuilt on each machine):
   oracle/_ref/libnclr_ref.so       the reference's own src/nclr.h + src/nclr_math.h compiled
                                    in place against the Eigen-API shim in oracle/ref_shim/;
                                    only built where the reference tree exists.
+
+The reference's src/ directory is taken from the environment variable NCLR_REFERENCE_SRC;
+without it, from the read-only checkout this recipe was written against.  A missing tree
+only skips the third library.
 """
 from __future__ import annotations
 
@@ -17,7 +21,7 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_SRC = "/root/reference/src"
+REFERENCE_SRC = os.environ.get("NCLR_REFERENCE_SRC") or "/root/reference/src"
 
 
 def _cmds():

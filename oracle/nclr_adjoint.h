@@ -1,14 +1,26 @@
 // CPU ORACLE -- test infrastructure only.
 //
 // Reverse-mode derivative (adjoint) of a rollout of MPMSimulation<dim>::advance() steps for
-// the jelly material (src/nclr.h:80-337 without plasticity), restated in plain C++ on top of
-// the forward restatement in nclr_oracle.h.  It is the checker of the GPU adjoint: FP64,
-// every intermediate state and grid of the rollout kept in memory (small cases only).
+// every material (src/nclr.h:80-372: jelly, and the plasticity of snow and liquid), restated
+// in plain C++ on top of the forward restatement in nclr_oracle.h.  It is the checker of the
+// GPU adjoint: FP64, every intermediate state and grid of the rollout kept in memory (small
+// cases only).
 //
-// One step maps s_t = (x, v, F, C) to s_{t+1}; its reverse maps the adjoint of s_{t+1} to
+// One step maps s_t = (x, v, F, C, Jp) to s_{t+1}; its reverse maps the adjoint of s_{t+1} to
 // the adjoint of s_t and accumulates the adjoints of mu_0 and lambda_0:
 //   G2P    v' = sum_o W_o vg_i,  C' = 4 inv_dx sum_o W_o vg_i (o - fx)^T,  x' = x + dt v',
-//          F' = (I + dt C') F                                           (src/nclr.h:167-230)
+//          F_hat = (I + dt C') F, then per material                    (src/nclr.h:167-259)
+//            jelly   F' = F_hat
+//            snow    F_hat = U S V^T, F' = U f(S) V^T with f the clamp to [1 - 2.5e-2,
+//                    1 + 4.5e-3], Jp' = clamp(Jp det F_hat / det F', 0.6, 20)
+//            liquid  F' = I with F'_00 = J = prod S (the signed det F_hat; |det F_hat| where
+//                    the 2D sign fix is a no-op)
+//          The snow F' is a function of the singular values: with P = U^T dF_hat V it moves by
+//          U K V^T, K_ii = f'(s_i) P_ii and, off the diagonal,
+//          K_ij = (a_ij + b_ij)/2 P_ij + (a_ij - b_ij)/2 P_ji, a_ij = (f_i - f_j) / (s_i - s_j),
+//          b_ij = (f_i + f_j) / (s_i + s_j) (f' = 0 where the clamp is active); the adjoint is
+//          the same map applied to U^T F'_bar V.  Jp' depends on the s_i through
+//          prod s / prod f(s) and is constant where its own clamp is active.
 //   grid   vg = clamp(mv / m + dt g e_y) unless m = 0 or the sticky boundary zeroes the node
 //                                                                        (src/nclr.h:263-310)
 //   P2G    mv_i = sum_p W_o (m v + A dpos_o), m_i = sum_p W_o m, dpos_o = (o - fx) dx,
@@ -25,6 +37,7 @@
 // rotation is the closed form of src/nclr_math.h:80-89 and is differentiated directly.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <stdexcept>
 #include <vector>
@@ -37,7 +50,65 @@ template <typename T, int D>
 struct StepAdjoint {
   std::vector<Vec<T, D>> x, v;
   std::vector<Mat<T, D>> F, C;
+  std::vector<T> Jp;  // empty: zero
 };
+
+// The snow clamp of src/nclr.h:237-241 and its derivative.
+template <typename T>
+T snow_clamp(T s) {
+  return std::clamp(s, T(1.0 - 2.5e-2), T(1.0 + 4.5e-3));
+}
+template <typename T>
+T snow_clamp_slope(T s) {
+  return (s > T(1.0 - 2.5e-2) && s < T(1.0 + 4.5e-3)) ? T(1) : T(0);
+}
+
+// Adjoint of the snow plasticity of one particle: F_hat -> (F', Jp') given the adjoints Fb of
+// F' and Jpb of Jp'; returns the adjoint of F_hat and adds that of the incoming Jp to *Jp_bar.
+template <typename T, int D>
+Mat<T, D> snow_backward(const Mat<T, D> &Fh, T Jp, const Mat<T, D> &Fb, T Jpb, Physics mode,
+                        T *Jp_bar) {
+  Mat<T, D> U, sig, V;
+  nclr_svd<T, D>(Fh, U, sig, V, mode);
+  T s[D], f[D], fp[D];
+  for (int i = 0; i < D; ++i) {
+    s[i] = sig(i, i);
+    f[i] = snow_clamp(s[i]);
+    fp[i] = snow_clamp_slope(s[i]);
+  }
+  const Mat<T, D> Pb = mul(mul(transpose(U), Fb), V);
+  Mat<T, D> K = Mat<T, D>::constant(T(0));
+  const T tiny = T(1e-12);
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j) {
+      if (i == j) {
+        K(i, i) = fp[i] * Pb(i, i);
+        continue;
+      }
+      const T a = std::fabs(s[i] - s[j]) > tiny ? (f[i] - f[j]) / (s[i] - s[j])
+                                                : T(0.5) * (fp[i] + fp[j]);
+      const T b = std::fabs(s[i] + s[j]) > tiny ? (f[i] + f[j]) / (s[i] + s[j]) : T(0);
+      K(i, j) = T(0.5) * (a + b) * Pb(i, j) + T(0.5) * (a - b) * Pb(j, i);
+    }
+  // Jp' = clamp(r, 0.6, 20), r = Jp prod s / prod f (the det U det V factors of det F_hat and
+  // det F' cancel)
+  T ps = T(1), pf = T(1);
+  for (int i = 0; i < D; ++i) {
+    ps *= s[i];
+    pf *= f[i];
+  }
+  const T r = Jp * ps / pf;
+  if (r > T(0.6) && r < T(20.0) && Jpb != T(0)) {
+    *Jp_bar += Jpb * ps / pf;
+    for (int i = 0; i < D; ++i) {
+      T others = T(1);
+      for (int k = 0; k < D; ++k)
+        if (k != i) others *= s[k];
+      K(i, i) += Jpb * (Jp * others / pf - r * fp[i] / f[i]);
+    }
+  }
+  return mul(mul(U, K), transpose(V));
+}
 
 // d det(F) / dF
 template <typename T>
@@ -104,7 +175,6 @@ class Adjoint {
   Adjoint(std::vector<Particle<T, D>> initial, Model model, int res, T dt, T E, T nu,
           T gravity, Physics mode, int nsteps, Stress stress = Stress::kCorotated)
       : sim_(initial, model, res, dt, E, nu, gravity, mode), mode_(mode) {
-    if (model != Model::kJelly) throw std::invalid_argument("the adjoint covers jelly");
     sim_.stress_ = stress;
     states_.push_back(sim_.particles());
     for (int t = 0; t < nsteps; ++t) {
@@ -206,6 +276,7 @@ class Adjoint {
     out.v.resize(n);
     out.F.resize(n);
     out.C.resize(n);
+    out.Jp.assign(n, T(0));
     std::vector<Vec<T, D>> VB(grid.size(), Vec<T, D>::constant(T(0)));
     const Mat<T, D> I = diag_of<T, D>(T(1), mode_);
     // ---- G2P reverse ----
@@ -216,9 +287,31 @@ class Adjoint {
       Mat<T, D> M;
       for (int i = 0; i < D; ++i)
         for (int j = 0; j < D; ++j) M(i, j) = I(i, j) + dt * Cn(i, j);
-      out.F[p] = mul(transpose(M), next.F[p]);
+      // the adjoint of F_hat = M F from that of F' (and Jp'), per material
+      const T Jpb = next.Jp.empty() ? T(0) : next.Jp[p];
+      Mat<T, D> Fhb = next.F[p];
+      out.Jp[p] = Jpb;  // jelly and liquid keep Jp
+      const Model model = sim_.model_of(P[p]);
+      if (model != Model::kJelly) {
+        const Mat<T, D> Fh = mul(M, F);
+        if (model == Model::kSnow) {
+          out.Jp[p] = T(0);
+          Fhb = snow_backward<T, D>(Fh, P[p].Jp, next.F[p], Jpb, mode_, &out.Jp[p]);
+        } else {  // liquid: F'_00 = prod of the signed singular values
+          Mat<T, D> U, sig, V;
+          nclr_svd<T, D>(Fh, U, sig, V, mode_);
+          T ps = T(1);
+          for (int i = 0; i < D; ++i) ps *= sig(i, i);
+          const T dF = det(Fh);
+          const T sgn = (dF == T(0)) ? T(0) : ps / dF;  // +1, or -1 where prod s = |det|
+          const Mat<T, D> cof = cofactor(Fh);
+          for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j) Fhb(i, j) = next.F[p](0, 0) * sgn * cof(i, j);
+        }
+      }
+      out.F[p] = mul(transpose(M), Fhb);
       Mat<T, D> gC = next.C[p];
-      const Mat<T, D> gFFt = mul(next.F[p], transpose(F));
+      const Mat<T, D> gFFt = mul(Fhb, transpose(F));
       for (int i = 0; i < D; ++i)
         for (int j = 0; j < D; ++j) gC(i, j) += dt * gFFt(i, j);
       Vec<T, D> gv;
@@ -312,7 +405,16 @@ class Adjoint {
         for (int j = 0; j < D; ++j) G(i, j) = -kappa * gA(i, j);
       const Mat<T, D> &F = q.F;
       const T J = det(F);
-      const T e = T(0.3);  // jelly hardening (src/nclr.h:362-364)
+      // the hardening factor e of mu = mu_0 e, lambda = lambda_0 e (src/nclr.h:351-372)
+      const Model model = sim_.model_of(q);
+      const T e = model == Model::kSnow ? (T)std::exp(10.0 * (1.0 - (double)q.Jp))
+                                        : (model == Model::kJelly ? T(0.3) : T(1.0));
+      const T mu_b = q.mu0 < T(0) ? sim_.mu_0 : q.mu0;          // base moduli
+      const T lambda_b = q.mu0 < T(0) ? sim_.lambda_0 : q.lambda0;
+      // snow: e = exp(10 (1 - Jp)), de/dJp = -10 e; the adjoint of e is mu_0 mu_bar + ...
+      auto harden = [&](T gmu_h, T glambda_h) {
+        if (model == Model::kSnow) out.Jp[p] += (gmu_h * mu_b + glambda_h * lambda_b) * T(-10) * e;
+      };
       if (sim_.stress_ == Stress::kNeoHookean) {
         const Mat<T, D> FFt = mul(F, transpose(F));
         T trG = 0, gmu = 0;
@@ -332,6 +434,7 @@ class Adjoint {
         glambda0 += e * (trG * std::log(J));
         if (rows_mu_) (*rows_mu_)[p] += e * gmu;
         if (rows_lambda_) (*rows_lambda_)[p] += e * (trG * std::log(J));
+        harden(gmu, trG * std::log(J));
         continue;
       }
       const Mat<T, D> R = nclr_polar_R<T, D>(F, mode_);
@@ -364,6 +467,7 @@ class Adjoint {
       glambda0 += e * glambda;
       if (rows_mu_) (*rows_mu_)[p] += e * gmu;
       if (rows_lambda_) (*rows_lambda_)[p] += e * glambda;
+      harden(gmu, glambda);
     }
     return out;
   }

@@ -116,7 +116,8 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
             double *CT, const double *gx, const double *gv, const double *gF, const double *gC,
             double *gx0, double *gv0, double *gF0, double *gC0, double *gmu_glambda,
             int stress, const double *E_p, const double *nu_p, double *gmu_rows,
-            double *glambda_rows) {
+            double *glambda_rows, int model = 1, const double *Jp0 = nullptr,
+            double *JpT = nullptr, const double *gJp = nullptr, double *gJp0 = nullptr) {
   using T = double;
   std::vector<Particle<T, D>> ps((size_t)n);
   for (int64_t p = 0; p < n; ++p) {
@@ -130,13 +131,13 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
         q.F(i, j) = F0[p * D * D + i * D + j];
         q.C(i, j) = C0[p * D * D + i * D + j];
       }
-    q.Jp = 1;
+    q.Jp = Jp0 ? Jp0[p] : 1.0;
     q.mass = mass[p];
     q.volume = volume[p];
     if (E_p && nu_p) std::tie(q.mu0, q.lambda0) = lame_of<T>(E_p[p], nu_p[p]);
   }
   try {
-    Adjoint<T, D> adj(std::move(ps), Model::kJelly, res, dt, E, nu, gravity, (Physics)physics,
+    Adjoint<T, D> adj(std::move(ps), (Model)model, res, dt, E, nu, gravity, (Physics)physics,
                       nsteps, (Stress)stress);
     const auto &fin = adj.final_state();
     StepAdjoint<T, D> seed;
@@ -144,8 +145,11 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
     seed.v.resize((size_t)n);
     seed.F.resize((size_t)n);
     seed.C.resize((size_t)n);
+    seed.Jp.assign((size_t)n, 0.0);
     for (int64_t p = 0; p < n; ++p) {
       const auto &q = fin[(size_t)p];
+      if (JpT) JpT[p] = q.Jp;
+      if (gJp) seed.Jp[(size_t)p] = gJp[p];
       for (int d = 0; d < D; ++d) {
         xT[p * D + d] = q.x[d];
         vT[p * D + d] = q.v[d];
@@ -180,6 +184,7 @@ int adjoint(int physics, int64_t n, const double *x0, const double *v0, const do
           gC0[p * D * D + i * D + j] = out.C[(size_t)p](i, j);
         }
     }
+    for (int64_t p = 0; gJp0 && p < n; ++p) gJp0[p] = out.Jp[(size_t)p];
     gmu_glambda[0] = gmu;
     gmu_glambda[1] = glam;
   } catch (const std::out_of_range &) {
@@ -216,6 +221,31 @@ int oracle_adjoint(int dim, int physics, int64_t n, const double *x0, const doub
     return adjoint<3>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
                       xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress,
                       E_p, nu_p, gmu_rows, glambda_rows);
+  return 1;
+}
+
+// oracle_adjoint for any material (`model`: 0 snow, 1 jelly, 2 liquid), with the plastic
+// volume ratio Jp in the state: Jp0 the initial one (NULL: 1), JpT (may be NULL) receives the
+// final one, gJp (may be NULL = 0) is its adjoint's seed and gJp0 (may be NULL) receives the
+// adjoint of Jp0.
+int oracle_adjoint_model(int dim, int physics, int model, int64_t n, const double *x0,
+                         const double *v0, const double *F0, const double *C0,
+                         const double *Jp0, const double *mass, const double *volume, int res,
+                         double dt, double E, double nu, double gravity, int nsteps, double *xT,
+                         double *vT, double *FT, double *CT, double *JpT, const double *gx,
+                         const double *gv, const double *gF, const double *gC,
+                         const double *gJp, double *gx0, double *gv0, double *gF0,
+                         double *gC0, double *gJp0, double *gmu_glambda, int stress) {
+  if (n < 0 || res < 1 || nsteps < 0 || stress < 0 || stress > 1 || model < 0 || model > 2)
+    return 1;
+  if (dim == 2)
+    return adjoint<2>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress,
+                      nullptr, nullptr, nullptr, nullptr, model, Jp0, JpT, gJp, gJp0);
+  if (dim == 3)
+    return adjoint<3>(physics, n, x0, v0, F0, C0, mass, volume, res, dt, E, nu, gravity, nsteps,
+                      xT, vT, FT, CT, gx, gv, gF, gC, gx0, gv0, gF0, gC0, gmu_glambda, stress,
+                      nullptr, nullptr, nullptr, nullptr, model, Jp0, JpT, gJp, gJp0);
   return 1;
 }
 

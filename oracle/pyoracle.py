@@ -51,6 +51,11 @@ def _load(name: str, sub: str) -> ctypes.CDLL:
             lib.oracle_adjoint.argtypes = ([ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [_dp] * 6 +
                                            [ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int] +
                                            [_dp] * 13 + [ctypes.c_int] + [_dp] * 4)
+            lib.oracle_adjoint_model.restype = ctypes.c_int
+            lib.oracle_adjoint_model.argtypes = (
+                [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [_dp] * 7 +
+                [ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int] + [_dp] * 16 +
+                [ctypes.c_int])
         else:
             lib.ref_advance.restype = ctypes.c_int
             lib.ref_advance.argtypes = [ctypes.c_int, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -126,6 +131,28 @@ def advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-
     return s, ((gv, gm) if want_grid else None), st, counters
 
 
+def _adjoint_model(state, *, dim, res, steps, dt, E, nu, gravity, physics, seed, stress, model):
+    n, s = _prep(state, dim)
+    out = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C", "Jp")}
+    g = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C", "Jp")}
+    sd = {k: (np.ascontiguousarray(seed[k], dtype=np.float64) if k in seed else None)
+          for k in ("x", "v", "F", "C", "Jp")}
+    ml = np.zeros(2)
+    st = oracle_lib().oracle_adjoint_model(
+        dim, physics, model, n, _p(s["x"]), _p(s["v"]), _p(s["F"]), _p(s["C"]), _p(s["Jp"]),
+        _p(s["mass"]), _p(s["volume"]), res, dt, E, nu, gravity, steps, _p(out["x"]),
+        _p(out["v"]), _p(out["F"]), _p(out["C"]), _p(out["Jp"]),
+        *(None if sd[k] is None else _p(sd[k]) for k in ("x", "v", "F", "C", "Jp")),
+        _p(g["x"]), _p(g["v"]), _p(g["F"]), _p(g["C"]), _p(g["Jp"]), _p(ml), int(stress))
+    if st != 0:
+        raise RuntimeError(f"oracle adjoint failed ({st})")
+    _, _, dmu, dlam = lame(E, nu)
+    g["mu0"], g["lambda0"] = float(ml[0]), float(ml[1])
+    g["E"] = ml[0] * dmu[0] + ml[1] * dlam[0]
+    g["nu"] = ml[0] * dmu[1] + ml[1] * dlam[1]
+    return out, g
+
+
 def ref_advance(state: dict, *, dim: int, model: int, res: int = 64, dt: float = 1e-4,
                 E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, steps: int = 1):
     """The reference's own MPMSimulation<dim>::advance() (compiled against the Eigen shim)."""
@@ -178,11 +205,19 @@ def lame(E: float, nu: float):
 
 def adjoint(state: dict, *, dim: int, res: int, steps: int, dt: float = 1e-4, E: float = 1e4,
             nu: float = 0.2, gravity: float = -100.0, physics: int = REFERENCE, seed: dict,
-            stress: int = COROTATED, E_particles=None, nu_particles=None):
-    """FP64 jelly rollout and its reverse pass.  `seed` holds the final state's adjoint (keys
-    among x, v, F, C).  Returns (final state, adjoint of the initial state incl. 'E' and 'nu').
-    With E_particles / nu_particles (one value per particle), 'E' and 'nu' (and 'mu0',
-    'lambda0') are arrays: every particle's own adjoints."""
+            stress: int = COROTATED, E_particles=None, nu_particles=None, model: int = JELLY):
+    """FP64 rollout and its reverse pass.  `seed` holds the final state's adjoint (keys among
+    x, v, F, C, and Jp for the plastic materials).  Returns (final state, adjoint of the
+    initial state incl. 'E' and 'nu').  With E_particles / nu_particles (one value per particle,
+    jelly), 'E' and 'nu' (and 'mu0', 'lambda0') are arrays: every particle's own adjoints.
+    `model` other than jelly (snow, liquid) also carries Jp: the state's 'Jp' (1 if absent) is
+    the initial one, and the results hold the final 'Jp' and its initial adjoint 'Jp'."""
+    if model != JELLY or "Jp" in seed:
+        if E_particles is not None:
+            raise ValueError("per-particle moduli are covered for jelly")
+        return _adjoint_model(state, dim=dim, res=res, steps=steps, dt=dt, E=E, nu=nu,
+                              gravity=gravity, physics=physics, seed=seed, stress=stress,
+                              model=model)
     n, s = _prep(state, dim)
     out = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C")}
     g = {k: np.zeros_like(s[k]) for k in ("x", "v", "F", "C")}

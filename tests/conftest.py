@@ -13,10 +13,40 @@ FIELDS = ("x", "v", "F", "C", "Jp")
 # Error of a field = max|a - b| / max(max|b|, floor); floors are in the field's natural units
 # (positions in the unit box, velocities of one gravity step, F and Jp near 1, C of order 1)
 # so that a field that is zero up to rounding does not produce a meaningless ratio.
-# Drift over many steps: the GPU's atomic summation order and its register SVD differ from the
-# reference in the last bits; the stress term amplifies those differences step by step.
-DRIFT = {"x": 2e-5, "v": 3e-3, "F": 3e-4, "C": 1e-2, "Jp": 3e-4}
+# Drift over many steps.  The GPU's atomic summation order and its register SVD differ from
+# the reference in the last bits, and the stress term amplifies such differences step by step,
+# as it amplifies the reference's own FP32 rounding.  The bound is derived from the reference
+# itself: REF_FP32_DRIFT is the largest distance, over every step of every golden fixture's run
+# (20-101 steps; 5 for the 3D snow scene that flies apart), between the reference's own FP32
+# state and the FP64 oracle's after the same steps (measured by
+# test_oracle.py::test_drift_bound_follows_reference_fp32_drift, which keeps it current).  The
+# largest values come early in the README snow run (v at step 3, C at step 4), while the
+# velocities and C are still small next to the rounding the stiff stress amplifies.  Two FP32
+# runs can each sit that far from FP64 in opposite directions, so a bound between two of them is
+# DRIFT_FACTOR = 3 times it (2 for the two sides, 1.5 for headroom), rounded up.
+REF_FP32_DRIFT = {"x": 1.27e-6, "v": 7.73e-4, "F": 2.51e-5, "C": 2.35e-3, "Jp": 6.89e-6}
+DRIFT_FACTOR = 3.0
+DRIFT = {"x": 4e-6, "v": 2.4e-3, "F": 8e-5, "C": 7.1e-3, "Jp": 2.1e-5}
 FLOORS = {"x": 1.0, "v": 1e-2, "F": 1.0, "C": 1.0, "Jp": 1.0, "grid_v": 1e-2, "grid_m": 1e-3}
+
+
+# "FP32 class": where a case is stiffer or finer than the fixtures the drift bound was derived
+# from (per-particle moduli up to 1e5, grids of 1024, deformed full-size scenes), the GPU is
+# held to the FP32 oracle's own distance from the FP64 oracle on the same case: its distance to
+# FP64 within FP32_CLASS_FACTOR times that (or under the case's base bound), and its distance to
+# the FP32 oracle within one more multiple (the two FP32 runs sit on either side of FP64).
+FP32_CLASS_FACTOR = 2.5
+
+
+def check_fp32_class(gpu: dict, o32: dict, o64: dict, base, fields=FIELDS, what=""):
+    """Asserts the FP32-class bounds per field; `base` is a number or a per-field dict."""
+    for f in fields:
+        b = base[f] if isinstance(base, dict) else base
+        own = field_err(o32[f], o64[f], f)
+        e64 = field_err(gpu[f], o64[f], f)
+        e32 = field_err(gpu[f], o32[f], f)
+        assert e64 <= max(b, FP32_CLASS_FACTOR * own), (what, f, "vs fp64", e64, own)
+        assert e32 <= max(b, (FP32_CLASS_FACTOR + 1.0) * own), (what, f, "vs fp32", e32, own)
 
 
 def pytest_configure(config):

@@ -35,6 +35,22 @@ def small_block_3d(seed: int, res: int = 16):
     return scenes.particles(x, v)
 
 
+def multiblock_3d(seed: int, res: int = 32, cubes: int = 3, side: int = 20):
+    """Several jittered jelly-style lattices (spacing dx/2, jitter +-0.25 cell, one N(0, 0.5^2)
+    velocity per cube) on a grid of many 4^3-cell blocks: dense blocks through the shared-memory
+    tiles, thin blocks at the cubes' edges, and the block sort all take part."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / res
+    edge = side * 0.5 * dx
+    parts = []
+    for _ in range(cubes):
+        lo = rng.uniform(0.2, 0.8 - edge, size=3)
+        x = scenes.jittered_block(rng, (side,) * 3, 0.5 * dx, lo, 0.25 * dx)
+        v = np.broadcast_to(rng.normal(0.0, 0.5, size=3).astype(np.float32), x.shape)
+        parts.append(scenes.particles(x, v))
+    return scenes.concat(*parts)
+
+
 def emit(name: str, state: dict, *, dim: int, model: int, res: int, steps: list[int],
          E: float = 1e4, nu: float = 0.2, gravity: float = -100.0, dt: float = 1e-4):
     out = {k: np.asarray(v, dtype=np.float32) for k, v in state.items()}
@@ -70,6 +86,13 @@ def main():
     emit("readme_liquid", readme, dim=2, model=scenes.LIQUID, res=64, steps=[1, 100])
     for model, tag in ((scenes.SNOW, "snow"), (scenes.JELLY, "jelly"), (scenes.LIQUID, "liquid")):
         emit(f"block3d_{tag}", small_block_3d(7), dim=3, model=model, res=16, steps=[1, 20, 21])
+    # many blocks: 3 cubes of 20^3 particles on a 32^3 grid (24,000 particles).  Jelly for
+    # 100 steps; snow for 5: under the reference's diag(1,1,0) the clamp lifts sigma_3 to 0.975
+    # every step, Jp drops to its floor and the scene flies apart (speeds ~280 after 5 steps),
+    # after which FP32 and FP64 runs of the reference's own step diverge by O(1) within 20 steps
+    emit("multiblock3d_jelly", multiblock_3d(11), dim=3, model=scenes.JELLY, res=32,
+         steps=[1, 100])
+    emit("multiblock3d_snow", multiblock_3d(11), dim=3, model=scenes.SNOW, res=32, steps=[1, 5])
     # solver.cpp's defaults (E=1000, nu=0.3) on a jelly cube, 2D
     cube = scenes.particles(scenes.cube(2, 25, 0.3, 0.5))
     emit("cli_cube_jelly", cube, dim=2, model=scenes.JELLY, res=64, steps=[1, 50], E=1000.0,

@@ -1,5 +1,7 @@
-"""GPU adjoint of jelly rollouts (nclr_rollout_* / nuclearmpm_gb300.autograd) against the FP64
-CPU adjoint of the oracle and FP64 finite differences of the oracle's forward step.
+"""GPU adjoint of rollouts (nclr_rollout_* / nuclearmpm_gb300.autograd) against the FP64 CPU
+adjoint of the oracle and FP64 finite differences of the oracle's forward step: jelly, and the
+plastic materials (the snow clamp with its Jp update and Jp-dependent hardening, the liquid
+reset).
 
 Bounds: the GPU runs FP32 forward and FP32 adjoint kernels (FP64 only for the E / nu sums),
 so its gradients sit within 1e-3 (normwise, relative to each field's largest entry) of the
@@ -24,10 +26,11 @@ def setup(dim, res, n, physics, seed=0):
     return s
 
 
-def gpu_grads(s, dim, res, steps, physics, every, seed_fn, E=1e4, nu=0.2, stress=0):
+def gpu_grads(s, dim, res, steps, physics, every, seed_fn, E=1e4, nu=0.2, stress=0,
+              model=scenes.JELLY):
     from nuclearmpm_gb300.autograd import Rollout
     roll = Rollout(s["x"], res=res, steps=steps, checkpoint_every=every, physics=physics,
-                   stress_model=stress)
+                   stress_model=stress, model=model)
     dev = torch.device("cuda", 0)
     x0 = torch.tensor(s["x"], device=dev, requires_grad=True)
     v0 = torch.tensor(s["v"], device=dev, requires_grad=True)
@@ -148,3 +151,75 @@ def test_gpu_per_particle_moduli_gradients_match_fp64_adjoint(oracle, dim, res, 
     _, o = oracle.adjoint(s, seed={"x": seed}, **kw)
     for f in ("x", "v", "F", "C", "E", "nu"):
         assert rel(g[f], o[f]) <= GRAD_TOL, (f, rel(g[f], o[f]))
+
+
+def plastic_setup(dim, res, n, physics, seed=0):
+    """The jittered block with F perturbed by 2%: singular values on both sides of the snow
+    clamp's bounds, so that clamped and free ones both enter."""
+    s = setup(dim, res, n, physics, seed)
+    rng = np.random.default_rng(seed + 7)
+    s["F"] = (s["F"] + rng.normal(0, 0.02, size=s["F"].shape)).astype(np.float32)
+    return s
+
+
+@pytest.mark.parametrize("dim,res,steps,n", [(2, 32, 30, 1024), (3, 16, 8, 512)])
+@pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
+@pytest.mark.parametrize("model", [scenes.SNOW, scenes.LIQUID])
+def test_gpu_plastic_adjoint_matches_fp64_adjoint(oracle, dim, res, steps, n, physics, model):
+    """Snow and liquid rollouts: every gradient (initial x, v, F, C; E and nu) against the FP64
+    CPU adjoint of the same rollout."""
+    if dim == 3 and physics == scenes.REFERENCE and model == scenes.LIQUID:
+        pytest.skip("3D liquid under the reference physics resets F to diag(J, 1, 0), whose "
+                    "polar rotation is not unique: the step is not differentiable there")
+    s = plastic_setup(dim, res, n, physics)
+    rng = np.random.default_rng(3)
+    kw = dict(dim=dim, res=res, steps=steps, physics=physics, model=model)
+    fwd, _ = oracle.adjoint(s, seed={}, **kw)
+    targets = (fwd["x"] + rng.normal(0, 1e-3, size=fwd["x"].shape)).astype(np.float32)
+    g = gpu_grads(s, dim, res, steps, physics, every=7, seed_fn=point_loss(targets), model=model)
+    seed = 2 * (g["xT"].astype(np.float64) - targets)  # the GPU's own final state
+    _, o = oracle.adjoint(s, seed={"x": seed}, **kw)
+    for f in ("x", "v", "F", "C"):
+        assert rel(g[f], o[f]) <= GRAD_TOL, (f, rel(g[f], o[f]))
+    for p in ("E", "nu"):
+        assert abs(g[p] - o[p]) <= GRAD_TOL * abs(o[p]), (p, g[p], o[p])
+
+
+def test_gpu_snow_gradients_match_finite_differences(oracle):
+    """The reduced 2D case in snow: 1,024 particles, 32^2 grid, 50 steps, a deformation-dependent
+    loss; directional derivatives of the initial velocities and positions and the E / nu
+    derivatives against FP64 central differences of the oracle's forward rollout (steps small
+    enough that no particle's clamp switches inside them: the loss is piecewise smooth)."""
+    dim, res, steps, n = 2, 32, 50, 1024
+    s = plastic_setup(dim, res, n, scenes.CORRECTED, seed=9)
+    fwd, _, st, _ = oracle.advance(s, dim=dim, model=scenes.SNOW, res=res, steps=steps,
+                                   fp64=True, physics=scenes.CORRECTED, want_grid=False)
+    assert st == 0
+    targets = fwd["x"] + np.random.default_rng(5).normal(0, 1e-3, size=fwd["x"].shape)
+    g = gpu_grads(s, dim, res, steps, scenes.CORRECTED, every=10,
+                  seed_fn=point_loss(targets.astype(np.float32)), model=scenes.SNOW)
+
+    def loss64(st, E=1e4, nu=0.2):
+        out, _, status, _ = oracle.advance(st, dim=dim, model=scenes.SNOW, res=res, steps=steps,
+                                           fp64=True, physics=scenes.CORRECTED, E=E, nu=nu,
+                                           want_grid=False)
+        assert status == 0
+        return float(((out["x"] - targets) ** 2).sum())
+
+    rng = np.random.default_rng(11)
+    s64 = {k: np.asarray(v, np.float64) for k, v in s.items()}
+    for field, h in (("v", 1e-7), ("x", 1e-8)):
+        for _ in range(3):
+            dirn = rng.normal(size=s64[field].shape)
+            sp, sm = dict(s64), dict(s64)
+            sp[field] = s64[field] + h * dirn
+            sm[field] = s64[field] - h * dirn
+            fd = (loss64(sp) - loss64(sm)) / (2 * h)
+            ad = float((g[field].astype(np.float64) * dirn).sum())
+            assert abs(ad - fd) <= GRAD_TOL * abs(fd), (field, ad, fd)
+    for name, h in (("E", 1e-2), ("nu", 1e-7)):
+        kp, km = {"E": 1e4, "nu": 0.2}, {"E": 1e4, "nu": 0.2}
+        kp[name] += h
+        km[name] -= h
+        fd = (loss64(s64, **kp) - loss64(s64, **km)) / (2 * h)
+        assert abs(float(g[name]) - fd) <= GRAD_TOL * abs(fd), (name, float(g[name]), fd)

@@ -1,25 +1,28 @@
 """The measured workloads at their full sizes, on the GPU.
 - The 1M-particle 3D jelly scene, the same in snow, and the 4.19M-particle liquid + snow
-  scene: one step against the FP32 oracle, run on all host cores.
+  scene, under both physics modes: one step from the scene against the FP32 oracle and against
+  the FP64 oracle, both run on all host cores, within 1e-5 for every field and the grid; one
+  step from the state after 10 steps (F, C and Jp deformed), where FP32 itself lands further
+  from FP64 in v and C, within 1e-5 or the FP32 class (conftest.check_fp32_class).
 - The same two scenes conserve their total mass, and with gravity off their total momentum,
   through a step.
 - The 256-scene batch: one step of the batch equals every scene stepped alone.
 
-Bound for a step against the oracle: 5e-5 (x, v, F, C, Jp and the grid), as for the seeded
-random states of test_gpu_step.py.  The sizes need a few GB of device memory and a few
-seconds of host time.
+The sizes need a few GB of device memory and a few seconds of host time per case.
 """
 import os
 
 import numpy as np
 import pytest
 
-from conftest import DRIFT, FIELDS, field_err
+from conftest import DRIFT, FIELDS, check_fp32_class, field_err
 from nuclearmpm_gb300 import BatchSimulation, MPMSimulation, scenes
 
 pytestmark = pytest.mark.gpu
 
-STEP_BOUND = 5e-5
+# One step at the measured sizes, normwise per field (conftest.field_err), against the FP32
+# and the FP64 oracle alike.  Measured on GB300: at most 3e-6 against either.
+STEP_BOUND = 1e-5
 THREADS = max(1, os.cpu_count() or 1)
 
 
@@ -33,23 +36,42 @@ def gpu_step(state, model, res, steps=1, material=None, **kw):
     return out, grid
 
 
-@pytest.mark.parametrize("scene", ["jelly_1M", "snow_1M", "mixed_4M"])
-def test_full_size_step_matches_oracle(oracle, scene):
+def full_scene(scene, physics):
     if scene == "jelly_1M":
-        s, mat, model, res = scenes.jelly_cubes_3d(seed=0, res=128), None, scenes.JELLY, 128
-    elif scene == "snow_1M":  # the same geometry in snow
-        s, mat, model, res = scenes.jelly_cubes_3d(seed=0, res=128), None, scenes.SNOW, 128
+        return scenes.jelly_cubes_3d(seed=0, res=128, physics=physics), None, scenes.JELLY, 128
+    if scene == "snow_1M":  # the same geometry in snow
+        return scenes.jelly_cubes_3d(seed=0, res=128, physics=physics), None, scenes.SNOW, 128
+    s, mat = scenes.liquid_snow_boxes_3d(seed=0, res=256, physics=physics)
+    return s, mat, scenes.SNOW, 256
+
+
+@pytest.mark.parametrize("start", ["scene", "after_10_steps"])
+@pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
+@pytest.mark.parametrize("scene", ["jelly_1M", "snow_1M", "mixed_4M"])
+def test_full_size_step_matches_oracle(oracle, scene, physics, start):
+    s, mat, model, res = full_scene(scene, physics)
+    if start == "after_10_steps":  # a deformed state: the GPU's own after 10 steps
+        run, _ = gpu_step(s, model, res, steps=10, material=mat, physics=physics)
+        s = {**run, "mass": s["mass"], "volume": s["volume"]}
+    out, grid = gpu_step(s, model, res, material=mat, physics=physics)
+    out = dict(out, grid_v=grid.velocity, grid_m=grid.mass)
+    refs = {}
+    for fp64 in (False, True):
+        ref, og, st, _ = oracle.advance(s, dim=3, model=model, res=res, steps=1, material=mat,
+                                        threads=THREADS, physics=physics, fp64=fp64)
+        assert st == 0
+        refs[fp64] = dict(ref, grid_v=og[0], grid_m=og[1])
+    fields = FIELDS + ("grid_v", "grid_m")
+    if start == "scene":
+        for fp64, ref in refs.items():
+            for f in fields:
+                e = field_err(out[f], ref[f], f)
+                assert e <= STEP_BOUND, (fp64, f, e)
     else:
-        s, mat = scenes.liquid_snow_boxes_3d(seed=0, res=256)
-        model, res = scenes.SNOW, 256
-    out, grid = gpu_step(s, model, res, material=mat)
-    ref, og, st, _ = oracle.advance(s, dim=3, model=model, res=res, steps=1, material=mat,
-                                    threads=THREADS)
-    assert st == 0
-    for f in FIELDS:
-        assert field_err(out[f], ref[f], f) <= STEP_BOUND, (f, field_err(out[f], ref[f], f))
-    assert field_err(grid.velocity, og[0], "grid_v") <= STEP_BOUND
-    assert field_err(grid.mass, og[1], "grid_m") <= STEP_BOUND
+        # from a deformed state the stiff stress amplifies FP32 rounding of the polar rotation
+        # (F - R cancels), and the FP32 oracle itself lands up to a few 1e-5 from FP64 in v
+        # and C: those fields are held to the FP32 class, the rest to 1e-5
+        check_fp32_class(out, refs[False], refs[True], STEP_BOUND, fields=fields, what=scene)
 
 
 @pytest.mark.parametrize("scene", ["jelly_1M", "mixed_4M"])

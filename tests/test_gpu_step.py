@@ -4,8 +4,10 @@ own outputs (tests/golden/, produced by the reference's src/nclr.h) and the CPU 
 Tolerances (FP32; error = max|gpu - ref| / max(max|ref|, floor), floors in conftest.FLOORS):
   * one step from a reference scene: every field (x, v, F, C, Jp) and the grid within 1e-5 of
     the reference's own output;
-  * 100 steps (2D) / 20 steps (3D): the drift bounds below, of the order of the reference's
-    own FP32-vs-FP64 drift over the same steps;
+  * the later snapshots (100 steps in 2D and on the multi-block 3D jelly scene, 20 on the
+    small 3D blocks, 5 on the multi-block 3D snow scene): conftest.DRIFT, three times the
+    reference's own largest FP32-vs-FP64 distance over such runs; and at every snapshot the
+    GPU's distance to the FP64 oracle within 4x the FP32 one (or under 1e-6);
   * seeded random states whose F is a rotation perturbed by 1%: the stress 2 mu (F - R) F^T
     cancels about two digits there, so every FP32 implementation (the reference's included)
     lands 1e-5-ish from FP64.  The GPU's error against the FP64 oracle must stay within 2.5x
@@ -14,7 +16,8 @@ Tolerances (FP32; error = max|gpu - ref| / max(max|ref|, floor), floors in conft
 import numpy as np
 import pytest
 
-from conftest import DRIFT, FIELDS, field_err, golden_names, load_golden, random_state, state_at
+from conftest import (DRIFT, FIELDS, check_fp32_class, field_err, golden_names, load_golden,
+                      random_state, state_at)
 from nuclearmpm_gb300 import MPMSimulation, OutOfRange, scenes
 
 pytestmark = pytest.mark.gpu
@@ -45,9 +48,18 @@ def run_gpu(state, params, steps, **kw):
 PATHS = {"small": {"small_scene_max": 1 << 30}, "tile": {"small_scene_max": 0}}
 
 
+# At every snapshot of a golden run, the GPU's distance to the FP64 oracle must stay within
+# this factor of the FP32 distance to it (the reference's own, or the FP32 oracle's where
+# larger), or under FP64_FLOOR.  The largest measured ratio is 3.5, on the small-scene path for
+# the 3D snow blocks (reference physics, where the scene flies apart): that path adds every
+# particle's contribution to the grid with global atomics, in whatever order they arrive.
+GOLDEN_FP64_FACTOR = 4.0
+FP64_FLOOR = 1e-6
+
+
 @pytest.mark.parametrize("path", sorted(PATHS))
 @pytest.mark.parametrize("name", golden_names())
-def test_matches_reference_goldens(name, path):
+def test_matches_reference_goldens(oracle, name, path):
     z, state, params, steps = load_golden(name)
     first = steps[0]
     out, grid = run_gpu(state, params, first, **PATHS[path])
@@ -55,10 +67,22 @@ def test_matches_reference_goldens(name, path):
         assert field_err(out[f], z[f"{f}@{first}"], f) <= ONE_STEP[f], f
     assert field_err(grid.velocity, z["grid_v"], "grid_v") <= GRID_ONE_STEP["grid_v"]
     assert field_err(grid.mass, z["grid_m"], "grid_m") <= GRID_ONE_STEP["grid_m"]
-    for k in steps[1:]:
-        out, _ = run_gpu(state, params, k, **PATHS[path])
+    for k in steps:
+        if k != first:
+            out, _ = run_gpu(state, params, k, **PATHS[path])
+            for f in FIELDS:
+                assert field_err(out[f], z[f"{f}@{k}"], f) <= DRIFT[f], (k, f)
+        o64, _, st, _ = oracle.advance(state, steps=k, fp64=True, want_grid=False, threads=4,
+                                       **params)
+        o32, _, st32, _ = oracle.advance(state, steps=k, want_grid=False, threads=4, **params)
+        assert st == 0 and st32 == 0
         for f in FIELDS:
-            assert field_err(out[f], z[f"{f}@{k}"], f) <= DRIFT[f], (k, f)
+            # the FP32 yardstick: the reference's own distance to FP64, or the FP32 oracle's
+            # where that is larger (the reference here computes its SVD in double, through
+            # the Eigen stand-in, so its snow and liquid sit closer to FP64 than an FP32 SVD)
+            own = max(field_err(z[f"{f}@{k}"], o64[f], f), field_err(o32[f], o64[f], f))
+            e64 = field_err(out[f], o64[f], f)
+            assert e64 <= max(GOLDEN_FP64_FACTOR * own, FP64_FLOOR), (k, f, e64, own)
 
 
 @pytest.mark.parametrize("name", ["readme_snow", "block3d_snow", "block3d_jelly"])
@@ -296,9 +320,11 @@ def test_largest_2d_grid_matches_oracle(oracle, path):
     out, grid = run_gpu(s, dict(model=scenes.SNOW, res=1024, dt=1e-5, E=1e4, nu=0.2,
                                 gravity=-100.0), 2, **PATHS[path])
     ref, og, st, _ = oracle.advance(s, dim=2, model=scenes.SNOW, res=1024, dt=1e-5, steps=2)
-    assert st == 0
-    for f in FIELDS:
-        assert field_err(out[f], ref[f], f) <= DRIFT[f], f
+    r64, _, st64, _ = oracle.advance(s, dim=2, model=scenes.SNOW, res=1024, dt=1e-5, steps=2,
+                                     fp64=True, want_grid=False)
+    assert st == 0 and st64 == 0
+    # a grid of 1024 makes the stress 256 times stiffer per unit of F than the fixtures' 64
+    check_fp32_class(out, ref, r64, DRIFT)
     assert field_err(grid.mass, og[1], "grid_m") <= 1e-4
 
 

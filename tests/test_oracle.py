@@ -30,6 +30,43 @@ def test_oracle_matches_reference_goldens(oracle, name):
             assert field_err(out[f], z[f"{f}@{k}"], f) <= DRIFT_100[f], (k, f)
 
 
+def test_drift_bound_follows_reference_fp32_drift(oracle):
+    """The drift bound of the GPU tests (conftest.DRIFT) is derived from the reference's own
+    FP32 drift: for every golden fixture's scene, the reference's own step (compiled from its
+    sources, where the tree exists) and the FP64 oracle advance side by side, one step at a
+    time, and the distance of the two states is taken after every step.  The largest of these
+    per field must be the recorded REF_FP32_DRIFT (to 2%), and DRIFT must be DRIFT_FACTOR times
+    it, rounded up by at most a third.  Where the reference tree is absent, the fixtures'
+    snapshots (the reference's own FP32 states) bound it from below."""
+    from conftest import DRIFT_FACTOR, REF_FP32_DRIFT
+    worst = {f: 0.0 for f in FIELDS}
+    have_ref = oracle.ref_available()
+    for name in golden_names():
+        z, state, params, steps = load_golden(name)
+        keep = {"mass": state["mass"], "volume": state["volume"]}
+        if have_ref:
+            r, d = dict(state), dict(state)
+            for _ in range(steps[-1]):
+                r, _, st = oracle.ref_advance(r, steps=1, **params)
+                d, _, st64, _ = oracle.advance(d, steps=1, fp64=True, want_grid=False, **params)
+                assert st == 0 and st64 == 0
+                r, d = {**r, **keep}, {**d, **keep}
+                for f in FIELDS:
+                    worst[f] = max(worst[f], field_err(r[f], d[f], f))
+        else:
+            for k in steps:
+                d, _, st64, _ = oracle.advance(state, steps=k, fp64=True, want_grid=False,
+                                               threads=4, **params)
+                for f in FIELDS:
+                    worst[f] = max(worst[f], field_err(z[f"{f}@{k}"], d[f], f))
+    for f in FIELDS:
+        if have_ref:
+            assert abs(worst[f] - REF_FP32_DRIFT[f]) <= 0.02 * REF_FP32_DRIFT[f], (f, worst[f])
+        else:
+            assert worst[f] <= 1.02 * REF_FP32_DRIFT[f], (f, worst[f])
+        assert DRIFT_FACTOR * REF_FP32_DRIFT[f] <= DRIFT[f] <= 1.34 * DRIFT_FACTOR * REF_FP32_DRIFT[f], f
+
+
 @pytest.mark.parametrize("name", ["readme_snow", "block3d_snow", "block3d_jelly"])
 def test_oracle_one_step_from_reference_state(oracle, name):
     """One step from the reference's own mid-run state: x, F, Jp within 1e-5; v and C

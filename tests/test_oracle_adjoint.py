@@ -122,3 +122,69 @@ def test_oracle_per_particle_moduli_adjoint_matches_finite_differences(oracle, s
             fd = (loss(*args) - loss(*argm)) / (2 * h)
             scale = np.abs(g[name]).max()
             assert abs(g[name][p] - fd) <= 1e-4 * abs(fd) + 1e-6 * scale, (name, p, g[name][p], fd)
+
+
+PLASTIC_CASES = [(2, 32, 30, 1024), (3, 16, 8, 216)]  # dim, res, steps, particles
+
+
+def plastic_setup(dim, res, n, physics, model, seed=0):
+    """A jittered block whose F already sits near the plastic limits: snow with singular values
+    scattered across the clamp bounds and Jp away from its own bounds, liquid with a perturbed
+    F (the reset keeps only det F)."""
+    s, target = setup(dim, res, n, physics, seed)
+    rng = np.random.default_rng(seed + 7)
+    s["F"] = s["F"] + rng.normal(0, 0.02, size=s["F"].shape)
+    s["Jp"] = rng.uniform(0.9, 1.1, size=n)
+    return s, target
+
+
+@pytest.mark.parametrize("dim,res,steps,n", PLASTIC_CASES)
+@pytest.mark.parametrize("physics", [scenes.REFERENCE, scenes.CORRECTED])
+@pytest.mark.parametrize("model", [scenes.SNOW, scenes.LIQUID])
+def test_oracle_plastic_adjoint_matches_finite_differences(oracle, dim, res, steps, n, physics,
+                                                           model):
+    """The adjoint through the snow clamp (SVD backward with the clamped singular values'
+    gradients masked, the Jp update, the Jp-dependent hardening) and through the liquid reset,
+    against FP64 central differences: initial velocities, positions, F and Jp with a
+    deformation-dependent loss, and E and nu."""
+    if dim == 3 and physics == scenes.REFERENCE and model == scenes.LIQUID:
+        pytest.skip("3D liquid under the reference physics resets F to diag(J, 1, 0), whose "
+                    "polar rotation is not unique: the step is not differentiable there")
+    s, _ = plastic_setup(dim, res, n, physics, model)
+    kw = dict(dim=dim, res=res, steps=steps, physics=physics, model=model)
+    out, _ = oracle.adjoint(s, seed={}, **kw)
+    targets = out["x"] + np.random.default_rng(2).normal(0, 1e-3, size=out["x"].shape)
+    _, seed = pointwise(out["x"], s["mass"], targets)
+    _, g = oracle.adjoint(s, seed={"x": seed}, **kw)
+
+    def loss(st, E=1e4, nu=0.2):
+        o, _, status, _ = oracle.advance(st, dim=dim, model=model, res=res, steps=steps,
+                                         fp64=True, physics=physics, E=E, nu=nu,
+                                         want_grid=False)
+        assert status == 0
+        return pointwise(o["x"], s["mass"], targets)[0]
+
+    rng = np.random.default_rng(1)
+    checks = []
+    for _ in range(3):
+        p, d = int(rng.integers(n)), int(rng.integers(dim))
+        checks += [("v", (p, d), 1e-6), ("x", (p, d), 1e-8)]
+    checks += [("F", (int(rng.integers(n)), 0, 1), 1e-7), ("Jp", (int(rng.integers(n)),), 1e-7)]
+    scale = max(np.abs(g["v"]).max(), np.abs(g["x"]).max())
+    for field, idx, h in checks:
+        sp = {k: v.copy() for k, v in s.items()}
+        sm = {k: v.copy() for k, v in s.items()}
+        sp[field][idx] += h
+        sm[field][idx] -= h
+        fd = (loss(sp) - loss(sm)) / (2 * h)
+        ad = g[field][idx]
+        assert abs(ad - fd) <= 1e-4 * abs(fd) + 1e-7 * scale, (field, idx, ad, fd)
+    # steps small enough that no particle's clamp switches inside +-h (the loss is piecewise
+    # smooth: larger steps cross those kinks and the central difference stops converging)
+    for name, h in (("E", 1e-2), ("nu", 1e-7)):
+        kp = {"E": 1e4, "nu": 0.2}
+        km = dict(kp)
+        kp[name] += h
+        km[name] -= h
+        fd = (loss(s, **kp) - loss(s, **km)) / (2 * h)
+        assert abs(g[name] - fd) <= 1e-4 * abs(fd) + 1e-12, (name, g[name], fd)

@@ -6,9 +6,10 @@ The caller owns every array; the transfer's accumulation grid is a static device
 the library.  Its output -- the grid after one step's particle-to-grid transfer and grid
 update -- must match what the regular entry points give for the same state
 (nclr_create + nclr_advance(sim, 1) + nclr_get_grid), within the one-step grid tolerance of the
-parity tests, on two calls in a row with different scenes (which also shows that each call
-starts from a cleared scratch grid).  This file is collected last so that a run stopping at
-the first failure has run every other test already.
+parity tests, on calls in a row with different scenes and materials (which also shows that
+each call starts from a cleared scratch grid), and an empty call in between must give an
+all-zero grid.  This file is collected last so that a run stopping at the first failure has
+run every other test already.
 """
 import ctypes
 
@@ -51,13 +52,37 @@ def _noalloc_grid(torch, state, params):
     return vel.cpu().numpy(), mass.cpu().numpy()
 
 
+def _empty_call(torch, dim, res):
+    """n = 0: no particle arrays; the grid update of a cleared scratch grid is all zeros."""
+    dev = torch.device("cuda", 0)
+    nodes = (res + 1) ** dim
+    vel = torch.full((nodes, dim), float("nan"), device=dev)
+    mass = torch.full((nodes,), float("nan"), device=dev)
+    msg = ctypes.create_string_buffer(256)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    st = capi.lib().nclr_grid_transfer_noalloc(dim, 0, None, None, None, None, None, None, None,
+                                               1, res, 1e-4, 1e4, 0.2, -100.0, vel.data_ptr(),
+                                               mass.data_ptr(), stream, msg, len(msg))
+    assert st == capi.NCLR_OK, (st, msg.value)
+    return vel.cpu().numpy(), mass.cpu().numpy()
+
+
 def test_noalloc_transfer_matches_regular_entry_points_twice():
     torch = pytest.importorskip("torch")
     assert torch.cuda.is_available()
-    # two calls in a row, 3D then 2D (different grid sizes), then the 3D scene again
-    cases = [load_golden("block3d_jelly"), load_golden("readme_snow"), load_golden("block3d_jelly")]
+    # calls in a row: 3D jelly, 2D snow, 2D liquid (different grid sizes and hardening), an
+    # empty call over the 3D grid (it must not see the earlier sums), then the 3D scene again
+    cases = [load_golden("block3d_jelly"), load_golden("readme_snow"),
+             load_golden("readme_liquid"), None, load_golden("block3d_jelly")]
     first = None
-    for z, state, params, _ in cases:
+    for case in cases:
+        if case is None:
+            ev, em = _empty_call(torch, 3, first_res)
+            assert np.all(ev == 0.0) and np.all(em == 0.0)
+            continue
+        z, state, params, _ = case
+        if first is None:
+            first_res = params["res"]
         rv, rm = _regular_grid(state, params)
         nv, nm = _noalloc_grid(torch, state, params)
         assert field_err(nv, rv, "grid_v") <= GRID_TOL["grid_v"]
