@@ -418,6 +418,35 @@ def adjoint_error_vs_fp64(device: int, sc: dict, v0: np.ndarray, target: np.ndar
             "oracle": "FP64 adjoint of the reference step (oracle/nclr_adjoint.h), one thread"}
 
 
+def run_adjoint_snow(device: int, sc: dict, v0, target, x0, steps: int = 500,
+                     every: int = 50) -> dict:
+    """The same scene, velocities and loss as a snow rollout (the plastic adjoint: the clamp's
+    singular-value backward, the Jp update and the Jp-dependent hardening) under the corrected
+    physics, `steps` steps with a checkpoint every `every`: device times of the forward and of
+    the backward."""
+    import torch
+
+    from nuclearmpm_gb300 import scenes
+    from nuclearmpm_gb300.autograd import Rollout
+    n = len(sc["x"])
+    roll = Rollout(sc["x"], res=64, steps=steps, checkpoint_every=every, device=device,
+                   physics=scenes.CORRECTED, model=scenes.SNOW)
+    v = v0.clone().requires_grad_(True)
+    E = torch.tensor(1e4, dtype=torch.float64, requires_grad=True)
+    nu = torch.tensor(0.2, dtype=torch.float64, requires_grad=True)
+    for _ in range(2):  # the second iteration is the measured one (F0 = I, C0 = 0)
+        v.grad = None
+        xT, _ = roll(x0, v, E, nu)
+        ((xT.mean(0) - target) ** 2).sum().backward()
+    fwd_ms, bwd_ms = roll.timing()
+    roll.close()
+    return {"value": n * steps / ((fwd_ms + bwd_ms) / 1e3), "unit": UNIT, "particles": n,
+            "steps": steps, "checkpoint_every": every, "forward_ms": fwd_ms,
+            "backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms,
+            "grad_norms": {"v0": float(v.grad.norm()), "E": float(E.grad), "nu": float(nu.grad)},
+            "config": "3D snow rollout, the adjoint form's scene and loss, corrected physics"}
+
+
 def run_adjoint(device: int, steps: int = 2000, every: int = 50) -> dict:
     """The differentiable form: 3D jelly, 64^3 grid, one 64x64x32 jittered lattice (131,072
     particles, seeded), `steps` steps with a checkpoint every `every`; loss = squared distance
@@ -473,7 +502,8 @@ def run_adjoint(device: int, steps: int = 2000, every: int = 50) -> dict:
         roofs[k] = roofline_of(k, alg, avg, launches=prof[k][1])
     dom = max(("adj_g2p", "adj_grid", "adj_p2g"), key=lambda k: prof[k][0])
     err = adjoint_error_vs_fp64(device, sc, v0.detach().cpu().numpy(), target.cpu().numpy())
-    return {"value": n * steps / ((fwd_ms + bwd_ms) / 1e3), "unit": UNIT,
+    snow = run_adjoint_snow(device, sc, v0.detach(), target, x0)
+    return {"value": n * steps / ((fwd_ms + bwd_ms) / 1e3), "unit": UNIT, "snow": snow,
             "roofline": dict(roofs[dom], kernels=roofs,
                              bytes_note="algorithmic bytes per launch: adj_g2p reads x, F, C', "
                              "gF', gC', gx', gv' and writes gx, gF (228 B per particle); adj_p2g "

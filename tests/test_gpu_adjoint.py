@@ -189,7 +189,9 @@ def test_gpu_snow_gradients_match_finite_differences(oracle):
     """The reduced 2D case in snow: 1,024 particles, 32^2 grid, 50 steps, a deformation-dependent
     loss; directional derivatives of the initial velocities and positions and the E / nu
     derivatives against FP64 central differences of the oracle's forward rollout (steps small
-    enough that no particle's clamp switches inside them: the loss is piecewise smooth)."""
+    enough that no particle's clamp switches inside them: the loss is piecewise smooth).  A
+    directional derivative sum_i g_i d_i over random directions cancels (the velocity one by
+    about two digits here), so it is held to 1e-3 of its uncancelled scale sum_i |g_i d_i|."""
     dim, res, steps, n = 2, 32, 50, 1024
     s = plastic_setup(dim, res, n, scenes.CORRECTED, seed=9)
     fwd, _, st, _ = oracle.advance(s, dim=dim, model=scenes.SNOW, res=res, steps=steps,
@@ -208,15 +210,16 @@ def test_gpu_snow_gradients_match_finite_differences(oracle):
 
     rng = np.random.default_rng(11)
     s64 = {k: np.asarray(v, np.float64) for k, v in s.items()}
-    for field, h in (("v", 1e-7), ("x", 1e-8)):
+    for field, h in (("v", 1e-6), ("x", 1e-8)):
         for _ in range(3):
             dirn = rng.normal(size=s64[field].shape)
             sp, sm = dict(s64), dict(s64)
             sp[field] = s64[field] + h * dirn
             sm[field] = s64[field] - h * dirn
             fd = (loss64(sp) - loss64(sm)) / (2 * h)
-            ad = float((g[field].astype(np.float64) * dirn).sum())
-            assert abs(ad - fd) <= GRAD_TOL * abs(fd), (field, ad, fd)
+            terms = g[field].astype(np.float64) * dirn
+            ad = float(terms.sum())
+            assert abs(ad - fd) <= GRAD_TOL * float(np.abs(terms).sum()), (field, ad, fd)
     for name, h in (("E", 1e-2), ("nu", 1e-7)):
         kp, km = {"E": 1e4, "nu": 0.2}, {"E": 1e4, "nu": 0.2}
         kp[name] += h
