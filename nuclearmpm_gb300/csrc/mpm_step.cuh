@@ -178,8 +178,8 @@ __device__ __forceinline__ void scale_mat(Mat<D> &C, float c) {
 }
 
 // FP64 threshold of the snow clamp (see snow_clamp_needs_fp64): the FP32 clamp's own error
-// measured about 2e-7 per unit of this gain, so below 25 it stays within about 5e-6.
-constexpr float kClampFP64Gain = 25.0f;
+// measured about 2e-7 per unit of this gain, so below 50 it stays within about 1e-5.
+constexpr float kClampFP64Gain = 50.0f;
 
 // Whether the snow clamp of F_hat (FP32 signed singular values sig, decreasing in magnitude)
 // must be recomputed in FP64.  With det F_hat < 0 the last singular value s_l is negative,
@@ -540,16 +540,10 @@ g2p2g_kernel(
   float4 *vt = smem + grp * kTiles * GS;  // the group's V tile
   float4 *gt = vt + GS;                   // its kWarps private G tiles: [warp][SIZE]
   __shared__ int s_items[kGroups];
-  // Per group, per axis and tile coordinate c: the warps whose stencils reached a node with
-  // coordinate c on that axis in the current item (bit w = warp w of the group).  A node's
-  // AND over its axes names the warp tiles that can hold contributions there: the flush reads
-  // (and clears) only those, instead of every warp's tile at every tile node.
-  __shared__ unsigned s_covs[kGroups][D * T];
   __shared__ Params sPs[kGroups];  // each item's scene (shared: keeps registers for the math)
   __shared__ int64_t s_node_offs[kGroups];
   __shared__ int s_block_offs[kGroups];
   int &s_item = s_items[grp];
-  unsigned *s_cov = s_covs[grp];
   Params &sP = sPs[grp];
   int64_t &s_node_off = s_node_offs[grp];
   int &s_block_off = s_block_offs[grp];
@@ -575,7 +569,6 @@ g2p2g_kernel(
 
   for (;;) {
     group_sync();
-    if (gtid < D * T) s_cov[gtid] = 0u;  // the last item's flush is done reading them
     if (gtid == 0) {  // the next block of the list, and its scene
       const int it = atomicAdd(work, 1);
       s_item = it;
@@ -646,8 +639,6 @@ g2p2g_kernel(
       // what the particle contributes to the next P2G
       bool fast_s = false;
       int tb_s = 0;
-      unsigned cov_s = 0;  // the tile nodes the stencil covers, per axis (bits c..c+2 of axis d
-                           // at d * T)
       float fx_s[D], w_s[3][D], mv[D], m = 0.0f;
       Mat<D> A;
       if (valid) {
@@ -746,8 +737,6 @@ g2p2g_kernel(
             fast_s &= in_range(lb[d], T - 3) && in_range(base[d], N - 3);
           }
           tb_s = tile_index<D>(lb[0], lb[1], lb[2]);
-#pragma unroll
-          for (int d = 0; d < D; ++d) cov_s |= 7u << (d * T + lb[d]);
           if (!fast_s) {  // outside the tile: straight to G
             const int64_t f0 = flat_index<D>(base, N);
 #pragma unroll
@@ -794,10 +783,6 @@ g2p2g_kernel(
           __syncwarp();
         }
       }
-      {  // the nodes this pass of the warp reached, per axis, into the item's coverage
-        const unsigned cov = __reduce_or_sync(0xffffffffu, tile_lane ? cov_s : 0u);
-        if (lane < D * T && ((cov >> lane) & 1u)) atomicOr(s_cov + lane, 1u << (gtid >> 5));
-      }
     }
     if (direct || kMode == kG2PFinal) continue;  // its P2G went straight to G (and the flags)
     group_sync();
@@ -813,23 +798,21 @@ g2p2g_kernel(
         r /= T;
         in &= g[d] >= 0 && g[d] < N;
       }
-      // the warps whose stencils reached this node's coordinates on every axis
-      unsigned mask = s_cov[l[0]] & s_cov[T + l[1]];
-      if constexpr (D == 3) mask &= s_cov[2 * T + l[2]];
-      if (!mask) continue;  // no warp's tile holds anything here
       const int ti = tile_index<D>(l[0], l[1], l[2]);
       float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      bool touched = false;
 #pragma unroll
       for (int wi = 0; wi < kWarps; ++wi) {
-        if (!((mask >> wi) & 1u)) continue;
-        float4 *e = gt + wi * GS + ti;
-        const float4 g4 = *e;
+        const float4 g4 = gt[wi * GS + ti];
         a[0] += g4.x;
         a[1] += g4.y;
         a[2] += g4.z;
         a[3] += g4.w;
-        *e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        touched |= g4.x != 0.0f || g4.y != 0.0f || g4.z != 0.0f || g4.w != 0.0f;
       }
+      if (!touched) continue;
+#pragma unroll
+      for (int wi = 0; wi < kWarps; ++wi) gt[wi * GS + ti] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (a[0] == 0.0f && a[1] == 0.0f && a[2] == 0.0f && a[3] == 0.0f) continue;
       if (in) red_add_v4(G + flat_index<D>(g, N), a[0], a[1], a[2], a[3]);
     }
@@ -1452,9 +1435,9 @@ void launch_snow_fix(const PState &s, const Params &P0, const Scene *scenes, con
                      float4 *G, bool scatter, bool ref, const Record &rec, int sms,
                      cudaStream_t st) {
   if (!fix.count) return;
-  // FP64 latency: several CTAs per SM (the list is usually empty, or a few percent of the
-  // particles)
-  const unsigned blocks = (unsigned)std::max(1, 4 * sms);
+  // two CTAs per SM: the list is usually empty or a small fraction of the particles, and the
+  // FP64 work of a full one is bound by the SMs' FP64 rate, not by latency
+  const unsigned blocks = (unsigned)std::max(1, 2 * sms);
   if (ref)
     snow_fix_kernel<D, true><<<blocks, 128, 0, st>>>(s, P0, scenes, fix, G, scatter ? 1 : 0, rec);
   else

@@ -191,7 +191,10 @@ def test_gpu_snow_gradients_match_finite_differences(oracle):
     derivatives against FP64 central differences of the oracle's forward rollout (steps small
     enough that no particle's clamp switches inside them: the loss is piecewise smooth).  A
     directional derivative sum_i g_i d_i over random directions cancels (the velocity one by
-    about two digits here), so it is held to 1e-3 of its uncancelled scale sum_i |g_i d_i|."""
+    about two digits here), so it is held to 1e-3 of its uncancelled scale sum_i |g_i d_i|; the
+    E and nu derivatives are sums over particles that cancel too, and are held to 1e-3 of
+    sum_p |g_p|, each particle's own derivative (the same rollout with one E and nu per
+    particle, all equal, whose gradients must also add up to the scene's)."""
     dim, res, steps, n = 2, 32, 50, 1024
     s = plastic_setup(dim, res, n, scenes.CORRECTED, seed=9)
     fwd, _, st, _ = oracle.advance(s, dim=dim, model=scenes.SNOW, res=res, steps=steps,
@@ -220,9 +223,14 @@ def test_gpu_snow_gradients_match_finite_differences(oracle):
             terms = g[field].astype(np.float64) * dirn
             ad = float(terms.sum())
             assert abs(ad - fd) <= GRAD_TOL * float(np.abs(terms).sum()), (field, ad, fd)
+    gp = gpu_grads(s, dim, res, steps, scenes.CORRECTED, every=10,
+                   seed_fn=point_loss(targets.astype(np.float32)), model=scenes.SNOW,
+                   E=np.full(n, 1e4, np.float32), nu=np.full(n, 0.2, np.float32))
     for name, h in (("E", 1e-2), ("nu", 1e-7)):
         kp, km = {"E": 1e4, "nu": 0.2}, {"E": 1e4, "nu": 0.2}
         kp[name] += h
         km[name] -= h
         fd = (loss64(s64, **kp) - loss64(s64, **km)) / (2 * h)
-        assert abs(float(g[name]) - fd) <= GRAD_TOL * abs(fd), (name, float(g[name]), fd)
+        scale = float(np.abs(gp[name].astype(np.float64)).sum())
+        assert abs(float(gp[name].astype(np.float64).sum()) - float(g[name])) <= GRAD_TOL * scale
+        assert abs(float(g[name]) - fd) <= GRAD_TOL * max(abs(fd), scale), (name, float(g[name]), fd, scale)

@@ -33,32 +33,32 @@ def test_oracle_matches_reference_goldens(oracle, name):
 def test_drift_bound_follows_reference_fp32_drift(oracle):
     """The drift bound of the GPU tests (conftest.DRIFT) is derived from the reference's own
     FP32 drift: for every golden fixture's scene, the reference's own step (compiled from its
-    sources, where the tree exists) and the FP64 oracle advance side by side, one step at a
-    time, and the distance of the two states is taken after every step.  The largest of these
-    per field must be the recorded REF_FP32_DRIFT (to 2%), and DRIFT must be DRIFT_FACTOR times
-    it, rounded up by at most a third.  Where the reference tree is absent, the fixtures'
-    snapshots (the reference's own FP32 states) bound it from below."""
+    sources, where the tree exists), the FP32 restatement and the FP64 oracle advance side by
+    side, one step at a time, and the distance of each FP32 state to the FP64 one is taken
+    after every step.  The largest of these per field must be the recorded REF_FP32_DRIFT (to
+    2%), and DRIFT must be DRIFT_FACTOR times it, rounded up by at most a third.  Where the
+    reference tree is absent, the FP32 restatement alone bounds it from below."""
     from conftest import DRIFT_FACTOR, REF_FP32_DRIFT
     worst = {f: 0.0 for f in FIELDS}
     have_ref = oracle.ref_available()
     for name in golden_names():
         z, state, params, steps = load_golden(name)
         keep = {"mass": state["mass"], "volume": state["volume"]}
-        if have_ref:
-            r, d = dict(state), dict(state)
-            for _ in range(steps[-1]):
+        r, d, o = dict(state), dict(state), dict(state)
+        for _ in range(steps[-1]):
+            d, _, st64, _ = oracle.advance(d, steps=1, fp64=True, want_grid=False, **params)
+            o, _, st32, _ = oracle.advance(o, steps=1, want_grid=False, **params)
+            assert st64 == 0 and st32 == 0
+            d, o = {**d, **keep}, {**o, **keep}
+            if have_ref:
                 r, _, st = oracle.ref_advance(r, steps=1, **params)
-                d, _, st64, _ = oracle.advance(d, steps=1, fp64=True, want_grid=False, **params)
-                assert st == 0 and st64 == 0
-                r, d = {**r, **keep}, {**d, **keep}
-                for f in FIELDS:
-                    worst[f] = max(worst[f], field_err(r[f], d[f], f))
-        else:
-            for k in steps:
-                d, _, st64, _ = oracle.advance(state, steps=k, fp64=True, want_grid=False,
-                                               threads=4, **params)
-                for f in FIELDS:
-                    worst[f] = max(worst[f], field_err(z[f"{f}@{k}"], d[f], f))
+                assert st == 0
+                r = {**r, **keep}
+            for f in FIELDS:
+                e = field_err(o[f], d[f], f)
+                if have_ref:
+                    e = max(e, field_err(r[f], d[f], f))
+                worst[f] = max(worst[f], e)
     for f in FIELDS:
         if have_ref:
             assert abs(worst[f] - REF_FP32_DRIFT[f]) <= 0.02 * REF_FP32_DRIFT[f], (f, worst[f])
