@@ -302,7 +302,8 @@ def run_batched(device: int, steps: int = 100, sequential: bool = True, repeats:
     scs = scenes.batched_scenes_2d(seed=0)
     total = sum(len(sc["x"]) for sc in scs)
     tuned = autotune.tune(lambda **o: BatchSimulation(scs, device=device, **o), key=None,
-                          steps=32, repeats=2, cache_path=None)
+                          candidates=autotune.BATCH_CANDIDATES, steps=32, repeats=2,
+                          cache_path=None)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def best_of(sim) -> float:

@@ -90,6 +90,11 @@ typedef struct nclr_options {
                               has at most 8 nodes per particle -- that kernel updates every
                               node each step; never a batch, where the tile path is faster) */
   int stress_model;        /* NCLR_STRESS_* (default COROTATED); a batch's scenes share it */
+  int batch_item_threads;  /* batches: threads that step one grid block of the fused step
+                              together -- 128 (half a CTA, each half with its own tiles; the
+                              2D default) or 256 (a whole CTA; the 3D one); 0 = the default.
+                              An autotuner knob: the best size depends on the particles per
+                              block. */
 } nclr_options;
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid

@@ -2,10 +2,12 @@
 interval, the number of steps per captured CUDA graph and, for single simulations, the
 thin-block threshold below which a block's particles skip the shared-memory tile.
 
-The tile and block sizes of the kernels (4^3 cells in 3D, 8^2 in 2D, 8^3 / 12^2 node tiles,
-256-thread CTAs) are compile-time constants fixed by the shared-memory layout; the knobs that
-trade work against locality at run time are tuned here by timing short runs of the workload
-itself through the public API, and the winner is cached per workload signature.
+The grid tiles of the kernels (4^3 cells in 3D, 8^2 in 2D, 8^3 / 12^2 node tiles) are
+compile-time constants fixed by the shared-memory layout and the sort's 64-cell blocks.  The
+knobs tuned here, by timing short runs of the workload itself through the public API (the
+winner cached per workload signature), trade work against locality at run time: the re-sort
+interval, the thin-block threshold, and for batches the threads that step one block together
+(128 or 256, each a compiled variant of the fused kernel).
 
     from nuclearmpm_gb300 import autotune
     best = autotune.tune(lambda **opt: BatchSimulation(scenes, **opt), key="batch256")
@@ -24,6 +26,10 @@ DEFAULT_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32]}
 # single simulations: also the thin-block threshold (particles per block; 0 = every block
 # through the tile); batches ignore it
 PLAIN_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32], "sparse_block_max": [0, 32, 64, 128, 256]}
+# batches: re-sort interval, threads per item of the fused kernel (2D: half or whole CTAs),
+# thin-block threshold
+BATCH_CANDIDATES = {"sort_interval": [4, 8, 16, 32], "batch_item_threads": [128, 256],
+                    "sparse_block_max": [0, 16, 32, 64]}
 # single simulations small enough for the small-scene kernel: its particles per thread
 SMALL_CANDIDATES = {"particles_per_thread": [1, 2, 4]}
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")

@@ -27,7 +27,8 @@ class Options(ctypes.Structure):
                 ("p2g_particles_per_thread", ctypes.c_int), ("device", ctypes.c_int),
                 ("use_graphs", ctypes.c_int), ("profile", ctypes.c_int),
                 ("graph_steps", ctypes.c_int), ("sparse_block_max", ctypes.c_int),
-                ("small_scene_max", ctypes.c_int), ("stress_model", ctypes.c_int)]
+                ("small_scene_max", ctypes.c_int), ("stress_model", ctypes.c_int),
+                ("batch_item_threads", ctypes.c_int)]
 
 
 class Scene(ctypes.Structure):

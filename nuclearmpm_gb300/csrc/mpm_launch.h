@@ -50,7 +50,8 @@ template <int D> void launch_g2p2g(const PState &s, const Params &P0, const Scen
                                    const float4 *V, float4 *G, uint8_t *flags, const int *blocks,
                                    const int *nactive, const int *bstart, const int *sparse, int *work,
                                    int *err, int next_slot, bool ref, int mode, int ctas, cudaStream_t st,
-                                   const Record &rec = Record{}, const SnowFix &fix = SnowFix{});
+                                   const Record &rec = Record{}, const SnowFix &fix = SnowFix{},
+                                   int item_threads = 0);
 template <int D> int g2p2g_ctas_per_sm();
 template <int D> int g2p_final_ctas_per_sm();
 // The small-scene kernels' grid barrier: how many polls a waiting CTA makes before it gives up

@@ -25,9 +25,11 @@ constexpr int kG2P2GThreads = 256;
 // own item, tiles and barrier.  That replaces a 256-thread pass and a mostly idle second one
 // (measured on 256 mixed scenes: 1.50-1.58e10 particle-steps/s against 1.37e10; one warp per
 // item measured 3x slower, and the half-CTA items slow a single 2D simulation's tile path).
-template <int D, bool kBatch>
+// kItem (batches): the threads per item chosen instead (128 or 256; 0 = the default above),
+// a knob of the autotuner.
+template <int D, bool kBatch, int kItem = 0>
 __host__ __device__ constexpr int g2p2g_group() {
-  return (D == 2 && kBatch) ? kG2P2GThreads / 2 : kG2P2GThreads;
+  return kItem ? kItem : ((D == 2 && kBatch) ? kG2P2GThreads / 2 : kG2P2GThreads);
 }
 
 // 0 <= v <= hi, as one unsigned compare that no large v (a saturated float-to-int conversion
@@ -516,7 +518,7 @@ enum : int { kStep = kModeStep, kFinalStep = kModeFinalStep, kP2GOnly = kModeP2G
 
 // kBatch: several scenes (per-block parameters from the scene table, staged in shared memory)
 // or one (its parameters are a kernel argument: constant-bank operands, no registers).
-template <int D, bool kRef, int kMode, bool kBatch, int kMat = -1>
+template <int D, bool kRef, int kMode, bool kBatch, int kMat = -1, int kItem = 0>
 // 3D: two CTAs per SM (the tiles take 106 KB of shared memory each), three for the G2P-only
 // step (one 12 KB tile); 2D: four, which keeps the 2D kernel within 64 registers without
 // spills.  kMat >= 0 fixes every particle's material at compile time (a single simulation
@@ -531,7 +533,7 @@ g2p2g_kernel(
   using Tl = Tiling<D>;
   constexpr int T = Tl::T, NODES = Tl::NODES, BS = Tl::BS, GS = Tl::SIZE;
   constexpr int S = (D == 3) ? 27 : 9;
-  constexpr int kGroup = g2p2g_group<D, kBatch>();  // threads per item
+  constexpr int kGroup = g2p2g_group<D, kBatch, kItem>();  // threads per item
   constexpr int kGroups = kG2P2GThreads / kGroup;  // items in flight per CTA
   constexpr int kWarps = kGroup / 32;              // warps per item, each with its G tile
   constexpr int kTiles = (kMode == kG2PFinal) ? 1 : 1 + kWarps;  // tiles per group
@@ -836,10 +838,10 @@ g2p2g_kernel(
 
 // Dynamic shared memory of g2p2g: per item group, the V tile plus one G tile per warp (the V
 // tile alone for kG2PFinal, which has no P2G and runs single simulations only).
-template <int D, bool kBatch>
+template <int D, bool kBatch, int kItem = 0>
 constexpr size_t g2p2g_smem_bytes() {
-  return sizeof(float4) * Tiling<D>::SIZE * (kG2P2GThreads / g2p2g_group<D, kBatch>()) *
-         (1 + g2p2g_group<D, kBatch>() / 32);
+  return sizeof(float4) * Tiling<D>::SIZE * (kG2P2GThreads / g2p2g_group<D, kBatch, kItem>()) *
+         (1 + g2p2g_group<D, kBatch, kItem>() / 32);
 }
 template <int D>
 constexpr size_t g2p_final_smem_bytes() {
@@ -1473,7 +1475,7 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                   const uint16_t *block_scene, const float4 *V, float4 *G, uint8_t *flags,
                   const int *blocks, const int *nactive, const int *bstart, const int *sparse,
                   int *work, int *err, int next_slot, bool ref, int mode, int ctas,
-                  cudaStream_t st, const Record &rec, const SnowFix &fix) {
+                  cudaStream_t st, const Record &rec, const SnowFix &fix, int item_threads) {
   if constexpr (D == 3) {  // one material for every particle: the specialised kernel
     if (!block_scene && !s.mat && (mode == kStep || mode == kFinalStep) &&
         (P0.model == kSnow || P0.model == kJelly || P0.model == kLiquid)) {
@@ -1488,11 +1490,19 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
                                                     : g2p2g_smem_bytes<D, B>(),           \
                                 st>>>(s, P0, scenes, block_scene, V, G, flags, blocks,   \
                                       nactive, bstart, sparse, work, err, next_slot, rec, fix)
-#define MPM_G2P2G_B(R, MODE)          \
-  if (block_scene) {                  \
-    MPM_G2P2G(R, MODE, true);         \
-  } else {                            \
-    MPM_G2P2G(R, MODE, false);        \
+// 2D batches with whole-CTA items (item_threads 256) instead of the default half-CTA ones
+#define MPM_G2P2G_ITEM(R, MODE)                                                           \
+  g2p2g_kernel<D, R, MODE, true, -1, kG2P2GThreads>                                       \
+      <<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D, true, kG2P2GThreads>(), st>>>(          \
+          s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart, sparse, work, err, \
+          next_slot, rec, fix)
+#define MPM_G2P2G_B(R, MODE)                                      \
+  if (block_scene && D == 2 && item_threads == kG2P2GThreads) {   \
+    MPM_G2P2G_ITEM(R, MODE);                                      \
+  } else if (block_scene) {                                       \
+    MPM_G2P2G(R, MODE, true);                                     \
+  } else {                                                        \
+    MPM_G2P2G(R, MODE, false);                                    \
   }
   if (mode == kG2PFinal && !block_scene) {  // single simulations only
     if (ref) {
@@ -1510,6 +1520,7 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
     else { MPM_G2P2G_B(false, kStep) }
   }
 #undef MPM_G2P2G_B
+#undef MPM_G2P2G_ITEM
 #undef MPM_G2P2G
 }
 
@@ -1646,7 +1657,7 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
   template void launch_g2p2g<D>(const PState &, const Params &, const Scene *, const uint16_t *, \
                                 const float4 *, float4 *, uint8_t *, const int *, const int *,   \
                                 const int *, const int *, int *, int *, int, bool, int, int,     \
-                                cudaStream_t, const Record &, const SnowFix &);                  \
+                                cudaStream_t, const Record &, const SnowFix &, int);             \
   template int g2p2g_ctas_per_sm<D>();                                                           \
   template int g2p_final_ctas_per_sm<D>();                                                       \
   template cudaError_t launch_small_steps<D>(const PState &, const Params &, float4 *, float4 *,   \

@@ -290,7 +290,7 @@ void enqueue_step(nclr_sim *s, bool sort, int final) {
                              : final == kNotFinal    ? mpm::kModeStep
                                                      : mpm::kModeFinalStep,
                              final == kFinalG2POnly ? s->g2p_ctas : s->g2p2g_ctas, s->stream,
-                             s->record, s->fix);
+                             s->record, s->fix, s->opt.batch_item_threads);
       });
       s->launches += 1;
       if (s->fix.count) {  // the snow clamps that launch left for FP64
@@ -320,7 +320,7 @@ void enqueue_pending_p2g(nclr_sim *s) {
         mpm::launch_g2p2g<D>(s->ps[s->cur], s->P0(), s->scenes_d, s->block_scene, s->V, s->G,
                              s->flags, s->blocks, s->nblocks_active, s->start, s->sparse,
                              s->work, s->err_d, 0, s->ref, mpm::kModeP2GOnly, s->g2p2g_ctas,
-                             s->stream);
+                             s->stream, mpm::Record{}, mpm::SnowFix{}, s->opt.batch_item_threads);
     });
   });
   s->launches += (s->n > 0) ? 2 : 1;
@@ -557,6 +557,11 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   nclr_default_options(&s->opt);
   if (opt) s->opt = *opt;
   if (s->opt.sort_interval < 0) s->opt.sort_interval = 0;
+  if (s->opt.batch_item_threads != 0 && s->opt.batch_item_threads != 128 &&
+      s->opt.batch_item_threads != 256) {
+    delete s;
+    return fail(nullptr, NCLR_ERR_INVALID, "batch_item_threads must be 0, 128 or 256");
+  }
   if (s->opt.stress_model != NCLR_STRESS_COROTATED && s->opt.stress_model != NCLR_STRESS_NEOHOOKEAN) {
     delete s;
     return fail(nullptr, NCLR_ERR_INVALID, "unknown stress model");
@@ -1026,6 +1031,7 @@ void nclr_default_options(nclr_options *opt) {
   opt->device = 0;
   opt->use_graphs = 1;
   opt->profile = 0;
+  opt->batch_item_threads = 0;
   opt->graph_steps = 0;
   opt->sparse_block_max = -1;
   opt->small_scene_max = -1;

@@ -352,7 +352,8 @@ class BatchSimulation:
                  physics: int = capi.PHYSICS_REFERENCE, sort_interval: int = 8, device: int = 0,
                  use_graphs: bool = True, graph_steps: int = 0, profile: bool = False,
                  small_scene_max: int = -1, particles_per_thread: int = 1,
-                 stress_model: int = capi.STRESS_COROTATED, sparse_block_max: int = -1):
+                 stress_model: int = capi.STRESS_COROTATED, sparse_block_max: int = -1,
+                 batch_item_threads: int = 0):
         L = capi.lib()
         if not scenes:
             raise ValueError("a batch needs at least one scene")
@@ -387,7 +388,8 @@ class BatchSimulation:
                                    use_graphs=int(use_graphs), profile=int(profile),
                                    graph_steps=graph_steps, small_scene_max=small_scene_max,
                                    p2g_particles_per_thread=particles_per_thread,
-                                   stress_model=stress_model, sparse_block_max=sparse_block_max)
+                                   stress_model=stress_model, sparse_block_max=sparse_block_max,
+                                   batch_item_threads=batch_item_threads)
         h = ctypes.c_void_p()
         capi.check(L.nclr_batch_create(ctypes.byref(h), self.dim, len(scenes), descs,
                                        ctypes.byref(opt)), None)

@@ -45,10 +45,11 @@ def alone(sc, steps, physics=scenes.REFERENCE):
     return {f: getattr(p, f) for f in FIELDS}, g
 
 
-# The batch's two step paths: "tile" the block-sorted fused kernel with CUDA graphs (the
-# default), "small" all of a call's steps in one cooperative launch with a group of CTAs per
+# The batch's step paths: "tile" the block-sorted fused kernel with CUDA graphs (the default;
+# 2D items of 128 threads), "tile256" the same with 256 threads per item (the autotuner's other
+# item size), "small" all of a call's steps in one cooperative launch with a group of CTAs per
 # scene (an option).
-PATHS = {"small": {"small_scene_max": 1 << 30}, "tile": {}}
+PATHS = {"small": {"small_scene_max": 1 << 30}, "tile": {}, "tile256": {"batch_item_threads": 256}}
 
 
 @pytest.mark.parametrize("path", sorted(PATHS))
