@@ -411,6 +411,16 @@ __global__ void __launch_bounds__(256) adj_grid_kernel(const float4 *__restrict_
   reinterpret_cast<float4 *>(VB)[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// (hi, lo) += (h2, l2) for sums kept as unevaluated pairs of floats: Knuth's TwoSum gives the
+// rounding error of hi + h2 exactly, and the low parts collect it.
+__device__ __forceinline__ void pair_add(float &hi, float &lo, float h2, float l2) {
+  const float s = __fadd_rn(hi, h2);
+  const float bp = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(h2, bp));
+  hi = s;
+  lo = lo + l2 + err;
+}
+
 // ---------------------------------------------------------------------------------------
 // adj_p2g: reverse of mv_i += W (m v + A dpos), m_i += W m, with the fused APIC + stress
 // A = -(dt vol Dinv) PF + m C (jelly: mu = 0.3 mu_0, lambda = 0.3 lambda_0) and PF the
@@ -596,16 +606,17 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
       rm.grad[2 * (size_t)p + 1] += glam;
     }
   }
-  // block reduction of the parameter adjoints, one double atomic per warp
-  double a = gmu, b = glam;
+  // warp reduction of the parameter adjoints, one double atomic per warp; the sums are carried
+  // as unevaluated FP32 pairs (hi + lo), so they keep double-class accuracy without the FP64 pipe
+  float ah = gmu, al = 0.0f, bh = glam, bl = 0.0f;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
+    pair_add(ah, al, __shfl_xor_sync(0xffffffffu, ah, o), __shfl_xor_sync(0xffffffffu, al, o));
+    pair_add(bh, bl, __shfl_xor_sync(0xffffffffu, bh, o), __shfl_xor_sync(0xffffffffu, bl, o));
   }
-  if ((threadIdx.x & 31) == 0 && (a != 0.0 || b != 0.0)) {
-    atomicAdd(gml, a);
-    atomicAdd(gml + 1, b);
+  if ((threadIdx.x & 31) == 0 && (ah != 0.0f || bh != 0.0f)) {
+    atomicAdd(gml, (double)ah + (double)al);
+    atomicAdd(gml + 1, (double)bh + (double)bl);
   }
 }
 

@@ -38,7 +38,13 @@ MPM_HD float rsqrt_(float x) {
   return 1.0f / sqrtf(x);
 #endif
 }
-MPM_HD double rsqrt_(double x) { return 1.0 / sqrt(x); }
+MPM_HD double rsqrt_(double x) {
+#ifdef __CUDA_ARCH__
+  return rsqrt(x);
+#else
+  return 1.0 / sqrt(x);
+#endif
+}
 
 // Scalar helpers in both precisions (the SVD below runs in FP32, and in FP64 where the snow
 // clamp needs it).
@@ -171,6 +177,21 @@ MPM_HD void svd2(const Mat<2> &A, Mat<2> &U, float sig[2], Mat<2> &V) {
 // ---------------------------------------------------------------------------------------
 namespace detail {
 
+// Jacobi sweeps and stopping threshold per precision: done once every S_pq^2 is below
+// (2 eps)^2 S_pp S_qq, eps the precision's unit roundoff (2.4e-7 in FP32; 1.1e-16 in FP64).
+template <typename T>
+struct JacobiLimits;
+template <>
+struct JacobiLimits<float> {
+  static constexpr int kSweeps = 4;
+  static constexpr float kDone = 2.3e-13f;  // (4.8e-7)^2
+};
+template <>
+struct JacobiLimits<double> {
+  static constexpr int kSweeps = 6;
+  static constexpr double kDone = 4.9e-32;  // (2.2e-16)^2
+};
+
 // Conjugate symmetric S (stored full) by the Jacobi rotation in the (p,q) plane that zeroes
 // S_pq (the symmetric Schur rotation of Golub & Van Loan, Alg. 8.4.2, in the numerically
 // stable small-angle form); accumulate it into V (V <- V Q).
@@ -179,28 +200,64 @@ namespace detail {
 // the identity and the singular values of a matrix that is the identity to within rounding
 // come out exactly 1.  Plasticity needs that (the liquid's J = prod sigma enters the
 // pressure lambda (J - 1) J on every entry; snow recomposes F from the clamped sigma); the
-// polar rotation of the stress does not.
+// polar rotation of the stress does not.  It only concerns FP32: the FP64 results are
+// rounded to FP32, and FP64 takes the cheaper form below whatever kExact says.
 template <int P, int Q, bool kExact, typename T>
 MPM_HD void jacobi_rotate(T S[3][3], T V[3][3]) {
+  constexpr int R = 3 - P - Q;
   const T app = S[P][P], aqq = S[Q][Q], apq = S[P][Q];
   if (apq == T(0)) return;
-  // tau and t only choose the angle; c and s below are formed from t consistently, so the
-  // fast reciprocal does here (|tau| -> inf gives t = 0, the identity)
-  const T tau = fast_div(aqq - app, T(2) * apq);
-  const T t = fast_div(copysign_(T(1), tau), fabs_(tau) + sqrt_(T(1) + tau * tau));
-  const T c = kExact ? T(1) / sqrt_(T(1) + t * t) : rsqrt_(T(1) + t * t), s = t * c;
-  // S <- Q^T S Q with Q = I except Q_pp = c, Q_pq = s, Q_qp = -s, Q_qq = c
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {  // columns: S Q
-    const T skp = S[k][P], skq = S[k][Q];
-    S[k][P] = c * skp - s * skq;
-    S[k][Q] = s * skp + c * skq;
+  T c, s, t;
+  if constexpr (sizeof(T) == 8) {
+    // FP64 (the snow clamp's fix-up, where the FP64 pipe is the limit): a pair already below
+    // the stopping threshold is left alone, the rotation comes from two reciprocal square roots
+    // and no division, and S is updated in five products (below).  With d = S_qq - S_pp,
+    // e = 2 S_pq and h = |(d, e)|: t = sgn(d) e / (h + |d|); with g = 1 / sqrt(2 h (h + |d|)),
+    // c = (h + |d|) g, s = sgn(d) e g (so c^2 + s^2 = 1) and t = s / c = 2 h g^2 sgn(d) e.
+    if (apq * apq <= JacobiLimits<T>::kDone * fabs_(app * aqq)) return;
+    const T d = aqq - app, e = T(2) * apq, ad = fabs_(d);
+    const T q = d * d + e * e;
+    const T h = q * rsqrt_(q);
+    const T g = rsqrt_(T(2) * h * (h + ad));
+    const T se = copysign_(T(1), d) * e;
+    c = (h + ad) * g;
+    s = se * g;
+    t = T(2) * h * g * g * se;
+  } else {
+    // tau and t only choose the angle; c and s below are formed from t consistently, so the
+    // fast reciprocal does here (|tau| -> inf gives t = 0, the identity)
+    const T tau = fast_div(aqq - app, T(2) * apq);
+    t = fast_div(copysign_(T(1), tau), fabs_(tau) + sqrt_(T(1) + tau * tau));
+    c = kExact ? T(1) / sqrt_(T(1) + t * t) : rsqrt_(T(1) + t * t);
+    s = t * c;
   }
+  // S <- Q^T S Q with Q = I except Q_pp = c, Q_pq = s, Q_qp = -s, Q_qq = c
+  if constexpr (sizeof(T) == 8) {
+    // the rotated diagonal is S_pp - t S_pq and S_qq + t S_pq, and only the two entries in the
+    // third row and column mix besides (the updates of Rutishauser's cyclic Jacobi, as in
+    // Numerical Recipes' `jacobi`): five products instead of the two-sided product
+    const T apr = S[P][R], aqr = S[Q][R];
+    S[P][P] = app - t * apq;
+    S[Q][Q] = aqq + t * apq;
+    const T npr = c * apr - s * aqr, nqr = s * apr + c * aqr;
+    S[P][R] = npr;
+    S[R][P] = npr;
+    S[Q][R] = nqr;
+    S[R][Q] = nqr;
+  } else {
+    // FP32: the two-sided product (the FP32 step's results are pinned to its rounding)
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {  // rows: Q^T (S Q)
-    const T spk = S[P][k], sqk = S[Q][k];
-    S[P][k] = c * spk - s * sqk;
-    S[Q][k] = s * spk + c * sqk;
+    for (int k = 0; k < 3; ++k) {  // columns: S Q
+      const T skp = S[k][P], skq = S[k][Q];
+      S[k][P] = c * skp - s * skq;
+      S[k][Q] = s * skp + c * skq;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {  // rows: Q^T (S Q)
+      const T spk = S[P][k], sqk = S[Q][k];
+      S[P][k] = c * spk - s * sqk;
+      S[Q][k] = s * spk + c * sqk;
+    }
   }
   S[P][Q] = T(0);
   S[Q][P] = T(0);
@@ -239,7 +296,7 @@ MPM_HD void qr_givens(T B[3][3], T U[3][3]) {
   const T n2 = a1 * a1 + a2 * a2;
   T c = T(1), s = T(0);
   if (n2 > T(1e-38)) {
-    if constexpr (kExact) {  // c = +-1, s = 0 exactly when a2 is negligible against a1
+    if constexpr (kExact && sizeof(T) == 4) {  // c = +-1, s = 0 exactly when a2 is negligible
       const T r = sqrt_(n2);
       c = a1 / r;
       s = a2 / r;
@@ -263,21 +320,6 @@ MPM_HD void qr_givens(T B[3][3], T U[3][3]) {
   }
 }
 
-// Jacobi sweeps and stopping threshold per precision: done once every S_pq^2 is below
-// (2 eps)^2 S_pp S_qq, eps the precision's unit roundoff (2.4e-7 in FP32; 1.1e-16 in FP64).
-template <typename T>
-struct JacobiLimits;
-template <>
-struct JacobiLimits<float> {
-  static constexpr int kSweeps = 4;
-  static constexpr float kDone = 2.3e-13f;  // (4.8e-7)^2
-};
-template <>
-struct JacobiLimits<double> {
-  static constexpr int kSweeps = 6;
-  static constexpr double kDone = 4.9e-32;  // (2.2e-16)^2
-};
-
 // Columns of V made orthonormal (modified Gram-Schmidt): a rotation given to lower precision
 // becomes one to the precision of T.
 template <typename T>
@@ -290,7 +332,7 @@ MPM_HD void orthonormalize_columns(T V[3][3]) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) V[k][c] -= d * V[k][p];
     }
-    const T inv = T(1) / sqrt_(V[0][c] * V[0][c] + V[1][c] * V[1][c] + V[2][c] * V[2][c]);
+    const T inv = rsqrt_(V[0][c] * V[0][c] + V[1][c] * V[1][c] + V[2][c] * V[2][c]);
 #pragma unroll
     for (int k = 0; k < 3; ++k) V[k][c] *= inv;
   }
