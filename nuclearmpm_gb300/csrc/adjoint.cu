@@ -56,22 +56,18 @@ __device__ __forceinline__ float wprod(const Stencil<D> &s, const int oo[3]) {
   return w;
 }
 
-// d fx from the adjoints of the stencil weights W_o = prod_d w_d(o_d).
+// d fx from the adjoint Wbar of one stencil weight W_o = prod_d w_d(o_d), accumulated node by
+// node (so no array of the 27 weight adjoints stays live across the stencil loop).
 template <int D>
-__device__ __forceinline__ void weight_backward(const Stencil<D> &s, const float *Wbar, float gfx[D]) {
-  constexpr int S = (D == 3) ? 27 : 9;
+__device__ __forceinline__ void weight_backward(const Stencil<D> &s, const int oo[3], float Wbar,
+                                                float gfx[D]) {
 #pragma unroll
-  for (int o = 0; o < S; ++o) {
-    int oo[3];
-    offs<D>(o, oo);
+  for (int d = 0; d < D; ++d) {
+    float other = 1.0f;
 #pragma unroll
-    for (int d = 0; d < D; ++d) {
-      float other = 1.0f;
-#pragma unroll
-      for (int e = 0; e < D; ++e)
-        if (e != d) other *= s.w[oo[e]][e];
-      gfx[d] += Wbar[o] * other * s.dw[oo[d]][d];
-    }
+    for (int e = 0; e < D; ++e)
+      if (e != d) other *= s.w[oo[e]][e];
+    gfx[d] += Wbar * other * s.dw[oo[d]][d];
   }
 }
 
@@ -273,16 +269,19 @@ __device__ __forceinline__ Mat<D> snow_backward(const Mat<D> &Fh, float Jp, cons
 // Writes the adjoint of x, F and Jp (partial; adj_p2g adds the P2G part) and scatters the
 // adjoint of the updated grid velocity into VB.
 // ---------------------------------------------------------------------------------------
-template <int D, bool kRef>
+// kMat >= 0 fixes the material at compile time (jelly: the plastic branches and their registers
+// drop out); -1 reads it from `model_rt`.
+template <int D, bool kRef, int kMat>
 __global__ void __launch_bounds__(128) adj_g2p_kernel(
     int n, const float *__restrict__ x, const float *__restrict__ F,
     const float *__restrict__ Jp, const float *__restrict__ Cn, const float4 *__restrict__ V,
-    Params P, int model, const float *__restrict__ gx, const float *__restrict__ gv,
+    Params P, int model_rt, const float *__restrict__ gx, const float *__restrict__ gv,
     const float *__restrict__ gF, const float *__restrict__ gC, const float *__restrict__ gJp,
     float *__restrict__ ox, float *__restrict__ oF, float *__restrict__ oJp,
     float *__restrict__ VB, int *err) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
+  const int model = kMat >= 0 ? kMat : model_rt;
   constexpr int S = (D == 3) ? 27 : 9;
   float xp[D];
 #pragma unroll
@@ -338,7 +337,7 @@ __global__ void __launch_bounds__(128) adj_g2p_kernel(
     gvt[i] = (gv ? gv[(size_t)p * D + i] : 0.0f) + P.dt * gxp[i];
   }
   const float cs = P.cscale;
-  float Wbar[S], gfx[D];
+  float gfx[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) gfx[d] = 0.0f;
   const int64_t f0 = flat_index<D>(st.base, P.N);
@@ -348,7 +347,6 @@ __global__ void __launch_bounds__(128) adj_g2p_kernel(
     offs<D>(o, oo);
     const int64_t f = (D == 3) ? f0 + ((int64_t)oo[0] * P.N + oo[1]) * P.N + oo[2]
                                : f0 + (int64_t)oo[0] * P.N + oo[1];
-    Wbar[o] = 0.0f;
     if (f < 0 || f >= P.nodes) {
       atomicOr(err, kErrOutOfRange);
       continue;
@@ -369,7 +367,7 @@ __global__ void __launch_bounds__(128) adj_g2p_kernel(
       wb += gvt[a] * vg[a] + cs * vg[a] * gcdu;
     }
     red_add_v4(reinterpret_cast<float4 *>(VB) + f, add[0], add[1], add[2], 0.0f);
-    Wbar[o] = wb;
+    weight_backward<D>(st, oo, wb, gfx);
 #pragma unroll
     for (int b = 0; b < D; ++b) {
       float gctv = 0.0f;
@@ -378,7 +376,6 @@ __global__ void __launch_bounds__(128) adj_g2p_kernel(
       gfx[b] -= cs * W * gctv;
     }
   }
-  weight_backward<D>(st, Wbar, gfx);
 #pragma unroll
   for (int d = 0; d < D; ++d) ox[(size_t)p * D + d] = gxp[d] + P.inv_dx * gfx[d];
 }
@@ -430,14 +427,15 @@ __device__ __forceinline__ void pair_add(float &hi, float &lo, float h2, float l
 // (rm.lame: each row's mu_0, lambda_0) it also accumulates each row's own adjoints into
 // rm.grad[2 row], rm.grad[2 row + 1]: one thread per row, so no atomics.
 // ---------------------------------------------------------------------------------------
-template <int D, int kStress>
+template <int D, int kStress, int kMat>
 __global__ void __launch_bounds__(128) adj_p2g_kernel(
     int n, const float *__restrict__ x, const float *__restrict__ v, const float *__restrict__ F,
     const float *__restrict__ C, const float *__restrict__ Jp, const float *__restrict__ mass,
-    const float *__restrict__ vol, const float4 *__restrict__ GB, Params P, int model,
+    const float *__restrict__ vol, const float4 *__restrict__ GB, Params P, int model_rt,
     float *__restrict__ ox, float *__restrict__ ov, float *__restrict__ oF,
     float *__restrict__ oC, float *__restrict__ oJp, double *gml, RowModuli rm, int *err) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int model = kMat >= 0 ? kMat : model_rt;  // as in adj_g2p_kernel
   constexpr int S = (D == 3) ? 27 : 9;
   float gmu = 0.0f, glam = 0.0f;
   if (p < n) {
@@ -461,7 +459,7 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
     for (int i = 0; i < D; ++i)
 #pragma unroll
       for (int j = 0; j < D; ++j) gA.a[i][j] = 0.0f;
-    float gvp[D], gfx[D], Wbar[S];
+    float gvp[D], gfx[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       gvp[d] = 0.0f;
@@ -474,7 +472,6 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
       offs<D>(o, oo);
       const int64_t f = (D == 3) ? f0 + ((int64_t)oo[0] * P.N + oo[1]) * P.N + oo[2]
                                  : f0 + (int64_t)oo[0] * P.N + oo[1];
-      Wbar[o] = 0.0f;
       if (f < 0 || f >= P.nodes) {
         atomicOr(err, kErrOutOfRange);
         continue;
@@ -497,7 +494,7 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
         gvp[a] += W * m * g[a];
         wb += g[a] * (m * vp[a] + ad);
       }
-      Wbar[o] = wb;
+      weight_backward<D>(st, oo, wb, gfx);
 #pragma unroll
       for (int b = 0; b < D; ++b) {
         float atg = 0.0f;
@@ -506,7 +503,6 @@ __global__ void __launch_bounds__(128) adj_p2g_kernel(
         gfx[b] -= P.dx * W * atg;
       }
     }
-    weight_backward<D>(st, Wbar, gfx);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       ox[(size_t)p * D + d] += P.inv_dx * gfx[d];
@@ -632,26 +628,42 @@ void launch_adjoint_step(int n, const float *x, const float *v, const float *F, 
   const unsigned pb = (unsigned)((n + 127) / 128);
   const int model = P.model;
   if (ev) cudaEventRecord(ev[0], st);
+  // jelly rollouts run the kernels with the material fixed (fewer registers, more warps
+  // resident to cover the grid gathers); snow and liquid the runtime-material ones
+  const bool jelly = model == kJelly;
+  auto g2p = [&](auto r, auto mat) {
+    adj_g2p_kernel<D, decltype(r)::value, decltype(mat)::value><<<pb, 128, 0, st>>>(
+        n, x, F, Jp, Cn, V, P, model, gx, gv, gF, gC, gJp, ox, oF, oJp, VB, err);
+  };
+  using Jel = std::integral_constant<int, kJelly>;
+  using Any = std::integral_constant<int, -1>;
   if (n > 0) {
-    if (ref)
-      adj_g2p_kernel<D, true><<<pb, 128, 0, st>>>(n, x, F, Jp, Cn, V, P, model, gx, gv, gF, gC,
-                                                  gJp, ox, oF, oJp, VB, err);
-    else
-      adj_g2p_kernel<D, false><<<pb, 128, 0, st>>>(n, x, F, Jp, Cn, V, P, model, gx, gv, gF, gC,
-                                                   gJp, ox, oF, oJp, VB, err);
+    if (ref) {
+      if (jelly) g2p(std::true_type{}, Jel{});
+      else g2p(std::true_type{}, Any{});
+    } else {
+      if (jelly) g2p(std::false_type{}, Jel{});
+      else g2p(std::false_type{}, Any{});
+    }
   }
   if (ev) cudaEventRecord(ev[1], st);
   adj_grid_kernel<D><<<(unsigned)((P.nodes + 255) / 256), 256, 0, st>>>(V, VB, GB, P);
   if (ev) cudaEventRecord(ev[2], st);
-  if (n > 0)
-    if (P.stress == kNeoHookean)
-      adj_p2g_kernel<D, kNeoHookean><<<pb, 128, 0, st>>>(n, x, v, F, C, Jp, mass, vol, GB, P,
-                                                         model, ox, ov, oF, oC, oJp, gml, rm,
-                                                         err);
-    else
-      adj_p2g_kernel<D, kCorotated><<<pb, 128, 0, st>>>(n, x, v, F, C, Jp, mass, vol, GB, P,
-                                                        model, ox, ov, oF, oC, oJp, gml, rm,
-                                                        err);
+  auto p2g = [&](auto stress, auto mat) {
+    adj_p2g_kernel<D, decltype(stress)::value, decltype(mat)::value><<<pb, 128, 0, st>>>(
+        n, x, v, F, C, Jp, mass, vol, GB, P, model, ox, ov, oF, oC, oJp, gml, rm, err);
+  };
+  using Neo = std::integral_constant<int, kNeoHookean>;
+  using Cor = std::integral_constant<int, kCorotated>;
+  if (n > 0) {
+    if (P.stress == kNeoHookean) {
+      if (jelly) p2g(Neo{}, Jel{});
+      else p2g(Neo{}, Any{});
+    } else {
+      if (jelly) p2g(Cor{}, Jel{});
+      else p2g(Cor{}, Any{});
+    }
+  }
   if (ev) cudaEventRecord(ev[3], st);
 }
 
