@@ -300,6 +300,20 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
   Mat<D> R = Fh;
   if (material == kJelly) {
     if (need_R) R = polar_R(Fh);
+  } else if (material == kLiquid) {
+    // src/nclr.h:253-257: F = diag(1) with F_00 = J = prod sigma.  The signed SVD's product
+    // is det F_hat (U, V rotations; |det F_hat| under the 2D reference physics, whose SVD
+    // keeps sigma >= 0), taken here from the determinant: no SVD, and no error from the
+    // singular values' rounding where F_hat is nearly singular (the reference physics' 3D
+    // diag(1, 1, 0) makes its third row O(dt C)).
+    float J = det(Fh);
+    if (D == 2 && kRef) J = fabsf(J);
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) Fh.a[i][j] = diag_one<D, kRef>(i, j);
+    Fh.a[0][0] = J;
+    R = need_R ? polar_R(Fh) : Fh;
   } else {
     Mat<D> U, Vm;
     float sig[D];
@@ -325,16 +339,6 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
         }
       }
       snow_clamp_fp32<D>(U, sig, Vm, Fh, Jp, R, need_R);
-    } else {  // liquid: J = prod sigma accumulated in double (src/nclr.h:253-257)
-      double J = 1.0;
-#pragma unroll
-      for (int d = 0; d < D; ++d) J *= (double)sig[d];
-#pragma unroll
-      for (int i = 0; i < D; ++i)
-#pragma unroll
-        for (int j = 0; j < D; ++j) Fh.a[i][j] = diag_one<D, kRef>(i, j);
-      Fh.a[0][0] = (float)J;
-      R = need_R ? polar_R(Fh) : Fh;
     }
   }
   F = Fh;
