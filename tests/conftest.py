@@ -40,17 +40,55 @@ FLOORS = {"x": 1.0, "v": 1e-2, "F": 1.0, "C": 1.0, "Jp": 1.0, "grid_v": 1e-2, "g
 # the FP32 oracle within one more multiple (the two FP32 runs sit on either side of FP64).  The
 # factor is measured: the largest error over millions of particles is set by the few particles
 # whose rounding the step amplifies most, and two FP32 summation orders pick different ones
-# (2.7x on Jp of the deformed 4.19M-particle liquid + snow scene).
+# (2.7x on Jp of the deformed 4.19M-particle liquid + snow scene).  The FP32 yardstick is
+# therefore taken over more than one summation order where the callers can (the threaded
+# oracle's P2G order follows its thread count: on the 3D snow golden after 20 steps, one thread
+# lands 2.8x further from FP64 in C than four).
 FP32_CLASS_FACTOR = 4.0
 
+# Where the snow clamp's result is discontinuous (det F_hat < 0 with |s_3| close to s_2: the
+# clamp lifts s_3, and which singular vector carries the sign flips at |s_3| = s_2), a particle
+# whose F_hat lies within rounding of the discontinuity gets an O(1)-different F from any two
+# implementations, and the normwise maximum over millions of particles is then set by whether
+# one such particle falls on the other side in this run.  For F and Jp, `ill(rows)` (when given)
+# says which rows are such points: the rows beyond the FP32-class bound must all be among them,
+# be few (CLAMP_ILL_MAX_FRACTION of the rows, at least 50), and the bulk must stay in the FP32
+# class by the 99.99th percentile of the per-row errors.
+CLAMP_ILL_FIELDS = ("F", "Jp")
+CLAMP_ILL_MAX_FRACTION = 1e-5
+ROW_QUANTILE = 0.9999
 
-def check_fp32_class(gpu: dict, o32: dict, o64: dict, base, fields=FIELDS, what=""):
-    """Asserts the FP32-class bounds per field; `base` is a number or a per-field dict."""
+
+def row_err(a, b, name):
+    """Per-row error of a field, normalised like field_err (the same denominator)."""
+    a = np.asarray(a, dtype=np.float64).reshape(len(a), -1)
+    b = np.asarray(b, dtype=np.float64).reshape(len(b), -1)
+    den = max(float(np.abs(b).max()), FLOORS.get(name, 1.0)) if b.size else 1.0
+    return np.abs(a - b).max(1) / den
+
+
+def check_fp32_class(gpu: dict, o32, o64: dict, base, fields=FIELDS, what="", ill=None):
+    """Asserts the FP32-class bounds per field; `base` is a number or a per-field dict; `o32`
+    one FP32 oracle result or a list of them in different summation orders (the yardstick is
+    the furthest from FP64; the GPU is compared with the nearest); `ill` (optional) marks the
+    snow clamp's ill-conditioned rows (see CLAMP_ILL_FIELDS)."""
+    o32s = o32 if isinstance(o32, (list, tuple)) else [o32]
     for f in fields:
         b = base[f] if isinstance(base, dict) else base
-        own = field_err(o32[f], o64[f], f)
+        own = max(field_err(o[f], o64[f], f) for o in o32s)
         e64 = field_err(gpu[f], o64[f], f)
-        e32 = field_err(gpu[f], o32[f], f)
+        e32 = min(field_err(gpu[f], o[f], f) for o in o32s)
+        if ill is not None and f in CLAMP_ILL_FIELDS and e64 > max(b, FP32_CLASS_FACTOR * own):
+            rg = row_err(gpu[f], o64[f], f)
+            qg = float(np.quantile(rg, ROW_QUANTILE))
+            qo = max(float(np.quantile(row_err(o[f], o64[f], f), ROW_QUANTILE)) for o in o32s)
+            assert qg <= max(b, FP32_CLASS_FACTOR * qo), (what, f, "bulk vs fp64", qg, qo)
+            beyond = np.nonzero(rg > max(b, FP32_CLASS_FACTOR * own))[0]
+            assert len(beyond) <= max(50, CLAMP_ILL_MAX_FRACTION * len(rg)), (what, f, len(beyond))
+            at_clamp = ill(beyond)
+            assert at_clamp.all(), (what, f, "rows beyond the FP32 class off the clamp's "
+                                    "ill-conditioned set", beyond[~at_clamp][:10])
+            continue
         assert e64 <= max(b, FP32_CLASS_FACTOR * own), (what, f, "vs fp64", e64, own)
         assert e32 <= max(b, (FP32_CLASS_FACTOR + 1.0) * own), (what, f, "vs fp32", e32, own)
 

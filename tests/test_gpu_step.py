@@ -49,13 +49,17 @@ PATHS = {"small": {"small_scene_max": 1 << 30}, "tile": {"small_scene_max": 0}}
 
 
 # At every snapshot of a golden run, the GPU's distance to the FP64 oracle must stay within
-# this factor of the FP32 distance to it (the reference's own, or the FP32 oracle's where
-# larger), or under FP64_FLOOR.  The largest measured ratios, 3.5 to 4.4, are on the
-# small-scene path for the 3D snow blocks (reference physics, where the scene flies apart):
-# that path adds every particle's contribution to the grid with global atomics, in whatever
-# order they arrive.
+# this factor of the FP32 distance to it, or under FP64_FLOOR.  The FP32 distance is the
+# largest of three FP32 runs of the same steps: the reference's own, and the FP32 oracle in two
+# summation orders (one thread, and four: its threaded P2G splits the grid into slabs by thread
+# count).  Over a trajectory that flies apart (the 3D snow blocks under the reference physics)
+# the distance after 20 steps depends on the summation order by a factor of 2.8 among those
+# runs alone, and the GPU's small-scene path adds every particle's contribution to the grid
+# with global atomics, in whatever order they arrive.  The largest measured ratios, 3.5 to 5.4
+# against the reference and the four-thread oracle alone, are on that path.
 GOLDEN_FP64_FACTOR = 5.0
 FP64_FLOOR = 1e-6
+FP32_ORDERS = (4, 1)  # oracle thread counts, i.e. P2G summation orders
 
 
 @pytest.mark.parametrize("path", sorted(PATHS))
@@ -75,13 +79,19 @@ def test_matches_reference_goldens(oracle, name, path):
                 assert field_err(out[f], z[f"{f}@{k}"], f) <= DRIFT[f], (k, f)
         o64, _, st, _ = oracle.advance(state, steps=k, fp64=True, want_grid=False, threads=4,
                                        **params)
-        o32, _, st32, _ = oracle.advance(state, steps=k, want_grid=False, threads=4, **params)
-        assert st == 0 and st32 == 0
+        o32s = []
+        for th in FP32_ORDERS:
+            o32, _, st32, _ = oracle.advance(state, steps=k, want_grid=False, threads=th,
+                                             **params)
+            assert st32 == 0
+            o32s.append(o32)
+        assert st == 0
         for f in FIELDS:
-            # the FP32 yardstick: the reference's own distance to FP64, or the FP32 oracle's
-            # where that is larger (the reference here computes its SVD in double, through
-            # the Eigen stand-in, so its snow and liquid sit closer to FP64 than an FP32 SVD)
-            own = max(field_err(z[f"{f}@{k}"], o64[f], f), field_err(o32[f], o64[f], f))
+            # the FP32 yardstick: the largest distance to FP64 of the reference's own run and the
+            # FP32 oracle's (the reference here computes its SVD in double, through the Eigen
+            # stand-in, so its snow and liquid sit closer to FP64 than an FP32 SVD)
+            own = max([field_err(z[f"{f}@{k}"], o64[f], f)] +
+                      [field_err(o[f], o64[f], f) for o in o32s])
             e64 = field_err(out[f], o64[f], f)
             assert e64 <= max(GOLDEN_FP64_FACTOR * own, FP64_FLOOR), (k, f, e64, own)
 
