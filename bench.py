@@ -245,11 +245,12 @@ def tune_plain(state: dict, model: int, res: int, device: int, physics: int = 0,
     """The project's autotuner (nuclearmpm_gb300.autotune) on this workload: re-sort interval
     and thin-block threshold, from short timed runs of the simulation itself."""
     from nuclearmpm_gb300 import MPMSimulation, autotune
-    # 64-step runs (about 12 ms each at 1M particles): the candidates differ by a few percent,
-    # which shorter runs timed on the host do not resolve
+    # 128-step runs, best of three (about 23 ms each at 1M particles): the candidates differ by
+    # a few percent (re-sorting every 8 steps against 16 trades sort time against a faster
+    # fused kernel), which shorter runs timed on the host resolve differently from run to run
     return autotune.tune(lambda **o: MPMSimulation(dict(state), model, res=res, device=device,
                                                    physics=physics, material=material, **o),
-                         key=None, candidates=autotune.PLAIN_CANDIDATES, steps=64, repeats=2,
+                         key=None, candidates=autotune.PLAIN_CANDIDATES, steps=128, repeats=3,
                          cache_path=None)
 
 
@@ -301,9 +302,11 @@ def run_batched(device: int, steps: int = 100, sequential: bool = True, repeats:
     from nuclearmpm_gb300 import BatchSimulation, MPMSimulation, autotune, scenes
     scs = scenes.batched_scenes_2d(seed=0)
     total = sum(len(sc["x"]) for sc in scs)
+    # tuned on runs as long as the timed one, best of three each: the candidates' times differ
+    # by a few percent, and shorter runs let the noise pick a different one from run to run
     tuned = autotune.tune(lambda **o: BatchSimulation(scs, device=device, **o), key=None,
-                          candidates=autotune.BATCH_CANDIDATES, steps=32, repeats=2,
-                          cache_path=None)
+                          candidates=autotune.BATCH_CANDIDATES, steps=steps, repeats=3,
+                          graph_steps=steps, cache_path=None)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def best_of(sim) -> float:
@@ -318,12 +321,13 @@ def run_batched(device: int, steps: int = 100, sequential: bool = True, repeats:
             best = min(best, a.elapsed_time(b) / 1e3)
         return best
 
-    batch = BatchSimulation(scs, device=device, graph_steps=steps, **tuned)
+    batch = BatchSimulation(scs, device=device, **tuned)  # tuned includes graph_steps = steps
     t_batch = best_of(batch)
     launches = batch.stats()[0]
     batch.close()
     # the fused kernel's roofline: the same batch with per-kernel CUDA events (direct launches)
-    pb = BatchSimulation(scs, device=device, profile=True, **tuned)
+    pb = BatchSimulation(scs, device=device, profile=True,
+                         **{k: v for k, v in tuned.items() if k != "graph_steps"})
     pb.advance(steps)
     pb.profile_reset()
     pb.advance(steps)
