@@ -437,34 +437,43 @@ __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
   }
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
-  for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < total_blocks;
-       gb += warps) {
-    const uint8_t fl = flags[gb];
-    if (!fl) continue;
-    int bc[D];
-    const int sid = block_origin<D>(gb, scenes, block_scene, bc);
-    const Params P = scenes[sid].P;
-    float4 *Gs = G + scenes[sid].node_off;
-    float4 *Vs = V + scenes[sid].node_off;
-    for (int t = lane; t < BN; t += 32) {
-      int idx[D];
-      bool in = true;
-      int r = t;
+  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  // This warp's blocks are wid, wid + warps, ...; their flags are read 32 at a time (one per
+  // lane) and only the flagged ones are visited, so the flag loads do not chain block by block.
+  for (int k0 = 0; wid + k0 * warps < total_blocks; k0 += 32) {
+    const int mine = wid + (k0 + lane) * warps;
+    const uint8_t fl_l = mine < total_blocks ? flags[mine] : 0;
+    unsigned todo = __ballot_sync(0xffffffffu, fl_l != 0);
+    while (todo) {
+      const int k = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int gb = wid + (k0 + k) * warps;
+      const uint8_t fl = __shfl_sync(0xffffffffu, fl_l, k);
+      int bc[D];
+      const int sid = block_origin<D>(gb, scenes, block_scene, bc);
+      const Params P = scenes[sid].P;
+      float4 *Gs = G + scenes[sid].node_off;
+      float4 *Vs = V + scenes[sid].node_off;
+      for (int t = lane; t < BN; t += 32) {
+        int idx[D];
+        bool in = true;
+        int r = t;
 #pragma unroll
-      for (int d = D - 1; d >= 0; --d) {
-        idx[d] = bc[d] + r % BS;
-        r /= BS;
-        in &= idx[d] < P.N;
+        for (int d = D - 1; d >= 0; --d) {
+          idx[d] = bc[d] + r % BS;
+          r /= BS;
+          in &= idx[d] < P.N;
+        }
+        if (!in) continue;
+        const int64_t f = flat_index<D>(idx, P.N);
+        const float4 g = Gs[f];
+        float v[D], m;
+        grid_update<D>(g, idx, P, v, m);
+        Vs[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
+        Gs[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
-      if (!in) continue;
-      const int64_t f = flat_index<D>(idx, P.N);
-      const float4 g = Gs[f];
-      float v[D], m;
-      grid_update<D>(g, idx, P, v, m);
-      Vs[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
-      Gs[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (lane == 0) flags[gb] = (fl & kPending) ? kVNonzero : 0;
     }
-    if (lane == 0) flags[gb] = (fl & kPending) ? kVNonzero : 0;
   }
 }
 
@@ -1356,8 +1365,15 @@ template <int D>
 void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
                        const uint16_t *block_scene, int total_blocks, int *work, int sms,
                        cudaStream_t st, int *fix_count) {
+  // one wave: as many CTAs as are resident at once (a second, partial wave left the SMs idle
+  // for 45% of the kernel)
+  static int resident = 0;
+  if (!resident) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, grid_sweep_kernel<D>, 256, 0);
+    if (resident < 1) resident = 1;
+  }
   int64_t blocks = blocks_for((int64_t)total_blocks * 32, 256);
-  if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
+  if (blocks > (int64_t)sms * resident) blocks = (int64_t)sms * resident;
   if (blocks < 1) blocks = 1;
   grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, flags, scenes, block_scene,
                                                           total_blocks, work, fix_count);
