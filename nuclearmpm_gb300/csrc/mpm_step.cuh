@@ -298,8 +298,11 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
     for (int j = 0; j < D; ++j) M.a[i][j] = diag_one<D, kRef>(i, j) + dt * C.a[i][j];
   Mat<D> Fh = mat_mul<D>(M, F);
   Mat<D> R = Fh;
+  // jelly and liquid take the polar rotation of their new F from one call after the branch
+  // (one inlined SVD for both in the kernels that read the material per particle)
+  bool polar = false;
   if (material == kJelly) {
-    if (need_R) R = polar_R(Fh);
+    polar = need_R;
   } else if (material == kLiquid) {
     // src/nclr.h:253-257: F = diag(1) with F_00 = J = prod sigma.  The signed SVD's product
     // is det F_hat (U, V rotations; |det F_hat| under the 2D reference physics, whose SVD
@@ -313,7 +316,8 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
 #pragma unroll
       for (int j = 0; j < D; ++j) Fh.a[i][j] = diag_one<D, kRef>(i, j);
     Fh.a[0][0] = J;
-    R = need_R ? polar_R(Fh) : Fh;
+    R = Fh;
+    polar = need_R;
   } else {
     Mat<D> U, Vm;
     float sig[D];
@@ -341,6 +345,7 @@ __device__ __forceinline__ Mat<D> update_F(const Mat<D> &C, Mat<D> &F, float &Jp
       snow_clamp_fp32<D>(U, sig, Vm, Fh, Jp, R, need_R);
     }
   }
+  if (polar) R = polar_R(Fh);
   F = Fh;
   return R;
 }
