@@ -590,7 +590,8 @@ g2p2g_kernel(
   // Single simulations: thread 0 claims item k+1 right after item k's particle loop, so the
   // claim's latency overlaps item k's flush, and publishes it in s_item after its own share
   // of the flush (everyone read s_item for item k before the tile-load barrier): three
-  // barriers per item (measured 0-4% faster than claiming at the top, never slower).
+  // barriers per item (measured up to 4% faster than claiming at the top; within noise on
+  // the dense jelly scene).
   // Batches claim at the top, behind a barrier, as their per-item parameters sit in shared
   // memory that the flush still reads.
   int nx_it = 0;
