@@ -68,6 +68,14 @@ template <int D> cudaError_t launch_small_steps(const PState &s, const Params &P
                                                int steps, int *err, unsigned *bar, bool ref, int ctas,
                                                cudaStream_t st, BarrierTest bt = BarrierTest{});
 template <int D> int small_ctas_per_sm(bool ref);
+// The small-scene kernel launched as one thread-block cluster (the step's barriers are the
+// cluster's hardware barrier): `ctas` <= small_cluster_max(ref, threads) CTAs of `threads`
+// (<= kSmallClusterThreads[dim]) threads.
+template <int D> cudaError_t launch_small_cluster(const PState &s, const Params &P, float4 *G,
+                                                  float4 *V, int steps, int *err, unsigned *bar,
+                                                  bool ref, int ctas, int threads, cudaStream_t st);
+template <int D> int small_cluster_max(bool ref, int threads);
+constexpr int kSmallClusterThreads2D = 640, kSmallClusterThreads3D = 512;
 // The same for a batch: CTA c works on scene cta_scene[c]; scene s owns CTAs
 // [group_first[s], group_first[s+1]) and the barrier bars[2s..2s+1] (zeroed).
 template <int D> cudaError_t launch_small_batch(const PState &s, const Scene *scenes, const uint16_t *cta_scene,

@@ -1125,12 +1125,31 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned c
   return s_ok != 0;
 }
 
-template <int D, bool kRef>
-__global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Params P,
-                                                                    float4 *__restrict__ G,
-                                                                    float4 *__restrict__ V,
-                                                                    int steps, int *err,
-                                                                    unsigned *bar, BarrierTest bt) {
+// The hardware barrier of a thread-block cluster, with release/acquire at cluster scope: every
+// CTA's global writes before it (the P2G reductions, V) are visible to every CTA after it.
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Threads per CTA of the small-scene kernel launched as one cluster (registers allow these
+// without spills: up to 80 a thread in 2D, 127 in 3D).
+template <int D>
+constexpr int small_cluster_threads() {
+  return D == 3 ? 512 : 640;
+}
+static_assert(small_cluster_threads<2>() == kSmallClusterThreads2D &&
+                  small_cluster_threads<3>() == kSmallClusterThreads3D,
+              "the host sizes cluster launches by these");
+
+// kCluster: the launch is a single thread-block cluster (every CTA resident on one GPC) and
+// the step's two barriers are the cluster's hardware barrier; otherwise a cooperative launch
+// with the bounded grid barrier above.
+template <int D, bool kRef, bool kCluster = false>
+__global__ void __launch_bounds__(kCluster ? small_cluster_threads<D>() : kSmallThreads)
+small_steps_kernel(PState s, Params P, float4 *__restrict__ G, float4 *__restrict__ V, int steps,
+                   int *err, unsigned *bar, BarrierTest bt) {
   constexpr int S = (D == 3) ? 27 : 9;
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1164,7 +1183,8 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
         red_add_v4(G + f, c[0], c[1], c[2], c[3]);
       }
     }
-    if (!grid_barrier(bar, err, gridDim.x + bt.extra, bt.spins)) return;
+    if constexpr (kCluster) cluster_barrier();
+    else if (!grid_barrier(bar, err, gridDim.x + bt.extra, bt.spins)) return;
     // ---- grid_op (src/nclr.h:263-310): V = op(G), and G cleared for the next p2g ----
     for (int64_t i = tid; i < P.nodes; i += stride) {
       int idx[D];
@@ -1174,7 +1194,8 @@ __global__ void __launch_bounds__(kSmallThreads) small_steps_kernel(PState s, Pa
       V[i] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
       G[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    if (!grid_barrier(bar, err, gridDim.x + bt.extra, bt.spins)) return;
+    if constexpr (kCluster) cluster_barrier();
+    else if (!grid_barrier(bar, err, gridDim.x + bt.extra, bt.spins)) return;
     // ---- g2p (src/nclr.h:167-261) ----
     for (int p = tid; p < P.n; p += stride) {
       float x[D], v[D], fx[D], w[3][D];
@@ -1578,6 +1599,58 @@ cudaError_t launch_small_steps(const PState &s, const Params &P, float4 *G, floa
   return cudaLaunchCooperativeKernel(fn, dim3((unsigned)ctas), dim3(kSmallThreads), args, 0, st);
 }
 
+// The small-scene kernel as one thread-block cluster of `ctas` CTAs of `threads` threads
+// (threads <= small_cluster_threads<D>(); ctas <= small_cluster_max<D>(threads)).
+template <int D>
+cudaError_t launch_small_cluster(const PState &s, const Params &P, float4 *G, float4 *V,
+                                 int steps, int *err, unsigned *bar, bool ref, int ctas,
+                                 int threads, cudaStream_t st) {
+  PState sv = s;
+  Params Pv = P;
+  BarrierTest bt{};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)ctas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return ref ? cudaLaunchKernelEx(&cfg, small_steps_kernel<D, true, true>, sv, Pv, G, V, steps,
+                                  err, bar, bt)
+             : cudaLaunchKernelEx(&cfg, small_steps_kernel<D, false, true>, sv, Pv, G, V, steps,
+                                  err, bar, bt);
+}
+
+// The largest cluster (CTAs) the small-scene kernel can be launched as with `threads` threads
+// per CTA: 16 where the device allows non-portable clusters, else 8 (0: no cluster launch).
+template <int D>
+int small_cluster_max(bool ref, int threads) {
+  const void *fn = ref ? (const void *)small_steps_kernel<D, true, true>
+                       : (const void *)small_steps_kernel<D, false, true>;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(16);
+  cfg.blockDim = dim3((unsigned)threads);
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 16;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int size = 0;
+  if (cudaOccupancyMaxPotentialClusterSize(&size, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return size >= 16 ? 16 : (size >= 8 ? 8 : size);
+}
+
 template <int D>
 cudaError_t launch_small_batch(const PState &s, const Scene *scenes, const uint16_t *cta_scene,
                                const int *group_first, float4 *G, float4 *V, uint8_t *flags,
@@ -1701,6 +1774,10 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
                                 cudaStream_t, const Record &, const SnowFix &, int);             \
   template int g2p2g_ctas_per_sm<D>();                                                           \
   template int g2p_final_ctas_per_sm<D>();                                                       \
+  template cudaError_t launch_small_cluster<D>(const PState &, const Params &, float4 *,          \
+                                               float4 *, int, int *, unsigned *, bool, int, int, \
+                                               cudaStream_t);                                    \
+  template int small_cluster_max<D>(bool, int);                                                  \
   template cudaError_t launch_small_steps<D>(const PState &, const Params &, float4 *, float4 *,   \
                                              int, int *, unsigned *, bool, int, cudaStream_t,   \
                                              BarrierTest);                                       \

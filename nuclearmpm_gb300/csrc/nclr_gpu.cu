@@ -75,6 +75,7 @@ struct nclr_sim {
   int small_max = 0;          // particles up to which advance() uses the small-scene kernel
   bool small_auto = false;    // the default limits: also at most kSmallNodesPerParticle nodes
   int small_ctas = 0;         // its CTAs that fit on the device at once (0: no cooperative launch)
+  int cluster_max = 0;        // CTAs of the largest cluster it can run as (0: no cluster launch)
   cudaEvent_t field_ev[5] = {};        // x, v, F, C, Jp ready (staged / imported)
   int *work = nullptr;        // fused kernel's block counter
   int *err_d = nullptr;       // per scene: [2s] this call's steps, [2s+1] the P2G after them
@@ -655,6 +656,8 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
     s->small_ctas = coop ? s->sms * (dim == 3 ? mpm::small_ctas_per_sm<3>(ref)
                                              : mpm::small_ctas_per_sm<2>(ref))
                          : 0;
+    s->cluster_max = dim == 3 ? mpm::small_cluster_max<3>(ref, mpm::kSmallClusterThreads3D)
+                              : mpm::small_cluster_max<2>(ref, mpm::kSmallClusterThreads2D);
     // batches keep the tile path unless asked: their small-scene kernel measured 2.9x slower
     // on 256 scenes of 1k-64k particles (its P2G scatters through L2 atomics)
     s->small_max = s->opt.small_scene_max >= 0 ? s->opt.small_scene_max
@@ -982,6 +985,20 @@ nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
       CUDA_TRY(s, cudaMemsetAsync(s->G, 0, sizeof(float4) * (size_t)s->total_nodes, s->stream));
     }
   }
+  // A single scene that fits one thread-block cluster runs as one: the step's two barriers are
+  // then the cluster's hardware barrier instead of an atomic and a poll in L2 (the barrier
+  // test hook keeps the bounded grid barrier, which is what it tests).
+  int cl_ctas = 0, cl_threads = 0;
+  if (!batch && s->cluster_max > 0 && s->bar_test.extra == 0) {
+    const int tmax = s->dim == 3 ? mpm::kSmallClusterThreads3D : mpm::kSmallClusterThreads2D;
+    const int64_t ppt = std::max(1, s->opt.p2g_particles_per_thread);
+    const int64_t c = std::min<int64_t>(s->cluster_max, std::max<int64_t>(1, ctas));
+    const int64_t t = ((s->n + c * ppt - 1) / (c * ppt) + 31) / 32 * 32;
+    if (t <= tmax) {
+      cl_ctas = (int)c;
+      cl_threads = (int)t;
+    }
+  }
   for (int64_t left = nsteps; left > 0;) {
     const int k = (int)std::min<int64_t>(left, (int64_t)1 << 30);
     CUDA_TRY(s, cudaMemsetAsync(s->bar, 0, 2 * sizeof(unsigned) * (size_t)s->nscenes, s->stream));
@@ -989,6 +1006,13 @@ nclr_status advance_small(nclr_sim *s, int64_t nsteps) {
     dispatch_dim(s->dim, [&](auto dc) {
       constexpr int D = decltype(dc)::value;
       phase(s, NCLR_PHASE_G2P2G, 1, [&] {
+        if (cl_ctas > 0) {
+          e = mpm::launch_small_cluster<D>(s->ps[s->cur], s->P0(), s->G, s->V, k, s->err_d,
+                                           s->bar, s->ref, cl_ctas, cl_threads, s->stream);
+          if (e == cudaSuccess) return;
+          cudaGetLastError();  // no cluster of that size now: the cooperative launch below
+          cl_ctas = 0;
+        }
         e = batch ? mpm::launch_small_batch<D>(s->ps[s->cur], s->scenes_d, s->cta_scene,
                                                s->group_first, s->G, s->V, s->flags, k, s->err_d,
                                                s->bar, s->ref, ctas, s->stream, s->bar_test)
