@@ -82,10 +82,12 @@ typedef struct nclr_options {
                               0 = never, -1 = the default (default -1: 64 in 3D and 32 in 2D
                               for one simulation, 32 for a batch) */
   int small_scene_max;     /* simulations of at most this many particles (per scene) run all
-                              the steps of an advance() call in one cooperative kernel launch
-                              (reference order p2g / grid_op / g2p, grid-wide barriers; a
-                              batch gives each scene its own group of CTAs) instead of two
-                              launches per step; 0 = never, -1 = automatic (default -1: one
+                              the steps of an advance() call in one kernel launch (reference
+                              order p2g / grid_op / g2p, grid-wide barriers: one scene that
+                              fits a thread-block cluster runs as one and uses its hardware
+                              barrier, others a cooperative launch; a batch gives each scene
+                              its own group of CTAs) instead of two launches per step;
+                              0 = never, -1 = automatic (default -1: one
                               scene of at most 65,536 particles in 2D or 32,768 in 3D whose grid
                               has at most 8 nodes per particle -- that kernel updates every
                               node each step; never a batch, where the tile path is faster) */
