@@ -302,11 +302,12 @@ def run_batched(device: int, steps: int = 100, sequential: bool = True, repeats:
     from nuclearmpm_gb300 import BatchSimulation, MPMSimulation, autotune, scenes
     scs = scenes.batched_scenes_2d(seed=0)
     total = sum(len(sc["x"]) for sc in scs)
-    # tuned on runs as long as the timed one, best of three each: the candidates' times differ
-    # by a few percent, and shorter runs let the noise pick a different one from run to run
+    # tuned on runs as long as the timed one, best of three each, and the pick confirmed
+    # against the defaults in two alternating rounds: the candidates' times differ by a few
+    # percent, and one noisy measurement can pick a set slower than the defaults
     tuned = autotune.tune(lambda **o: BatchSimulation(scs, device=device, **o), key=None,
                           candidates=autotune.BATCH_CANDIDATES, steps=steps, repeats=3,
-                          graph_steps=steps, cache_path=None)
+                          graph_steps=steps, cache_path=None, confirm=2)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def best_of(sim) -> float:

@@ -54,9 +54,13 @@ def _time(sim, steps: int, repeats: int) -> float:
 
 
 def tune(make_sim, *, key: str | None = None, candidates: dict | None = None, steps: int = 32,
-         repeats: int = 3, cache_path: str | None = CACHE, graph_steps: int | None = None) -> dict:
+         repeats: int = 3, cache_path: str | None = CACHE, graph_steps: int | None = None,
+         confirm: int = 0) -> dict:
     """Returns the fastest option set {knob: value}; `make_sim(**options)` builds the
     simulation.  Knobs are tuned one after another (coordinate descent from the defaults).
+    With `confirm` > 0, the descent's pick is then timed against the defaults (no knob set)
+    in `confirm` alternating rounds, and the defaults win if they are faster: the candidates
+    differ by a few percent, so one noisy measurement in the descent can pick a worse set.
     With `key`, results are cached in `cache_path` and reused."""
     cands = dict(DEFAULT_CANDIDATES if candidates is None else candidates)
     cache = _load(cache_path) if (key and cache_path) else {}
@@ -78,6 +82,20 @@ def tune(make_sim, *, key: str | None = None, candidates: dict | None = None, st
             scored.append((t, v))
             timings[f"{knob}={v}"] = t
         best[knob] = min(scored)[1]
+    if confirm > 0:
+        base = {} if graph_steps is None else {"graph_steps": graph_steps}
+        if best != base:
+            t = {0: float("inf"), 1: float("inf")}
+            for _ in range(confirm):
+                for which, opts in ((0, best), (1, base)):
+                    sim = make_sim(**opts)
+                    try:
+                        t[which] = min(t[which], _time(sim, steps, repeats))
+                    finally:
+                        sim.close()
+            timings["confirm: tuned"], timings["confirm: defaults"] = t[0], t[1]
+            if t[1] < t[0]:
+                best = dict(base)
     if key and cache_path:
         os.makedirs(os.path.dirname(cache_path), exist_ok=True)
         cache[key] = {"best": best, "seconds": timings, "steps": steps}

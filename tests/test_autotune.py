@@ -38,3 +38,34 @@ def test_graph_steps_is_carried():
     best = autotune.tune(lambda **o: FakeSim(**o), candidates={"sort_interval": [2, 4]},
                          steps=1, repeats=1, cache_path=None, graph_steps=100)
     assert best == {"graph_steps": 100, "sort_interval": 4}
+
+
+class LuckySim(FakeSim):
+    """sort_interval 16 measures fast on its first instance only (a noisy measurement), and is
+    slower than the default afterwards."""
+    made = {}
+
+    def __init__(self, sort_interval=8, graph_steps=0):
+        super().__init__(sort_interval, graph_steps)
+        k = LuckySim.made.get(sort_interval, 0)
+        LuckySim.made[sort_interval] = k + 1
+        if sort_interval == 16:
+            self.cost = 1e-5 if k == 0 else 2e-3
+        elif sort_interval == 8:
+            self.cost = 5e-4
+
+
+def test_confirmation_reverts_a_lucky_pick():
+    LuckySim.made = {}
+    cands = {"sort_interval": [4, 16]}
+    assert autotune.tune(lambda **o: LuckySim(**o), candidates=cands, steps=1, repeats=1,
+                         cache_path=None) == {"sort_interval": 16}
+    LuckySim.made = {}
+    assert autotune.tune(lambda **o: LuckySim(**o), candidates=cands, steps=1, repeats=1,
+                         cache_path=None, confirm=2) == {}
+
+
+def test_confirmation_keeps_a_real_gain():
+    cands = {"sort_interval": [1, 4, 16]}
+    assert autotune.tune(lambda **o: FakeSim(**o), candidates=cands, steps=1, repeats=1,
+                         cache_path=None, confirm=2) == {"sort_interval": 4}
