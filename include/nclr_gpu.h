@@ -97,6 +97,12 @@ typedef struct nclr_options {
                               2D default) or 256 (a whole CTA; the 3D one); 0 = the default.
                               An autotuner knob: the best size depends on the particles per
                               block. */
+  int tail_max;            /* one simulation: a grid block of more than 256 particles (at the
+                              last sort) steps them in passes of 256 through its tiles; when
+                              its last pass would hold fewer than this many, those particles
+                              are stepped particle by particle like a thin block's instead, so
+                              that no pass runs a few particles while the rest of the CTA
+                              waits.  0 = never, -1 = the default (64); batches never */
 } nclr_options;
 
 /* Kernel phases reported by nclr_profile_get: the block sort of the particles, the grid

@@ -24,8 +24,10 @@ import time
 
 DEFAULT_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32]}
 # single simulations: also the thin-block threshold (particles per block; 0 = every block
-# through the tile); batches ignore it
-PLAIN_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32], "sparse_block_max": [0, 32, 64, 128, 256]}
+# through the tile) and the tail threshold (a block's last pass of fewer particles goes to the
+# thin-block chunks; 0 = never); batches ignore both
+PLAIN_CANDIDATES = {"sort_interval": [2, 4, 8, 16, 32], "sparse_block_max": [0, 32, 64, 128, 256],
+                    "tail_max": [0, 32, 64, 96, 128]}
 # batches: re-sort interval, threads per item of the fused kernel (2D: half or whole CTAs),
 # thin-block threshold
 BATCH_CANDIDATES = {"sort_interval": [4, 8, 16, 32], "batch_item_threads": [128, 256],

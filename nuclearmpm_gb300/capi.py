@@ -28,7 +28,7 @@ class Options(ctypes.Structure):
                 ("use_graphs", ctypes.c_int), ("profile", ctypes.c_int),
                 ("graph_steps", ctypes.c_int), ("sparse_block_max", ctypes.c_int),
                 ("small_scene_max", ctypes.c_int), ("stress_model", ctypes.c_int),
-                ("batch_item_threads", ctypes.c_int)]
+                ("batch_item_threads", ctypes.c_int), ("tail_max", ctypes.c_int)]
 
 
 class Scene(ctypes.Structure):

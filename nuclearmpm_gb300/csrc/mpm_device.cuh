@@ -62,6 +62,8 @@ struct Params {
   float dt_gravity;     // dt * gravity (src/nclr.h:292)
   int stress;           // kCorotated or kNeoHookean
   int thin_max;         // batches: blocks with fewer particles skip the shared-memory tiles
+  int tail_max;         // single simulations: a block's last pass of fewer particles than
+                        // this goes to the thin-block chunks (compact_blocks_kernel)
   int64_t nodes;        // N^dim
   int nb;               // grid blocks per axis: ceil(N / Tiling<dim>::BS)
   int nblocks;          // nb^dim

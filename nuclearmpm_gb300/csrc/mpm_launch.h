@@ -103,16 +103,21 @@ template <int D> void launch_block_keys(const PState &s, int n, const Scene *sce
                                         cudaStream_t st);
 // Also records inv[id] = new slot and slot_block[new slot] = its grid block.
 template <int D> void launch_sort_move(const PState &src, const PState &dst, int n, const int *key, const int *rank, const int *bstart, const int4 *rounds, const int *count, bool move_vc, int *inv, int *slot_block, cudaStream_t st);
-// The non-empty blocks of the sort: those with at least sparse_max particles (all of them when
-// sparse_max <= 0) into list / nlist[0]; the particle slots of the others, block by block,
-// into sparse / nlist[1].  nlist[0..1] must be zero on entry.
 // The block sort's per-block round tables (block_tables_kernel in scan.cu): btotal[b] and
 // rounds[b * kRoundTable + r] for the nblocks blocks of kCellsPerBlock cells.
 constexpr int kCellsPerBlock = 64;  // Tiling<2>::CPB and Tiling<3>::CPB
 constexpr int kRoundTable = 12;     // rounds with a table entry; later ranks count cell by cell
 void launch_block_tables(const int *count, int nblocks, int *btotal, int4 *rounds, cudaStream_t st);
-void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int *list,
-                           int *nlist, int *sparse, cudaStream_t st);
+// Threads of the fused step's CTA; a single simulation's item steps a block's particles in
+// passes of this many.
+constexpr int kG2P2GThreads = 256;
+// The non-empty blocks of the sort: those with at least sparse_max particles (all of them when
+// sparse_max <= 0) into list / nlist[0]; the particle slots of the others, block by block,
+// into sparse / nlist[1].  A listed block of more than kG2P2GThreads particles whose last pass
+// would hold fewer than tail_max (0: none) also puts those last slots into sparse.  nlist[0..1]
+// must be zero on entry.
+void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int tail_max,
+                           int *list, int *nlist, int *sparse, cudaStream_t st);
 
 // Counts material[] entries above NCLR_LIQUID into *out (host); synchronises `st`
 // (scene_build.cu).

@@ -17,8 +17,6 @@
 
 namespace mpm {
 
-constexpr int kG2P2GThreads = 256;
-
 // Threads that work on one item of the fused kernel (a grid block, or a chunk of thin-block
 // particles): the whole CTA, except in 2D batches.  There the tiles are small (2.3 KB), and a
 // block of a few hundred particles runs in passes of 128, with each half of the CTA on its
@@ -555,6 +553,7 @@ g2p2g_kernel(
   constexpr int kGroups = kG2P2GThreads / kGroup;  // items in flight per CTA
   constexpr int kWarps = kGroup / 32;              // warps per item, each with its G tile
   constexpr int kTiles = (kMode == kG2PFinal) ? 1 : 1 + kWarps;  // tiles per group
+  static_assert(kBatch || kGroup == kG2P2GThreads, "the tail rule counts passes of the CTA");
   extern __shared__ float4 smem[];
   const int grp = threadIdx.x / kGroup, gtid = threadIdx.x % kGroup;
   float4 *vt = smem + grp * kTiles * GS;  // the group's V tile
@@ -637,7 +636,10 @@ g2p2g_kernel(
     // The block's particles, stored cell by cell in rounds (see sort_move_kernel), or a chunk's.
     const int c0 = (item - nact) * kGroup;
     const int p0 = chunk ? 0 : bstart[gb];
-    const int np = chunk ? min(kGroup, nsp - c0) : bstart[gb + 1] - p0;
+    int np = chunk ? min(kGroup, nsp - c0) : bstart[gb + 1] - p0;
+    // A single simulation's block whose last pass would hold fewer than P.tail_max particles
+    // left them to the chunks (compact_blocks_kernel): its item runs whole passes only.
+    if (!kBatch && !chunk && np > kGroup && np % kGroup < P.tail_max) np -= np % kGroup;
     // A batch's thin block (fewer than P.thin_max particles) skips the tiles like a chunk:
     // gathered from V and scattered into G directly (CTA-uniform).
     const bool direct = chunk || (kBatch && np < P.thin_max);

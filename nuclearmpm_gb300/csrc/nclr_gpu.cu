@@ -59,6 +59,7 @@ struct nclr_sim {
   int *nblocks_active = nullptr;  // [0] dense blocks in `blocks`, [1] slots in `sparse`
   int *sparse = nullptr;      // particle slots of the thin blocks (stepped without a tile)
   int sparse_max = 0;         // blocks with fewer particles than this are thin
+  int tail_max = 0;           // a block's last pass of fewer particles goes to the chunks
   mpm::Record record{};       // where final-mode steps also write the caller-order state
   int *inv = nullptr;         // global caller id -> slot (the permutation of the last sort)
   int *slot_block = nullptr;  // slot -> grid block it was sorted into
@@ -127,6 +128,13 @@ thread_local std::string g_create_error;
 constexpr int kSparseMax3 = 64;
 constexpr int kSparseMax2 = 32;
 constexpr int kBatchThin = 32;  // batches: blocks below this many particles skip the tiles
+// Default tail threshold of a single simulation: a block's last 256-particle pass of fewer
+// particles than this goes to the thin-block chunks.  Measured per fused launch against no
+// tail rule, twice each: 1M-particle jelly 144-148 -> 142-144 us (reference physics) and
+// 162-165 -> 157-158 us (corrected), corrected snow 180 -> 174 us, the 4.19M-particle liquid
+// + snow scene 1297 -> 1271 us.  32 and 96 come within 1-2% of 64; 128 is slower on jelly
+// and 192 everywhere (too many particles leave the tiles).
+constexpr int kTailMax = 64;
 // Default small-scene limits: up to them one persistent launch per advance() call beats two
 // launches per step.  Measured on GB300: up to 64k particles in 2D and 32k in 3D, and only
 // while the grid has at most about 8 nodes per particle -- the small kernel updates every
@@ -255,8 +263,8 @@ void enqueue_sort(nclr_sim *s, bool move_vc) {
                                 s->stream);
       mpm::launch_block_tables(s->count, nb, s->btotal, s->rounds, s->stream);
       mpm::launch_exclusive_scan(s->btotal, nb, s->start, s->tile_sums, s->stream);
-      mpm::launch_compact_blocks(s->start, nb, 1, s->sparse_max, s->blocks, s->nblocks_active,
-                                 s->sparse, s->stream);
+      mpm::launch_compact_blocks(s->start, nb, 1, s->sparse_max, s->tail_max, s->blocks,
+                                 s->nblocks_active, s->sparse, s->stream);
       mpm::launch_sort_move<D>(s->ps[s->cur], s->ps[s->cur ^ 1], (int)s->n, s->key, s->rank,
                                s->start, s->rounds, s->count, move_vc, s->inv, s->slot_block,
                                s->stream);
@@ -587,6 +595,8 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
                    : dim == 3                   ? kSparseMax3
                                                 : kSparseMax2;
   s->sparse_max = nscenes > 1 ? 0 : thin;
+  // the tail rule needs the chunks, which only single simulations have
+  s->tail_max = nscenes > 1 ? 0 : s->opt.tail_max >= 0 ? s->opt.tail_max : kTailMax;
   s->deferred_err.assign((size_t)nscenes, 0);
   s->scene_err.assign((size_t)nscenes, 0);
 
@@ -598,6 +608,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
     sc.P = scene_params(dim, d.n, d.model, d.res, d.dt, d.E, d.nu, d.gravity);
     sc.P.stress = s->opt.stress_model;
     sc.P.thin_max = nscenes > 1 ? thin : 0;
+    sc.P.tail_max = s->tail_max;
     sc.slot_off = (int)slot;
     sc.node_off = node;
     sc.block_off = (int)std::min<int64_t>(block, 0x7fffffff);
@@ -1059,6 +1070,7 @@ void nclr_default_options(nclr_options *opt) {
   opt->graph_steps = 0;
   opt->sparse_block_max = -1;
   opt->small_scene_max = -1;
+  opt->tail_max = -1;
   opt->stress_model = NCLR_STRESS_COROTATED;
 }
 

@@ -135,10 +135,13 @@ __global__ void __launch_bounds__(kThreads) count_active_kernel(const float4 *__
 
 // The non-empty blocks (start[b*cpb] < start[(b+1)*cpb]): those with at least sparse_max
 // particles go to the block list, the particle slots of the thinner ones to the sparse list
-// (stepped particle by particle).  One atomic per warp and list for the append position, so
-// the sparse slots stay in block order within each warp's run of 32 blocks.
+// (stepped particle by particle), and so do the last np % kG2P2GThreads slots of a listed
+// block of np > kG2P2GThreads particles when they are fewer than tail_max: the fused kernel
+// would otherwise run a last pass of a few particles with the rest of the CTA waiting (the
+// fused kernel applies the same rule).  One atomic per warp and list for the append position,
+// so the sparse slots stay in block order within each warp's run of 32 blocks.
 __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks, int cpb,
-                                      int sparse_max, int *__restrict__ list,
+                                      int sparse_max, int tail_max, int *__restrict__ list,
                                       int *__restrict__ nlist, int *__restrict__ sparse) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   int s0 = 0, np = 0;
@@ -148,6 +151,8 @@ __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks
   }
   const bool thin = np > 0 && np < sparse_max;
   const bool act = np > 0 && !thin;
+  const int tail = np % kG2P2GThreads;
+  const bool cut = act && np > kG2P2GThreads && tail < tail_max;
   const int lane = threadIdx.x & 31;
   const unsigned mask = __ballot_sync(0xffffffffu, act);
   if (mask) {
@@ -156,7 +161,8 @@ __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks
     base = __shfl_sync(0xffffffffu, base, 0);
     if (act) list[base + __popc(mask & ((1u << lane) - 1u))] = b;
   }
-  const int cnt = thin ? np : 0;
+  const int cnt = thin ? np : (cut ? tail : 0);
+  if (cut) s0 += np - tail;
   const int inc = warp_inclusive(cnt);
   const int tot = __shfl_sync(0xffffffffu, inc, 31);
   if (tot) {
@@ -176,11 +182,11 @@ void launch_block_tables(const int *count, int nblocks, int *btotal, int4 *round
       count, nblocks, btotal, rounds);
 }
 
-void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int *list,
-                           int *nlist, int *sparse, cudaStream_t st) {
+void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int tail_max,
+                           int *list, int *nlist, int *sparse, cudaStream_t st) {
   if (nblocks <= 0) return;
   compact_blocks_kernel<<<(unsigned)((nblocks + kThreads - 1) / kThreads), kThreads, 0, st>>>(
-      start, nblocks, cpb, sparse_max, list, nlist, sparse);
+      start, nblocks, cpb, sparse_max, tail_max, list, nlist, sparse);
 }
 
 void launch_count_active(const float4 *grid, int64_t nodes, unsigned long long *out, cudaStream_t st) {

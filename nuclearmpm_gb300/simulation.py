@@ -170,7 +170,7 @@ class MPMSimulation:
                  sort_interval: int = 8, particles_per_thread: int = 1, device: int = 0,
                  use_graphs: bool = True, profile: bool = False, graph_steps: int = 0,
                  sparse_block_max: int = -1, small_scene_max: int = -1,
-                 stress_model: int = capi.STRESS_COROTATED):
+                 stress_model: int = capi.STRESS_COROTATED, tail_max: int = -1):
         L = capi.lib()
         self.dim, soa = _soa_from(particles, dim)
         self._c = soa.pop("c")
@@ -184,7 +184,8 @@ class MPMSimulation:
                                    p2g_particles_per_thread=particles_per_thread, device=device,
                                    use_graphs=int(use_graphs), profile=int(profile),
                                    graph_steps=graph_steps, sparse_block_max=sparse_block_max,
-                                   small_scene_max=small_scene_max, stress_model=stress_model)
+                                   small_scene_max=small_scene_max, stress_model=stress_model,
+                                   tail_max=tail_max)
         h = ctypes.c_void_p()
         st = L.nclr_create(ctypes.byref(h), self.dim, self.n, _ptr(soa["x"]), _ptr(soa["v"]),
                            _ptr(soa["F"]), _ptr(soa["C"]), _ptr(soa["Jp"]), _ptr(soa["mass"]),
@@ -205,7 +206,7 @@ class MPMSimulation:
                     device: int | None = None, use_graphs: bool = True, profile: bool = False,
                     graph_steps: int = 0, sparse_block_max: int = -1,
                     small_scene_max: int = -1,
-                    stress_model: int = capi.STRESS_COROTATED) -> "MPMSimulation":
+                    stress_model: int = capi.STRESS_COROTATED, tail_max: int = -1) -> "MPMSimulation":
         """A simulation created from CUDA tensors (nclr_create_device): x (n, dim) and the
         optional fields in the layouts of the constructor, already on the GPU (e.g. from
         scenes.cubes_device), never staged through the host."""
@@ -233,7 +234,8 @@ class MPMSimulation:
         opt = capi.default_options(physics=physics, sort_interval=sort_interval, device=dev,
                                    use_graphs=int(use_graphs), profile=int(profile),
                                    graph_steps=graph_steps, sparse_block_max=sparse_block_max,
-                                   small_scene_max=small_scene_max, stress_model=stress_model)
+                                   small_scene_max=small_scene_max, stress_model=stress_model,
+                                   tail_max=tail_max)
         h = ctypes.c_void_p()
         st = L.nclr_create_device(ctypes.byref(h), self.dim, self.n, ptr(x.contiguous()), ptr(v),
                                   ptr(F), ptr(C), ptr(Jp), ptr(mass), ptr(volume),

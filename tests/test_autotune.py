@@ -49,10 +49,8 @@ class LuckySim(FakeSim):
         super().__init__(sort_interval, graph_steps)
         k = LuckySim.made.get(sort_interval, 0)
         LuckySim.made[sort_interval] = k + 1
-        if sort_interval == 16:
-            self.cost = 1e-5 if k == 0 else 2e-3
-        elif sort_interval == 8:
-            self.cost = 5e-4
+        # milliseconds apart, well above the jitter of time.sleep
+        self.cost = {4: 3e-3, 8: 1e-3}.get(sort_interval, 1e-5 if k == 0 else 4e-3)
 
 
 def test_confirmation_reverts_a_lucky_pick():

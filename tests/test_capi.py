@@ -29,7 +29,7 @@ def test_every_declared_symbol_is_exported_and_bound():
 def test_default_options():
     o = capi.default_options()
     assert (o.physics, o.sort_interval, o.p2g_particles_per_thread, o.device, o.use_graphs) == (0, 8, 1, 0, 1)
-    assert (o.sparse_block_max, o.small_scene_max) == (-1, -1)
+    assert (o.sparse_block_max, o.small_scene_max, o.tail_max) == (-1, -1, -1)
     assert o.stress_model == capi.STRESS_COROTATED
 
 

@@ -10,9 +10,12 @@ pytestmark = pytest.mark.gpu
 
 # One step: the one-step parity bound of the plain step.  Ten steps: the plain step's
 # multi-step drift bounds (runs differ only in the atomic summation order, which stiff scenes
-# -- E up to 1e5 with unit particle mass and volume -- amplify from step to step).
+# -- E up to 1e5 with unit particle mass and volume -- amplify from step to step), or twice
+# the FP32 oracle's own distance to the FP64 oracle over the same steps where that is larger
+# (the summation order alone moves a scene that far: 3.3e-3 in v on one scene below).
 ONE_STEP = 1e-5
 TEN_STEPS = {"x": 2e-5, "v": 3e-3, "F": 3e-4, "C": 1e-2, "Jp": 3e-4}
+FP32_SPREAD_FACTOR = 2.0
 
 
 def small_batch(seed=0, count=6, dim=2):
@@ -56,7 +59,7 @@ PATHS = {"small": {"small_scene_max": 1 << 30}, "tile": {}, "tile256": {"batch_i
 @pytest.mark.parametrize("dim,physics,steps", [(2, scenes.REFERENCE, 10),
                                                (3, scenes.REFERENCE, 1),
                                                (3, scenes.CORRECTED, 10)])
-def test_batch_matches_scenes_stepped_alone(dim, physics, steps, path):
+def test_batch_matches_scenes_stepped_alone(oracle, dim, physics, steps, path):
     """Ten steps where the physics is well conditioned; under the reference's 3D physics the
     snow scenes clamp a zero singular value every step and their velocities grow towards the
     clip, so two runs that differ only in summation order part after a few steps: one step."""
@@ -66,10 +69,18 @@ def test_batch_matches_scenes_stepped_alone(dim, physics, steps, path):
             sc["F"] = np.broadcast_to(np.eye(3, dtype=np.float32), sc["F"].shape).copy()
     batch = BatchSimulation(scs, sort_interval=4, graph_steps=8, physics=physics, **PATHS[path])
     batch.advance(steps)
-    tol = TEN_STEPS if steps > 1 else {f: ONE_STEP for f in FIELDS}
     for i, sc in enumerate(scs):
         ref, rg = alone(sc, steps, physics)
         got = batch.particles(i)
+        tol = {f: ONE_STEP for f in FIELDS}
+        if steps > 1:
+            st = {k: sc[k] for k in ("x", "v", "F", "C", "Jp", "mass", "volume")}
+            kw = dict(dim=dim, model=sc["model"], res=sc["res"], dt=sc["dt"], E=sc["E"],
+                      nu=sc["nu"], gravity=sc["gravity"], steps=steps, physics=physics,
+                      want_grid=False)
+            o32, o64 = oracle.advance(st, **kw)[0], oracle.advance(st, fp64=True, **kw)[0]
+            tol = {f: max(TEN_STEPS[f], FP32_SPREAD_FACTOR * field_err(o32[f], o64[f], f))
+                   for f in FIELDS}
         for f in FIELDS:
             assert field_err(got[f], ref[f], f) <= tol[f], (i, f)
         g = batch.grid(i)

@@ -138,6 +138,31 @@ def test_one_step_vs_oracle_random(oracle, dim, model, physics, thin):
         assert e64 <= max(RANDOM_FP64_FACTOR * own, 1e-5), (f, e64, own)
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("tail", [0, 64, 1 << 30])
+def test_dense_blocks_with_tails_vs_oracle(oracle, dim, tail):
+    """Blocks of several hundred (3D) to a few thousand (2D) particles, which the tile path
+    steps in passes of 256: a block's last pass of fewer than `tail_max` particles goes to the
+    thin-block chunks instead (never, the default 64, every last pass).  One step vs the FP32
+    and FP64 oracles, as above (it runs the P2G-only launch and a step, both with the rule)."""
+    rng = np.random.default_rng(7 + dim)
+    res = 16 if dim == 3 else 32
+    s = random_state(rng, dim, 12000, res, scenes.CORRECTED)
+    out, grid = run_gpu(s, dict(model=scenes.JELLY, res=res, dt=1e-4, E=1e4, nu=0.2, gravity=-100.0),
+                        1, physics=scenes.CORRECTED, small_scene_max=0, tail_max=tail)
+    kw = dict(dim=dim, model=scenes.JELLY, res=res, steps=1, physics=scenes.CORRECTED)
+    o32, og, st, _ = oracle.advance(s, **kw)
+    o64, og64, _, _ = oracle.advance(s, fp64=True, **kw)
+    assert st == 0
+    pairs = [(out[f], o32[f], o64[f], f) for f in FIELDS]
+    pairs += [(grid.velocity, og[0], og64[0], "grid_v"), (grid.mass, og[1], og64[1], "grid_m")]
+    for gpu, ref32, ref64, f in pairs:
+        e32 = field_err(gpu, ref32, f)
+        own = field_err(ref32, ref64, f)
+        assert e32 <= RANDOM_VS_FP32, (f, e32)
+        assert field_err(gpu, ref64, f) <= max(RANDOM_FP64_FACTOR * own, 1e-5), f
+
+
 def test_sort_graph_and_threading_options_agree():
     """Cell sort on/off, graphs on/off, particles-per-thread, the sparse-block threshold and
     the small-scene kernel change only the summation order: the results agree to FP32
@@ -151,6 +176,8 @@ def test_sort_graph_and_threading_options_agree():
                dict(sort_interval=8, use_graphs=False, particles_per_thread=8, **tile),
                dict(sort_interval=2, sparse_block_max=0, **tile),
                dict(sort_interval=2, sparse_block_max=1 << 30, **tile),
+               dict(sort_interval=2, tail_max=0, **tile),
+               dict(sort_interval=2, tail_max=1 << 30, **tile),
                dict(small_scene_max=1 << 30),
                dict(small_scene_max=1 << 30, particles_per_thread=3)):
         runs.append(run_gpu(state, params, 20, **kw)[0])
