@@ -576,7 +576,11 @@ g2p2g_kernel(
   const int st = s.stride;
   // work items: the dense blocks of the list, then chunks of kG2P2GThreads particles of the
   // sparse blocks (single simulations only; see compact_blocks_kernel)
-  const int nact = nactive[0];
+  // the block list: nactive[0] blocks of more than one pass at its front, nactive[2] others at
+  // its back (capacity nactive[3]; compact_blocks_kernel), taken in that order
+  const int nfront = nactive[0], lcap = nactive[3];
+  const int nact = nfront + nactive[2];
+  auto block_at = [&](int it) { return blocks[it < nfront ? it : lcap - 1 - (it - nfront)]; };
   const int nsp = kBatch ? 0 : nactive[1];
   const int nitems = nact + (nsp + kGroup - 1) / kGroup;
   const int lane = threadIdx.x & 31;
@@ -601,7 +605,7 @@ g2p2g_kernel(
       const int it = atomicAdd(work, 1);
       s_item = it;
       if (kBatch && it < nact) {
-        const int sid0 = (int)block_scene[blocks[it]];
+        const int sid0 = (int)block_scene[block_at(it)];
         sP = scenes[sid0].P;
         s_node_off = scenes[sid0].node_off;
         s_block_off = scenes[sid0].block_off;
@@ -613,7 +617,7 @@ g2p2g_kernel(
     // a sparse chunk: particles of blocks too thin for the tile to pay, one per thread,
     // gathered from V and scattered into G directly (CTA-uniform)
     const bool chunk = !kBatch && item >= nact;
-    const int gb = chunk ? 0 : blocks[item];  // global block (scene-major)
+    const int gb = chunk ? 0 : block_at(item);  // global block (scene-major)
     const int sid = kBatch ? (int)block_scene[gb] : 0;
     const Params &P = kBatch ? sP : P0;
     const int64_t node_off = kBatch ? s_node_off : 0;

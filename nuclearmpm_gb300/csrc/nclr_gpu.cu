@@ -56,7 +56,8 @@ struct nclr_sim {
   int *start = nullptr;       // first slot of every grid block (exclusive scan of btotal)
   int4 *rounds = nullptr;     // per-block round tables of the slot order (see sort_move_kernel)
   int *blocks = nullptr;      // non-empty blocks of the last sort (the dense ones)
-  int *nblocks_active = nullptr;  // [0] dense blocks in `blocks`, [1] slots in `sparse`
+  int *nblocks_active = nullptr;  // [0], [2]: blocks at the front and back of `blocks`, [1]
+                                  // slots in `sparse`, [3] capacity of `blocks`
   int *sparse = nullptr;      // particle slots of the thin blocks (stepped without a tile)
   int sparse_max = 0;         // blocks with fewer particles than this are thin
   int tail_max = 0;           // a block's last pass of fewer particles goes to the chunks
@@ -258,7 +259,7 @@ void enqueue_sort(nclr_sim *s, bool move_vc) {
     static_assert(cpb == mpm::kCellsPerBlock, "the round tables assume 64 cells per block");
     phase(s, NCLR_PHASE_SORT, 7, [&] {
       cudaMemsetAsync(s->count, 0, sizeof(int) * (size_t)s->nkeys, s->stream);
-      cudaMemsetAsync(s->nblocks_active, 0, 2 * sizeof(int), s->stream);
+      cudaMemsetAsync(s->nblocks_active, 0, 4 * sizeof(int), s->stream);
       mpm::launch_block_keys<D>(s->ps[s->cur], (int)s->n, s->scenes_d, s->key, s->rank, s->count,
                                 s->stream);
       mpm::launch_block_tables(s->count, nb, s->btotal, s->rounds, s->stream);
@@ -742,7 +743,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMalloc((void **)&s->rounds, sizeof(int4) * mpm::kRoundTable * std::max<size_t>(nblk, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->tile_sums, sizeof(int) * (size_t)std::max<int64_t>(mpm::scan_tiles(s->nkeys), 1)));
   CREATE_TRY(cudaMalloc((void **)&s->blocks, sizeof(int) * nblk));
-  CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, 2 * sizeof(int)));
+  CREATE_TRY(cudaMalloc((void **)&s->nblocks_active, 4 * sizeof(int)));
   CREATE_TRY(cudaMalloc((void **)&s->sparse, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
   CREATE_TRY(cudaMalloc((void **)&s->bar, 2 * sizeof(unsigned) * (size_t)nscenes));
   CREATE_TRY(cudaMalloc((void **)&s->inv, sizeof(int) * (size_t)std::max<int64_t>(s->n, 1)));
@@ -766,7 +767,7 @@ nclr_status create_scenes(nclr_sim **out, int dim, int nscenes, const nclr_scene
   CREATE_TRY(cudaMemsetAsync(s->G, 0, sizeof(float4) * nodes, s->stream));
   CREATE_TRY(cudaMemsetAsync(s->V, 0, sizeof(float4) * nodes, s->stream));
   CREATE_TRY(cudaMemsetAsync(s->flags, 0, nblk, s->stream));
-  CREATE_TRY(cudaMemsetAsync(s->nblocks_active, 0, 2 * sizeof(int), s->stream));
+  CREATE_TRY(cudaMemsetAsync(s->nblocks_active, 0, 4 * sizeof(int), s->stream));
 
   if (total_n > 0) {
     // Per-particle scalars go straight into the SoA (component stride == n there).

@@ -138,8 +138,12 @@ __global__ void __launch_bounds__(kThreads) count_active_kernel(const float4 *__
 // (stepped particle by particle), and so do the last np % kG2P2GThreads slots of a listed
 // block of np > kG2P2GThreads particles when they are fewer than tail_max: the fused kernel
 // would otherwise run a last pass of a few particles with the rest of the CTA waiting (the
-// fused kernel applies the same rule).  One atomic per warp and list for the append position,
-// so the sparse slots stay in block order within each warp's run of 32 blocks.
+// fused kernel applies the same rule).  Item order: blocks of more than one pass go to the
+// front of the list, one-pass blocks to its back, so the fused kernel's CTAs take the long
+// items first and the launch ends on short ones (measured per fused launch, 1M particles:
+// corrected snow 183 -> 169 us, exploding snow 707 -> 668, corrected jelly 162 -> 157, jelly
+// 142-144 -> 142).  One atomic per warp and list for the append
+// position, so the sparse slots stay in block order within each warp's run of 32 blocks.
 __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks, int cpb,
                                       int sparse_max, int tail_max, int *__restrict__ list,
                                       int *__restrict__ nlist, int *__restrict__ sparse) {
@@ -153,14 +157,25 @@ __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks
   const bool act = np > 0 && !thin;
   const int tail = np % kG2P2GThreads;
   const bool cut = act && np > kG2P2GThreads && tail < tail_max;
+  const bool multi = act && (cut ? np - tail : np) > kG2P2GThreads;
   const int lane = threadIdx.x & 31;
-  const unsigned mask = __ballot_sync(0xffffffffu, act);
-  if (mask) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(nlist, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (act) list[base + __popc(mask & ((1u << lane) - 1u))] = b;
+  const unsigned below = (1u << lane) - 1u;
+  const unsigned mfront = __ballot_sync(0xffffffffu, multi);
+  const unsigned mback = __ballot_sync(0xffffffffu, act && !multi);
+  if (mfront | mback) {
+    int front = 0, back = 0;
+    if (lane == 0) {
+      if (mfront) front = atomicAdd(nlist, __popc(mfront));
+      if (mback) back = atomicAdd(nlist + 2, __popc(mback));
+    }
+    front = __shfl_sync(0xffffffffu, front, 0);
+    back = __shfl_sync(0xffffffffu, back, 0);
+    if (multi)
+      list[front + __popc(mfront & below)] = b;
+    else if (act)
+      list[nblocks - 1 - (back + __popc(mback & below))] = b;
   }
+  if (b == 0) nlist[3] = nblocks;
   const int cnt = thin ? np : (cut ? tail : 0);
   if (cut) s0 += np - tail;
   const int inc = warp_inclusive(cnt);
