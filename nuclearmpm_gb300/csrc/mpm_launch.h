@@ -33,9 +33,11 @@ struct SnowFix {
   float *Jp = nullptr;
 };
 
+// P0: the one scene's parameters when block_scene is null (a single simulation).
 template <int D> void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
-                                        const uint16_t *block_scene, int total_blocks, int *work, int sms,
-                                        cudaStream_t st, int *fix_count = nullptr);
+                                        const uint16_t *block_scene, const Params &P0,
+                                        int total_blocks, int *work, int sms, cudaStream_t st,
+                                        int *fix_count = nullptr);
 // The FP64 snow clamps of the last fused launch (see SnowFix); scatter: that launch did the next
 // step's P2G (not the G2P-only final step), whose accumulator G receives the correction.
 template <int D> void launch_snow_fix(const PState &s, const Params &P0, const Scene *scenes,

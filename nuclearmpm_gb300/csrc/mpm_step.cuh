@@ -405,8 +405,9 @@ __device__ __forceinline__ void mark_node(uint8_t *flags, int64_t f, const Param
 // ---------------------------------------------------------------------------------------
 // grid_sweep: grid_op (src/nclr.h:263-310) on the flagged blocks: V = update(G), G = 0, and
 // the flags roll over (pending -> V non-zero).  Blocks never flagged hold V = 0 = update(0)
-// (a massless node's velocity is zero and stays zero through the boundary rule).  One warp
-// per block; also resets the g2p2g work counter.
+// (a massless node's velocity is zero and stays zero through the boundary rule).  Eight lanes
+// per block (eight nodes each), four blocks per warp at a time; also resets the g2p2g work
+// counter.
 // ---------------------------------------------------------------------------------------
 // Scene of global block gb, and the block's first node per axis inside that scene.
 template <int D>
@@ -423,41 +424,64 @@ __device__ __forceinline__ int block_origin(int gb, const Scene *scenes,
   return sid;
 }
 
-template <int D>
+// kBatch: the scene of each block from the scene table; otherwise the one scene's parameters
+// come by value (no dependent loads before the nodes').
+template <int D, bool kBatch>
 __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
                                                          float4 *__restrict__ V,
                                                          uint8_t *__restrict__ flags,
                                                          const Scene *__restrict__ scenes,
                                                          const uint16_t *__restrict__ block_scene,
-                                                         int total_blocks,
+                                                         Params P0, int total_blocks,
                                                          int *__restrict__ work,
                                                          int *__restrict__ fix_count) {
   constexpr int BS = Tiling<D>::BS;
   constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;  // nodes per block
+  constexpr int kLanes = 8, kPer = BN / kLanes;          // lanes per block, nodes per lane
+  static_assert(BN % kLanes == 0, "whole nodes per lane");
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *work = 0;
     if (fix_count) *fix_count = 0;  // the FP64 snow list of the step that follows
   }
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane / kLanes, l8 = lane % kLanes;
   const int warps = gridDim.x * (blockDim.x >> 5);
   const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   // This warp's blocks are wid, wid + warps, ...; their flags are read 32 at a time (one per
-  // lane) and only the flagged ones are visited, so the flag loads do not chain block by block.
+  // lane) and only the flagged ones are visited, four at a time (the sub-th lowest flagged
+  // block goes to lanes 8 sub .. 8 sub + 7), so neither the flag loads nor the blocks chain
+  // one after another.
   for (int k0 = 0; wid + k0 * warps < total_blocks; k0 += 32) {
     const int mine = wid + (k0 + lane) * warps;
     const uint8_t fl_l = mine < total_blocks ? flags[mine] : 0;
     unsigned todo = __ballot_sync(0xffffffffu, fl_l != 0);
     while (todo) {
-      const int k = __ffs(todo) - 1;
-      todo &= todo - 1;
+      unsigned pick = todo;
+      for (int i = 0; i < sub; ++i) pick &= pick - 1;  // drop the sub lowest
+      const int k = pick ? __ffs(pick) - 1 : -1;
+#pragma unroll
+      for (int i = 0; i < 32 / kLanes; ++i) todo &= todo - 1;
+      const uint8_t fl = __shfl_sync(0xffffffffu, fl_l, k < 0 ? 0 : k);
+      if (k < 0) continue;
       const int gb = wid + (k0 + k) * warps;
-      const uint8_t fl = __shfl_sync(0xffffffffu, fl_l, k);
       int bc[D];
-      const int sid = block_origin<D>(gb, scenes, block_scene, bc);
-      const Params P = scenes[sid].P;
-      float4 *Gs = G + scenes[sid].node_off;
-      float4 *Vs = V + scenes[sid].node_off;
-      for (int t = lane; t < BN; t += 32) {
+      const int sid = kBatch ? block_origin<D>(gb, scenes, block_scene, bc) : 0;
+      if constexpr (!kBatch) {
+        int r = gb;
+#pragma unroll
+        for (int d = D - 1; d >= 0; --d) {
+          bc[d] = (r % P0.nb) * BS;
+          r /= P0.nb;
+        }
+      }
+      const Params &P = kBatch ? scenes[sid].P : P0;
+      const int64_t off = kBatch ? scenes[sid].node_off : 0;
+      float4 *Gs = G + off;
+      float4 *Vs = V + off;
+      int f[kPer];  // node within the scene (res <= 1024: below 2^31)
+      float4 g[kPer];
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) {  // every load first
+        const int t = l8 + kLanes * j;
         int idx[D];
         bool in = true;
         int r = t;
@@ -467,15 +491,26 @@ __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
           r /= BS;
           in &= idx[d] < P.N;
         }
-        if (!in) continue;
-        const int64_t f = flat_index<D>(idx, P.N);
-        const float4 g = Gs[f];
-        float v[D], m;
-        grid_update<D>(g, idx, P, v, m);
-        Vs[f] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
-        Gs[f] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        f[j] = in ? (int)flat_index<D>(idx, P.N) : -1;
+        g[j] = in ? Gs[f[j]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
-      if (lane == 0) flags[gb] = (fl & kPending) ? kVNonzero : 0;
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) {
+        if (f[j] < 0) continue;
+        const int t = l8 + kLanes * j;
+        int idx[D];
+        int r = t;
+#pragma unroll
+        for (int d = D - 1; d >= 0; --d) {
+          idx[d] = bc[d] + r % BS;
+          r /= BS;
+        }
+        float v[D], m;
+        grid_update<D>(g[j], idx, P, v, m);
+        Vs[f[j]] = make_float4(v[0], v[1], D == 3 ? v[D - 1] : 0.0f, m);
+        Gs[f[j]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+      if (l8 == 0) flags[gb] = (fl & kPending) ? kVNonzero : 0;
     }
   }
 }
@@ -1396,20 +1431,29 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 
 template <int D>
 void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes,
-                       const uint16_t *block_scene, int total_blocks, int *work, int sms,
-                       cudaStream_t st, int *fix_count) {
+                       const uint16_t *block_scene, const Params &P0, int total_blocks,
+                       int *work, int sms, cudaStream_t st, int *fix_count) {
   // one wave: as many CTAs as are resident at once (a second, partial wave left the SMs idle
   // for 45% of the kernel)
-  static int resident = 0;
-  if (!resident) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, grid_sweep_kernel<D>, 256, 0);
-    if (resident < 1) resident = 1;
+  static int resident[2] = {0, 0};
+  const bool batch = block_scene != nullptr;
+  int &res = resident[batch];
+  if (!res) {
+    if (batch)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&res, grid_sweep_kernel<D, true>, 256, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&res, grid_sweep_kernel<D, false>, 256, 0);
+    if (res < 1) res = 1;
   }
   int64_t blocks = blocks_for((int64_t)total_blocks * 32, 256);
-  if (blocks > (int64_t)sms * resident) blocks = (int64_t)sms * resident;
+  if (blocks > (int64_t)sms * res) blocks = (int64_t)sms * res;
   if (blocks < 1) blocks = 1;
-  grid_sweep_kernel<D><<<(unsigned)blocks, 256, 0, st>>>(G, V, flags, scenes, block_scene,
-                                                          total_blocks, work, fix_count);
+  if (batch)
+    grid_sweep_kernel<D, true><<<(unsigned)blocks, 256, 0, st>>>(
+        G, V, flags, scenes, block_scene, P0, total_blocks, work, fix_count);
+  else
+    grid_sweep_kernel<D, false><<<(unsigned)blocks, 256, 0, st>>>(
+        G, V, flags, scenes, block_scene, P0, total_blocks, work, fix_count);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1768,7 +1812,8 @@ void launch_sort_move(const PState &src, const PState &dst, int n, const int *ke
 
 #define MPM_INSTANTIATE(D)                                                                       \
   template void launch_grid_sweep<D>(float4 *, float4 *, uint8_t *, const Scene *,              \
-                                     const uint16_t *, int, int *, int, cudaStream_t, int *);    \
+                                     const uint16_t *, const Params &, int, int *, int,          \
+                                     cudaStream_t, int *);                                       \
   template void launch_snow_fix<D>(const PState &, const Params &, const Scene *,                \
                                    const SnowFix &, float4 *, bool, bool, const Record &, int,   \
                                    cudaStream_t);                                                \

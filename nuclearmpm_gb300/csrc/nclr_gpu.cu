@@ -287,7 +287,7 @@ void enqueue_step(nclr_sim *s, bool sort, int final) {
   dispatch_dim(s->dim, [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     phase(s, NCLR_PHASE_GRID, 1, [&] {
-      mpm::launch_grid_sweep<D>(s->G, s->V, s->flags, s->scenes_d, s->block_scene,
+      mpm::launch_grid_sweep<D>(s->G, s->V, s->flags, s->scenes_d, s->block_scene, s->P0(),
                                 s->total_blocks, s->work, s->sms, s->stream, s->fix.count);
     });
     s->launches += 1;
