@@ -11,11 +11,39 @@
 
 #include <algorithm>
 #include <type_traits>
+#include <utility>
 
 #include "mpm_device.cuh"
 #include "mpm_launch.h"
 
 namespace mpm {
+
+// Programmatic dependent launch: a kernel launched by launch_overlapped may start while the
+// kernel before it in the stream drains.  wait_prior_grid() holds it until that kernel has
+// finished and its writes are visible (a no-op for an ordinary launch), and
+// allow_next_grid() lets the kernel after it launch once every CTA of this one has run it.
+// Used for a single simulation's grid sweep and its fused step with the material fixed at
+// compile time: 3D jelly 164 -> 159 us per step in CUDA graphs.  Launching the FP64 snow
+// fix-up and the other fused variants this way measured 5-13% slower on the scenes that have
+// fix-ups (the next kernel's CTAs wait on SMs that the FP64-bound fix-up runs on).
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_next_grid() { asm volatile("griddepcontrol.launch_dependents;"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_overlapped(void (*k)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                              cudaStream_t st, Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // Threads that work on one item of the fused kernel (a grid block, or a chunk of thin-block
 // particles): the whole CTA, except in 2D batches.  There the tiles are small (2.3 KB), and a
@@ -439,6 +467,8 @@ __global__ void __launch_bounds__(256) grid_sweep_kernel(float4 *__restrict__ G,
   constexpr int BN = (D == 3) ? BS * BS * BS : BS * BS;  // nodes per block
   constexpr int kLanes = 8, kPer = BN / kLanes;          // lanes per block, nodes per lane
   static_assert(BN % kLanes == 0, "whole nodes per lane");
+  wait_prior_grid();  // the fused launch before it wrote G and the flags
+  allow_next_grid();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *work = 0;
     if (fix_count) *fix_count = 0;  // the FP64 snow list of the step that follows
@@ -589,6 +619,8 @@ g2p2g_kernel(
   constexpr int kWarps = kGroup / 32;              // warps per item, each with its G tile
   constexpr int kTiles = (kMode == kG2PFinal) ? 1 : 1 + kWarps;  // tiles per group
   static_assert(kBatch || kGroup == kG2P2GThreads, "the tail rule counts passes of the CTA");
+  wait_prior_grid();  // the sweep before it wrote V, the flags and the item counter
+  allow_next_grid();
   extern __shared__ float4 smem[];
   const int grp = threadIdx.x / kGroup, gtid = threadIdx.x % kGroup;
   float4 *vt = smem + grp * kTiles * GS;  // the group's V tile
@@ -1452,8 +1484,8 @@ void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes
     grid_sweep_kernel<D, true><<<(unsigned)blocks, 256, 0, st>>>(
         G, V, flags, scenes, block_scene, P0, total_blocks, work, fix_count);
   else
-    grid_sweep_kernel<D, false><<<(unsigned)blocks, 256, 0, st>>>(
-        G, V, flags, scenes, block_scene, P0, total_blocks, work, fix_count);
+    launch_overlapped(grid_sweep_kernel<D, false>, (unsigned)blocks, 256, 0, st, G, V, flags,
+                      scenes, block_scene, P0, total_blocks, work, fix_count);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -11,10 +11,11 @@ void launch_g2p2g_fixed(const PState &s, const Params &P0, const float4 *V, floa
                         bool ref, int mode, int material, int ctas, cudaStream_t st,
                         const Record &rec, const SnowFix &fix) {
   auto go = [&](auto r, auto m, auto mat) {
-    g2p2g_kernel<D, decltype(r)::value, decltype(m)::value, false, decltype(mat)::value>
-        <<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D, false>(), st>>>(
-            s, P0, nullptr, nullptr, V, G, flags, blocks, nactive, bstart, sparse, work, err,
-            next_slot, rec, fix);
+    launch_overlapped(
+        g2p2g_kernel<D, decltype(r)::value, decltype(m)::value, false, decltype(mat)::value>,
+        (unsigned)ctas, kG2P2GThreads, g2p2g_smem_bytes<D, false>(), st, s, P0,
+        (const Scene *)nullptr, (const uint16_t *)nullptr, V, G, flags, blocks, nactive, bstart,
+        sparse, work, err, next_slot, rec, fix);
   };
   auto by_material = [&](auto r, auto m) {
     if (material == kSnow) go(r, m, std::integral_constant<int, kSnow>{});
