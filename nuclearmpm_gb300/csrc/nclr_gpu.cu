@@ -131,10 +131,13 @@ constexpr int kSparseMax2 = 32;
 constexpr int kBatchThin = 32;  // batches: blocks below this many particles skip the tiles
 // Default tail threshold of a single simulation: a block's last 256-particle pass of fewer
 // particles than this goes to the thin-block chunks.  Measured per fused launch against no
-// tail rule, twice each: 1M-particle jelly 144-148 -> 142-144 us (reference physics) and
-// 162-165 -> 157-158 us (corrected), corrected snow 180 -> 174 us, the 4.19M-particle liquid
-// + snow scene 1297 -> 1271 us.  32 and 96 come within 1-2% of 64; 128 is slower on jelly
-// and 192 everywhere (too many particles leave the tiles).
+// tail rule, twice each: with the block list in list order, 1M-particle jelly 144-148 ->
+// 142-144 us (reference physics) and 162-165 -> 157-158 us (corrected), corrected snow 180
+// -> 174 us, the 4.19M-particle liquid + snow scene 1297 -> 1271 us.  With multi-pass blocks
+// first (compact_blocks_kernel) most of that gain is already there: jelly 141 -> 142 us,
+// corrected jelly 158 -> 157, corrected snow 170 -> 169, liquid + snow 1289 -> 1267.  32 and
+// 96 come within 1-2% of 64; 128 is slower on jelly and 192 everywhere (too many particles
+// leave the tiles).  The autotuner has it as a knob.
 constexpr int kTailMax = 64;
 // Default small-scene limits: up to them one persistent launch per advance() call beats two
 // launches per step.  Measured on GB300: up to 64k particles in 2D and 32k in 3D, and only
