@@ -22,10 +22,10 @@ namespace mpm {
 // kernel before it in the stream drains.  wait_prior_grid() holds it until that kernel has
 // finished and its writes are visible (a no-op for an ordinary launch), and
 // allow_next_grid() lets the kernel after it launch once every CTA of this one has run it.
-// Used for a single simulation's grid sweep and its fused step with the material fixed at
-// compile time: 3D jelly 164 -> 159 us per step in CUDA graphs.  Launching the FP64 snow
-// fix-up and the other fused variants this way measured 5-13% slower on the scenes that have
-// fix-ups (the next kernel's CTAs wait on SMs that the FP64-bound fix-up runs on).
+// Used for the grid sweeps and every fused launch: 3D jelly 164 -> 159 us per step in CUDA
+// graphs, the 256-scene 2D batch 2-4% faster.  The FP64 snow fix-up launches as before: with
+// it overlapped too, the scenes that have fix-ups ran 5-13% slower (the next kernel's CTAs
+// wait on SMs that the FP64-bound fix-up runs on).
 __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void allow_next_grid() { asm volatile("griddepcontrol.launch_dependents;"); }
 
@@ -1481,8 +1481,8 @@ void launch_grid_sweep(float4 *G, float4 *V, uint8_t *flags, const Scene *scenes
   if (blocks > (int64_t)sms * res) blocks = (int64_t)sms * res;
   if (blocks < 1) blocks = 1;
   if (batch)
-    grid_sweep_kernel<D, true><<<(unsigned)blocks, 256, 0, st>>>(
-        G, V, flags, scenes, block_scene, P0, total_blocks, work, fix_count);
+    launch_overlapped(grid_sweep_kernel<D, true>, (unsigned)blocks, 256, 0, st, G, V, flags,
+                      scenes, block_scene, P0, total_blocks, work, fix_count);
   else
     launch_overlapped(grid_sweep_kernel<D, false>, (unsigned)blocks, 256, 0, st, G, V, flags,
                       scenes, block_scene, P0, total_blocks, work, fix_count);
@@ -1628,18 +1628,17 @@ void launch_g2p2g(const PState &s, const Params &P0, const Scene *scenes,
       return;
     }
   }
-#define MPM_G2P2G(R, MODE, B)                                                            \
-  g2p2g_kernel<D, R, MODE, B><<<ctas, kG2P2GThreads,                                      \
-                                (MODE) == kG2PFinal ? g2p_final_smem_bytes<D>()           \
-                                                    : g2p2g_smem_bytes<D, B>(),           \
-                                st>>>(s, P0, scenes, block_scene, V, G, flags, blocks,   \
-                                      nactive, bstart, sparse, work, err, next_slot, rec, fix)
+#define MPM_G2P2G(R, MODE, B)                                                                \
+  launch_overlapped(g2p2g_kernel<D, R, MODE, B>, (unsigned)ctas, kG2P2GThreads,               \
+                    (MODE) == kG2PFinal ? g2p_final_smem_bytes<D>() : g2p2g_smem_bytes<D, B>(), \
+                    st, s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart,      \
+                    sparse, work, err, next_slot, rec, fix)
 // 2D batches with whole-CTA items (item_threads 256) instead of the default half-CTA ones
-#define MPM_G2P2G_ITEM(R, MODE)                                                           \
-  g2p2g_kernel<D, R, MODE, true, -1, kG2P2GThreads>                                       \
-      <<<ctas, kG2P2GThreads, g2p2g_smem_bytes<D, true, kG2P2GThreads>(), st>>>(          \
-          s, P0, scenes, block_scene, V, G, flags, blocks, nactive, bstart, sparse, work, err, \
-          next_slot, rec, fix)
+#define MPM_G2P2G_ITEM(R, MODE)                                                               \
+  launch_overlapped(g2p2g_kernel<D, R, MODE, true, -1, kG2P2GThreads>, (unsigned)ctas,        \
+                    kG2P2GThreads, g2p2g_smem_bytes<D, true, kG2P2GThreads>(), st, s, P0,      \
+                    scenes, block_scene, V, G, flags, blocks, nactive, bstart, sparse, work,   \
+                    err, next_slot, rec, fix)
 #define MPM_G2P2G_B(R, MODE)                                      \
   if (block_scene && D == 2 && item_threads == kG2P2GThreads) {   \
     MPM_G2P2G_ITEM(R, MODE);                                      \
