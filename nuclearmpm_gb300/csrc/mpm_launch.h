@@ -117,8 +117,9 @@ constexpr int kG2P2GThreads = 256;
 // sparse_max <= 0) go to list, the particle slots of the others, block by block, to sparse /
 // nlist[1].  A listed block of more than kG2P2GThreads particles whose last pass would hold
 // fewer than tail_max (0: none) also puts those last slots into sparse.  list (capacity
-// nblocks) holds the blocks of more than one pass at its front (list[0 .. nlist[0])) and the
-// others at its back (list[nblocks - 1 - k], k < nlist[2]); nlist[3] = nblocks.  nlist[0..2]
+// nblocks) holds the blocks of more than kG2P2GThreads particles (after that rule) at its
+// front (list[0 .. nlist[0])) and the others at its back (list[nblocks - 1 - k],
+// k < nlist[2]); nlist[3] = nblocks.  nlist[0..2]
 // must be zero on entry.
 void launch_compact_blocks(const int *start, int nblocks, int cpb, int sparse_max, int tail_max,
                            int *list, int *nlist, int *sparse, cudaStream_t st);

@@ -131,7 +131,7 @@ constexpr int kSparseMax2 = 32;
 constexpr int kBatchThin = 32;  // batches: blocks below this many particles skip the tiles
 // Default tail threshold of a single simulation: a block's last 256-particle pass of fewer
 // particles than this goes to the thin-block chunks.  Measured per fused launch against no
-// tail rule, twice each: with the block list in list order, 1M-particle jelly 144-148 ->
+// tail rule, twice each: with the block list in block order, 1M-particle jelly 144-148 ->
 // 142-144 us (reference physics) and 162-165 -> 157-158 us (corrected), corrected snow 180
 // -> 174 us, the 4.19M-particle liquid + snow scene 1297 -> 1271 us.  With multi-pass blocks
 // first (compact_blocks_kernel) most of that gain is already there: jelly 141 -> 142 us,

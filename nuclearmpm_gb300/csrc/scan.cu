@@ -138,12 +138,13 @@ __global__ void __launch_bounds__(kThreads) count_active_kernel(const float4 *__
 // (stepped particle by particle), and so do the last np % kG2P2GThreads slots of a listed
 // block of np > kG2P2GThreads particles when they are fewer than tail_max: the fused kernel
 // would otherwise run a last pass of a few particles with the rest of the CTA waiting (the
-// fused kernel applies the same rule).  Item order: blocks of more than one pass go to the
-// front of the list, one-pass blocks to its back, so the fused kernel's CTAs take the long
-// items first and the launch ends on short ones (measured per fused launch, 1M particles:
-// corrected snow 183 -> 169 us, exploding snow 707 -> 668, corrected jelly 162 -> 157, jelly
-// 142-144 -> 142).  One atomic per warp and list for the append
-// position, so the sparse slots stay in block order within each warp's run of 32 blocks.
+// fused kernel applies the same rule).  Item order: blocks of more than kG2P2GThreads
+// particles (after the tail rule) go to the front of the list, the others to its back, so the
+// fused kernel's CTAs take the long items first and the launch ends on short ones (measured
+// per fused launch, 1M particles: corrected snow 183 -> 169 us, exploding snow 707 -> 668,
+// corrected jelly 162 -> 157, jelly 142-144 -> 142).  One atomic per warp and list for the
+// append position, so the sparse slots stay in block order within each warp's run of 32
+// blocks.
 __global__ void compact_blocks_kernel(const int *__restrict__ start, int nblocks, int cpb,
                                       int sparse_max, int tail_max, int *__restrict__ list,
                                       int *__restrict__ nlist, int *__restrict__ sparse) {
