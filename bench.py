@@ -247,11 +247,12 @@ def tune_plain(state: dict, model: int, res: int, device: int, physics: int = 0,
     from nuclearmpm_gb300 import MPMSimulation, autotune
     # 128-step runs, best of three (about 23 ms each at 1M particles): the candidates differ by
     # a few percent (re-sorting every 8 steps against 16 trades sort time against a faster
-    # fused kernel), which shorter runs timed on the host resolve differently from run to run
+    # fused kernel), which shorter runs timed on the host resolve differently from run to run;
+    # the pick is then confirmed against the defaults in two alternating rounds
     return autotune.tune(lambda **o: MPMSimulation(dict(state), model, res=res, device=device,
                                                    physics=physics, material=material, **o),
                          key=None, candidates=autotune.PLAIN_CANDIDATES, steps=128, repeats=3,
-                         cache_path=None)
+                         cache_path=None, confirm=2)
 
 
 def make_scene():
@@ -633,7 +634,7 @@ def run_readme(device: int, steps: int = 4000, cpu_steps: int = 400) -> dict:
     n = len(sc["x"])
     tuned = autotune.tune(lambda **o: MPMSimulation(dict(sc), scenes.SNOW, res=64, device=device, **o),
                           key=None, candidates=autotune.SMALL_CANDIDATES, steps=200, repeats=2,
-                          cache_path=None)
+                          cache_path=None, confirm=2)
     sim = MPMSimulation(dict(sc), scenes.SNOW, res=64, graph_steps=200, device=device, **tuned)
     sim.advance(200)
     st = torch.cuda.ExternalStream(sim.stream)
