@@ -245,13 +245,14 @@ def tune_plain(state: dict, model: int, res: int, device: int, physics: int = 0,
     """The project's autotuner (nuclearmpm_gb300.autotune) on this workload: re-sort interval
     and thin-block threshold, from short timed runs of the simulation itself."""
     from nuclearmpm_gb300 import MPMSimulation, autotune
-    # 128-step runs, best of three (about 23 ms each at 1M particles): the candidates differ by
+    # 256-step runs, best of three (about 42 ms each at 1M particles): the candidates differ by
     # a few percent (re-sorting every 8 steps against 16 trades sort time against a faster
-    # fused kernel), which shorter runs timed on the host resolve differently from run to run;
-    # the pick is then confirmed against the defaults in two alternating rounds
+    # fused kernel, 2% apart on the 1M jelly scene), which 128-step runs timed on the host
+    # resolved differently from run to run; the pick is then confirmed against the defaults
+    # in two alternating rounds
     return autotune.tune(lambda **o: MPMSimulation(dict(state), model, res=res, device=device,
                                                    physics=physics, material=material, **o),
-                         key=None, candidates=autotune.PLAIN_CANDIDATES, steps=128, repeats=3,
+                         key=None, candidates=autotune.PLAIN_CANDIDATES, steps=256, repeats=3,
                          cache_path=None, confirm=2)
 
 
