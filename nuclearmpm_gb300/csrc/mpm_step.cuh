@@ -1251,17 +1251,68 @@ small_steps_kernel(PState s, Params P, float4 *__restrict__ G, float4 *__restric
       red_add_v4(G + f, c[0], c[1], c[2], c[3]);
     }
   };
-  // ---- p2g of the first step (src/nclr.h:104-165) from the stored state ----
-  for (int p = tid; p < P.n; p += stride) {
-    float x[D], v[D];
+  // G2P of one particle (src/nclr.h:167-261): gathers v and C from V, advects x, updates F
+  // and Jp; returns the rotation of the new F when need_R (see update_F)
+  auto g2p_one = [&](float x[D], float v[D], Mat<D> &F, Mat<D> &C, float &Jp, int material,
+                     bool need_R) {
+    float fx[D], w[3][D];
+    int base[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) v[d] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) C.a[i][j] = 0.0f;
+    stencil<D>(x, P.inv_dx, base, fx, w);
+    const int64_t f0 = flat_index<D>(base, N);
+    g2p_gather<D>(
+        [&](int o) {
+          const int64_t f = stencil_flat<D>(f0, o, N);
+          if (f >= 0 && f < P.nodes) return __ldcg(V + f);
+          atomicOr(err, kErrOutOfRange);
+          return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        },
+        fx, w, v, C);
+    scale_mat<D>(C, P.cscale);
+#pragma unroll
+    for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];
+    return update_F<D, kRef>(C, F, Jp, material, P.dt, need_R);
+  };
+  if (steps <= 0) return;
+  // With at most one particle per thread (thread tid owns particle tid), the particle's state
+  // stays in registers for the whole call: read once here, written once after the last step
+  // (README scene 6.89 -> 6.64 us per step, a 22k-particle 3D block 18.5 -> 18.0 us).
+  const bool resident = P.n <= stride;
+  const bool mine = resident && tid < P.n;
+  float rx[D], rv[D], rJp = 0.0f;
+  Mat<D> rF, rC;
+  int rmat = P.model;
+  if (mine) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      x[d] = s.x[(size_t)d * st + p];
-      v[d] = s.v[(size_t)d * st + p];
+      rx[d] = s.x[(size_t)d * st + tid];
+      rv[d] = s.v[(size_t)d * st + tid];
     }
-    const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
-    const int material = s.mat ? (int)s.mat[p] : P.model;
-    p2g_one(p, x, v, F, C, s.Jp[p], stress_R<D>(F, P, material), material);
+    rF = load_mat<D>(s.F, st, tid);
+    rC = load_mat<D>(s.C, st, tid);
+    rJp = s.Jp[tid];
+    rmat = s.mat ? (int)s.mat[tid] : P.model;
+  }
+  // ---- p2g of the first step (src/nclr.h:104-165) from the stored state ----
+  if (resident) {
+    if (mine) p2g_one(tid, rx, rv, rF, rC, rJp, stress_R<D>(rF, P, rmat), rmat);
+  } else {
+    for (int p = tid; p < P.n; p += stride) {
+      float x[D], v[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        x[d] = s.x[(size_t)d * st + p];
+        v[d] = s.v[(size_t)d * st + p];
+      }
+      const Mat<D> F = load_mat<D>(s.F, st, p), C = load_mat<D>(s.C, st, p);
+      const int material = s.mat ? (int)s.mat[p] : P.model;
+      p2g_one(p, x, v, F, C, s.Jp[p], stress_R<D>(F, P, material), material);
+    }
   }
   for (int step = 0; step < steps; ++step) {
     if constexpr (kCluster) cluster_barrier();
@@ -1277,44 +1328,28 @@ small_steps_kernel(PState s, Params P, float4 *__restrict__ G, float4 *__restric
     }
     if constexpr (kCluster) cluster_barrier();
     else if (!grid_barrier(bar, err, gridDim.x + bt.extra, bt.spins)) return;
-    // ---- g2p (src/nclr.h:167-261), then the next step's p2g of the same particle from its
-    // new state in registers (each thread keeps its particles from step to step, so no
-    // barrier is needed between the two; G was cleared above), with the stress rotation from
-    // the F update's own decomposition.  Measured against a separate p2g pass at the top of
-    // each step: the README scene 7.25 -> 6.86 us per step, a 22k-particle 3D jelly block
-    // 18.7 -> 18.4 us. ----
+    // ---- g2p, then the next step's p2g of the same particle from its new state in
+    // registers (each thread keeps its particles from step to step, so no barrier is needed
+    // between the two; G was cleared above), with the stress rotation from the F update's own
+    // decomposition.  Measured against a separate p2g pass at the top of each step: the
+    // README scene 7.25 -> 6.86 us per step, a 22k-particle 3D jelly block 18.7 -> 18.4 us ----
     const bool next = step + 1 < steps;
-    for (int p = tid; p < P.n; p += stride) {
-      float x[D], v[D], fx[D], w[3][D];
-      int base[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        x[d] = s.x[(size_t)d * st + p];
-        v[d] = 0.0f;
+    const bool need_R = next && P.stress == kCorotated;
+    if (resident) {
+      if (mine) {
+        const Mat<D> R = g2p_one(rx, rv, rF, rC, rJp, rmat, need_R);
+        if (next) p2g_one(tid, rx, rv, rF, rC, rJp, R, rmat);
       }
-      Mat<D> C;
+      continue;
+    }
+    for (int p = tid; p < P.n; p += stride) {
+      float x[D], v[D];
 #pragma unroll
-      for (int i = 0; i < D; ++i)
-#pragma unroll
-        for (int j = 0; j < D; ++j) C.a[i][j] = 0.0f;
-      stencil<D>(x, P.inv_dx, base, fx, w);
-      const int64_t f0 = flat_index<D>(base, N);
-      g2p_gather<D>(
-          [&](int o) {
-            const int64_t f = stencil_flat<D>(f0, o, N);
-            if (f >= 0 && f < P.nodes) return __ldcg(V + f);
-            atomicOr(err, kErrOutOfRange);
-            return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-          },
-          fx, w, v, C);
-      scale_mat<D>(C, P.cscale);
-#pragma unroll
-      for (int d = 0; d < D; ++d) x[d] += P.dt * v[d];
-      Mat<D> F = load_mat<D>(s.F, st, p);
+      for (int d = 0; d < D; ++d) x[d] = s.x[(size_t)d * st + p];
+      Mat<D> F = load_mat<D>(s.F, st, p), C;
       float Jp = s.Jp[p];
       const int material = s.mat ? (int)s.mat[p] : P.model;
-      const Mat<D> R =
-          update_F<D, kRef>(C, F, Jp, material, P.dt, next && P.stress == kCorotated);
+      const Mat<D> R = g2p_one(x, v, F, C, Jp, material, need_R);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         s.x[(size_t)d * st + p] = x[d];
@@ -1325,6 +1360,16 @@ small_steps_kernel(PState s, Params P, float4 *__restrict__ G, float4 *__restric
       s.Jp[p] = Jp;
       if (next) p2g_one(p, x, v, F, C, Jp, R, material);
     }
+  }
+  if (mine) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      s.x[(size_t)d * st + tid] = rx[d];
+      s.v[(size_t)d * st + tid] = rv[d];
+    }
+    store_mat<D>(s.F, st, tid, rF);
+    store_mat<D>(s.C, st, tid, rC);
+    s.Jp[tid] = rJp;
   }
 }
 
