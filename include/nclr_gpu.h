@@ -359,9 +359,10 @@ void nclr_rollout_destroy(nclr_rollout *r);
  * each call clears it before use.  Calls whose GPU work overlaps (other threads or streams at
  * the same time) race on it: serialise them (the library does not).  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) and keeps it for the
- * context it was made in; make that first call before any stream capture.  A call in another
- * context of the device (after cudaDeviceReset, or in a caller's own context) looks the address
- * up again, so that call too belongs before any stream capture.  Errors: NCLR_ERR_INVALID (bad argument, grid too large), NCLR_ERR_OUT_OF_RANGE (a
+ * context it was made in; a call in another context of the device (after cudaDeviceReset, or
+ * in a caller's own context) looks the address up again.  No call can run inside a stream
+ * capture: each one reads its status back and synchronises its stream.  Errors:
+ * NCLR_ERR_INVALID (bad argument, grid too large), NCLR_ERR_OUT_OF_RANGE (a
  * stencil left the grid, the reference's std::out_of_range), NCLR_ERR_CUDA; when `message`
  * is non-NULL, up to message_len - 1 bytes of explanation are written there.
  * --------------------------------------------------------------------------------------- */
