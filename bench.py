@@ -532,41 +532,51 @@ def run_adjoint(device: int, steps: int = 2000, every: int = 50) -> dict:
 
 def run_plain_form(scene: dict, model: int, res: int, device: int, steps: int, *, physics: int,
                    material=None, label: str, tune: bool = True) -> dict:
-    """One single-simulation form: the autotuned simulation advances `steps` steps after a
-    10-step warm-up, timed with CUDA events on its stream; per-kernel CUDA events in the same
-    region (direct launches) give the fused kernel's roofline; then the error of one step from
-    the state the timed region ended in, against the FP64 oracle."""
+    """One single-simulation form: the autotuned simulation (the library's defaults otherwise:
+    CUDA graphs, overlapped launches) advances `steps` steps after a 10-step warm-up, timed
+    with CUDA events on its stream; the same steps on a profiled handle (direct launches with
+    CUDA events around every kernel) give the fused kernel's roofline; then the error of one
+    step from the state the timed region ended in, against the FP64 oracle."""
     import torch
 
     from nuclearmpm_gb300 import MPMSimulation
     n = len(scene["x"])
     tuned = tune_plain(scene, model, res, device, physics, material) if tune else {}
-    sim = MPMSimulation(dict(scene), model, res=res, material=material, physics=physics,
-                        profile=True, device=device, **tuned)
-    sim.advance(10)
-    sim.profile_reset()
-    st = torch.cuda.ExternalStream(sim.stream)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(st)
-    sim.advance(steps)
-    b.record(st)
-    b.synchronize()
-    t = a.elapsed_time(b) / 1e3
-    prof = sim.profile()
-    active = sim.active_nodes()
+
+    def timed(profile: bool):
+        sim = MPMSimulation(dict(scene), model, res=res, material=material, physics=physics,
+                            profile=profile, device=device, **tuned)
+        sim.advance(10)
+        sim.profile_reset()
+        st = torch.cuda.ExternalStream(sim.stream)
+        a.record(st)
+        sim.advance(steps)
+        b.record(st)
+        b.synchronize()
+        return sim, a.elapsed_time(b) / 1e3
+
+    sim, t = timed(False)
     launches = sim.stats()[0]
     end_state = state_of(sim, scene)
     sim.close()
+    psim, pt = timed(True)
+    prof = psim.profile()
+    active = psim.active_nodes()
+    psim.close()
     g_ms = prof["g2p2g"][0] / max(prof["g2p2g"][1], 1)
     alg = algorithmic_bytes(3, n, active)["g2p2g"] + (n if material is not None else 0)
     kernels = {k: {"total_ms": v[0], "launches": v[1], "avg_ms": v[0] / max(v[1], 1),
-                   "share": v[0] / max(t * 1e3, 1e-9)} for k, v in prof.items() if v[1] > 0}
+                   "share": v[0] / max(pt * 1e3, 1e-9)} for k, v in prof.items() if v[1] > 0}
     err = error_vs_fp64(end_state, dim=3, model=model, res=res, device=device, material=material,
                         physics=physics, what=f"the state after the {10 + steps} steps run")
     return {"value": n * steps / t, "unit": UNIT, "particles": n, "steps": steps,
             "ms_per_step": t / steps * 1e3, "gpu_launches": launches,
             "physics": "reference" if physics == 0 else "corrected", "tuned": tuned,
-            "roofline": roofline_of("g2p2g", alg, g_ms, kernels=kernels, active_nodes=active),
+            "roofline": dict(roofline_of("g2p2g", alg, g_ms, kernels=kernels, active_nodes=active),
+                             timing="CUDA events around every kernel, the same steps on a "
+                                    "profiled handle (direct launches: "
+                                    f"{pt / steps * 1e3:.4f} ms per step there)"),
             "error_vs_fp64": err, "config": label}
 
 
@@ -668,7 +678,8 @@ def run_models(device: int, steps: int = 100) -> dict:
     Three runs: the reference's fixed-corotated stress; the neo-Hookean stress; and the
     corotated stress with every particle's own E (log-uniform in [1e3, 1e4]) and nu (uniform
     in [0.1, 0.4]). Each is `steps` steps, timed with CUDA events on the simulation's stream
-    after warm-up."""
+    after warm-up, with the library's defaults (CUDA graphs, overlapped launches); the same
+    steps on a profiled handle give the fused kernel's time."""
     import torch
 
     from nuclearmpm_gb300 import MPMSimulation, capi, scenes
@@ -681,28 +692,37 @@ def run_models(device: int, steps: int = 100) -> dict:
     for name, stress, own in (("corotated", capi.STRESS_COROTATED, False),
                               ("neohookean", capi.STRESS_NEOHOOKEAN, False),
                               ("per_particle_moduli", capi.STRESS_COROTATED, True)):
-        sim = MPMSimulation(dict(sc), scenes.JELLY, res=128, physics=scenes.CORRECTED,
-                            stress_model=stress, device=device, profile=True)
-        if own:
-            sim.set_moduli(E, nu)
-        sim.advance(10)
-        sim.profile_reset()
-        st = torch.cuda.ExternalStream(sim.stream)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(st)
-        sim.advance(steps)
-        b.record(st)
-        b.synchronize()
-        t = a.elapsed_time(b) / 1e3
-        prof = sim.profile()
-        active = sim.active_nodes()
+
+        def timed(profile: bool):
+            sim = MPMSimulation(dict(sc), scenes.JELLY, res=128, physics=scenes.CORRECTED,
+                                stress_model=stress, device=device, profile=profile)
+            if own:
+                sim.set_moduli(E, nu)
+            sim.advance(10)
+            sim.profile_reset()
+            st = torch.cuda.ExternalStream(sim.stream)
+            a.record(st)
+            sim.advance(steps)
+            b.record(st)
+            b.synchronize()
+            return sim, a.elapsed_time(b) / 1e3
+
+        sim, t = timed(False)
+        launches = sim.stats()[0]
+        end_state = state_of(sim, sc)
+        sim.close()
+        psim, pt = timed(True)
+        prof = psim.profile()
+        active = psim.active_nodes()
+        psim.close()
         g_ms = prof["g2p2g"][0] / max(prof["g2p2g"][1], 1)
         alg = algorithmic_bytes(3, n, active)["g2p2g"] + (8 * n if own else 0)
-        end_state = state_of(sim, sc)
         out[name] = {"value": n * steps / t, "ms_per_step": t / steps * 1e3,
-                     "gpu_launches": sim.stats()[0],
-                     "roofline": roofline_of("g2p2g", alg, g_ms, active_nodes=active)}
-        sim.close()
+                     "gpu_launches": launches,
+                     "roofline": dict(roofline_of("g2p2g", alg, g_ms, active_nodes=active),
+                                      timing="the same steps on a profiled handle (direct "
+                                             f"launches: {pt / steps * 1e3:.4f} ms per step)")}
         out[name]["error_vs_fp64"] = error_vs_fp64(
             end_state, dim=3, model=scenes.JELLY, res=128, device=device,
             physics=scenes.CORRECTED, stress=stress, E_p=E if own else None,
