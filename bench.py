@@ -848,7 +848,6 @@ def run_ours(args):
     ms_max = max_over_ranks(ms)
     clk = clocks.summary()
     value = replica_value(world, n, args.steps, ms_max)
-    gsim.close()
 
     # ---- per-kernel times for the roofline: the same steps on a profiled handle (direct
     # launches with CUDA events around every kernel on its stream), timed the same way ------
@@ -866,6 +865,7 @@ def run_ours(args):
     prof_ms = pstart.elapsed_time(pstop)
     prof = sim.profile()
     active = sim.active_nodes()
+    sim.close()
 
     # ---- roofline of the dominant kernel ------------------------------------------------
     hbm_peak, peak_kind = peaks()
@@ -902,12 +902,12 @@ def run_ours(args):
     from nuclearmpm_gb300 import capi
     from nuclearmpm_gb300.simulation import _ptr
     L = capi.lib()
-    h = sim._h
+    h = gsim._h  # the headline's handle: the library's defaults, as a caller's
 
     def e2e_step():
         capi.check(L.nclr_set_particles(h, _ptr(hx), _ptr(hv), _ptr(hF), _ptr(hC), _ptr(hJ)), h)
         capi.check(L.nclr_advance(h, 1), h)
-        launches = sim.stats()[0]
+        launches = gsim.stats()[0]
         capi.check(L.nclr_get_particles(h, _ptr(ox), _ptr(ov), _ptr(oF), _ptr(oC), _ptr(oJ)), h)
         return launches
 
@@ -979,7 +979,7 @@ def run_ours(args):
                 "readme": readme, "models": models, "gpu_launches": launches_total,
                 "clocks": clk}
         print(json.dumps(line), flush=True)
-    sim.close()
+    gsim.close()
     ranks.close()
     return 0
 
